@@ -1,0 +1,216 @@
+"""Generates the committed golden fixtures in tests/golden/ from the reference itself.
+
+Run here (where the reference checkout and oracle/_ref exist):
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+Every fixture records the inputs (initial state, excitations, order, Hamiltonian as
+triplets or integrals, angles) and the reference's outputs for them, produced by
+oracle/_ref/ref_driver through the reference's public stateAnsatzManager API.
+Sources of the inputs:
+  f90      -- the Fortran binding test's arrays, parsed from src/test.F90
+  ferm     -- Hams/TestFermionic (sparse Hamiltonian, number-only sector)
+  h4       -- Hams/H4/L1 integrals / operators / order / parameters (+ optimise)
+  h4c      -- Hams/H4_Complex/L1 (complex build, diagonal U3 operators)
+  syn8     -- synthetic 8-orbital TUPS, seed 0 (ansatzevolve_gb300.synthetic)
+  syn6     -- synthetic 6-orbital TUPS, seed 3, plus the excitation rule table
+"""
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from ansatzevolve_gb300.synthetic import (hartree_fock_index, synthetic_integrals,  # noqa: E402
+                                          tups_operators, write_integrals)
+
+REF = os.environ.get("AE_REFERENCE", "/root/reference")
+DRV = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def run(spec_lines, cplx=False):
+    with tempfile.TemporaryDirectory() as td:
+        sp, op = os.path.join(td, "spec"), os.path.join(td, "out")
+        open(sp, "w").write("\n".join(spec_lines) + "\nend\n")
+        drv = DRV + ("_cplx" if cplx else "")
+        subprocess.run([drv, sp, op], check=True, stderr=subprocess.DEVNULL, stdout=subprocess.DEVNULL,
+                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+        return np.fromfile(op, dtype="<f8")
+
+
+def spec(nq, init, ops0, param0, scale, ham, anglesets, want=(1, 1, 1, 1), pairs=0, optimise=0, nuclear=0.0):
+    s = [f"nqubits {nq}", f"initial {len(init)}"]
+    s += [f"{i} {re!r} {im!r}" for i, re, im in init]
+    s += [f"ops {len(ops0)}"] + [" ".join(str(int(v)) for v in o) for o in ops0]
+    s += [f"order {len(param0)}"] + [f"{int(p)} {float(c)!r}" for p, c in zip(param0, scale)]
+    s += ham
+    s += [f"nuclear {float(nuclear)!r}"]
+    s += [f"anglesets {len(anglesets)} {len(anglesets[0])}"] + [" ".join(repr(float(a)) for a in A) for A in anglesets]
+    s += ["want " + " ".join(str(w) for w in want), f"pairs {pairs}", f"optimise {optimise}"]
+    return s
+
+
+def split_outputs(d, nsets, P, nstate, want, cplx=False):
+    out = {"E": [], "G": [], "H": [], "S": []}
+    w = 2 if cplx else 1
+    k = 0
+    for _ in range(nsets):
+        if want[0]:
+            out["E"].append(d[k]); k += 1
+        if want[1]:
+            out["G"].append(d[k:k + P]); k += P
+        if want[2]:
+            out["H"].append(d[k:k + P * P].reshape(P, P, order="F")); k += P * P
+        if want[3]:
+            out["S"].append(d[k:k + nstate * w]); k += nstate * w
+    return {key: np.array(v) for key, v in out.items() if v}, d[k:]
+
+
+def fortran_case():
+    src = open(os.path.join(REF, "src", "test.F90")).read()
+
+    def arr(pat):
+        m = re.search(pat + r"\s*=\s*(?:transpose\(reshape\()?\[([^\]]*)\]", src)
+        return [t.strip() for t in m.group(1).split(",")]
+
+    hi = np.array([int(x) for x in arr("HamiIndexes")], dtype=np.int32)
+    hj = np.array([int(x) for x in arr("HamjIndexes")], dtype=np.int32)
+    hv = np.array([float(x.replace("_dp", "")) for x in arr("HamCoeffs")])
+    ops = np.array([int(x) for x in arr(r"dimension\(15, 4\) :: operators")], dtype=np.int32).reshape(15, 4)
+    order = np.array([int(x) for x in arr(r"dimension\(15\) :: order")], dtype=np.int32)
+    angmin = np.array([float(x.replace("_dp", "")) for x in re.findall(
+        r"angles\s*=\s*\[([^\]]*)\]", src)[1].split(",")])
+    expected = {}
+    for key, pat in [("E0", r'"Expected:", (-?[0-9.]+)_dp'), ("G0", r'"gradient Norm Expected:", ([0-9.E-]+)_dp')]:
+        expected[key] = [float(v) for v in re.findall(pat, src)]
+    rng = np.random.default_rng(11)
+    sets = [np.zeros(9), angmin, rng.uniform(-1, 1, 9)]
+    ops0 = ops - 1
+    s = spec(8, [(170, 1.0, 0.0)], ops0, order - 1, np.ones(15),
+             [f"ham triplets {len(hv)}"] + [f"{a - 1} {b - 1} {float(c)!r}" for a, b, c in zip(hi, hj, hv)],
+             sets, pairs=1)
+    d = run(s)
+    res, rest = split_outputs(d, len(sets), 9, 256, (1, 1, 1, 1))
+    pairs = rest.reshape(15, 256, 2)
+    np.savez_compressed(os.path.join(OUT, "f90.npz"), nq=8, init_idx=[170], init_re=[1.0], ops_1b=ops,
+                        order_1b=order, scale=np.ones(15), ham_i_1b=hi, ham_j_1b=hj, ham_v=hv,
+                        angles=np.array(sets), E=res["E"], G=res["G"], H=res["H"], S=res["S"],
+                        pair_partner=pairs[..., 0].astype(np.uint32), pair_sign=pairs[..., 1].astype(np.int8),
+                        known_E=np.array(expected["E0"]), known_gnorm=np.array(expected["G0"]))
+    print("f90", res["E"], np.linalg.norm(res["G"], axis=1))
+
+
+def read_order(path):
+    param, scale = [], []
+    for line in open(path):
+        line = line.strip()
+        if not line:
+            continue
+        parts = line.split(",")
+        param.append(int(parts[0]))
+        scale.append(float(parts[1]) if len(parts) > 1 else 1.0)
+    return np.array(param, dtype=np.int32), np.array(scale)
+
+
+def read_params(path):
+    toks = open(path).read().split("\n")
+    sets, k = [], 0
+    while k < len(toks):
+        t = toks[k].strip()
+        if not t:
+            k += 1
+            continue
+        n = int(t)
+        vals = [float(toks[k + 2 + i]) for i in range(n)]
+        sets.append(vals)
+        k += 2 + n
+    return np.array(sets)
+
+
+def read_initial(path, nq_hint=None):
+    init = []
+    for line in open(path):
+        line = line.strip()
+        if not line:
+            continue
+        parts = line.split(",")
+        bits = parts[0].strip()
+        re_ = float(parts[1]) if len(parts) > 1 and parts[1].strip() else 1.0
+        im_ = float(parts[2]) if len(parts) > 2 and parts[2].strip() else 0.0
+        init.append((int(bits, 2), re_, im_, len(bits)))
+    return init
+
+
+def hams_case(name, sub, cplx=False, optimise=False, tag=None):
+    base = os.path.join(REF, "Hams", name, sub, name.split("_")[0]) if sub else os.path.join(REF, "Hams", name, name)
+    init = read_initial(base + "_Initial.dat")
+    nq = init[0][3]
+    ops = np.loadtxt(base + "_Operators.dat", dtype=np.int32).reshape(-1, 4)
+    param, scale = read_order(base + "_Order.dat")
+    params = read_params(base + "_Parameters.dat")
+    nuclear = float(open(base + "_Nuclear_Energy.dat").read()) if os.path.exists(base + "_Nuclear_Energy.dat") else 0.0
+    P = int(param.max())
+    rng = np.random.default_rng(5)
+    sets = [params[-1][:P], rng.uniform(-0.5, 0.5, P), params[0][:P]]  # optimise() starts from the last set
+    fx = dict(nq=nq, init_idx=[i[0] for i in init], init_re=[i[1] for i in init], init_im=[i[2] for i in init],
+              ops_1b=ops, order_1b=param, scale=scale, nuclear=nuclear, angles=np.array(sets))
+    if os.path.exists(base + "_oneEInts.bin"):
+        N = nq // 2
+        fx["h1"] = np.fromfile(base + "_oneEInts.bin").reshape(N, N)
+        fx["g2"] = np.fromfile(base + "_twoEInts.bin").reshape(N, N, N, N)
+        ham = [f"ham ints {base}"]
+    else:
+        cv = np.loadtxt(base + "_Ham_Coeff.dat", delimiter=",", ndmin=2)[:, 0]
+        ij = np.loadtxt(base + "_Ham_Index.dat", dtype=np.int64, ndmin=2)
+        fx.update(ham_i_1b=ij[:, 0].astype(np.int32), ham_j_1b=ij[:, 1].astype(np.int32), ham_v=cv)
+        ham = [f"ham triplets {len(cv)}"] + [f"{a - 1} {b - 1} {float(c)!r}" for (a, b), c in zip(ij, cv)]
+    s = spec(nq, [(i[0], i[1], i[2]) for i in init], ops - 1, param - 1, scale, ham, sets,
+             optimise=int(optimise), nuclear=nuclear)
+    d = run(s, cplx)
+    res, rest = split_outputs(d, len(sets), P, 1 << nq, (1, 1, 1, 1), cplx)
+    fx.update(E=res["E"], G=res["G"], H=res["H"], S=res["S"])
+    if optimise:
+        fx["opt_E"] = rest[0]
+        fx["opt_angles"] = rest[3:3 + int(rest[2])]
+    np.savez_compressed(os.path.join(OUT, (tag or name.lower()) + ".npz"), **fx)
+    print(tag or name, res["E"], fx.get("opt_E"))
+
+
+def synthetic_case(tag, N, na, nb, layers, seed, pairs=False, hess=True):
+    h, g = synthetic_integrals(N, seed)
+    ops, param, scale = tups_operators(N, layers)
+    P = int(param.max())
+    rng = np.random.default_rng(seed + 100)
+    sets = [rng.uniform(-0.1, 0.1, P), rng.uniform(-0.3, 0.3, P)]
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, "syn")
+        write_integrals(prefix, h, g)
+        hf = hartree_fock_index(N, na, nb)
+        s = spec(2 * N, [(hf, 1.0, 0.0)], ops - 1, param - 1, scale, [f"ham ints {prefix}"], sets,
+                 want=(1, 1, int(hess), 1), pairs=int(pairs))
+        d = run(s)
+    res, rest = split_outputs(d, len(sets), P, 1 << (2 * N), (1, 1, int(hess), 1))
+    # keep the final states compressed to the sector to keep the fixture small
+    sect = [s_ for s_ in range(1 << (2 * N)) if bin(s_ >> N).count("1") == na and bin(s_ & ((1 << N) - 1)).count("1") == nb]
+    fx = dict(N=N, na=na, nb=nb, layers=layers, seed=seed, hf=hf, ops_1b=ops, order_1b=param, scale=scale,
+              angles=np.array(sets), E=res["E"], G=res["G"], S_sector=res["S"][:, sect], sector=np.array(sect, dtype=np.uint32))
+    if hess:
+        fx["H"] = res["H"]
+    if pairs:
+        pr = rest.reshape(len(ops), 1 << (2 * N), 2)
+        fx["pair_partner"] = pr[..., 0].astype(np.uint32)
+        fx["pair_sign"] = pr[..., 1].astype(np.int8)
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), **fx)
+    print(tag, res["E"])
+
+
+if __name__ == "__main__":
+    fortran_case()
+    hams_case("TestFermionic", None, tag="ferm")
+    hams_case("H4", "L1", optimise=True, tag="h4")
+    hams_case("H4_Complex", "L1", cplx=True, tag="h4c")
+    synthetic_case("syn6", 6, 3, 3, 2, 3, pairs=True)
+    synthetic_case("syn8", 8, 4, 4, 2, 0)
