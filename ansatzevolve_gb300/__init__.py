@@ -1,0 +1,396 @@
+"""GB300-native statevector engine for TUPS / U3 fermionic ansatze.
+
+The product is the in-tree shared library ``libansatzevolve_gb300.so``: hand-written
+sm_103a CUDA kernels behind a thin C ABI (``include/aegpu.h``) and, on top of it,
+the reference's own drop-in interface -- the C++ ``stateAnsatzManager`` and the
+``AnsatzSynthInterface`` C functions (``include/AnsatzSynthInterface.h``).
+This module only loads that library with ctypes and mirrors the reference's
+Python binding (PyAnsatzEvolve.cpp:17-148) on top of the C ABI.  There is no
+CPU implementation of the path here: without the library or a CUDA device every
+entry point raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
+_LIB = None
+
+HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
+BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
+
+_P = ctypes.c_void_p
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+
+
+class AegpuError(RuntimeError):
+    pass
+
+
+def lib(build_if_missing=True):
+    """The loaded extension (builds it in-tree first if it is missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise AegpuError("libansatzevolve_gb300.so is not built")
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(LIB_PATH)
+    i64 = ctypes.c_int64
+    sig = {
+        "aegpu_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
+        "aegpu_destroy": (None, [_P]),
+        "aegpu_last_error": (ctypes.c_char_p, [_P]),
+        "aegpu_set_problem": (ctypes.c_int, [_P] + [ctypes.c_int] * 7 + [_IP]),
+        "aegpu_dim": (i64, [_P]),
+        "aegpu_basis_states": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+        "aegpu_num_blocks": (ctypes.c_int, [_P]),
+        "aegpu_block_layout": (ctypes.c_int, [_P, _IP, _IP]),
+        "aegpu_set_initial": (ctypes.c_int, [_P, _DP]),
+        "aegpu_set_ham_csr": (ctypes.c_int, [_P, i64, ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int32), _DP]),
+        "aegpu_set_ham_integrals": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
+        "aegpu_ham_info": (ctypes.c_int, [_P, _IP, ctypes.POINTER(i64)]),
+        "aegpu_evolve": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_energy": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_gradient": (ctypes.c_int, [_P, _DP, _DP, _DP]),
+        "aegpu_hessian": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, _DP, _DP, _DP]),
+        "aegpu_apply_h": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_gradient_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+        "aegpu_energy_dev": (ctypes.c_int, [_P, _P, _P, _P]),
+        "aegpu_state_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+        "aegpu_host_block_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, _IP, _IP, _IP]),
+        "aegpu_host_orbits": (ctypes.c_int, [ctypes.c_int] * 6 + [_IP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
+                                                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
+                                                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64)]),
+        "aegpu_apply_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+        "aegpu_phase_timing": (ctypes.c_int, [_P, ctypes.c_int]),
+        "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
+        "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
+        "aegpu_device_bytes": (i64, [_P]),
+        "aegpu_launch_count": (i64, [_P]),
+        # reference C ABI
+        "init": (_P, []),
+        "cleanup": (ctypes.c_int, [_P]),
+        "setExcitation": (ctypes.c_int, [ctypes.c_int, _IP, _IP, _P]),
+        "setExcitationScale": (ctypes.c_int, [ctypes.c_int, _IP, _IP, _DP, _P]),
+        "setHamiltonian": (ctypes.c_int, [ctypes.c_int, _IP, _IP, _DP, _P]),
+        "setInitialState": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, _DP, _P]),
+        "setInitialStateComplex": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, _DP, _P]),
+        "getEnergy": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+        "getFinalState": (ctypes.c_int, [ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
+        "getFinalStateComplex": (ctypes.c_int, [ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
+        "getGradient_COMP": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+        "getHessian_COMP": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+        "setTraceInterfaceCalls": (None, [ctypes.c_int]),
+        "setRunPath": (ctypes.c_int, [ctypes.c_char_p, _P]),
+        "setIntegrals": (ctypes.c_int, [ctypes.c_int, _DP, _DP, ctypes.c_int, _P]),
+        "setNuclearEnergy": (ctypes.c_int, [ctypes.c_double, _P]),
+        "optimise": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = L
+    return L
+
+
+def dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_IP)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Engine:
+    """The aegpu C ABI for one problem (sector basis + excitations + Hamiltonian)."""
+
+    def __init__(self, nq, basis_kind, n_elec, n_alpha, n_beta, ops0, complex_mode=False):
+        self.L = lib()
+        h = _P()
+        rc = self.L.aegpu_create(ctypes.byref(h))
+        if rc:
+            raise AegpuError("aegpu_create failed (%d): no usable CUDA device" % rc)
+        self.h = h
+        ops = _i32(ops0).reshape(-1, 4)
+        self.nops = len(ops)
+        self.W = 2 if complex_mode else 1
+        self._check(self.L.aegpu_set_problem(h, nq, basis_kind, n_elec, n_alpha, n_beta, int(complex_mode), self.nops,
+                                             iptr(ops.reshape(-1))))
+        self.D = int(self.L.aegpu_dim(h))
+
+    def _check(self, rc):
+        if rc:
+            raise AegpuError("aegpu error %d: %s" % (rc, self.L.aegpu_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aegpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def states(self):
+        out = np.zeros(self.D, dtype=np.uint32)
+        self._check(self.L.aegpu_basis_states(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        return out
+
+    def block_layout(self):
+        nb = self.L.aegpu_num_blocks(self.h)
+        perm = np.zeros(self.nops, dtype=np.int32)
+        sizes = np.zeros(nb, dtype=np.int32)
+        self._check(self.L.aegpu_block_layout(self.h, iptr(perm), iptr(sizes)))
+        return perm, sizes
+
+    def set_initial(self, amps):
+        a = _f64(amps)
+        assert a.size == self.D * self.W
+        self._check(self.L.aegpu_set_initial(self.h, dptr(a)))
+
+    def set_ham_csr(self, rowptr, col, val):
+        rp = np.ascontiguousarray(rowptr, dtype=np.int64)
+        c = np.ascontiguousarray(col, dtype=np.int32)
+        v = _f64(val)
+        self._check(self.L.aegpu_set_ham_csr(self.h, len(v), rp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                             c.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), dptr(v)))
+
+    def set_ham_integrals(self, h1, g2, mode=HAM_AUTO):
+        a, b = _f64(h1), _f64(g2)
+        self._check(self.L.aegpu_set_ham_integrals(self.h, dptr(a), dptr(b), mode))
+
+    def ham_info(self):
+        k = ctypes.c_int()
+        n = ctypes.c_int64()
+        self._check(self.L.aegpu_ham_info(self.h, ctypes.byref(k), ctypes.byref(n)))
+        return k.value, n.value
+
+    def evolve(self, angles_ops):
+        a = _f64(angles_ops)
+        out = np.zeros(self.D * self.W)
+        self._check(self.L.aegpu_evolve(self.h, dptr(a), dptr(out)))
+        return out
+
+    def energy(self, angles_ops):
+        a = _f64(angles_ops)
+        E = np.zeros(1)
+        self._check(self.L.aegpu_energy(self.h, dptr(a), dptr(E)))
+        return E[0]
+
+    def gradient(self, angles_ops):
+        a = _f64(angles_ops)
+        E = np.zeros(1)
+        g = np.zeros(self.nops)
+        self._check(self.L.aegpu_gradient(self.h, dptr(a), dptr(E), dptr(g)))
+        return E[0], g
+
+    def hessian(self, angles_ops, param0, scale):
+        a = _f64(angles_ops)
+        p = _i32(param0)
+        s = _f64(scale)
+        P = int(p.max()) + 1
+        E = np.zeros(1)
+        g = np.zeros(P)
+        H = np.zeros((P, P))
+        self._check(self.L.aegpu_hessian(self.h, dptr(a), iptr(p), dptr(s), P, dptr(E), dptr(g), dptr(H)))
+        return E[0], g, H
+
+    def apply_h(self, x):
+        x = _f64(x)
+        y = np.zeros_like(x)
+        self._check(self.L.aegpu_apply_h(self.h, dptr(x), dptr(y)))
+        return y
+
+    def gradient_dev(self, angles_ptr, energy_ptr, grad_ptr, stream=0):
+        self._check(self.L.aegpu_gradient_dev(self.h, angles_ptr, energy_ptr, grad_ptr, stream or None))
+
+    def energy_dev(self, angles_ptr, energy_ptr, stream=0):
+        self._check(self.L.aegpu_energy_dev(self.h, angles_ptr, energy_ptr, stream or None))
+
+    def apply_dev(self, x_ptr, y_ptr, energy_ptr=None, stream=0):
+        self._check(self.L.aegpu_apply_dev(self.h, x_ptr, y_ptr, energy_ptr, stream or None))
+
+    def phase_timing(self, enable=True):
+        self._check(self.L.aegpu_phase_timing(self.h, int(enable)))
+
+    def phase_times(self):
+        ms = np.zeros(3)
+        n = ctypes.c_int64()
+        self._check(self.L.aegpu_phase_times(self.h, dptr(ms), ctypes.byref(n)))
+        return ms, n.value
+
+    def info(self):
+        out = np.zeros(7, dtype=np.int64)
+        self._check(self.L.aegpu_problem_info(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active")
+        return dict(zip(keys, map(int, out)))
+
+    def device_bytes(self):
+        return int(self.L.aegpu_device_bytes(self.h))
+
+    def launch_count(self):
+        return int(self.L.aegpu_launch_count(self.h))
+
+
+def host_block_layout(nq, ops0):
+    """Operator application order and fused block sizes (host setup, no GPU)."""
+    L = lib()
+    ops = _i32(ops0).reshape(-1, 4)
+    perm = np.zeros(len(ops), dtype=np.int32)
+    sizes = np.zeros(len(ops), dtype=np.int32)
+    nb = ctypes.c_int(len(ops))
+    rc = L.aegpu_host_block_layout(nq, len(ops), iptr(ops.reshape(-1)), iptr(perm), iptr(sizes), ctypes.byref(nb))
+    if rc:
+        raise AegpuError("aegpu_host_block_layout returned %d" % rc)
+    return perm, sizes[:nb.value]
+
+
+def host_orbits(nq, kind, ne, na, nb, ops0):
+    """Orbit tables of one block of commuting excitations (host setup, no GPU):
+    (ranks, groups[:, idx_off n_orbits k mask], tiles[:, group orbit0 n_orbits elem_off])."""
+    L = lib()
+    ops = _i32(ops0).reshape(-1, 4)
+    u32 = ctypes.POINTER(ctypes.c_uint32)
+    ni, ng, nt = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+    args = [nq, kind, ne, na, nb, len(ops), iptr(ops.reshape(-1))]
+    rc = L.aegpu_host_orbits(*args, None, ctypes.byref(ni), None, ctypes.byref(ng), None, ctypes.byref(nt))
+    if rc:
+        raise AegpuError("aegpu_host_orbits returned %d" % rc)
+    idx = np.zeros(ni.value, dtype=np.uint32)
+    g = np.zeros((ng.value, 4), dtype=np.uint32)
+    t = np.zeros((nt.value, 4), dtype=np.uint32)
+    rc = L.aegpu_host_orbits(*args, idx.ctypes.data_as(u32), ctypes.byref(ni), g.ctypes.data_as(u32), ctypes.byref(ng),
+                             t.ctypes.data_as(u32), ctypes.byref(nt))
+    if rc:
+        raise AegpuError("aegpu_host_orbits returned %d" % rc)
+    return idx, g, t
+
+
+class stateAnsatzManager:
+    """Python mirror of the reference binding (PyAnsatzEvolve.cpp:17-148) over the
+    C ABI: same method names, 1-based operators for storeOperators, 0-based
+    indices for storeInitial / storeHamiltonian, compressed or per-operator angles."""
+
+    def __init__(self):
+        self.L = lib()
+        self.ctx = _P(self.L.init())
+        self._ops = None
+        self._order = None
+        self._nq = None
+        self._P = None
+
+    def close(self):
+        if getattr(self, "ctx", None) is not None and self.ctx.value:
+            self.L.cleanup(ctypes.byref(self.ctx))
+
+    def __del__(self):
+        self.close()
+
+    def _push_excitations(self):
+        if self._ops is None or self._order is None:
+            return True
+        ops = np.asarray(self._ops, dtype=np.int32).reshape(-1, 4)
+        n = len(ops)
+        fortran = _i32(ops.T.reshape(-1))  # operators[n*j + i]
+        order = _i32([o[0] + 1 for o in self._order])
+        scale = _f64([o[1] for o in self._order])
+        if len(order) != n:
+            return False
+        return self.L.setExcitationScale(n, iptr(fortran), iptr(order), dptr(scale), self.ctx) == 0
+
+    def storeOperators(self, operators):
+        self._ops = [list(map(int, o)) for o in operators]
+        if any(len(o) != 4 for o in self._ops):
+            raise ValueError("Operator must be 4 long")
+        return self._push_excitations()
+
+    def storeParameterDependencies(self, dep):
+        self._order = [(int(p), float(s)) for p, s in dep]
+        self._P = max(p for p, _ in self._order) + 1
+        return self._push_excitations()
+
+    def storeInitial(self, numberOfQubits, indexes, coeffs):
+        idx = _i32(np.asarray(indexes) + 1)
+        c = np.asarray(coeffs)
+        self._nq = int(numberOfQubits)
+        if np.iscomplexobj(c):
+            cc = np.ascontiguousarray(c, dtype=np.complex128)
+            return self.L.setInitialStateComplex(self._nq, len(idx), iptr(idx), cc.ctypes.data_as(_DP), self.ctx) == 0
+        return self.L.setInitialState(self._nq, len(idx), iptr(idx), dptr(_f64(c)), self.ctx) == 0
+
+    def storeHamiltonian(self, iIndexes, jIndexes, coeffs):
+        i = _i32(np.asarray(iIndexes) + 1)
+        j = _i32(np.asarray(jIndexes) + 1)
+        return self.L.setHamiltonian(len(i), iptr(i), iptr(j), dptr(_f64(coeffs)), self.ctx) == 0
+
+    def storeNuclearEnergy(self, e):
+        return self.L.setNuclearEnergy(float(e), self.ctx) == 0
+
+    def storeRunPath(self, path):
+        return self.L.setRunPath(path.encode(), self.ctx) == 0
+
+    def storeIntegrals(self, h1, g2, mode=HAM_AUTO):
+        h1 = _f64(h1)
+        return self.L.setIntegrals(h1.shape[0], dptr(h1), dptr(_f64(g2)), mode, self.ctx) == 0
+
+    def getExpectationValue(self, angles):
+        a = _f64(angles)
+        E = np.zeros(1)
+        rc = self.L.getEnergy(len(a), dptr(a), dptr(E), self.ctx)
+        if rc:
+            raise AegpuError("getEnergy returned %d" % rc)
+        return E[0]
+
+    def getFinalState(self, angles, complex_state=False):
+        a = _f64(angles)
+        n = 1 << self._nq
+        if complex_state:
+            out = np.zeros(n, dtype=np.complex128)
+            rc = self.L.getFinalStateComplex(len(a), dptr(a), n, out.ctypes.data_as(_DP), self.ctx)
+        else:
+            out = np.zeros(n)
+            rc = self.L.getFinalState(len(a), dptr(a), n, dptr(out), self.ctx)
+        if rc:
+            raise AegpuError("getFinalState returned %d" % rc)
+        return out
+
+    def getGradientComp(self, angles):
+        a = _f64(angles)
+        g = np.zeros(len(a))
+        rc = self.L.getGradient_COMP(len(a), dptr(a), dptr(g), self.ctx)
+        if rc:
+            raise AegpuError("getGradient_COMP returned %d" % rc)
+        return g
+
+    def getHessianComp(self, angles):
+        a = _f64(angles)
+        H = np.zeros(len(a) * len(a))
+        rc = self.L.getHessian_COMP(len(a), dptr(a), dptr(H), self.ctx)
+        if rc:
+            raise AegpuError("getHessian_COMP returned %d" % rc)
+        return H.reshape(len(a), len(a), order="F")
+
+    def getExpectationValues(self, angles):
+        return np.array([self.getExpectationValue(row) for row in np.atleast_2d(angles)])
+
+    def optimise(self, angles):
+        a = _f64(angles).copy()
+        E = np.zeros(1)
+        rc = self.L.optimise(len(a), dptr(a), dptr(E), self.ctx)
+        if rc:
+            raise AegpuError("optimise returned %d" % rc)
+        return E[0], a

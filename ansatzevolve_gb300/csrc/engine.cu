@@ -1,0 +1,1730 @@
+// GB300 statevector engine: the CUDA side of the aegpu C ABI (include/aegpu.h).
+//
+// Data layout in HBM (one problem per engine):
+//   psi, hpsi          FP64[D*W]      W = 1 (real) or 2 (complex, re/im interleaved)
+//   basis tables       Sz sector: alpha/beta strings + 2^N rank tables (a few KB);
+//                      other sectors: D bitstrings + 2^nq rank table
+//   orbit tables       per fused block: uint32 ranks of every touched determinant,
+//                      grouped into orbits (hypercubes of the active excitations),
+//                      plus group/tile descriptors (setup.cpp)
+//   Hamiltonian        CSR (general) or fixed-width ELL rows built from integrals
+//   Hessian scratch    per-operator tangents FP64[nops][D*W], compressed tangents
+//                      and H*tangents in [D][W][P+1] layout
+//
+// Kernels (all FP64; bandwidth- or FP64-pipe-bound, no tensor cores):
+//   k_block_rot      one fused block of commuting excitations on 1..n vectors; a CTA
+//                    stages whole orbits (<= 4096 amplitudes) in shared memory and
+//                    applies every butterfly layer there (reference RunFuseN,
+//                    fusedevolve.cpp:917-1774)
+//   k_block_bwd      the adjoint sweep of one block on (psi, H psi) with the gradient
+//                    partial sums of every excitation (fusedevolve.cpp:461-485)
+//   k_block_tangent  forward block + tangents T_op = G_op psi (fusedevolve.cpp:492-518)
+//   k_block_hess     backward sweep of many tangents against H psi for the second-
+//                    derivative term of the Hessian (fusedevolve.cpp:2670-2761)
+//   k_diag_*         the same four for diagonal (number / density-density) blocks,
+//                    complex mode (fusedevolve.cpp:625-717)
+//   k_spmv_csr/_ell  warp-per-row y = H x fused with the <x|y> partial sums
+//   k_spmm_*         H on P+1 vectors at once for the Hessian (matrix read once)
+//   k_ell_build      fixed-width rows of H generated from h_pq/(pq|rs): diagonal,
+//                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
+//   k_otf_apply      y = H x with the rows regenerated on the fly (no stored matrix)
+// All reductions are two-stage and in a fixed order, so results are bit-identical
+// from run to run.
+#include "../../include/aegpu.h"
+#include "exc_rule.h"
+#include "setup.h"
+
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+using namespace ae;
+
+namespace {
+
+constexpr int kMaxSlots = 12;          // excitations per fused block (the reference's maxFuse)
+constexpr int kRotThreads = 256;
+constexpr int kSpmvThreads = 256;
+constexpr int kDiagGrid = 152 * 4;
+
+struct DevBasis {
+    int kind, N, nq;
+    uint32_t nA, nB;
+    uint64_t D;
+    const uint32_t *strA, *strB;
+    const int32_t *rankA, *rankB;
+    const uint32_t *states;
+    const int32_t *rank;
+
+    __device__ __forceinline__ uint32_t bits(uint32_t z) const
+    {
+        if (kind == BASIS_SZ) return (strA[z / nB] << N) | strB[z % nB];
+        return states[z];
+    }
+    __device__ __forceinline__ int64_t rank_of(uint32_t s) const
+    {
+        if (kind == BASIS_SZ) {
+            int32_t a = rankA[s >> N], b = rankB[s & ((1u << N) - 1u)];
+            return (a < 0 || b < 0) ? -1 : (int64_t)a * nB + b;
+        }
+        return rank[s];
+    }
+};
+
+struct BlockArgs {
+    const uint32_t *idx;
+    const OrbitGroup *groups;
+    const OrbitTile *tiles;
+    const int *ops;          // slot -> operator
+    int nslots;
+    const ExcCode *codes;    // per operator
+    const double *sc;        // per operator: sin, cos
+    double dir;              // +1 forward, -1 backward
+    DevBasis basis;
+};
+
+__device__ __forceinline__ uint32_t insert_zero_bit(uint32_t p, int i)
+{
+    return ((p >> i) << (i + 1)) | (p & ((1u << i) - 1u));
+}
+
+// ---------------------------------------------------------------- utilities --
+__global__ void k_sincos(const double *__restrict__ ang, double *__restrict__ sc, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        double s, c;
+        sincos(ang[i], &s, &c);
+        sc[2 * i] = s;
+        sc[2 * i + 1] = c;
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order block sum; result valid in thread 0.  red needs blockDim/32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *red)
+{
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) s += red[k];
+    return s;
+}
+
+__global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__restrict__ out, double scale)
+{
+    __shared__ double red[32];
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += parts[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) out[0] = s * scale;
+}
+
+// -------------------------------------------------------- block rotations --
+// Stage the tile's ranks' bitstrings and load the layer constants.
+struct TileCtx {
+    uint32_t n;       // amplitudes in the tile
+    int k;            // layers
+    const uint32_t *idx;
+};
+
+__device__ __forceinline__ TileCtx load_tile(const BlockArgs &a, uint32_t *bits, ExcCode *code, double *C,
+                                             double *S, int *slot)
+{
+    const OrbitTile t = a.tiles[blockIdx.x];
+    const OrbitGroup &g = a.groups[t.group];
+    TileCtx c;
+    c.k = (int)g.k;
+    c.n = t.n_orbits << g.k;
+    c.idx = a.idx + t.elem_off;
+    if (threadIdx.x < (unsigned)c.k) {
+        int s = g.slot[threadIdx.x];
+        int op = a.ops[s];
+        slot[threadIdx.x] = s;
+        code[threadIdx.x] = a.codes[op];
+        S[threadIdx.x] = a.dir * a.sc[2 * op];
+        C[threadIdx.x] = a.sc[2 * op + 1];
+    }
+    for (uint32_t e = threadIdx.x; e < c.n; e += blockDim.x) bits[e] = a.basis.bits(c.idx[e]);
+    __syncthreads();
+    return c;
+}
+
+template <int W>
+__device__ __forceinline__ void gather(double *v, const double *__restrict__ src, const TileCtx &c)
+{
+    for (uint32_t e = threadIdx.x; e < c.n; e += blockDim.x) {
+        const size_t z = c.idx[e];
+#pragma unroll
+        for (int w = 0; w < W; ++w) v[e * W + w] = src[z * W + w];
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void scatter(const double *v, double *__restrict__ dst, const TileCtx &c)
+{
+    for (uint32_t e = threadIdx.x; e < c.n; e += blockDim.x) {
+        const size_t z = c.idx[e];
+#pragma unroll
+        for (int w = 0; w < W; ++w) dst[z * W + w] = v[e * W + w];
+    }
+}
+
+// One butterfly layer: x' = C x + s S y, y' = C y - s S x (fusedevolve.cpp:461-468).
+template <int W>
+__device__ __forceinline__ void layer(double *v, const uint32_t *bits, const TileCtx &c, int i, const ExcCode &code,
+                                      double Ci, double Si)
+{
+    const uint32_t half = c.n >> 1;
+    for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
+        const uint32_t lo = insert_zero_bit(p, i), hi = lo | (1u << i);
+        const double sS = exc_sign(code, bits[lo]) * Si;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const double x = v[lo * W + w], y = v[hi * W + w];
+            v[lo * W + w] = fma(sS, y, Ci * x);
+            v[hi * W + w] = fma(-sS, x, Ci * y);
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kRotThreads) k_block_rot(BlockArgs a, double *vecs, size_t vstride, int nvec)
+{
+    extern __shared__ double sm[];
+    double *v = sm;
+    uint32_t *bits = (uint32_t *)(sm + kTileElems * W);
+    __shared__ ExcCode code[kMaxSlots];
+    __shared__ double C[kMaxSlots], S[kMaxSlots];
+    __shared__ int slot[kMaxSlots];
+    const TileCtx c = load_tile(a, bits, code, C, S, slot);
+    for (int vec = 0; vec < nvec; ++vec) {
+        double *psi = vecs + vec * vstride;
+        gather<W>(v, psi, c);
+        __syncthreads();
+        for (int i = 0; i < c.k; ++i) {
+            layer<W>(v, bits, c, i, code[i], C[i], S[i]);
+            __syncthreads();
+        }
+        scatter<W>(v, psi, c);
+        __syncthreads();
+    }
+}
+
+// Adjoint sweep of one block: rotates psi and h = H psi by -theta and accumulates
+// g_slot += s (h_x y - h_y x) with the values before each layer (fusedevolve.cpp:470-483).
+template <int W>
+__global__ void __launch_bounds__(kRotThreads) k_block_bwd(BlockArgs a, double *psi, double *h, double *partials)
+{
+    extern __shared__ double sm[];
+    double *v = sm, *hv = sm + kTileElems * W;
+    uint32_t *bits = (uint32_t *)(sm + 2 * kTileElems * W);
+    __shared__ ExcCode code[kMaxSlots];
+    __shared__ double C[kMaxSlots], S[kMaxSlots];
+    __shared__ int slot[kMaxSlots];
+    __shared__ double red[kRotThreads / 32];
+    __shared__ double acc[kMaxSlots];
+    if (threadIdx.x < kMaxSlots) acc[threadIdx.x] = 0;
+    const TileCtx c = load_tile(a, bits, code, C, S, slot);
+    gather<W>(v, psi, c);
+    gather<W>(hv, h, c);
+    __syncthreads();
+    for (int i = 0; i < c.k; ++i) {
+        const uint32_t half = c.n >> 1;
+        const double Ci = C[i], Si = S[i];
+        double g = 0;
+        for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
+            const uint32_t lo = insert_zero_bit(p, i), hi = lo | (1u << i);
+            const double s = exc_sign(code[i], bits[lo]);
+            const double sS = s * Si;
+            double t = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                const double x = v[lo * W + w], y = v[hi * W + w];
+                const double hx = hv[lo * W + w], hy = hv[hi * W + w];
+                t = fma(hx, y, t);
+                t = fma(-hy, x, t);
+                v[lo * W + w] = fma(sS, y, Ci * x);
+                v[hi * W + w] = fma(-sS, x, Ci * y);
+                hv[lo * W + w] = fma(sS, hy, Ci * hx);
+                hv[hi * W + w] = fma(-sS, hx, Ci * hy);
+            }
+            g = fma(s, t, g);
+        }
+        g = block_sum(g, red);
+        if (threadIdx.x == 0) acc[slot[i]] = g;
+        __syncthreads();
+    }
+    scatter<W>(v, psi, c);
+    scatter<W>(hv, h, c);
+    if (threadIdx.x < kMaxSlots) partials[(size_t)blockIdx.x * kMaxSlots + threadIdx.x] = acc[threadIdx.x];
+}
+
+// Forward block that also writes the tangents T_slot = G_slot psi (after the block,
+// which equals G psi before it because the block's excitations commute).
+template <int W>
+__global__ void __launch_bounds__(kRotThreads) k_block_tangent(BlockArgs a, double *psi, double *T, size_t tstride,
+                                                               const int *tpos)
+{
+    extern __shared__ double sm[];
+    double *v = sm;
+    uint32_t *bits = (uint32_t *)(sm + kTileElems * W);
+    __shared__ ExcCode code[kMaxSlots];
+    __shared__ double C[kMaxSlots], S[kMaxSlots];
+    __shared__ int slot[kMaxSlots];
+    const TileCtx c = load_tile(a, bits, code, C, S, slot);
+    gather<W>(v, psi, c);
+    __syncthreads();
+    for (int i = 0; i < c.k; ++i) {
+        layer<W>(v, bits, c, i, code[i], C[i], S[i]);
+        __syncthreads();
+    }
+    scatter<W>(v, psi, c);
+    for (int i = 0; i < c.k; ++i) {
+        double *Ti = T + (size_t)tpos[a.ops[slot[i]]] * tstride;
+        for (uint32_t e = threadIdx.x; e < c.n; e += blockDim.x) {
+            const uint32_t pe = e ^ (1u << i);
+            const double s = exc_sign(code[i], bits[e]);
+            const size_t z = c.idx[e];
+#pragma unroll
+            for (int w = 0; w < W; ++w) Ti[z * W + w] = s * v[pe * W + w];
+        }
+    }
+}
+
+// Second-derivative sweeps: for every live tangent T_v (vectors [0, nvec) of T),
+// rotate (T_v, h) backward through the block and accumulate <h|G_j T_v> for the
+// block's excitations j whose application position is >= v.  h is read (not
+// written); each vector works on its own copy.  partials[(tile*nvec+v)*12+slot].
+template <int W>
+__global__ void __launch_bounds__(kRotThreads) k_block_hess(BlockArgs a, const double *h, double *T, size_t tstride,
+                                                            int nvec, int vchunk, int block_pos0, double *partials)
+{
+    extern __shared__ double sm[];
+    double *h0 = sm, *hv = sm + kTileElems * W, *v = sm + 2 * kTileElems * W;
+    uint32_t *bits = (uint32_t *)(sm + 3 * kTileElems * W);
+    __shared__ ExcCode code[kMaxSlots];
+    __shared__ double C[kMaxSlots], S[kMaxSlots];
+    __shared__ int slot[kMaxSlots];
+    __shared__ double red[kRotThreads / 32];
+    __shared__ double acc[kMaxSlots];
+    const TileCtx c = load_tile(a, bits, code, C, S, slot);
+    gather<W>(h0, h, c);
+    const int v0 = blockIdx.y * vchunk, v1 = min(nvec, v0 + vchunk);
+    for (int vec = v0; vec < v1; ++vec) {
+        double *t = T + (size_t)vec * tstride;
+        if (threadIdx.x < kMaxSlots) acc[threadIdx.x] = 0;
+        gather<W>(v, t, c);
+        for (uint32_t e = threadIdx.x; e < c.n * W; e += blockDim.x) hv[e] = h0[e];
+        __syncthreads();
+        for (int i = 0; i < c.k; ++i) {
+            const uint32_t half = c.n >> 1;
+            const double Ci = C[i], Si = S[i];
+            const bool want = block_pos0 + slot[i] >= vec;
+            double g = 0;
+            for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
+                const uint32_t lo = insert_zero_bit(p, i), hi = lo | (1u << i);
+                const double s = exc_sign(code[i], bits[lo]);
+                const double sS = s * Si;
+                double tt = 0;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    const double x = v[lo * W + w], y = v[hi * W + w];
+                    const double hx = hv[lo * W + w], hy = hv[hi * W + w];
+                    tt = fma(hx, y, tt);
+                    tt = fma(-hy, x, tt);
+                    v[lo * W + w] = fma(sS, y, Ci * x);
+                    v[hi * W + w] = fma(-sS, x, Ci * y);
+                    hv[lo * W + w] = fma(sS, hy, Ci * hx);
+                    hv[hi * W + w] = fma(-sS, hx, Ci * hy);
+                }
+                g = fma(s, tt, g);
+            }
+            if (want) {
+                g = block_sum(g, red);
+                if (threadIdx.x == 0) acc[slot[i]] = g;
+            }
+            __syncthreads();
+        }
+        scatter<W>(v, t, c);
+        if (threadIdx.x < kMaxSlots)
+            partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + threadIdx.x] = acc[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------- diagonal blocks --
+// Complex mode only: number / density-density operators multiply every active
+// amplitude by exp(+i * sum of the active angles) (RunFuseNDiagonal,
+// fusedevolve.cpp:625-717).  table[m] = (cos, sin) of dir * sum_{i in m} theta_i.
+__global__ void k_diag_table(const double *__restrict__ ang, const int *__restrict__ ops, int nslots, double dir,
+                             double *__restrict__ table)
+{
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= (1u << nslots)) return;
+    double th = 0;
+    for (int i = 0; i < nslots; ++i)
+        if (m & (1u << i)) th += ang[ops[i]];
+    double s, c;
+    sincos(dir * th, &s, &c);
+    table[2 * m] = c;
+    table[2 * m + 1] = s;
+}
+
+struct DiagArgs {
+    const int *ops;
+    int nslots;
+    const ExcCode *codes;
+    const double *table;
+    DevBasis basis;
+};
+
+__device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
+{
+    uint32_t m = 0;
+    for (int i = 0; i < a.nslots; ++i) {
+        const uint32_t ann = a.codes[a.ops[i]].annihilate;
+        if ((bits & ann) == ann) m |= 1u << i;
+    }
+    return m;
+}
+
+__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec)
+{
+    const uint64_t D = a.basis.D;
+    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        if (!m) continue;
+        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+        for (int vec = 0; vec < nvec; ++vec) {
+            double *p = vecs + vec * vstride + 2 * z;
+            const double re = p[0], im = p[1];
+            p[0] = c * re - s * im;
+            p[1] = s * re + c * im;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_diag_bwd(DiagArgs a, double *psi, double *h, double *partials)
+{
+    __shared__ double red[8];
+    double acc[kMaxSlots];
+#pragma unroll
+    for (int i = 0; i < kMaxSlots; ++i) acc[i] = 0;
+    const uint64_t D = a.basis.D;
+    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        if (!m) continue;
+        double *x = psi + 2 * z, *y = h + 2 * z;
+        const double xr = x[0], xi = x[1], hr = y[0], hi = y[1];
+        const double q = hi * xr - hr * xi;
+#pragma unroll
+        for (int i = 0; i < kMaxSlots; ++i)
+            if (m & (1u << i)) acc[i] += q;
+        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+        x[0] = c * xr - s * xi;
+        x[1] = s * xr + c * xi;
+        y[0] = c * hr - s * hi;
+        y[1] = s * hr + c * hi;
+    }
+    for (int i = 0; i < kMaxSlots; ++i) {
+        const double g = block_sum(acc[i], red);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kMaxSlots + i] = g;
+    }
+}
+
+__global__ void k_diag_tangent(DiagArgs a, double *psi, double *T, size_t tstride, const int *tpos)
+{
+    const uint64_t D = a.basis.D;
+    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        if (!m) continue;
+        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+        double *p = psi + 2 * z;
+        const double re = c * p[0] - s * p[1], im = s * p[0] + c * p[1];
+        p[0] = re;
+        p[1] = im;
+        for (int i = 0; i < a.nslots; ++i)
+            if (m & (1u << i)) {
+                double *t = T + (size_t)tpos[a.ops[i]] * tstride + 2 * z;
+                t[0] = -im;
+                t[1] = re;
+            }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, double *T, size_t tstride, int nvec,
+                                                   int block_pos0, double *partials)
+{
+    __shared__ double red[8];
+    const int vec = blockIdx.y;
+    double acc[kMaxSlots];
+#pragma unroll
+    for (int i = 0; i < kMaxSlots; ++i) acc[i] = 0;
+    const uint64_t D = a.basis.D;
+    double *t = T + (size_t)vec * tstride;
+    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        if (!m) continue;
+        double *x = t + 2 * z;
+        const double xr = x[0], xi = x[1], hr = h[2 * z], hi = h[2 * z + 1];
+        const double q = hi * xr - hr * xi;
+#pragma unroll
+        for (int i = 0; i < kMaxSlots; ++i)
+            if ((m & (1u << i)) && block_pos0 + i >= vec) acc[i] += q;
+        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+        x[0] = c * xr - s * xi;
+        x[1] = s * xr + c * xi;
+    }
+    for (int i = 0; i < kMaxSlots; ++i) {
+        const double g = block_sum(acc[i], red);
+        if (threadIdx.x == 0) partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + i] = g;
+    }
+}
+
+// ------------------------------------------------------------ reductions --
+// grad[op] = scale * sum over the tiles of op's block of partials[tile][slot].
+__global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t *__restrict__ op_part_off,
+                              const int *__restrict__ op_ntiles, const int *__restrict__ op_slot, int nops, double scale,
+                              double *__restrict__ grad)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nops) return;
+    const double *p = partials + op_part_off[warp];
+    const int nt = op_ntiles[warp], sl = op_slot[warp];
+    double s = 0;
+    for (int t = lane; t < nt; t += 32) s += p[(size_t)t * kMaxSlots + sl];
+    s = warp_sum(s);
+    if (lane == 0) grad[warp] = scale * s;
+}
+
+// Hessian second-derivative partials of one block -> Hops (nops x nops, row-major).
+__global__ void k_hess_reduce(const double *__restrict__ partials, int ntiles, int nvec, int nslots,
+                              const int *__restrict__ pos_op, const int *__restrict__ block_ops, int block_pos0,
+                              double *__restrict__ Hops, int nops)
+{
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= nvec * nslots) return;
+    const int vec = warp / nslots, sl = warp % nslots;
+    if (block_pos0 + sl < vec) return;
+    double s = 0;
+    for (int t = lane; t < ntiles; t += 32) s += partials[((size_t)t * nvec + vec) * kMaxSlots + sl];
+    s = warp_sum(s);
+    if (lane == 0) {
+        const int i = pos_op[vec], j = block_ops[sl];
+        Hops[(size_t)i * nops + j] += 2.0 * s;
+        if (i != j) Hops[(size_t)j * nops + i] += 2.0 * s;
+    }
+}
+
+// -------------------------------------------------------------- H * psi --
+// Warp per row, y_j = sum_k val[k] x[col[k]], fused with partial sums of <x|y>.
+template <int W, bool ELL>
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv(const int64_t *__restrict__ rowptr, int ell_width,
+                                                       const int32_t *__restrict__ col, const double *__restrict__ val,
+                                                       const double *__restrict__ x, double *__restrict__ y, int64_t D,
+                                                       double *__restrict__ epart)
+{
+    __shared__ double red[kSpmvThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    double e = 0;
+    for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < D; r += warps) {
+        const int64_t b = ELL ? r * ell_width : rowptr[r], end = ELL ? b + ell_width : rowptr[r + 1];
+        double acc[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = 0;
+        for (int64_t k = b + lane; k < end; k += 32) {
+            const double h = __ldg(val + k);
+            const size_t c = (size_t)__ldg(col + k);
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] = fma(h, __ldg(x + c * W + w), acc[w]);
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = warp_sum(acc[w]);
+        if (lane == 0) {
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                y[r * W + w] = acc[w];
+                e = fma(acc[w], x[r * W + w], e);
+            }
+        }
+    }
+    e = block_sum(e, red);
+    if (threadIdx.x == 0 && epart) epart[blockIdx.x] = e;
+}
+
+// H applied to V interleaved vectors X[D][W][V] -> Y[D][W][V] (one CTA per row).
+template <bool ELL>
+__global__ void k_spmm(const int64_t *__restrict__ rowptr, int ell_width, const int32_t *__restrict__ col,
+                       const double *__restrict__ val, const double *__restrict__ X, double *__restrict__ Y, int VW,
+                       int64_t D)
+{
+    for (int64_t r = blockIdx.x; r < D; r += gridDim.x) {
+        const int64_t b = ELL ? r * ell_width : rowptr[r], end = ELL ? b + ell_width : rowptr[r + 1];
+        for (int t = threadIdx.x; t < VW; t += blockDim.x) {
+            double acc = 0;
+            for (int64_t k = b; k < end; ++k) acc = fma(__ldg(val + k), __ldg(X + (size_t)__ldg(col + k) * VW + t), acc);
+            Y[(size_t)r * VW + t] = acc;
+        }
+    }
+}
+
+// Compressed tangents T_C[j][w][mu] = sum_{op: param(op)=mu} scale_op T[pos(op)][j][w];
+// column P holds psi (fusedevolve.cpp:2609-2612, m_compressMatrixPsi).
+__global__ void k_tc_build(const double *__restrict__ T, size_t tstride, const double *__restrict__ psi,
+                           const int *__restrict__ prm_ptr, const int *__restrict__ prm_pos,
+                           const double *__restrict__ prm_scale, int P, int W, int64_t D, double *__restrict__ TC)
+{
+    const int V = P + 1;
+    const int64_t total = D * W * V;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int mu = (int)(t % V);
+        const int64_t jw = t / V;
+        double s;
+        if (mu == P) {
+            s = psi[jw];
+        } else {
+            s = 0;
+            for (int k = prm_ptr[mu]; k < prm_ptr[mu + 1]; ++k) s += prm_scale[k] * T[(size_t)prm_pos[k] * tstride + jw];
+        }
+        TC[t] = s;
+    }
+}
+
+// --------------------------------------------- Hamiltonian from integrals --
+struct IntArgs {
+    int N, nq;
+    const double *h1, *g2;
+    DevBasis basis;
+    int nOa, nVa, nOb, nVb;
+    int64_t width;
+};
+
+__device__ __forceinline__ double two_e(const IntArgs &a, int p, int q, int r, int s)
+{
+    // op a^+_p a^+_q a_r a_s, p<q, r<s (hamiltonianmatrix.cpp:456-470, 479-505)
+    const int N = a.N;
+    const int sp = p >= N, sq = q >= N, sr = r >= N, ss = s >= N;
+    const int P = p - sp * N, Q = q - sq * N, R = r - sr * N, S = s - ss * N;
+    double E = 0;
+    if (sp == sr && sq == ss) E += a.g2[(((size_t)Q * N + S) * N + P) * N + R];
+    if (sp == ss && sq == sr) E -= a.g2[(((size_t)Q * N + R) * N + P) * N + S];
+    return fabs(E) > 1e-13 ? E : 0.0;
+}
+
+__device__ __forceinline__ uint32_t below(int x) { return (1u << x) - 1u; }
+
+__device__ __forceinline__ double op_sign(uint32_t J, uint32_t mask) { return (__popc(J & mask) & 1) ? -1.0 : 1.0; }
+
+__device__ __forceinline__ double double_val(const IntArgs &a, uint32_t J, int p, int q, int r, int s)
+{
+    // created p<q (in J), destroyed r<s
+    uint32_t m = below(p) ^ below(q) ^ below(r) ^ below(s);
+    m &= ~((1u << p) | (1u << q) | (1u << r) | (1u << s));
+    return op_sign(J, m) * two_e(a, p, q, r, s);
+}
+
+// Single p <- r (J holds p, the input determinant holds r): one-electron op plus the
+// two-electron ops a^+_p a^+_t a_r a_t over the other occupied orbitals t of J.
+__device__ double single_val(const IntArgs &a, uint32_t J, int p, int r)
+{
+    const int N = a.N;
+    uint32_t m = (below(p) ^ below(r)) & ~((1u << p) | (1u << r));
+    double h = a.h1[(p % N) * N + (r % N)];
+    double v = 0;
+    uint32_t occ = J & ~(1u << p);
+    while (occ) {
+        const int t = __ffs(occ) - 1;
+        occ &= occ - 1;
+        const int c0 = min(p, t), c1 = max(p, t), d0 = min(r, t), d1 = max(r, t);
+        v += double_val(a, J, c0, c1, d0, d1);
+    }
+    return v + (fabs(h) > 1e-13 ? op_sign(J, m) * h : 0.0);
+}
+
+__device__ double diag_val(const IntArgs &a, uint32_t J)
+{
+    const int N = a.N;
+    double v = 0;
+    uint32_t o1 = J;
+    while (o1) {
+        const int p = __ffs(o1) - 1;
+        o1 &= o1 - 1;
+        uint32_t o2 = o1;
+        while (o2) {
+            const int q = __ffs(o2) - 1;
+            o2 &= o2 - 1;
+            v += two_e(a, p, q, p, q);
+        }
+    }
+    uint32_t o = J;
+    while (o) {
+        const int p = __ffs(o) - 1;
+        o &= o - 1;
+        const double h = a.h1[(p % N) * N + (p % N)];
+        if (fabs(h) > 1e-13) v += h;
+    }
+    return v;
+}
+
+// k-th set bit of x (0-based)
+__device__ __forceinline__ int nth_bit(uint32_t x, int k)
+{
+    for (int i = 0; i < k; ++i) x &= x - 1;
+    return __ffs(x) - 1;
+}
+
+// pair index -> (i < j) in lexicographic order over n items
+__device__ __forceinline__ void pair_of(int k, int n, int &i, int &j)
+{
+    i = 0;
+    while (k >= n - 1 - i) {
+        k -= n - 1 - i;
+        ++i;
+    }
+    j = i + 1 + k;
+}
+
+// Entry e of row J: returns the input determinant and the matrix element.
+// Order: diagonal; alpha singles; beta singles; aa doubles; bb doubles; ab doubles.
+__device__ void row_entry(const IntArgs &a, uint32_t J, int64_t e, uint32_t &I, double &v)
+{
+    const int N = a.N;
+    const uint32_t full = below(N);
+    const uint32_t Ja = J >> N, Jb = J & full;
+    const uint32_t Va = ~Ja & full, Vb = ~Jb & full;
+    const int64_t Sa = (int64_t)a.nOa * a.nVa, Sb = (int64_t)a.nOb * a.nVb;
+    const int64_t Daa = (int64_t)(a.nOa * (a.nOa - 1) / 2) * (a.nVa * (a.nVa - 1) / 2);
+    const int64_t Dbb = (int64_t)(a.nOb * (a.nOb - 1) / 2) * (a.nVb * (a.nVb - 1) / 2);
+    if (e == 0) {
+        I = J;
+        v = diag_val(a, J);
+        return;
+    }
+    e -= 1;
+    if (e < Sa) {
+        const int p = nth_bit(Ja, (int)(e / a.nVa)) + N, r = nth_bit(Va, (int)(e % a.nVa)) + N;
+        I = J ^ (1u << p) ^ (1u << r);
+        v = single_val(a, J, p, r);
+        return;
+    }
+    e -= Sa;
+    if (e < Sb) {
+        const int p = nth_bit(Jb, (int)(e / a.nVb)), r = nth_bit(Vb, (int)(e % a.nVb));
+        I = J ^ (1u << p) ^ (1u << r);
+        v = single_val(a, J, p, r);
+        return;
+    }
+    e -= Sb;
+    if (e < Daa + Dbb) {
+        const bool alpha = e < Daa;
+        if (!alpha) e -= Daa;
+        const uint32_t O = alpha ? Ja : Jb, Vv = alpha ? Va : Vb;
+        const int nO = alpha ? a.nOa : a.nOb, nV = alpha ? a.nVa : a.nVb, off = alpha ? N : 0;
+        const int nvp = nV * (nV - 1) / 2;
+        int i0, i1, j0, j1;
+        pair_of((int)(e / nvp), nO, i0, i1);
+        pair_of((int)(e % nvp), nV, j0, j1);
+        const int p = nth_bit(O, i0) + off, q = nth_bit(O, i1) + off;
+        const int r = nth_bit(Vv, j0) + off, s = nth_bit(Vv, j1) + off;
+        I = J ^ (1u << p) ^ (1u << q) ^ (1u << r) ^ (1u << s);
+        v = double_val(a, J, p, q, r, s);
+        return;
+    }
+    e -= Daa + Dbb;
+    {
+        const int64_t ea = e / Sb, eb = e % Sb;
+        const int pa = nth_bit(Ja, (int)(ea / a.nVa)) + N, ra = nth_bit(Va, (int)(ea % a.nVa)) + N;
+        const int pb = nth_bit(Jb, (int)(eb / a.nVb)), rb = nth_bit(Vb, (int)(eb % a.nVb));
+        I = J ^ (1u << pa) ^ (1u << ra) ^ (1u << pb) ^ (1u << rb);
+        v = double_val(a, J, pb, pa, rb, ra);
+    }
+}
+
+__global__ void k_ell_build(IntArgs a, int32_t *__restrict__ col, double *__restrict__ val, int64_t r0, int64_t r1)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = r0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < r1; r += warps) {
+        const uint32_t J = a.basis.bits((uint32_t)r);
+        for (int64_t e = lane; e < a.width; e += 32) {
+            uint32_t I;
+            double v;
+            row_entry(a, J, e, I, v);
+            col[r * a.width + e] = (int32_t)a.basis.rank_of(I);
+            val[r * a.width + e] = v;
+        }
+    }
+}
+
+// y = H x with rows regenerated on the fly (no stored matrix), fused with <x|y>.
+template <int W>
+__global__ void __launch_bounds__(kSpmvThreads) k_otf_apply(IntArgs a, const double *__restrict__ x,
+                                                            double *__restrict__ y, double *__restrict__ epart)
+{
+    __shared__ double red[kSpmvThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t D = a.basis.D;
+    double en = 0;
+    for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < D; r += warps) {
+        const uint32_t J = a.basis.bits((uint32_t)r);
+        double acc[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = 0;
+        for (int64_t e = lane; e < a.width; e += 32) {
+            uint32_t I;
+            double v;
+            row_entry(a, J, e, I, v);
+            const size_t c = (size_t)a.basis.rank_of(I);
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] = fma(v, __ldg(x + c * W + w), acc[w]);
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) acc[w] = warp_sum(acc[w]);
+        if (lane == 0) {
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                y[r * W + w] = acc[w];
+                en = fma(acc[w], x[r * W + w], en);
+            }
+        }
+    }
+    en = block_sum(en, red);
+    if (threadIdx.x == 0 && epart) epart[blockIdx.x] = en;
+}
+
+// ------------------------------------------------------------------ host --
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { reset(); }
+    void reset()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+}  // namespace
+
+struct aegpu_engine {
+    std::string err;
+    int64_t dev_bytes = 0;
+    int64_t launches = 0;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t cublas = nullptr;
+    int sm_count = 152;
+
+    Basis B;
+    bool cplx = false;
+    int W = 1;
+    std::vector<Exc> excs;
+    std::vector<ExcCode> codes;
+    std::vector<Block> blocks;
+    std::vector<int> perm;        // application order of the operators
+    std::vector<int> pos_of_op;   // inverse of perm
+    std::vector<int> block_pos0;  // first application position of every block
+    std::vector<int> op_block, op_slot;
+
+    struct DevBlock {
+        bool diagonal = false;
+        int nslots = 0;
+        int ntiles = 0;
+        int64_t part_off = 0;     // offset of this block's gradient partials
+        uint32_t *idx = nullptr;
+        OrbitGroup *groups = nullptr;
+        OrbitTile *tiles = nullptr;
+        int *ops = nullptr;
+        uint64_t active = 0;
+    };
+    std::vector<DevBlock> dblocks;
+    std::vector<void *> allocs;
+
+    // device basis
+    DevBasis db{};
+    // device arrays
+    ExcCode *d_codes = nullptr;
+    int *d_tpos = nullptr;          // op -> tangent slot (application position)
+    int *d_pos_op = nullptr;        // application position -> op
+    int64_t *d_op_part_off = nullptr;
+    int *d_op_ntiles = nullptr, *d_op_slot = nullptr;
+    double *d_ang = nullptr, *d_sc = nullptr, *d_diag_table = nullptr;
+    double *d_start = nullptr, *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
+    double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
+    int64_t n_partials = 0;
+    int spmv_grid = 0;
+
+    // Hamiltonian
+    int ham_kind = 0;  // 1 CSR, 2 ELL, 3 on the fly
+    int64_t ham_entries = 0;
+    int64_t *d_rowptr = nullptr;
+    int32_t *d_col = nullptr;
+    double *d_val = nullptr;
+    IntArgs ints{};
+    double *d_h1 = nullptr, *d_g2 = nullptr;
+    int ell_width = 0;
+
+    // optional CUDA-event timing of the phases of *_dev evaluations
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::array<cudaEvent_t, 4>> ev_marks;
+    double phase_ms[3] = {0, 0, 0};
+    int64_t phase_n = 0;
+    cudaEvent_t next_event()
+    {
+        cudaEvent_t ev;
+        if (!ev_pool.empty()) {
+            ev = ev_pool.back();
+            ev_pool.pop_back();
+        } else {
+            cudaEventCreate(&ev);
+        }
+        return ev;
+    }
+
+    // state caching: psi / hpsi valid for these angles
+    std::vector<double> cached_angles;
+    bool psi_valid = false, h_valid = false;
+
+    ~aegpu_engine()
+    {
+        for (void *p : allocs) cudaFree(p);
+        for (auto &m : ev_marks)
+            for (auto ev : m) cudaEventDestroy(ev);
+        for (auto ev : ev_pool) cudaEventDestroy(ev);
+        if (cublas) cublasDestroy(cublas);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <typename T>
+    T *alloc(size_t n)
+    {
+        void *p = nullptr;
+        if (n == 0) n = 1;
+        cudaError_t rc = cudaMalloc(&p, n * sizeof(T));
+        if (rc != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        allocs.push_back(p);
+        dev_bytes += (int64_t)(n * sizeof(T));
+        return (T *)p;
+    }
+    void release(void *p, size_t bytes)
+    {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p);
+        dev_bytes -= (int64_t)bytes;
+    }
+    int fail(int code, const std::string &m)
+    {
+        err = m;
+        return code;
+    }
+    int cuda_check(const char *where)
+    {
+        cudaError_t rc = cudaGetLastError();
+        if (rc != cudaSuccess) return fail(AEGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(rc));
+        return AEGPU_OK;
+    }
+    template <typename T>
+    T *upload(const std::vector<T> &v)
+    {
+        T *p = alloc<T>(v.size());
+        if (p && !v.empty()) cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return p;
+    }
+
+    BlockArgs block_args(const DevBlock &b, double dir) const
+    {
+        BlockArgs a;
+        a.idx = b.idx;
+        a.groups = b.groups;
+        a.tiles = b.tiles;
+        a.ops = b.ops;
+        a.nslots = b.nslots;
+        a.codes = d_codes;
+        a.sc = d_sc;
+        a.dir = dir;
+        a.basis = db;
+        return a;
+    }
+    DiagArgs diag_args(const DevBlock &b) const
+    {
+        DiagArgs a;
+        a.ops = b.ops;
+        a.nslots = b.nslots;
+        a.codes = d_codes;
+        a.table = d_diag_table;
+        a.basis = db;
+        return a;
+    }
+    size_t rot_smem(int nvec_tiles) const { return (size_t)kTileElems * (nvec_tiles * W * 8 + 4); }
+};
+
+namespace {
+
+int set_smem_limits()
+{
+    const int maxsm = 227 * 1024;
+    cudaFuncSetAttribute(k_block_rot<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_rot<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_bwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_bwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_tangent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_tangent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_hess<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncSetAttribute(k_block_hess<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    return 0;
+}
+
+// Forward evolution of psi from the start vector (angles already in d_sc / d_ang).
+int run_evolve(aegpu_engine *e)
+{
+    const size_t n = (size_t)e->B.D * e->W;
+    cudaMemcpyAsync(e->d_psi, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
+    for (auto &b : e->dblocks) {
+        if (b.diagonal) {
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, 1.0,
+                                                                              e->d_diag_table);
+            k_diag_rot<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1);
+            e->launches += 2;
+        } else if (b.ntiles) {
+            BlockArgs a = e->block_args(b, 1.0);
+            if (e->W == 1)
+                k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), e->stream>>>(a, e->d_psi, 0, 1);
+            else
+                k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), e->stream>>>(a, e->d_psi, 0, 1);
+            e->launches += 1;
+        }
+    }
+    return e->cuda_check("evolve");
+}
+
+int upload_angles(aegpu_engine *e, const double *angles, bool host)
+{
+    const int n = (int)e->excs.size();
+    cudaMemcpyAsync(e->d_ang, angles, n * sizeof(double), host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                    e->stream);
+    k_sincos<<<(n + 127) / 128, 128, 0, e->stream>>>(e->d_ang, e->d_sc, n);
+    e->launches += 1;
+    return e->cuda_check("angles");
+}
+
+// y = H x on device vectors, with E partials into d_epart (nullable).
+int run_apply(aegpu_engine *e, const double *x, double *y, double *epart)
+{
+    const int64_t D = (int64_t)e->B.D;
+    const int grid = e->spmv_grid;
+    if (e->ham_kind == 1) {
+        if (e->W == 1)
+            k_spmv<1, false><<<grid, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+        else
+            k_spmv<2, false><<<grid, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+    } else if (e->ham_kind == 2) {
+        if (e->W == 1)
+            k_spmv<1, true><<<grid, kSpmvThreads, 0, e->stream>>>(nullptr, e->ell_width, e->d_col, e->d_val, x, y, D, epart);
+        else
+            k_spmv<2, true><<<grid, kSpmvThreads, 0, e->stream>>>(nullptr, e->ell_width, e->d_col, e->d_val, x, y, D, epart);
+    } else if (e->ham_kind == 3) {
+        if (e->W == 1)
+            k_otf_apply<1><<<grid, kSpmvThreads, 0, e->stream>>>(e->ints, x, y, epart);
+        else
+            k_otf_apply<2><<<grid, kSpmvThreads, 0, e->stream>>>(e->ints, x, y, epart);
+    } else {
+        return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    }
+    e->launches += 1;
+    return e->cuda_check("apply H");
+}
+
+int run_energy(aegpu_engine *e, double *E_dev)
+{
+    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart);
+    if (rc) return rc;
+    k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, e->spmv_grid, E_dev, 1.0);
+    e->launches += 1;
+    return e->cuda_check("energy");
+}
+
+// Adjoint sweep over all blocks (psi, h updated in place), per-op gradient in grad_dev.
+int run_backward(aegpu_engine *e, double *grad_dev)
+{
+    for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
+        auto &b = e->dblocks[bi];
+        double *part = e->d_partials + b.part_off;
+        if (b.diagonal) {
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, -1.0,
+                                                                              e->d_diag_table);
+            k_diag_bwd<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, e->d_h, part);
+            e->launches += 2;
+        } else if (b.ntiles) {
+            BlockArgs a = e->block_args(b, -1.0);
+            if (e->W == 1)
+                k_block_bwd<1><<<b.ntiles, kRotThreads, e->rot_smem(2), e->stream>>>(a, e->d_psi, e->d_h, part);
+            else
+                k_block_bwd<2><<<b.ntiles, kRotThreads, e->rot_smem(2), e->stream>>>(a, e->d_psi, e->d_h, part);
+            e->launches += 1;
+        }
+    }
+    const int nops = (int)e->excs.size();
+    k_grad_reduce<<<(nops * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
+                                                                  e->d_op_slot, nops, 2.0, grad_dev);
+    e->launches += 1;
+    return e->cuda_check("backward");
+}
+
+bool same_angles(const aegpu_engine *e, const double *angles)
+{
+    return e->psi_valid && e->cached_angles.size() == e->excs.size() &&
+           std::equal(e->cached_angles.begin(), e->cached_angles.end(), angles);
+}
+
+int ensure_state(aegpu_engine *e, const double *angles)
+{
+    if (same_angles(e, angles)) return AEGPU_OK;
+    int rc = upload_angles(e, angles, true);
+    if (!rc) rc = run_evolve(e);
+    if (rc) return rc;
+    e->cached_angles.assign(angles, angles + e->excs.size());
+    e->psi_valid = true;
+    e->h_valid = false;
+    return AEGPU_OK;
+}
+
+int stream_sync(aegpu_engine *e, const char *where)
+{
+    cudaError_t rc = cudaStreamSynchronize(e->stream);
+    if (rc != cudaSuccess) return e->fail(AEGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(rc));
+    return e->cuda_check(where);
+}
+
+}  // namespace
+
+// ==================================================================== C ABI ==
+extern "C" {
+
+int aegpu_create(aegpu_engine **out)
+{
+    if (!out) return AEGPU_ERR_ARG;
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return AEGPU_ERR_CUDA;
+    }
+    auto *e = new aegpu_engine();
+    cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete e;
+        return AEGPU_ERR_CUDA;
+    }
+    set_smem_limits();
+    e->spmv_grid = e->sm_count * 8;
+    *out = e;
+    return AEGPU_OK;
+}
+
+void aegpu_destroy(aegpu_engine *e) { delete e; }
+
+const char *aegpu_last_error(const aegpu_engine *e) { return e ? e->err.c_str() : "null engine"; }
+
+int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int complex_mode,
+                      int nops, const int *ops)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (nops < 1 || !ops) return e->fail(AEGPU_ERR_ARG, "no excitations");
+    if (!e->B.init(nq, basis_kind, n_elec, n_alpha, n_beta, e->err)) return AEGPU_ERR_ARG;
+    e->cplx = complex_mode != 0;
+    e->W = e->cplx ? 2 : 1;
+    e->excs.resize(nops);
+    e->codes.resize(nops);
+    for (int i = 0; i < nops; ++i) {
+        for (int j = 0; j < 4; ++j) {
+            int v = ops[4 * i + j];
+            if (v < -1 || v >= nq) return e->fail(AEGPU_ERR_ARG, "excitation index out of range");
+            e->excs[i].v[j] = (int8_t)v;
+        }
+        const Exc &x = e->excs[i];
+        bool single = x.v[0] >= 0 && x.v[1] >= 0 && x.v[2] < 0 && x.v[3] < 0;
+        bool dbl = x.v[0] >= 0 && x.v[1] >= 0 && x.v[2] >= 0 && x.v[3] >= 0;
+        if (!single && !dbl) return e->fail(AEGPU_ERR_ARG, "excitation is neither a single nor a double");
+        if (exc_is_diagonal(x) != exc_has_diagonal(x))
+            return e->fail(AEGPU_ERR_UNSUPPORTED, "excitation with a repeated orbital that is not diagonal");
+        if (dbl && (x.v[0] == x.v[1] || x.v[2] == x.v[3]) && !exc_is_diagonal(x))
+            return e->fail(AEGPU_ERR_ARG, "double excitation creates or destroys one orbital twice");
+        if (exc_is_diagonal(x) && !e->cplx)
+            return e->fail(AEGPU_ERR_UNSUPPORTED, "diagonal (number) operators need complex mode");
+        e->codes[i] = make_exc_code(x.v[0], x.v[1], x.v[2], x.v[3]);
+    }
+    e->blocks = group_blocks(e->excs, kMaxSlots, e->perm);
+    e->pos_of_op.assign(nops, 0);
+    for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;
+
+    // device basis
+    DevBasis db{};
+    db.kind = e->B.kind;
+    db.N = e->B.N;
+    db.nq = nq;
+    db.nA = e->B.nA;
+    db.nB = e->B.nB;
+    db.D = e->B.D;
+    if (e->B.kind == BASIS_SZ) {
+        db.strA = e->upload(e->B.strA);
+        db.strB = e->upload(e->B.strB);
+        db.rankA = e->upload(e->B.rankA);
+        db.rankB = e->upload(e->B.rankB);
+    } else {
+        db.states = e->upload(e->B.states);
+        db.rank = e->upload(e->B.rank);
+    }
+    e->db = db;
+    e->d_codes = e->upload(e->codes);
+
+    // orbit tables per block
+    const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    e->dblocks.clear();
+    e->block_pos0.clear();
+    e->op_block.assign(nops, 0);
+    e->op_slot.assign(nops, 0);
+    int64_t part_off = 0;
+    int pos = 0;
+    for (size_t bi = 0; bi < e->blocks.size(); ++bi) {
+        const Block &b = e->blocks[bi];
+        aegpu_engine::DevBlock d;
+        d.diagonal = b.diagonal;
+        d.nslots = (int)b.ops.size();
+        d.ops = e->upload(b.ops);
+        e->block_pos0.push_back(pos);
+        for (int s = 0; s < d.nslots; ++s) {
+            e->op_block[b.ops[s]] = (int)bi;
+            e->op_slot[b.ops[s]] = s;
+        }
+        pos += d.nslots;
+        if (!b.diagonal) {
+            std::vector<ExcCode> bc;
+            for (int op : b.ops) bc.push_back(e->codes[op]);
+            OrbitTables T = build_orbits(e->B, bc, (int)hw);
+            if (!T.ok) return e->fail(AEGPU_ERR_UNSUPPORTED, "an excitation leaves the determinant sector");
+            d.idx = e->upload(T.idx);
+            d.groups = e->upload(T.groups);
+            d.tiles = e->upload(T.tiles);
+            d.ntiles = (int)T.tiles.size();
+            d.active = T.active;
+        } else {
+            d.ntiles = kDiagGrid;
+        }
+        d.part_off = part_off;
+        part_off += (int64_t)d.ntiles * kMaxSlots;
+        e->dblocks.push_back(d);
+    }
+    e->n_partials = part_off;
+    std::vector<int64_t> opo(nops);
+    std::vector<int> opn(nops), ops_slot(nops);
+    for (int o = 0; o < nops; ++o) {
+        const auto &d = e->dblocks[e->op_block[o]];
+        opo[o] = d.part_off;
+        opn[o] = d.ntiles;
+        ops_slot[o] = e->op_slot[o];
+    }
+    e->d_op_part_off = e->upload(opo);
+    e->d_op_ntiles = e->upload(opn);
+    e->d_op_slot = e->upload(ops_slot);
+    e->d_tpos = e->upload(e->pos_of_op);
+    e->d_pos_op = e->upload(e->perm);
+
+    const size_t n = (size_t)e->B.D * e->W;
+    e->d_ang = e->alloc<double>(nops);
+    e->d_sc = e->alloc<double>(2 * nops);
+    e->d_diag_table = e->alloc<double>(2 * (1 << kMaxSlots));
+    e->d_start = e->alloc<double>(n);
+    e->d_psi = e->alloc<double>(n);
+    e->d_h = e->alloc<double>(n);
+    e->d_tmp = e->alloc<double>(n);
+    e->d_partials = e->alloc<double>(std::max<int64_t>(part_off, 1));
+    e->d_epart = e->alloc<double>(e->spmv_grid);
+    e->d_scalar = e->alloc<double>(4);
+    e->d_grad = e->alloc<double>(nops);
+    if (!e->d_tmp || !e->d_partials || !e->d_grad) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
+    cudaMemset(e->d_start, 0, n * sizeof(double));
+    e->psi_valid = e->h_valid = false;
+    // setup copies ran on the legacy stream: finish them before any engine-stream work
+    if (cudaDeviceSynchronize() != cudaSuccess) return e->cuda_check("set_problem");
+    return e->cuda_check("set_problem");
+}
+
+int64_t aegpu_dim(const aegpu_engine *e) { return e ? (int64_t)e->B.D : -1; }
+
+int aegpu_basis_states(const aegpu_engine *e, uint32_t *out)
+{
+    if (!e || !out) return AEGPU_ERR_ARG;
+    for (uint64_t z = 0; z < e->B.D; ++z) out[z] = e->B.bits(z);
+    return AEGPU_OK;
+}
+
+int aegpu_num_blocks(const aegpu_engine *e) { return e ? (int)e->blocks.size() : -1; }
+
+int aegpu_block_layout(const aegpu_engine *e, int *perm, int *block_sizes)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (perm) std::copy(e->perm.begin(), e->perm.end(), perm);
+    if (block_sizes)
+        for (size_t b = 0; b < e->blocks.size(); ++b) block_sizes[b] = (int)e->blocks[b].ops.size() * (e->blocks[b].diagonal ? -1 : 1);
+    return AEGPU_OK;
+}
+
+int aegpu_set_initial(aegpu_engine *e, const double *amps)
+{
+    if (!e || !amps) return AEGPU_ERR_ARG;
+    if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    cudaMemcpy(e->d_start, amps, (size_t)e->B.D * e->W * sizeof(double), cudaMemcpyHostToDevice);
+    e->psi_valid = e->h_valid = false;
+    cudaDeviceSynchronize();
+    return e->cuda_check("set_initial");
+}
+
+int aegpu_set_ham_csr(aegpu_engine *e, int64_t nnz, const int64_t *rowptr, const int32_t *col, const double *val)
+{
+    if (!e || !rowptr || (nnz > 0 && (!col || !val))) return AEGPU_ERR_ARG;
+    if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    const int64_t D = (int64_t)e->B.D;
+    if (rowptr[0] != 0 || rowptr[D] != nnz) return e->fail(AEGPU_ERR_ARG, "inconsistent CSR row pointers");
+    for (int64_t k = 0; k < nnz; ++k)
+        if (col[k] < 0 || col[k] >= D) return e->fail(AEGPU_ERR_ARG, "CSR column out of range");
+    e->d_rowptr = e->alloc<int64_t>(D + 1);
+    e->d_col = e->alloc<int32_t>(nnz);
+    e->d_val = e->alloc<double>(nnz);
+    if (!e->d_rowptr || !e->d_col || !e->d_val) return e->fail(AEGPU_ERR_NOMEM, "CSR allocation failed");
+    cudaMemcpy(e->d_rowptr, rowptr, (D + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (nnz) {
+        cudaMemcpy(e->d_col, col, nnz * sizeof(int32_t), cudaMemcpyHostToDevice);
+        cudaMemcpy(e->d_val, val, nnz * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    e->ham_kind = 1;
+    e->ham_entries = nnz;
+    e->h_valid = false;
+    cudaDeviceSynchronize();
+    return e->cuda_check("set_ham_csr");
+}
+
+int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2, int mode)
+{
+    if (!e || !h1 || !g2) return AEGPU_ERR_ARG;
+    if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    if (e->B.kind != BASIS_SZ) return e->fail(AEGPU_ERR_UNSUPPORTED, "integral Hamiltonians need the Sz sector");
+    const int N = e->B.N;
+    IntArgs a{};
+    a.N = N;
+    a.nq = e->B.nq;
+    a.basis = e->db;
+    a.nOa = e->B.na;
+    a.nVa = N - e->B.na;
+    a.nOb = e->B.nb;
+    a.nVb = N - e->B.nb;
+    auto c2 = [](int64_t n) { return n * (n - 1) / 2; };
+    a.width = 1 + (int64_t)a.nOa * a.nVa + (int64_t)a.nOb * a.nVb + c2(a.nOa) * c2(a.nVa) + c2(a.nOb) * c2(a.nVb) +
+              (int64_t)a.nOa * a.nVa * a.nOb * a.nVb;
+    e->d_h1 = e->alloc<double>((size_t)N * N);
+    e->d_g2 = e->alloc<double>((size_t)N * N * N * N);
+    if (!e->d_h1 || !e->d_g2) return e->fail(AEGPU_ERR_NOMEM, "integral allocation failed");
+    cudaMemcpy(e->d_h1, h1, sizeof(double) * N * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_g2, g2, sizeof(double) * N * N * N * N, cudaMemcpyHostToDevice);
+    cudaDeviceSynchronize();
+    a.h1 = e->d_h1;
+    a.g2 = e->d_g2;
+    e->ints = a;
+    e->ell_width = (int)a.width;
+    const int64_t D = (int64_t)e->B.D;
+    const double ell_bytes = (double)D * a.width * 12.0;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    if (mode == AEGPU_HAM_AUTO) mode = ell_bytes < 0.6 * (double)free_b ? AEGPU_HAM_STORED : AEGPU_HAM_ON_THE_FLY;
+    if (mode == AEGPU_HAM_STORED) {
+        e->d_col = e->alloc<int32_t>((size_t)D * a.width);
+        e->d_val = e->alloc<double>((size_t)D * a.width);
+        if (!e->d_col || !e->d_val) return e->fail(AEGPU_ERR_NOMEM, "ELL allocation failed");
+        const int64_t chunk = 1 << 16;
+        for (int64_t r0 = 0; r0 < D; r0 += chunk) {
+            k_ell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, e->d_col, e->d_val, r0, std::min(D, r0 + chunk));
+            e->launches += 1;
+        }
+        e->ham_kind = 2;
+        e->ham_entries = D * a.width;
+    } else {
+        e->ham_kind = 3;
+        e->ham_entries = 0;
+    }
+    e->h_valid = false;
+    return stream_sync(e, "set_ham_integrals");
+}
+
+int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (kind) *kind = e->ham_kind;
+    if (stored) *stored = e->ham_entries;
+    return AEGPU_OK;
+}
+
+int aegpu_evolve(aegpu_engine *e, const double *angles, double *state)
+{
+    if (!e || !angles) return AEGPU_ERR_ARG;
+    if (!e->d_psi) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    int rc = ensure_state(e, angles);
+    if (rc) return rc;
+    if (state)
+        cudaMemcpyAsync(state, e->d_psi, (size_t)e->B.D * e->W * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    return stream_sync(e, "evolve");
+}
+
+int aegpu_energy(aegpu_engine *e, const double *angles, double *energy)
+{
+    if (!e || !angles || !energy) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    int rc = ensure_state(e, angles);
+    if (rc) return rc;
+    if (!e->h_valid) {
+        rc = run_energy(e, e->d_scalar);
+        if (rc) return rc;
+        e->h_valid = true;
+    }
+    cudaMemcpyAsync(energy, e->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    return stream_sync(e, "energy");
+}
+
+int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double *grad_ops)
+{
+    if (!e || !angles || !grad_ops) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    int rc = ensure_state(e, angles);
+    if (rc) return rc;
+    if (!e->h_valid) {
+        rc = run_energy(e, e->d_scalar);
+        if (rc) return rc;
+    }
+    // the sweep destroys psi / hpsi: keep the evolved state for later calls
+    const size_t n = (size_t)e->B.D * e->W;
+    cudaMemcpyAsync(e->d_tmp, e->d_psi, n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
+    rc = run_backward(e, e->d_grad);
+    if (rc) return rc;
+    std::swap(e->d_tmp, e->d_psi);
+    e->h_valid = false;
+    if (energy) cudaMemcpyAsync(energy, e->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    return stream_sync(e, "gradient");
+}
+
+int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream)
+{
+    if (!e || !angles_dev || !grad_dev) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    cudaStream_t saved = e->stream;
+    if (stream) e->stream = (cudaStream_t)stream;
+    std::array<cudaEvent_t, 4> ev{};
+    if (e->timing)
+        for (auto &x : ev) x = e->next_event();
+    if (e->timing) cudaEventRecord(ev[0], e->stream);
+    int rc = upload_angles(e, angles_dev, false);
+    if (!rc) rc = run_evolve(e);
+    if (e->timing) cudaEventRecord(ev[1], e->stream);
+    if (!rc) rc = run_energy(e, energy_dev ? energy_dev : e->d_scalar);
+    if (e->timing) cudaEventRecord(ev[2], e->stream);
+    if (!rc) rc = run_backward(e, grad_dev);
+    if (e->timing) {
+        cudaEventRecord(ev[3], e->stream);
+        e->ev_marks.push_back(ev);
+    }
+    e->stream = saved;
+    e->psi_valid = e->h_valid = false;
+    return rc;
+}
+
+int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, void *stream)
+{
+    if (!e || !angles_dev || !energy_dev) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    cudaStream_t saved = e->stream;
+    if (stream) e->stream = (cudaStream_t)stream;
+    int rc = upload_angles(e, angles_dev, false);
+    if (!rc) rc = run_evolve(e);
+    if (!rc) rc = run_energy(e, energy_dev);
+    e->stream = saved;
+    e->psi_valid = e->h_valid = false;
+    return rc;
+}
+
+int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (psi) *psi = e->d_psi;
+    if (hpsi) *hpsi = e->d_h;
+    return AEGPU_OK;
+}
+
+int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
+{
+    if (!e || !x || !y) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    const size_t n = (size_t)e->B.D * e->W;
+    double *dx = e->alloc<double>(n), *dy = e->alloc<double>(n);
+    if (!dx || !dy) return e->fail(AEGPU_ERR_NOMEM, "apply_h scratch");
+    cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+    int rc = run_apply(e, dx, dy, nullptr);
+    if (!rc) {
+        cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        rc = stream_sync(e, "apply_h");
+    }
+    e->release(dx, n * sizeof(double));
+    e->release(dy, n * sizeof(double));
+    return rc;
+}
+
+int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                  double *energy, double *grad_comp, double *hess_comp)
+{
+    if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    const int nops = (int)e->excs.size();
+    const int W = e->W;
+    const int64_t D = (int64_t)e->B.D;
+    const size_t n = (size_t)D * W;
+    for (int o = 0; o < nops; ++o)
+        if (param[o] < 0 || param[o] >= nparams) return e->fail(AEGPU_ERR_ARG, "parameter index out of range");
+    const int V = nparams + 1;
+    // scratch: tangents by application position, compressed tangents and H * them
+    double *T = e->alloc<double>(n * nops);
+    double *TC = e->alloc<double>(n * V);
+    double *HTC = e->alloc<double>(n * V);
+    double *THT = e->alloc<double>((size_t)V * V);
+    double *Hops = e->alloc<double>((size_t)nops * nops);
+    int64_t maxpart = 0;
+    for (auto &b : e->dblocks) maxpart = std::max<int64_t>(maxpart, (int64_t)b.ntiles * nops * kMaxSlots);
+    double *hpart = e->alloc<double>(maxpart);
+    // parameter -> (application position, scale) lists
+    std::vector<int> pptr(nparams + 1, 0), ppos, pcnt(nparams, 0);
+    std::vector<double> pscale;
+    for (int o = 0; o < nops; ++o) pcnt[param[o]]++;
+    for (int m = 0; m < nparams; ++m) pptr[m + 1] = pptr[m] + pcnt[m];
+    ppos.assign(nops, 0);
+    pscale.assign(nops, 0);
+    std::vector<int> fill(pptr.begin(), pptr.end() - 1);
+    for (int o = 0; o < nops; ++o) {
+        ppos[fill[param[o]]] = e->pos_of_op[o];
+        pscale[fill[param[o]]++] = scale[o];
+    }
+    int *d_pptr = e->upload(pptr), *d_ppos = e->upload(ppos);
+    double *d_pscale = e->upload(pscale);
+    cudaDeviceSynchronize();
+    auto cleanup = [&]() {
+        e->release(T, n * nops * 8);
+        e->release(TC, n * V * 8);
+        e->release(HTC, n * V * 8);
+        e->release(THT, (size_t)V * V * 8);
+        e->release(Hops, (size_t)nops * nops * 8);
+        e->release(hpart, maxpart * 8);
+        e->release(d_pptr, pptr.size() * 4);
+        e->release(d_ppos, ppos.size() * 4);
+        e->release(d_pscale, pscale.size() * 8);
+    };
+    if (!T || !TC || !HTC || !THT || !Hops || !hpart || !d_pptr || !d_ppos || !d_pscale) {
+        cleanup();
+        return e->fail(AEGPU_ERR_NOMEM, "Hessian scratch allocation failed");
+    }
+    int rc = upload_angles(e, angles, true);
+    if (rc) { cleanup(); return rc; }
+    cudaStream_t s = e->stream;
+    cudaMemsetAsync(T, 0, n * nops * sizeof(double), s);
+    cudaMemsetAsync(Hops, 0, (size_t)nops * nops * sizeof(double), s);
+    cudaMemcpyAsync(e->d_psi, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    // 1. forward: tangents of every block, earlier tangents carried along
+    for (size_t bi = 0; bi < e->dblocks.size(); ++bi) {
+        auto &b = e->dblocks[bi];
+        const int p0 = e->block_pos0[bi];
+        if (b.diagonal) {
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table);
+            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0);
+            k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_psi, T, n, e->d_tpos);
+            e->launches += 3;
+        } else if (b.ntiles) {
+            BlockArgs a = e->block_args(b, 1.0);
+            if (W == 1) {
+                if (p0 > 0) k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                k_block_tangent<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
+            } else {
+                if (p0 > 0) k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                k_block_tangent<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
+            }
+            e->launches += 2;
+        }
+    }
+    // 2. compressed tangents, H on all of them, Gram matrix 2 T_C^T H T_C
+    k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
+    const int VW = V * W;
+    if (e->ham_kind == 1)
+        k_spmm<false><<<e->sm_count * 16, 128, 0, s>>>(e->d_rowptr, 0, e->d_col, e->d_val, TC, HTC, VW, D);
+    else if (e->ham_kind == 2)
+        k_spmm<true><<<e->sm_count * 16, 128, 0, s>>>(nullptr, e->ell_width, e->d_col, e->d_val, TC, HTC, VW, D);
+    else {
+        // on the fly: one column at a time through strided copies
+        for (int v = 0; v < V; ++v) {
+            cudaMemcpy2DAsync(e->d_tmp, sizeof(double), TC + v, (size_t)V * sizeof(double), sizeof(double), n,
+                              cudaMemcpyDeviceToDevice, s);
+            run_apply(e, e->d_tmp, e->d_h, nullptr);
+            cudaMemcpy2DAsync(HTC + v, (size_t)V * sizeof(double), e->d_h, sizeof(double), sizeof(double), n,
+                              cudaMemcpyDeviceToDevice, s);
+        }
+    }
+    e->launches += 2;
+    if (!e->cublas) {
+        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) {
+            cleanup();
+            return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
+        }
+    }
+    cublasSetStream(e->cublas, s);
+    const double two = 2.0, zero = 0.0;
+    // TC, HTC are row-major (D*W) x V == column-major V x (D*W)
+    cublasDgemm(e->cublas, CUBLAS_OP_N, CUBLAS_OP_T, V, V, (int)(D * W), &two, TC, V, HTC, V, &zero, THT, V);
+    // H psi for the backward sweeps: last column of HTC
+    cudaMemcpy2DAsync(e->d_h, sizeof(double), HTC + nparams, (size_t)V * sizeof(double), sizeof(double), n,
+                      cudaMemcpyDeviceToDevice, s);
+    // 3. second-derivative sweeps
+    for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
+        auto &b = e->dblocks[bi];
+        const int p0 = e->block_pos0[bi];
+        const int nvec = p0 + b.nslots;
+        if (b.diagonal) {
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table);
+            dim3 g(kDiagGrid, nvec);
+            k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b), e->d_h, T, n, nvec, p0, hpart);
+            k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
+                                                                            b.ops, p0, Hops, nops);
+            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1);
+            e->launches += 4;
+        } else if (b.ntiles) {
+            BlockArgs a = e->block_args(b, -1.0);
+            const int vchunk = 8;
+            dim3 g(b.ntiles, (nvec + vchunk - 1) / vchunk);
+            if (W == 1) {
+                k_block_hess<1><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);
+            } else {
+                k_block_hess<2><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);
+            }
+            k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, b.ntiles, nvec, b.nslots, e->d_pos_op,
+                                                                            b.ops, p0, Hops, nops);
+            if (W == 1)
+                k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_h, 0, 1);
+            else
+                k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_h, 0, 1);
+            e->launches += 3;
+        }
+    }
+    std::vector<double> hops((size_t)nops * nops), tht((size_t)V * V);
+    cudaMemcpyAsync(hops.data(), Hops, hops.size() * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(tht.data(), THT, tht.size() * 8, cudaMemcpyDeviceToHost, s);
+    rc = stream_sync(e, "hessian");
+    cleanup();
+    e->psi_valid = e->h_valid = false;
+    if (rc) return rc;
+    // Hessian = C Hops C^T + THT (fusedevolve.cpp:2762-2763); THT column-major V x V
+    for (int i = 0; i < nparams; ++i)
+        for (int j = 0; j < nparams; ++j) hess_comp[(size_t)i * nparams + j] = tht[(size_t)j * V + i];
+    for (int a = 0; a < nops; ++a)
+        for (int b = 0; b < nops; ++b)
+            hess_comp[(size_t)param[a] * nparams + param[b]] += scale[a] * scale[b] * hops[(size_t)a * nops + b];
+    if (grad_comp)
+        for (int i = 0; i < nparams; ++i) grad_comp[i] = tht[(size_t)nparams * V + i];
+    if (energy) *energy = tht[(size_t)nparams * V + nparams] / 2.0;
+    return AEGPU_OK;
+}
+
+int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream)
+{
+    if (!e || !x_dev || !y_dev) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    cudaStream_t saved = e->stream;
+    if (stream) e->stream = (cudaStream_t)stream;
+    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr);
+    if (!rc && energy_dev) {
+        k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, e->spmv_grid, energy_dev, 1.0);
+        e->launches += 1;
+        rc = e->cuda_check("apply_dev");
+    }
+    e->stream = saved;
+    return rc;
+}
+
+int aegpu_phase_timing(aegpu_engine *e, int enable)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    e->timing = enable != 0;
+    return AEGPU_OK;
+}
+
+int aegpu_phase_times(aegpu_engine *e, double *ms, int64_t *count)
+{
+    if (!e || !ms) return AEGPU_ERR_ARG;
+    for (auto &m : e->ev_marks) {
+        cudaEventSynchronize(m[3]);
+        for (int p = 0; p < 3; ++p) {
+            float t = 0;
+            cudaEventElapsedTime(&t, m[p], m[p + 1]);
+            e->phase_ms[p] += t;
+        }
+        e->phase_n += 1;
+        for (auto ev : m) e->ev_pool.push_back(ev);
+    }
+    e->ev_marks.clear();
+    for (int p = 0; p < 3; ++p) ms[p] = e->phase_ms[p];
+    if (count) *count = e->phase_n;
+    e->phase_ms[0] = e->phase_ms[1] = e->phase_ms[2] = 0;
+    e->phase_n = 0;
+    return e->cuda_check("phase_times");
+}
+
+int aegpu_problem_info(const aegpu_engine *e, int64_t *info)
+{
+    // D, nops, blocks, ham kind, ham entries, ell width, active (touched) amplitudes summed over blocks
+    if (!e || !info) return AEGPU_ERR_ARG;
+    info[0] = (int64_t)e->B.D;
+    info[1] = (int64_t)e->excs.size();
+    info[2] = (int64_t)e->blocks.size();
+    info[3] = e->ham_kind;
+    info[4] = e->ham_entries;
+    info[5] = e->ell_width;
+    int64_t act = 0;
+    for (auto &b : e->dblocks) act += b.diagonal ? (int64_t)e->B.D : (int64_t)b.active;
+    info[6] = act;
+    return AEGPU_OK;
+}
+
+int64_t aegpu_device_bytes(const aegpu_engine *e) { return e ? e->dev_bytes : -1; }
+int64_t aegpu_launch_count(const aegpu_engine *e) { return e ? e->launches : -1; }
+
+}  // extern "C"

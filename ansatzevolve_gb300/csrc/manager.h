@@ -1,0 +1,110 @@
+// stateAnsatzManager: drop-in replacement of the reference's manager class
+// (AnsatzManager.h:59-295).  Same lifecycle: store* calls record the setup, the
+// first evaluation validates it, picks the determinant sector, builds the
+// Hamiltonian and the GPU engine, and later calls only re-evolve when the angles
+// change.  All evaluation work runs on the GPU through the aegpu C ABI.
+#pragma once
+#include "../../include/aegpu.h"
+
+#include <complex>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+namespace ae {
+
+struct Exc4 {
+    int8_t first, second, third, fourth;  // 0-based, -1 absent (stateRotate::exc)
+};
+
+class stateAnsatzManager {
+public:
+    // Per-context lock for external interfaces (AnsatzManager.h:115-121); not taken internally.
+    std::mutex m_interfaceLock;
+
+    stateAnsatzManager();
+    ~stateAnsatzManager();
+    stateAnsatzManager(const stateAnsatzManager &) = delete;
+    stateAnsatzManager &operator=(const stateAnsatzManager &) = delete;
+
+    bool storeOperators(const std::vector<Exc4> &excs);
+    bool storeInitial(int numberOfQubits, const std::vector<int> &indexes, const std::vector<double> &coeffs);
+    bool storeInitial(int numberOfQubits, const std::vector<int> &indexes, const std::vector<std::complex<double>> &coeffs);
+    bool storeHamiltonian(std::vector<int> &&iIndexes, std::vector<int> &&jIndexes, std::vector<double> &&coeffs);
+    bool storeNuclearEnergy(double nuclearEnergy);
+    bool storeParameterDependencies(const std::vector<std::pair<int, double>> &parameterDependency);
+    bool storeRunPath(const std::string &runPath);
+    // Extension: integrals from memory (h[p*N+q], g[((p*N+q)*N+r)*N+s] = (pq|rs)), same
+    // meaning as the <runPath>_oneEInts.bin / _twoEInts.bin files.  mode: AEGPU_HAM_*.
+    bool storeIntegrals(int nOrbitals, const std::vector<double> &h1, const std::vector<double> &g2, int mode = 0);
+
+    bool setAngles(std::vector<double> angles);
+    std::vector<double> getAngles();  // compressed (m_normCompressMatrix)
+
+    bool getExpectationValue(double &exptValue);
+    bool getFinalState(std::vector<double> &finalState);                 // real part, 2^nq entries
+    bool getFinalState(std::vector<std::complex<double>> &finalState);   // 2^nq entries
+    bool getGradientComp(std::vector<double> &gradient);
+    bool getHessianComp(std::vector<double> &hessian);                   // P x P, row-major (symmetric)
+
+    bool getExpectationValue(const std::vector<double> &angles, double &exptValue);
+    bool getFinalState(const std::vector<double> &angles, std::vector<double> &finalState);
+    bool getFinalState(const std::vector<double> &angles, std::vector<std::complex<double>> &finalState);
+    bool getGradientComp(const std::vector<double> &angles, std::vector<double> &gradient);
+    bool getHessianComp(const std::vector<double> &angles, std::vector<double> &hessian);
+    // rows of `angles` (row-major, nrows x ncols) are angle sets; ncols = P or nOps
+    bool getExpectationValues(const std::vector<double> &angles, int nrows, int ncols, std::vector<double> &exptValues);
+
+    // Newton-Raphson with cubic backtracking (TUPSQuantities::OptimiseTups).
+    bool optimise();
+
+    // introspection (not in the reference API)
+    int numberOfQubits() const { return m_numberOfQubits; }
+    int numberOfParameters() const { return m_numberOfUniqueParameters; }
+    int numberOfOperators() const { return (int)m_excitations.size(); }
+    bool isComplex() const { return m_complex; }
+    aegpu_engine *engine() { return m_engine; }
+    double nuclearEnergy() const { return m_nuclearEnergy; }
+    const std::vector<int> &params() const { return m_param; }
+    const std::vector<double> &scales() const { return m_scale; }
+    int64_t optimiseHessianEvals = 0, optimiseEnergyEvals = 0;
+
+private:
+    bool validateToRun();
+    bool construct();
+    bool setHamiltonian();
+    void setOperatorSymmetry();
+    bool decompress(const std::vector<double> &in, std::vector<double> &out);
+    bool evolveIfNeeded();
+
+    std::vector<Exc4> m_excitations;
+    std::vector<int> m_initIdx;
+    std::vector<std::complex<double>> m_initCoeff;
+    bool m_initComplex = false;
+    std::vector<int> m_iIndexes, m_jIndexes;
+    std::vector<double> m_coeffs;
+    std::vector<double> m_h1, m_g2;
+    int m_intsN = 0, m_intsMode = 0;
+    std::vector<std::pair<int, double>> m_parameterDependency;
+    std::vector<int> m_param;
+    std::vector<double> m_scale;
+    std::string m_runPath;
+    double m_nuclearEnergy = 0;
+    int m_numberOfUniqueParameters = -1;
+    int m_numberOfQubits = -1;
+    int m_numberOfParticles = -1, m_spinUp = -1, m_spinDown = -1;
+    bool m_particleSym = false, m_InitialSZSym = false, m_OperatorSZSym = false;
+    bool m_complex = false;
+    bool m_isConstructed = false;
+    int m_basisKind = 0;
+
+    aegpu_engine *m_engine = nullptr;
+    std::vector<double> m_angles;          // per operator
+    bool m_haveEvolved = false;
+};
+
+void log_line(const std::string &s);
+
+}  // namespace ae

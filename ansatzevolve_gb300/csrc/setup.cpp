@@ -1,0 +1,260 @@
+// Host-side setup: basis enumeration, commuting-block grouping, orbit tables.
+#include "setup.h"
+
+#include <algorithm>
+#include <numeric>
+#include <thread>
+
+namespace ae {
+
+static int popc(uint32_t x) { return __builtin_popcount(x); }
+
+bool Basis::init(int nq_, int kind_, int ne_, int na_, int nb_, std::string &err)
+{
+    nq = nq_; kind = kind_; ne = ne_; na = na_; nb = nb_; N = nq / 2;
+    if (nq < 1 || nq > 30) { err = "number of qubits out of range (1..30)"; return false; }
+    if (kind == BASIS_SZ) {
+        if (nq % 2) { err = "Sz sector needs an even number of qubits"; return false; }
+        rankA.assign(1u << N, -1);
+        rankB.assign(1u << N, -1);
+        strA.clear(); strB.clear();
+        for (uint32_t s = 0; s < (1u << N); ++s) {
+            if (popc(s) == na) { rankA[s] = (int32_t)strA.size(); strA.push_back(s); }
+            if (popc(s) == nb) { rankB[s] = (int32_t)strB.size(); strB.push_back(s); }
+        }
+        nA = (uint32_t)strA.size();
+        nB = (uint32_t)strB.size();
+        D = (uint64_t)nA * nB;
+    } else {
+        if (nq > 28) { err = "sectors without Sz symmetry are limited to 28 qubits"; return false; }
+        rank.assign(1ull << nq, -1);
+        states.clear();
+        for (uint64_t s = 0; s < (1ull << nq); ++s)
+            if (kind == BASIS_FULL || popc((uint32_t)s) == ne) {
+                rank[s] = (int32_t)states.size();
+                states.push_back((uint32_t)s);
+            }
+        D = states.size();
+    }
+    if (D == 0) { err = "empty determinant sector"; return false; }
+    if (D >= (1ull << 31)) { err = "determinant sector too large"; return false; }
+    return true;
+}
+
+// stateRotate::exc helpers, operatorpool.h:140-197.
+bool exc_is_diagonal(const Exc &e)
+{
+    if (e.v[2] == -1) return e.v[0] == e.v[1];
+    uint32_t c = (1u << e.v[0]) | (1u << e.v[1]), a = (1u << e.v[2]) | (1u << e.v[3]);
+    return (c ^ a) == 0;
+}
+
+bool exc_has_diagonal(const Exc &e)
+{
+    if (e.v[2] == -1 && e.v[3] == -1) return e.v[0] == e.v[1];
+    for (int i = 0; i < 4; ++i)
+        for (int j = i + 1; j < 4; ++j)
+            if (e.v[i] == e.v[j]) return true;
+    return false;
+}
+
+bool exc_commutes(const Exc &x, const Exc &y)
+{
+    uint32_t f = 0, s = 0;
+    for (int i = 0; i < 4; ++i) {
+        if (x.v[i] != -1) f |= 1u << x.v[i];
+        if (y.v[i] != -1) s |= 1u << y.v[i];
+    }
+    return !(f & s) || (exc_is_diagonal(x) && exc_is_diagonal(y));
+}
+
+std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std::vector<int> &perm)
+{
+    const size_t n = excs.size();
+    perm.resize(n);
+    std::iota(perm.begin(), perm.end(), 0);
+    auto diag = [&](size_t i) { return exc_is_diagonal(excs[perm[i]]); };
+    if (n > 1) {
+        size_t start = 0, end = 1;
+        while (end < n) {
+            bool all = true;
+            while (all && end < n) {
+                for (size_t k = start; k < end; ++k) {
+                    bool ok = exc_commutes(excs[perm[k]], excs[perm[end]]) && diag(k) == diag(end);
+                    if (!ok) { all = false; break; }
+                }
+                if (all) end++;
+            }
+            for (size_t trial = end; trial < n; ++trial) {
+                bool all2 = true;
+                for (size_t k = start; k < trial; ++k) {
+                    if (diag(start) != diag(trial)) { all2 = false; break; }
+                    if (!exc_commutes(excs[perm[k]], excs[perm[trial]])) { all2 = false; break; }
+                }
+                if (all2) {
+                    for (size_t k = trial; k > end; --k) std::swap(perm[k], perm[k - 1]);
+                    end++;
+                }
+            }
+            start = end;
+            end = start + 1;
+        }
+    }
+    std::vector<size_t> bounds{0};
+    for (size_t i = 0; i < n; ++i)
+        for (size_t j = bounds.back(); j < i; ++j) {
+            bool ext = exc_commutes(excs[perm[i]], excs[perm[j]]) && diag(i) == diag(j);
+            if (!ext) { bounds.push_back(i); break; }
+        }
+    bounds.push_back(n);
+    std::vector<Block> out;
+    for (size_t b = 0; b + 1 < bounds.size(); ++b) {
+        size_t len = bounds[b + 1] - bounds[b];
+        size_t fuse = len;
+        if ((int)len > max_fuse)
+            for (int f = max_fuse; f > 0; --f)
+                if (len % f == 0) { fuse = f; break; }
+        for (size_t c = bounds[b]; c < bounds[b + 1]; c += fuse) {
+            Block blk;
+            blk.diagonal = diag(c);
+            for (size_t k = c; k < c + fuse; ++k) blk.ops.push_back(perm[k]);
+            out.push_back(std::move(blk));
+        }
+    }
+    return out;
+}
+
+OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int nthreads)
+{
+    const int nb = (int)codes.size();
+    const uint32_t nmask = 1u << nb;
+    const uint64_t D = B.D;
+    if (nthreads < 1) nthreads = 1;
+    // pass 1 (parallel over rank ranges): per chunk, the roots of every mask in ascending order
+    struct Chunk { std::vector<std::vector<uint32_t>> roots; };
+    std::vector<Chunk> chunks(nthreads);
+    auto work = [&](int t) {
+        uint64_t lo = D * t / nthreads, hi = D * (t + 1) / nthreads;
+        auto &roots = chunks[t].roots;
+        roots.assign(nmask, {});
+        for (uint64_t z = lo; z < hi; ++z) {
+            uint32_t s = B.bits(z), m = 0;
+            bool root = true;
+            for (int i = 0; i < nb; ++i) {
+                uint32_t p; int sg;
+                if (apply_exc(codes[i], s, p, sg) == 1) {
+                    if (p < s) { root = false; break; }
+                    m |= 1u << i;
+                }
+            }
+            if (root && m) roots[m].push_back((uint32_t)z);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nthreads; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto &x : th) x.join();
+
+    OrbitTables T;
+    for (uint32_t m = 1; m < nmask; ++m) {
+        uint64_t nroots = 0;
+        for (auto &c : chunks) nroots += c.roots[m].size();
+        if (!nroots) continue;
+        OrbitGroup g{};
+        g.idx_off = (uint32_t)T.idx.size();
+        g.n_orbits = (uint32_t)nroots;
+        g.mask = m;
+        g.k = 0;
+        for (int i = 0; i < nb; ++i)
+            if (m & (1u << i)) g.slot[g.k++] = (int8_t)i;
+        const uint32_t osz = 1u << g.k;
+        T.idx.reserve(T.idx.size() + nroots * osz);
+        std::vector<uint32_t> orb(osz);
+        for (auto &c : chunks)
+            for (uint32_t root : c.roots[m]) {
+                orb[0] = B.bits(root);
+                for (uint32_t i = 0; i < g.k; ++i) {
+                    const uint32_t stride = 1u << i;
+                    for (uint32_t q = 0; q < stride; ++q) {
+                        uint32_t p; int sg;
+                        apply_exc(codes[g.slot[i]], orb[q], p, sg);
+                        orb[q + stride] = p;
+                    }
+                }
+                for (uint32_t q = 0; q < osz; ++q) {
+                    int64_t r = B.rank_of(orb[q]);
+                    if (r < 0) T.ok = false;
+                    T.idx.push_back((uint32_t)(r < 0 ? 0 : r));
+                }
+            }
+        const uint32_t per_tile = osz >= (uint32_t)kTileElems ? 1u : (uint32_t)kTileElems / osz;
+        for (uint32_t o = 0; o < g.n_orbits; o += per_tile) {
+            OrbitTile t{};
+            t.group = (uint32_t)T.groups.size();
+            t.orbit0 = o;
+            t.n_orbits = std::min(per_tile, g.n_orbits - o);
+            t.elem_off = g.idx_off + o * osz;
+            T.tiles.push_back(t);
+        }
+        T.groups.push_back(g);
+        T.active += nroots * osz;
+    }
+    return T;
+}
+
+}  // namespace ae
+
+// ------------------------------------------------------------ host inspection --
+#include "../../include/aegpu.h"
+
+extern "C" int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *block_sizes, int *n_blocks)
+{
+    if (nops < 1 || !ops || !n_blocks) return AEGPU_ERR_ARG;
+    std::vector<ae::Exc> excs(nops);
+    for (int i = 0; i < nops; ++i)
+        for (int j = 0; j < 4; ++j) {
+            if (ops[4 * i + j] < -1 || ops[4 * i + j] >= nq) return AEGPU_ERR_ARG;
+            excs[i].v[j] = (int8_t)ops[4 * i + j];
+        }
+    std::vector<int> p;
+    auto blocks = ae::group_blocks(excs, 12, p);
+    if (perm) std::copy(p.begin(), p.end(), perm);
+    if (block_sizes)
+        for (size_t b = 0; b < blocks.size() && (int)b < *n_blocks; ++b)
+            block_sizes[b] = (int)blocks[b].ops.size() * (blocks[b].diagonal ? -1 : 1);
+    *n_blocks = (int)blocks.size();
+    return AEGPU_OK;
+}
+
+extern "C" int aegpu_host_orbits(int nq, int kind, int ne, int na, int nb, int nops, const int *ops, uint32_t *idx,
+                                 int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles)
+{
+    if (nops < 1 || nops > 12 || !ops || !n_idx || !n_groups || !n_tiles) return AEGPU_ERR_ARG;
+    ae::Basis B;
+    std::string err;
+    if (!B.init(nq, kind, ne, na, nb, err)) return AEGPU_ERR_ARG;
+    std::vector<ae::ExcCode> codes;
+    for (int i = 0; i < nops; ++i) codes.push_back(ae::make_exc_code(ops[4 * i], ops[4 * i + 1], ops[4 * i + 2], ops[4 * i + 3]));
+    ae::OrbitTables T = ae::build_orbits(B, codes, 2);
+    if (!T.ok) return AEGPU_ERR_UNSUPPORTED;
+    const int64_t ci = *n_idx, cg = *n_groups, ct = *n_tiles;
+    *n_idx = (int64_t)T.idx.size();
+    *n_groups = (int64_t)T.groups.size();
+    *n_tiles = (int64_t)T.tiles.size();
+    if (idx && ci >= *n_idx) std::copy(T.idx.begin(), T.idx.end(), idx);
+    if (groups && cg >= *n_groups)
+        for (size_t g = 0; g < T.groups.size(); ++g) {
+            groups[4 * g] = T.groups[g].idx_off;
+            groups[4 * g + 1] = T.groups[g].n_orbits;
+            groups[4 * g + 2] = T.groups[g].k;
+            groups[4 * g + 3] = T.groups[g].mask;
+        }
+    if (tiles && ct >= *n_tiles)
+        for (size_t t = 0; t < T.tiles.size(); ++t) {
+            tiles[4 * t] = T.tiles[t].group;
+            tiles[4 * t + 1] = T.tiles[t].orbit0;
+            tiles[4 * t + 2] = T.tiles[t].n_orbits;
+            tiles[4 * t + 3] = T.tiles[t].elem_off;
+        }
+    return AEGPU_OK;
+}

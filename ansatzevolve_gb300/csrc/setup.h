@@ -1,0 +1,104 @@
+// Host-side setup for the GPU engine: determinant basis, commuting-block grouping
+// and per-block orbit tables.  Runs once per problem shape; the tables are then
+// uploaded to HBM and consumed by the block-rotation kernels in engine.cu.
+#pragma once
+#include "exc_rule.h"
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace ae {
+
+enum BasisKind { BASIS_FULL = 0, BASIS_NUMBER = 1, BASIS_SZ = 2 };
+
+// Sector basis in ascending bitstring order (the reference's decompressPerm,
+// operatorpool.cpp:207-242 / operatorpool.h:49-77).  In the Sz sector a
+// determinant is (alpha string << N) | beta string, so its rank is
+// rankA[alpha] * nB + rankB[beta]: alpha strings select rows of a nA x nB matrix.
+struct Basis {
+    int nq = 0, N = 0, kind = BASIS_FULL;
+    int ne = 0, na = 0, nb = 0;
+    uint64_t D = 0;
+    uint32_t nA = 0, nB = 0;
+    std::vector<uint32_t> strA, strB;    // Sz: alpha / beta strings, ascending
+    std::vector<int32_t> rankA, rankB;   // Sz: 2^N tables, -1 outside the sector
+    std::vector<uint32_t> states;        // FULL / NUMBER: rank -> bitstring
+    std::vector<int32_t> rank;           // FULL / NUMBER: 2^nq table, -1 outside
+
+    bool init(int nq, int kind, int ne, int na, int nb, std::string &err);
+    uint32_t bits(uint64_t z) const
+    {
+        if (kind == BASIS_SZ) return (strA[z / nB] << N) | strB[z % nB];
+        return states[z];
+    }
+    int64_t rank_of(uint32_t s) const
+    {
+        if (kind == BASIS_SZ) {
+            int32_t a = rankA[s >> N], b = rankB[s & ((1u << N) - 1u)];
+            return (a < 0 || b < 0) ? -1 : (int64_t)a * nB + b;
+        }
+        if (s >= (1ull << nq)) return -1;
+        return rank[s];
+    }
+};
+
+struct Exc {
+    int8_t v[4];
+};
+
+// One fused pass: a run of mutually commuting excitations (all diagonal or all
+// paired) applied as a single sweep over the statevector.
+struct Block {
+    bool diagonal = false;
+    std::vector<int> ops;   // operator indices (original order) in application order
+};
+
+// Greedy commuting-block grouping with forward moves, restating
+// FusedEvolve::regenCache (fusedevolve.cpp:1797-1967): a block grows while the next
+// operator commutes with all members (diagonal only with diagonal); later operators
+// that commute with the block and with everything they jump over are moved
+// forward into it; blocks longer than max_fuse are cut into equal chunks of the
+// largest divisor <= max_fuse (fusedevolve.cpp:1915-1926).
+std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std::vector<int> &perm);
+
+bool exc_is_diagonal(const Exc &e);
+bool exc_has_diagonal(const Exc &e);
+bool exc_commutes(const Exc &x, const Exc &y);
+
+// Orbit tables of one paired block (fusedevolve.cpp:718-915 restated for the GPU).
+// Every determinant on which at least one block excitation acts lies on exactly one
+// orbit: the hypercube {apply(T, root) : T subset of its active excitations}; the
+// root is the member that every active excitation maps to a larger bitstring.
+// Orbits are grouped by active mask; inside a group they are listed by ascending
+// root, each as 2^k ranks in hypercube order (bit i of the position = i-th active
+// excitation applied).  A tile is a run of whole orbits of one group with at most
+// kTileElems members: one CTA stages a tile in shared memory and applies all k
+// butterfly layers there, so the statevector crosses HBM once per block.
+constexpr int kTileElems = 4096;
+
+struct OrbitGroup {
+    uint32_t idx_off;    // first entry in the block's rank list
+    uint32_t n_orbits;
+    uint32_t k;          // active excitations per orbit
+    uint32_t mask;       // block-local active mask
+    int8_t slot[16];     // block-local excitation slot of layer i
+};
+
+struct OrbitTile {
+    uint32_t group;
+    uint32_t orbit0;
+    uint32_t n_orbits;
+    uint32_t elem_off;   // first entry in the block's rank list
+};
+
+struct OrbitTables {
+    std::vector<uint32_t> idx;        // ranks, grouped / ordered as described
+    std::vector<OrbitGroup> groups;
+    std::vector<OrbitTile> tiles;
+    uint64_t active = 0;              // number of determinants touched by the block
+    bool ok = true;                   // false if an excitation leaves the sector
+};
+
+OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int nthreads);
+
+}  // namespace ae

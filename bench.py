@@ -1,0 +1,311 @@
+"""Benchmark: TUPS energy+gradient evaluations per second on GB300 (FP64).
+
+Workload (the configuration the metric is quoted on): tUPS, 12 spatial orbitals,
+6 alpha + 6 beta electrons (853,776 determinants), 3 layers (99 parameters, 165
+excitations), seeded synthetic random integrals, H stored as fixed-width rows in
+HBM.  One step = one energy+gradient evaluation: forward evolution of the fused
+blocks, H*psi fused with <psi|H psi>, and the adjoint sweep that yields every
+operator's gradient (the reference's FusedEvolve::evolve + evolveDerivative(&E)).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`value` is measured with the inputs resident in HBM (CUDA events on the engine's
+stream); `e2e` is the same metric through the reference-compatible C ABI
+(getEnergy + getGradient_COMP with host buffers, copies inside the timed region).
+Under torchrun every rank runs an independent replica (the path does not shard),
+timing is the max over ranks and `value` sums all ranks' evaluations.
+`--impl reference` times the reference algorithm's CPU implementation (the C
+restatement in oracle/, all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TUPS energy+gradient evals/s (12 orb, FP64) and time-to-converge vs plain"
+N_ORB, N_A, N_B, LAYERS, SEED = 12, 6, 6, 3, 0
+
+
+def workload_desc(D, P, nops, ham):
+    return {"workload": "tUPS 12 orbitals, 6a+6b electrons (D=%d), 3 layers (%d parameters, %d excitations), "
+                        "synthetic random integrals seed 0, H %s" % (D, P, nops, ham),
+            "global_batch": 1, "parallelism": "replicas", "l2": "inputs larger than L2 (H rows stream from HBM every step)"}
+
+
+def problem():
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
+    h1, g2 = synthetic_integrals(N_ORB, SEED)
+    ops, param, scale = tups_operators(N_ORB, LAYERS)
+    P = int(param.max())
+    x = np.random.default_rng(SEED + 1).uniform(-0.1, 0.1, P)
+    return dict(h1=h1, g2=g2, ops0=ops - 1, ops1=ops, p0=param - 1, scale=scale, P=P, x=x,
+                hf=hartree_fock_index(N_ORB, N_A, N_B))
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for k, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(k)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(pb, max_seconds=30.0):
+    """The oracle (C restatement of the reference algorithm, OpenMP) on a bounded sample."""
+    from oracle.oracle import Oracle, lib as olib
+    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B)
+    o.set_initial([pb["hf"]], [1.0])
+    o.set_ops(pb["ops0"], pb["p0"], pb["scale"])
+    o.set_ham_integrals(pb["h1"], pb["g2"], csr=False)
+    times = []
+    t_end = time.perf_counter() + max_seconds
+    for k in range(3):
+        t0 = time.perf_counter()
+        E, g = o.gradient_comp(pb["x"] + 1e-3 * k)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() > t_end:
+            break
+    t = float(np.median(times[1:])) if len(times) > 1 else times[0]
+    return {"value": 1.0 / t, "unit": "evals/s", "cores": int(olib().or_num_threads()), "kind": "port",
+            "sample": "%d energy+gradient evaluations of the same 12-orbital workload (%s), operator-list H*psi "
+                      "as the reference picks for this size" % (len(times), "median of all but the first"
+                                                                  if len(times) > 1 else "single evaluation")}, E, g
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    pb = problem()
+    from oracle.oracle import Oracle, lib as olib
+    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B)
+    o.set_initial([pb["hf"]], [1.0])
+    o.set_ops(pb["ops0"], pb["p0"], pb["scale"])
+    o.set_ham_integrals(pb["h1"], pb["g2"], csr=False)
+    budget = float(os.environ.get("AE_REFERENCE_BUDGET_S", "150"))
+    for w in range(min(args.warmup, 1)):
+        o.gradient_comp(pb["x"])
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        o.gradient_comp(pb["x"] + 1e-4 * done)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    v = done / dt
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1),
+            "ms_per_step": 1e3 * dt / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_desc(853776, pb["P"], len(pb["ops0"]), "applied from the operator list on the fly"),
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": int(olib().or_num_threads()), "kind": "port",
+                             "sample": "%d of %d requested steps within the %.0f s budget" % (done, args.steps, budget)},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def e2e_c_abi(pb, steps, warmup):
+    """getEnergy + getGradient_COMP through the reference-compatible C ABI, host buffers."""
+    import ansatzevolve_gb300 as ae
+    m = ae.stateAnsatzManager()
+    assert m.storeInitial(2 * N_ORB, [pb["hf"]], [1.0])
+    assert m.storeOperators(pb["ops1"].tolist())
+    assert m.storeParameterDependencies(list(zip(pb["p0"], pb["scale"])))
+    assert m.storeIntegrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    xs = [pb["x"], pb["x"] + 1e-3]
+    for k in range(warmup):
+        m.getExpectationValue(xs[k % 2])
+        m.getGradientComp(xs[k % 2])
+    t0 = time.perf_counter()
+    for k in range(steps):
+        E = m.getExpectationValue(xs[k % 2])
+        g = m.getGradientComp(xs[k % 2])
+    dt = time.perf_counter() - t0
+    P = pb["P"]
+    m.close()
+    return {"value": steps / dt, "unit": "evals/s", "h2d_bytes_per_step": 2 * 8 * P, "d2h_bytes_per_step": 8 + 8 * P,
+            "ms_per_step": 1e3 * dt / steps, "api": "getEnergy + getGradient_COMP (H*psi cached between the pair)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--ham", default="stored", choices=["stored", "otf"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import ansatzevolve_gb300 as ae
+    pb = problem()
+    mode = ae.HAM_STORED if args.ham == "stored" else ae.HAM_ON_THE_FLY
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_c_abi(pb, max(10, args.steps // 10), 2)
+
+    eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"])
+    init = np.zeros(eng.D)
+    init[np.searchsorted(eng.states(), pb["hf"])] = 1.0
+    eng.set_initial(init)
+    t0 = time.perf_counter()
+    eng.set_ham_integrals(pb["h1"], pb["g2"], mode)
+    setup_s = time.perf_counter() - t0
+    info = eng.info()
+    D = info["D"]
+    ang = torch.tensor(pb["scale"] * pb["x"][pb["p0"]], dtype=torch.float64, device="cuda")
+    E_d = torch.zeros(1, dtype=torch.float64, device="cuda")
+    g_d = torch.zeros(len(pb["ops0"]), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
+    torch.cuda.synchronize()
+    eng.phase_timing(True)
+    eng.phase_times()
+    launches0 = eng.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = eng.launch_count() - launches0
+    phase_ms, nph = eng.phase_times()
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        dist.barrier()
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    ms_step = t_max / args.steps
+    value = world * args.steps / (t_max / 1e3)
+
+    # roofline of the dominant kernel (H*psi): algorithmic bytes per launch
+    peak, peak_kind = measured_peak()
+    nnz = info["ham_entries"]
+    hpsi_bytes = nnz * 12 + 16 * D if mode == ae.HAM_STORED else 16 * D
+    t_hpsi = phase_ms[1] / max(nph, 1) / 1e3
+    achieved = hpsi_bytes / t_hpsi / 1e9
+    # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
+    passes = info["blocks"]
+    step_bytes = passes * 16 * D + hpsi_bytes + passes * 32 * D
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random integrals)",
+        "config": workload_desc(D, pb["P"], len(pb["ops0"]),
+                                "stored as %d-wide rows in HBM (%.1f GB)" % (info["ell_width"], nnz * 12 / 1e9)
+                                if mode == ae.HAM_STORED else "regenerated on the fly"),
+        "roofline": {"bound": "hbm", "kernel": "k_spmv (H*psi)" if mode == ae.HAM_STORED else "k_otf_apply",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "algorithmic_bytes": hpsi_bytes,
+                     "launch_ms": t_hpsi * 1e3},
+        "step_roofline": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms_step / 1e3) / 1e9,
+                          "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
+                          "phase_ms": {"evolve": phase_ms[0] / max(nph, 1), "hpsi_energy": phase_ms[1] / max(nph, 1),
+                                       "adjoint": phase_ms[2] / max(nph, 1)}},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "setup_s": setup_s,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu:
+        cb, Eo, go = cpu_baseline(pb)
+        line["cpu_baseline"] = cb
+        # parity of this very run against the oracle
+        g_ops = g_d.cpu().numpy()
+        g = np.zeros(pb["P"])
+        np.add.at(g, pb["p0"], pb["scale"] * g_ops)
+        line["parity"] = {"dE": abs(float(E_d.item()) - Eo), "max_dg": float(np.max(np.abs(g - go)))}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,65 @@
+/*
+ * AnsatzSynthInterface.h -- the reference's C / Fortran entry points, kept verbatim
+ * as the drop-in boundary (signatures of src/Generated/AnsatzSynthInterface.h:14-26,
+ * behaviour of src/AnsatzSynthInterface.cpp:18-629).  Exported by
+ * libansatzevolve_gb300.so; every statevector operation behind them runs on the GPU.
+ *
+ *   init                 AnsatzSynthInterface.cpp:28   new manager handle
+ *   cleanup              :42   takes the ADDRESS of the handle (void**); 0 ok, 1 null
+ *   setExcitation        :64   = setExcitationScale(..., scale = NULL)
+ *   setExcitationScale   :84   Fortran column-major 1-based operators[n*j+i]; 1-based order
+ *   setHamiltonian       :154  1-based (i, j, coeff) triplets of the 2^nq matrix
+ *   setInitialState      :201  1-based basis indices, real amplitudes
+ *   setInitialStateComplex :252  complex amplitudes (always available here)
+ *   getEnergy            :313  angles compressed or per operator; <psi|H|psi> + nuclear
+ *   getFinalState        :362  dense 2^nq real state (real part in complex mode)
+ *   getFinalStateComplex :440  dense 2^nq complex state
+ *   getGradient_COMP     :519  compressed gradient; -6 on an internal size mismatch
+ *   getHessian_COMP      :578  compressed Hessian, column-major hessian[n*j+i]
+ *   setTraceInterfaceCalls :18 log every call's arguments
+ * Return codes are the reference's: 0 ok, small positive per-argument errors, and
+ * -6 for implementation faults.  No call traps.
+ */
+#ifndef ANSATZSYNTHINTERFACE_H
+#define ANSATZSYNTHINTERFACE_H
+#include <stddef.h>
+#ifdef __cplusplus
+#include <complex>
+#define AE_DOUBLE_COMPLEX std::complex<double>
+extern "C" {
+#else
+#define AE_DOUBLE_COMPLEX double _Complex
+#endif
+
+int cleanup(void *ctx);
+int getEnergy(int nangles, const double *angles, double *energy, void *ctx);
+int getFinalState(int nangles, const double *angles, int nbasisvectors, double *finalstate, void *ctx);
+int getFinalStateComplex(int nangles, const double *angles, int nbasisvectors, AE_DOUBLE_COMPLEX *finalstate, void *ctx);
+int getGradient_COMP(int nangles, const double *angles, double *gradient, void *ctx);
+int getHessian_COMP(int nangles, const double *angles, double *hessian, void *ctx);
+void *init(void);
+int setExcitation(int nparams, const int *operators, const int *orderfile, void *ctx);
+int setExcitationScale(int nparams, const int *operators, const int *orderfile, const double *scalefactor, void *ctx);
+int setHamiltonian(int n, const int *iindexes, const int *jindexes, const double *coeffs, void *ctx);
+int setInitialState(int numqubits, int n, const int *iindexes, const double *coeffs, void *ctx);
+int setInitialStateComplex(int numqubits, int n, const int *iindexes, const AE_DOUBLE_COMPLEX *coeffs, void *ctx);
+void setTraceInterfaceCalls(int val);
+
+/* Extensions (no counterpart in the reference's C ABI, which has no way to pass
+ * integrals; the reference reaches them only through stateAnsatzManager::storeRunPath):
+ * setRunPath       -- prefix of <prefix>_oneEInts.bin / _twoEInts.bin (or _Ham_*.dat)
+ * setIntegrals     -- integrals from memory: h[p*N+q], g[((p*N+q)*N+r)*N+s] = (pq|rs);
+ *                     mode 0 auto, 1 stored rows, 2 on the fly
+ * setNuclearEnergy -- constant added to every energy
+ * optimise         -- Newton-Raphson from the current angles; writes the optimised
+ *                     compressed angles and energy
+ * All return 0 on success, 1 for a null handle, 2 for bad arguments, 3 on failure. */
+int setRunPath(const char *path, void *ctx);
+int setIntegrals(int norb, const double *h1, const double *g2, int mode, void *ctx);
+int setNuclearEnergy(double e, void *ctx);
+int optimise(int nangles, double *angles, double *energy, void *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

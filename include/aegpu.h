@@ -1,0 +1,119 @@
+/*
+ * aegpu.h -- thin C ABI of the GB300 statevector engine.
+ *
+ * The drop-in layer (stateAnsatzManager and the AnsatzSynthInterface functions,
+ * include/AnsatzSynthInterface.h) calls CUDA only through these entry points.
+ * Plain pointers and sizes only; all arrays are host memory unless a name ends in
+ * _dev, in which case they are device pointers and `stream` is a cudaStream_t.
+ * Every call returns AEGPU_OK (0) or a positive status and never traps; the text
+ * of the last failure is available from aegpu_last_error().
+ *
+ * Conventions (the reference's, see SURVEY of AnsatzEvolve):
+ *  - spin orbital k < N is beta (low bits), k >= N is alpha (high bits);
+ *  - excitations are 4 signed 0-based orbital indices, -1 = absent, op-major;
+ *  - the sector basis is the ascending list of bitstrings in the sector; vectors
+ *    are "compressed" (one entry per sector determinant; complex mode interleaves
+ *    re, im);
+ *  - angles are per operator, in the order the operators were given;
+ *  - H is applied as y = H x with rows = output determinants.
+ */
+#ifndef AEGPU_H
+#define AEGPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AEGPU_OK 0
+#define AEGPU_ERR_ARG 1          /* invalid argument (null pointer, size, index) */
+#define AEGPU_ERR_STATE 2        /* call out of order (no problem / Hamiltonian set) */
+#define AEGPU_ERR_CUDA 3         /* CUDA runtime failure (message in aegpu_last_error) */
+#define AEGPU_ERR_NOMEM 4        /* device allocation failed */
+#define AEGPU_ERR_UNSUPPORTED 5  /* input outside what the engine implements */
+
+#define AEGPU_BASIS_FULL 0
+#define AEGPU_BASIS_NUMBER 1
+#define AEGPU_BASIS_SZ 2
+
+#define AEGPU_HAM_AUTO 0         /* stored ELL rows if they fit in HBM, else on the fly */
+#define AEGPU_HAM_STORED 1       /* fixed-width (ELL) rows built on the GPU from the integrals */
+#define AEGPU_HAM_ON_THE_FLY 2   /* rows regenerated from h_pq / (pq|rs) on every apply */
+
+typedef struct aegpu_engine aegpu_engine;
+
+/* Context lifetime.  One engine = one problem on the current CUDA device. */
+int aegpu_create(aegpu_engine **out);
+void aegpu_destroy(aegpu_engine *e);
+const char *aegpu_last_error(const aegpu_engine *e);
+
+/* Problem definition: sector basis + excitation list (replaces the setup of
+ * FusedEvolve::updateExc / regenCache, fusedevolve.cpp:2085-2095, 1797-1967). */
+int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n_alpha, int n_beta,
+                      int complex_mode, int nops, const int *ops);
+int64_t aegpu_dim(const aegpu_engine *e);
+int aegpu_basis_states(const aegpu_engine *e, uint32_t *out);
+int aegpu_num_blocks(const aegpu_engine *e);
+/* Operator application order (the reference's m_excPerm) and the size of every pass. */
+int aegpu_block_layout(const aegpu_engine *e, int *perm, int *block_sizes);
+
+/* Initial state in the sector (D doubles, 2D in complex mode). */
+int aegpu_set_initial(aegpu_engine *e, const double *amps);
+
+/* Hamiltonian as a sector CSR matrix (row = output determinant); duplicates must
+ * already be summed.  Replaces HamiltonianMatrix(value, i, j, comp),
+ * hamiltonianmatrix.cpp:628-659. */
+int aegpu_set_ham_csr(aegpu_engine *e, int64_t nnz, const int64_t *rowptr, const int32_t *col, const double *val);
+/* Hamiltonian from molecular-orbital integrals h[p*N+q], g[((p*N+q)*N+r)*N+s] = (pq|rs)
+ * (the layout of <prefix>_oneEInts.bin / _twoEInts.bin, hamiltonianmatrix.cpp:402-554).
+ * Needs the Sz sector. */
+int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2, int mode);
+/* Which representation is in use: 1 CSR, 2 stored ELL, 3 on the fly; and its stored entries. */
+int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored_entries);
+
+/* Evaluations (FusedEvolve::evolve / getEnergy / evolveDerivative / evolveHessian,
+ * fusedevolve.cpp:2105-2159, 2782-2795, 2263-2346, 2437-2780).  Energies exclude
+ * any nuclear constant.  state may be NULL. */
+int aegpu_evolve(aegpu_engine *e, const double *angles, double *state);
+int aegpu_energy(aegpu_engine *e, const double *angles, double *energy);
+int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double *grad_ops);
+/* Hessian in the compressed parameters: theta_op = scale[op] * x[param[op]]. */
+int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                  double *energy, double *grad_comp, double *hess_comp);
+int aegpu_apply_h(aegpu_engine *e, const double *x, double *y);
+
+/* Device-resident variants (inputs already in HBM): angles_dev[nops], energy_dev[1],
+ * grad_dev[nops].  Enqueued on `stream`; nothing is synchronised. */
+int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream);
+int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, void *stream);
+/* y_dev = H x_dev on device vectors; energy_dev (nullable) receives <x|H x>. */
+int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream);
+/* CUDA-event timing of the phases of aegpu_gradient_dev (evolve, H*psi + energy,
+ * adjoint sweep): enable, then read the accumulated milliseconds (and the number of
+ * evaluations) -- reading resets the accumulators. */
+int aegpu_phase_timing(aegpu_engine *e, int enable);
+int aegpu_phase_times(aegpu_engine *e, double *ms3, int64_t *count);
+/* info[7]: D, operators, fused blocks, Hamiltonian kind, stored H entries, ELL width,
+ * amplitudes touched per full sweep over all blocks. */
+int aegpu_problem_info(const aegpu_engine *e, int64_t *info);
+/* Device pointers of the current state and of H*state (D or 2D doubles). */
+int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi);
+
+/* Host-only inspection of the setup (no GPU needed): the operator application order
+ * and block sizes (negative = diagonal block) that aegpu_set_problem would use, and
+ * the orbit tables of one block of excitations.  For tests of the setup logic.
+ * aegpu_host_orbits: n_idx / n_groups / n_tiles are in/out capacities -> sizes;
+ * groups are 4 uint32 (idx_off, n_orbits, k, mask) each, tiles 4 uint32 each. */
+int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *block_sizes, int *n_blocks);
+int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int nops, const int *ops,
+                      uint32_t *idx, int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles);
+
+/* Bytes of HBM held by the engine, and kernel launches issued since creation. */
+int64_t aegpu_device_bytes(const aegpu_engine *e);
+int64_t aegpu_launch_count(const aegpu_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,102 @@
+"""CPU tests of the host-side setup logic and of the library boundary (no GPU).
+
+* fused-block grouping reproduces the reference's regenCache layout
+  (fusedevolve.cpp:1797-1967) for the TUPS circuits of the benchmark configurations;
+* orbit tables, interpreted step by step in numpy, evolve a vector exactly like the
+  oracle applying the same excitations one at a time;
+* the shared library exports every symbol declared in include/*.h.
+"""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from ansatzevolve_gb300 import host_block_layout, host_orbits, LIB_PATH, lib
+from ansatzevolve_gb300.synthetic import tups_operators
+from oracle.oracle import Oracle, exc_apply
+from tests.conftest import ROOT
+
+
+@pytest.mark.parametrize("N,layers,expected", [
+    (8, 2, [8, 4, 8, 6, 3, 6] * 2),
+    (10, 3, [10, 5, 10, 8, 4, 8] * 3),
+    (12, 3, [12, 6, 12, 10, 5, 10] * 3),
+    (14, 4, [7, 7, 7, 7, 7, 12, 6, 12] * 4),
+])
+def test_block_layout_matches_reference_grouping(N, layers, expected):
+    ops, _, _ = tups_operators(N, layers)
+    perm, sizes = host_block_layout(2 * N, ops - 1)
+    assert list(sizes) == expected
+    assert sorted(perm) == list(range(len(ops)))
+
+
+def _interpret_orbits(st, ops0, idx, groups, ang, v):
+    """Apply one block through its orbit tables the way the GPU kernel does."""
+    v = v.copy()
+    for off, norb, k, mask in groups:
+        slots = [i for i in range(len(ops0)) if mask & (1 << i)]
+        assert len(slots) == k
+        n = 1 << k
+        for o in range(norb):
+            mem = idx[off + o * n: off + (o + 1) * n].astype(np.int64)
+            x = v[mem]
+            for layer, sl in enumerate(slots):
+                S, C = np.sin(ang[sl]), np.cos(ang[sl])
+                for p in range(n // 2):
+                    lo = ((p >> layer) << (layer + 1)) | (p & ((1 << layer) - 1))
+                    hi = lo | (1 << layer)
+                    kind, partner, s = exc_apply(int(st[mem[lo]]), ops0[sl])
+                    assert kind == 1 and partner == st[mem[hi]]
+                    a, b = x[lo], x[hi]
+                    x[lo] = s * S * b + C * a
+                    x[hi] = -s * S * a + C * b
+            v[mem] = x
+    return v
+
+
+@pytest.mark.parametrize("N,na,nb", [(4, 2, 2), (5, 3, 2)])
+def test_orbit_tables_reproduce_sequential_rotations(N, na, nb):
+    ops, _, _ = tups_operators(N, 1)
+    ops0 = ops - 1
+    perm, sizes = host_block_layout(2 * N, ops0)
+    rng = np.random.default_rng(7)
+    o = Oracle(2 * N, 2, na + nb, na, nb)
+    st = o.states()
+    start = 0
+    for bs in sizes:
+        blk = ops0[perm[start:start + bs]]
+        start += bs
+        idx, groups, tiles = host_orbits(2 * N, 2, na + nb, na, nb, blk)
+        # every determinant appears at most once, tiles cover the rank list in order
+        assert len(np.unique(idx)) == len(idx)
+        assert tiles[0, 3] == 0 and tiles[-1, 3] + (tiles[-1, 2] << groups[tiles[-1, 0], 2]) == len(idx)
+        ang = rng.uniform(-1, 1, bs)
+        v = rng.normal(size=len(st))
+        got = _interpret_orbits(st, blk, idx, groups, ang, v)
+        o.set_initial(st, v)
+        o.set_ops(blk, np.arange(bs), np.ones(bs))
+        want = o.evolve_ops(ang)
+        np.testing.assert_allclose(got, want, atol=1e-14, rtol=0)
+
+
+def _declared_symbols():
+    names = set()
+    for h in ("aegpu.h", "AnsatzSynthInterface.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(\w+)\s*\(", src, flags=re.M):
+            if m.group(1) not in ("if", "defined", "extern"):
+                names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    declared = _declared_symbols()
+    assert len(declared) >= 40
+    missing = sorted(declared - exported)
+    assert not missing, missing
