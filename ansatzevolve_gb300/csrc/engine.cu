@@ -989,18 +989,40 @@ struct aegpu_engine {
 
 namespace {
 
-int set_smem_limits()
+template <typename K>
+int set_smem(K kernel, size_t need, int optin)
 {
-    const int maxsm = 227 * 1024;
-    cudaFuncSetAttribute(k_block_rot<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_rot<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_bwd<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_bwd<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_tangent<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_tangent<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_hess<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
-    cudaFuncSetAttribute(k_block_hess<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (need + fa.sharedSizeBytes > (size_t)optin) return 1;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
     return 0;
+}
+
+// Opt the tile kernels into the shared memory they use (1, 2 or 3 staged vectors of
+// kTileElems amplitudes plus the bitstrings), within the device's per-block limit.
+int set_smem_limits(int dev)
+{
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    auto need = [](int nv, int W) { return (size_t)kTileElems * (nv * W * 8 + 4); };
+    int bad = 0;
+    bad += set_smem(k_block_rot<1>, need(1, 1), optin);
+    bad += set_smem(k_block_rot<2>, need(1, 2), optin);
+    bad += set_smem(k_block_tangent<1>, need(1, 1), optin);
+    bad += set_smem(k_block_tangent<2>, need(1, 2), optin);
+    bad += set_smem(k_block_bwd<1>, need(2, 1), optin);
+    bad += set_smem(k_block_bwd<2>, need(2, 2), optin);
+    bad += set_smem(k_block_hess<1>, need(3, 1), optin);
+    bad += set_smem(k_block_hess<2>, need(3, 2), optin);
+    cudaGetLastError();
+    return bad;
 }
 
 // Forward evolution of psi from the start vector (angles already in d_sc / d_ang).
@@ -1145,7 +1167,10 @@ int aegpu_create(aegpu_engine **out)
         delete e;
         return AEGPU_ERR_CUDA;
     }
-    set_smem_limits();
+    if (set_smem_limits(dev)) {
+        delete e;
+        return AEGPU_ERR_CUDA;
+    }
     e->spmv_grid = e->sm_count * 8;
     *out = e;
     return AEGPU_OK;
