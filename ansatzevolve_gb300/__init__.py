@@ -68,6 +68,7 @@ def lib(build_if_missing=True):
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64)]),
         "aegpu_apply_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
+        "aegpu_use_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_phase_timing": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
         "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
@@ -224,6 +225,9 @@ class Engine:
     def apply_dev(self, x_ptr, y_ptr, energy_ptr=None, stream=0):
         self._check(self.L.aegpu_apply_dev(self.h, x_ptr, y_ptr, energy_ptr, stream or None))
 
+    def use_graphs(self, enable=True):
+        self._check(self.L.aegpu_use_graphs(self.h, int(enable)))
+
     def phase_timing(self, enable=True):
         self._check(self.L.aegpu_phase_timing(self.h, int(enable)))
 
@@ -234,9 +238,9 @@ class Engine:
         return ms, n.value
 
     def info(self):
-        out = np.zeros(7, dtype=np.int64)
+        out = np.zeros(8, dtype=np.int64)
         self._check(self.L.aegpu_problem_info(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
-        keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active")
+        keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active", "nnz")
         return dict(zip(keys, map(int, out)))
 
     def device_bytes(self):

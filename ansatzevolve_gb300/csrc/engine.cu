@@ -59,15 +59,25 @@ constexpr int kDiagGrid = 152 * 4;
 struct DevBasis {
     int kind, N, nq;
     uint32_t nA, nB;
+    uint32_t div_m, div_l;  // z / nB = (hi + ((z - hi) >> 1)) >> (l - 1), hi = umulhi(m, z)
     uint64_t D;
     const uint32_t *strA, *strB;
     const int32_t *rankA, *rankB;
     const uint32_t *states;
     const int32_t *rank;
 
+    __device__ __forceinline__ uint32_t div_nB(uint32_t z) const
+    {
+        if (div_l == 0) return z;
+        const uint32_t hi = __umulhi(div_m, z);
+        return (hi + ((z - hi) >> 1)) >> (div_l - 1);
+    }
     __device__ __forceinline__ uint32_t bits(uint32_t z) const
     {
-        if (kind == BASIS_SZ) return (strA[z / nB] << N) | strB[z % nB];
+        if (kind == BASIS_SZ) {
+            const uint32_t a = div_nB(z);
+            return (strA[a] << N) | strB[z - a * nB];
+        }
         return states[z];
     }
     __device__ __forceinline__ int64_t rank_of(uint32_t s) const
@@ -95,6 +105,15 @@ struct BlockArgs {
 __device__ __forceinline__ uint32_t insert_zero_bit(uint32_t p, int i)
 {
     return ((p >> i) << (i + 1)) | (p & ((1u << i) - 1u));
+}
+
+// Stored Hamiltonian rows ("sliced ELL"): rows are grouped in slabs of 32; inside a
+// slab, entry group g (4 consecutive entries of a row) of the 32 rows is contiguous,
+// so thread r of a warp reads its row with 16-byte column loads and 32-byte value
+// loads that coalesce across the warp.  q = entries per row / 4.
+__device__ __forceinline__ size_t ell_pos(int64_t r, int64_t e, int64_t q)
+{
+    return ((((size_t)(r >> 5) * q + (size_t)(e >> 2)) << 5) + (size_t)(r & 31)) * 4 + (size_t)(e & 3);
 }
 
 // ---------------------------------------------------------------- utilities --
@@ -372,6 +391,204 @@ __global__ void __launch_bounds__(kRotThreads) k_block_hess(BlockArgs a, const d
     }
 }
 
+// ------------------------------------------------ warp-register passes --
+// A pass holds <= 6 commuting excitations, so every orbit has <= 64 members and a
+// warp keeps a whole task (one or more orbits) in registers: two amplitudes per
+// lane, positions p = lane and lane + 32.  Layer i pairs p with p ^ (1 << i): a
+// shuffle for i < 5, the lane's other register for i = 5.  No shared-memory
+// staging and no block barriers.  Each layer is applied in a scaled ("fast
+// Givens") form with one FP64 FMA per amplitude:
+//   |C| >= |S|:  v'' = v + (S/C) s v_p,   true value = C v''
+//   |C| <  |S|:  v'' = (C/S) v + s v_p,   true value = S v''
+// and the product of the per-layer scales is applied once when the task is
+// written back.  The adjoint sweep accumulates <h|G_j psi> = sum_z h_z s_z psi_p(z)
+// in the scaled frame (stored = true / product of the scales applied so far) and
+// multiplies it by the squared product of those scales.  (Per-element form of
+// fusedevolve.cpp:461-483.)
+constexpr int kWarpThreads = 256;
+
+struct PassConst {
+    ExcCode code;
+    double f;      // layer scale (C or dir*S)
+    double m;      // S/C (tan form) or C/S (cot form), with dir applied to S
+    double f2;     // f^2
+    int tan_form;
+};
+
+__device__ __forceinline__ double flip(double x, int s)
+{
+    return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)(s < 0) << 63));
+}
+
+__device__ __forceinline__ double rot_scaled(const PassConst &q, double v, double vp, int s)
+{
+    return q.tan_form ? fma(flip(q.m, s), vp, v) : fma(q.m, v, flip(vp, s));
+}
+
+__device__ __forceinline__ void pass_consts(const BlockArgs &a, PassConst *pc)
+{
+    if (threadIdx.x < (unsigned)a.nslots) {
+        const int op = a.ops[threadIdx.x];
+        const double S = a.dir * a.sc[2 * op], C = a.sc[2 * op + 1];
+        PassConst q;
+        q.code = a.codes[op];
+        if (fabs(C) >= fabs(S)) {
+            q.tan_form = 1;
+            q.f = C;
+            q.m = S / C;
+        } else {
+            q.tan_form = 0;
+            q.f = S;
+            q.m = C / S;
+        }
+        q.f2 = q.f * q.f;
+        pc[threadIdx.x] = q;
+    }
+    __syncthreads();
+}
+
+template <int W>
+__global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
+                                                           double *vecs, size_t vstride, int nvec)
+{
+    __shared__ PassConst pc[kMaxWarpLayers];
+    pass_consts(a, pc);
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
+        const WarpTask task = tasks[t];
+        const uint32_t mask = a.groups[task.group].mask;
+        const uint32_t *idx = a.idx + task.elem_off;
+        const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
+        const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
+        const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
+        double sigma = 1.0;
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j)
+            if (mask & (1u << j)) sigma *= pc[j].f;
+        for (int vec = 0; vec < nvec; ++vec) {
+            double *psi = vecs + vec * vstride;
+            double v0[W], v1[W];
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                v0[w] = ok0 ? psi[(size_t)z0 * W + w] : 0.0;
+                v1[w] = ok1 ? psi[(size_t)z1 * W + w] : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < kMaxWarpLayers; ++j) {
+                if (!(mask & (1u << j))) continue;
+                const int i = __popc(mask & ((1u << j) - 1u));
+                const PassConst &q = pc[j];
+                const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    double p0, p1;
+                    if (i < 5) {
+                        p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                        p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                    } else {
+                        p0 = v1[w];
+                        p1 = v0[w];
+                    }
+                    v0[w] = rot_scaled(q, v0[w], p0, s0);
+                    v1[w] = rot_scaled(q, v1[w], p1, s1);
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                if (ok0) psi[(size_t)z0 * W + w] = sigma * v0[w];
+                if (ok1) psi[(size_t)z1 * W + w] = sigma * v1[w];
+            }
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(kWarpThreads) k_warp_bwd(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
+                                                           double *psi, double *h, double *partials)
+{
+    __shared__ PassConst pc[kMaxWarpLayers];
+    __shared__ double red[kWarpThreads / 32][kMaxWarpLayers];
+    pass_consts(a, pc);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double accS[kMaxWarpLayers];
+#pragma unroll
+    for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
+        const WarpTask task = tasks[t];
+        const uint32_t mask = a.groups[task.group].mask;
+        const uint32_t *idx = a.idx + task.elem_off;
+        const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
+        const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
+        const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
+        double v0[W], v1[W], h0[W], h1[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            v0[w] = ok0 ? psi[(size_t)z0 * W + w] : 0.0;
+            v1[w] = ok1 ? psi[(size_t)z1 * W + w] : 0.0;
+            h0[w] = ok0 ? h[(size_t)z0 * W + w] : 0.0;
+            h1[w] = ok1 ? h[(size_t)z1 * W + w] : 0.0;
+        }
+        double sig2 = 1.0, sigma = 1.0;  // stored = true / sigma
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j) {
+            if (!(mask & (1u << j))) continue;
+            const int i = __popc(mask & ((1u << j) - 1u));
+            const PassConst &q = pc[j];
+            const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
+            double g = 0.0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double pv0, pv1, ph0, ph1;
+                if (i < 5) {
+                    pv0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                    pv1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                    ph0 = __shfl_xor_sync(0xffffffffu, h0[w], 1 << i);
+                    ph1 = __shfl_xor_sync(0xffffffffu, h1[w], 1 << i);
+                } else {
+                    pv0 = v1[w];
+                    pv1 = v0[w];
+                    ph0 = h1[w];
+                    ph1 = h0[w];
+                }
+                g = fma(h0[w], flip(pv0, s0), g);
+                g = fma(h1[w], flip(pv1, s1), g);
+                v0[w] = rot_scaled(q, v0[w], pv0, s0);
+                v1[w] = rot_scaled(q, v1[w], pv1, s1);
+                h0[w] = rot_scaled(q, h0[w], ph0, s0);
+                h1[w] = rot_scaled(q, h1[w], ph1, s1);
+            }
+            accS[j] = fma(g, sig2, accS[j]);
+            sig2 *= q.f2;
+            sigma *= q.f;
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            if (ok0) {
+                psi[(size_t)z0 * W + w] = sigma * v0[w];
+                h[(size_t)z0 * W + w] = sigma * h0[w];
+            }
+            if (ok1) {
+                psi[(size_t)z1 * W + w] = sigma * v1[w];
+                h[(size_t)z1 * W + w] = sigma * h1[w];
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kMaxWarpLayers; ++j) {
+        const double v = warp_sum(accS[j]);
+        if (lane == 0) red[warp][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaxSlots) {
+        double s = 0.0;
+        if (threadIdx.x < kMaxWarpLayers)
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * kMaxSlots + threadIdx.x] = s;
+    }
+}
+
 // ------------------------------------------------------- diagonal blocks --
 // Complex mode only: number / density-density operators multiply every active
 // amplitude by exp(+i * sum of the active angles) (RunFuseNDiagonal,
@@ -573,17 +790,62 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(const int64_t *__restrict
     if (threadIdx.x == 0 && epart) epart[blockIdx.x] = e;
 }
 
+// Sliced-ELL product, one thread per row: 4 independent FP64 accumulators, no
+// cross-lane reduction (its shuffles and adds would cost FP64 issue slots, the
+// binding pipe of this kernel on GB300), fused with the partial sums of <x|y>.
+template <int W>
+__global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int32_t *__restrict__ col,
+                                                            const double *__restrict__ val,
+                                                            const double *__restrict__ x, double *__restrict__ y,
+                                                            int64_t D, double *__restrict__ epart)
+{
+    __shared__ double red[kSpmvThreads / 32];
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (r < D) {
+        const size_t base = ell_pos(r, 0, q);  // group g of this row starts at base + 128 g
+        const int4 *c4 = reinterpret_cast<const int4 *>(col + base);
+        const double2 *v2 = reinterpret_cast<const double2 *>(val + base);
+        double a0[W], a1[W], a2[W], a3[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) a0[w] = a1[w] = a2[w] = a3[w] = 0.0;
+        for (int64_t g = 0; g < q; ++g) {
+            const int4 c = __ldg(c4 + 32 * g);
+            const double2 h01 = __ldg(v2 + 64 * g), h23 = __ldg(v2 + 64 * g + 1);
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                a0[w] = fma(h01.x, __ldg(x + (size_t)c.x * W + w), a0[w]);
+                a1[w] = fma(h01.y, __ldg(x + (size_t)c.y * W + w), a1[w]);
+                a2[w] = fma(h23.x, __ldg(x + (size_t)c.z * W + w), a2[w]);
+                a3[w] = fma(h23.y, __ldg(x + (size_t)c.w * W + w), a3[w]);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const double acc = (a0[w] + a1[w]) + (a2[w] + a3[w]);
+            y[r * W + w] = acc;
+            e = fma(acc, x[r * W + w], e);
+        }
+    }
+    e = block_sum(e, red);
+    if (threadIdx.x == 0 && epart) epart[blockIdx.x] = e;
+}
+
 // H applied to V interleaved vectors X[D][W][V] -> Y[D][W][V] (one CTA per row).
 template <bool ELL>
 __global__ void k_spmm(const int64_t *__restrict__ rowptr, int ell_width, const int32_t *__restrict__ col,
                        const double *__restrict__ val, const double *__restrict__ X, double *__restrict__ Y, int VW,
                        int64_t D)
 {
+    const int64_t q = ell_width >> 2;
     for (int64_t r = blockIdx.x; r < D; r += gridDim.x) {
-        const int64_t b = ELL ? r * ell_width : rowptr[r], end = ELL ? b + ell_width : rowptr[r + 1];
+        const int64_t b = ELL ? 0 : rowptr[r], end = ELL ? ell_width : rowptr[r + 1];
         for (int t = threadIdx.x; t < VW; t += blockDim.x) {
             double acc = 0;
-            for (int64_t k = b; k < end; ++k) acc = fma(__ldg(val + k), __ldg(X + (size_t)__ldg(col + k) * VW + t), acc);
+            for (int64_t k = b; k < end; ++k) {
+                const size_t p = ELL ? ell_pos(r, k, q) : (size_t)k;
+                acc = fma(__ldg(val + p), __ldg(X + (size_t)__ldg(col + p) * VW + t), acc);
+            }
             Y[(size_t)r * VW + t] = acc;
         }
     }
@@ -617,7 +879,8 @@ struct IntArgs {
     const double *h1, *g2;
     DevBasis basis;
     int nOa, nVa, nOb, nVb;
-    int64_t width;
+    int64_t width;    // entries per row
+    int64_t stride;   // stored entries per row (width rounded up to a multiple of 4; padding is col = row, val = 0)
 };
 
 __device__ __forceinline__ double two_e(const IntArgs &a, int p, int q, int r, int s)
@@ -765,14 +1028,21 @@ __global__ void k_ell_build(IntArgs a, int32_t *__restrict__ col, double *__rest
 {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t q = a.stride >> 2, D = (int64_t)a.basis.D;
     for (int64_t r = r0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < r1; r += warps) {
-        const uint32_t J = a.basis.bits((uint32_t)r);
-        for (int64_t e = lane; e < a.width; e += 32) {
-            uint32_t I;
-            double v;
-            row_entry(a, J, e, I, v);
-            col[r * a.width + e] = (int32_t)a.basis.rank_of(I);
-            val[r * a.width + e] = v;
+        // rows past D pad the last slab: column 0, value 0
+        const uint32_t J = r < D ? a.basis.bits((uint32_t)r) : 0u;
+        for (int64_t e = lane; e < a.stride; e += 32) {
+            uint32_t I = J;
+            double v = 0.0;
+            int32_t c = 0;
+            if (r < D) {
+                if (e < a.width) row_entry(a, J, e, I, v);
+                c = (int32_t)a.basis.rank_of(I);
+            }
+            const size_t p = ell_pos(r, e, q);
+            col[p] = c;
+            val[p] = v;
         }
     }
 }
@@ -852,7 +1122,10 @@ struct aegpu_engine {
     struct DevBlock {
         bool diagonal = false;
         int nslots = 0;
-        int ntiles = 0;
+        int ntiles = 0;           // shared-memory tiles (multi-vector Hessian kernels)
+        int nwtasks = 0;          // warp tasks (evolve / adjoint kernels)
+        int wgrid = 0;            // CTAs of the warp kernels; also partial-sum rows
+        WarpTask *wtasks = nullptr;
         int64_t part_off = 0;     // offset of this block's gradient partials
         uint32_t *idx = nullptr;
         OrbitGroup *groups = nullptr;
@@ -905,6 +1178,12 @@ struct aegpu_engine {
         return ev;
     }
 
+    // CUDA graph of one energy + gradient evaluation (angles from d_ang, results in
+    // d_scalar / d_grad), captured on first use of aegpu_gradient_dev
+    cudaGraphExec_t grad_graph = nullptr;
+    int64_t graph_launches = 0;  // kernels inside the graph
+    bool use_graph = true;
+
     // state caching: psi / hpsi valid for these angles
     std::vector<double> cached_angles;
     bool psi_valid = false, h_valid = false;
@@ -915,6 +1194,7 @@ struct aegpu_engine {
         for (auto &m : ev_marks)
             for (auto ev : m) cudaEventDestroy(ev);
         for (auto ev : ev_pool) cudaEventDestroy(ev);
+        if (grad_graph) cudaGraphExecDestroy(grad_graph);
         if (cublas) cublasDestroy(cublas);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -1036,12 +1316,12 @@ int run_evolve(aegpu_engine *e)
                                                                               e->d_diag_table);
             k_diag_rot<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1);
             e->launches += 2;
-        } else if (b.ntiles) {
+        } else if (b.nwtasks) {
             BlockArgs a = e->block_args(b, 1.0);
             if (e->W == 1)
-                k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), e->stream>>>(a, e->d_psi, 0, 1);
+                k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1);
             else
-                k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), e->stream>>>(a, e->d_psi, 0, 1);
+                k_warp_rot<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1);
             e->launches += 1;
         }
     }
@@ -1058,9 +1338,11 @@ int upload_angles(aegpu_engine *e, const double *angles, bool host)
     return e->cuda_check("angles");
 }
 
-// y = H x on device vectors, with E partials into d_epart (nullable).
-int run_apply(aegpu_engine *e, const double *x, double *y, double *epart)
+// y = H x on device vectors, with <x|y> partial sums into epart (nullable); *nparts
+// receives how many partial sums the launch wrote.
+int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int *nparts = nullptr)
 {
+    if (nparts) *nparts = e->spmv_grid;
     const int64_t D = (int64_t)e->B.D;
     const int grid = e->spmv_grid;
     if (e->ham_kind == 1) {
@@ -1069,10 +1351,12 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart)
         else
             k_spmv<2, false><<<grid, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
     } else if (e->ham_kind == 2) {
+        const int sg = (int)((D + kSpmvThreads - 1) / kSpmvThreads);
         if (e->W == 1)
-            k_spmv<1, true><<<grid, kSpmvThreads, 0, e->stream>>>(nullptr, e->ell_width, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv_sell<1><<<sg, kSpmvThreads, 0, e->stream>>>(e->ell_width >> 2, e->d_col, e->d_val, x, y, D, epart);
         else
-            k_spmv<2, true><<<grid, kSpmvThreads, 0, e->stream>>>(nullptr, e->ell_width, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv_sell<2><<<sg, kSpmvThreads, 0, e->stream>>>(e->ell_width >> 2, e->d_col, e->d_val, x, y, D, epart);
+        if (nparts) *nparts = sg;
     } else if (e->ham_kind == 3) {
         if (e->W == 1)
             k_otf_apply<1><<<grid, kSpmvThreads, 0, e->stream>>>(e->ints, x, y, epart);
@@ -1087,9 +1371,10 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart)
 
 int run_energy(aegpu_engine *e, double *E_dev)
 {
-    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart);
+    int np = 0;
+    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, &np);
     if (rc) return rc;
-    k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, e->spmv_grid, E_dev, 1.0);
+    k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0);
     e->launches += 1;
     return e->cuda_check("energy");
 }
@@ -1105,13 +1390,15 @@ int run_backward(aegpu_engine *e, double *grad_dev)
                                                                               e->d_diag_table);
             k_diag_bwd<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, e->d_h, part);
             e->launches += 2;
-        } else if (b.ntiles) {
+        } else if (b.nwtasks) {
             BlockArgs a = e->block_args(b, -1.0);
             if (e->W == 1)
-                k_block_bwd<1><<<b.ntiles, kRotThreads, e->rot_smem(2), e->stream>>>(a, e->d_psi, e->d_h, part);
+                k_warp_bwd<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, e->d_h, part);
             else
-                k_block_bwd<2><<<b.ntiles, kRotThreads, e->rot_smem(2), e->stream>>>(a, e->d_psi, e->d_h, part);
+                k_warp_bwd<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, e->d_h, part);
             e->launches += 1;
+        } else {
+            cudaMemsetAsync(part, 0, (size_t)b.wgrid * kMaxSlots * sizeof(double), e->stream);
         }
     }
     const int nops = (int)e->excs.size();
@@ -1208,7 +1495,9 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             return e->fail(AEGPU_ERR_UNSUPPORTED, "diagonal (number) operators need complex mode");
         e->codes[i] = make_exc_code(x.v[0], x.v[1], x.v[2], x.v[3]);
     }
-    e->blocks = group_blocks(e->excs, kMaxSlots, e->perm);
+    // the reference's commuting blocks, cut into passes of <= 6 excitations so that
+    // every orbit fits one warp's registers
+    e->blocks = split_passes(group_blocks(e->excs, kMaxSlots, e->perm), kMaxWarpLayers);
     e->pos_of_op.assign(nops, 0);
     for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;
 
@@ -1220,6 +1509,16 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     db.nA = e->B.nA;
     db.nB = e->B.nB;
     db.D = e->B.D;
+    // unsigned division by the constant nB with a multiply-high (round-up method)
+    if (db.nB > 1) {
+        uint32_t l = 0;
+        while ((1ull << l) < db.nB) ++l;
+        db.div_l = l;
+        db.div_m = (uint32_t)(((1ull << 32) * ((1ull << l) - db.nB)) / db.nB + 1);
+    } else {
+        db.div_l = 0;
+        db.div_m = 0;
+    }
     if (e->B.kind == BASIS_SZ) {
         db.strA = e->upload(e->B.strA);
         db.strB = e->upload(e->B.strB);
@@ -1261,12 +1560,16 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             d.groups = e->upload(T.groups);
             d.tiles = e->upload(T.tiles);
             d.ntiles = (int)T.tiles.size();
+            d.wtasks = e->upload(T.wtasks);
+            d.nwtasks = (int)T.wtasks.size();
+            d.wgrid = std::max(1, std::min(e->sm_count * 8, (d.nwtasks + 7) / 8));
             d.active = T.active;
         } else {
             d.ntiles = kDiagGrid;
+            d.wgrid = kDiagGrid;
         }
         d.part_off = part_off;
-        part_off += (int64_t)d.ntiles * kMaxSlots;
+        part_off += (int64_t)d.wgrid * kMaxSlots;
         e->dblocks.push_back(d);
     }
     e->n_partials = part_off;
@@ -1275,7 +1578,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     for (int o = 0; o < nops; ++o) {
         const auto &d = e->dblocks[e->op_block[o]];
         opo[o] = d.part_off;
-        opn[o] = d.ntiles;
+        opn[o] = d.wgrid;
         ops_slot[o] = e->op_slot[o];
     }
     e->d_op_part_off = e->upload(opo);
@@ -1293,7 +1596,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->d_h = e->alloc<double>(n);
     e->d_tmp = e->alloc<double>(n);
     e->d_partials = e->alloc<double>(std::max<int64_t>(part_off, 1));
-    e->d_epart = e->alloc<double>(e->spmv_grid);
+    e->d_epart = e->alloc<double>(std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D + kSpmvThreads - 1) / kSpmvThreads));
     e->d_scalar = e->alloc<double>(4);
     e->d_grad = e->alloc<double>(nops);
     if (!e->d_tmp || !e->d_partials || !e->d_grad) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
@@ -1383,24 +1686,26 @@ int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2,
     cudaDeviceSynchronize();
     a.h1 = e->d_h1;
     a.g2 = e->d_g2;
+    a.stride = (a.width + 3) & ~(int64_t)3;
     e->ints = a;
-    e->ell_width = (int)a.width;
+    e->ell_width = (int)a.stride;
     const int64_t D = (int64_t)e->B.D;
-    const double ell_bytes = (double)D * a.width * 12.0;
+    const double ell_bytes = (double)((D + 31) & ~(int64_t)31) * a.stride * 12.0;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     if (mode == AEGPU_HAM_AUTO) mode = ell_bytes < 0.6 * (double)free_b ? AEGPU_HAM_STORED : AEGPU_HAM_ON_THE_FLY;
     if (mode == AEGPU_HAM_STORED) {
-        e->d_col = e->alloc<int32_t>((size_t)D * a.width);
-        e->d_val = e->alloc<double>((size_t)D * a.width);
+        const int64_t Dpad = (D + 31) & ~(int64_t)31;
+        e->d_col = e->alloc<int32_t>((size_t)Dpad * a.stride);
+        e->d_val = e->alloc<double>((size_t)Dpad * a.stride);
         if (!e->d_col || !e->d_val) return e->fail(AEGPU_ERR_NOMEM, "ELL allocation failed");
         const int64_t chunk = 1 << 16;
-        for (int64_t r0 = 0; r0 < D; r0 += chunk) {
-            k_ell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, e->d_col, e->d_val, r0, std::min(D, r0 + chunk));
+        for (int64_t r0 = 0; r0 < Dpad; r0 += chunk) {
+            k_ell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, e->d_col, e->d_val, r0, std::min(Dpad, r0 + chunk));
             e->launches += 1;
         }
         e->ham_kind = 2;
-        e->ham_entries = D * a.width;
+        e->ham_entries = D * a.stride;
     } else {
         e->ham_kind = 3;
         e->ham_entries = 0;
@@ -1465,10 +1770,54 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
     return stream_sync(e, "gradient");
 }
 
+// Capture evolve + H psi + adjoint sweep (reading d_ang) into one CUDA graph.
+static int capture_grad_graph(aegpu_engine *e)
+{
+    cudaStream_t cap = nullptr, saved = e->stream;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return e->cuda_check("graph stream");
+    const int64_t l0 = e->launches;
+    e->stream = cap;
+    cudaGraph_t g = nullptr;
+    int rc = AEGPU_OK;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = e->cuda_check("begin capture");
+    if (!rc) {
+        k_sincos<<<((int)e->excs.size() + 127) / 128, 128, 0, cap>>>(e->d_ang, e->d_sc, (int)e->excs.size());
+        e->launches += 1;
+        rc = run_evolve(e);
+        if (!rc) rc = run_energy(e, e->d_scalar);
+        if (!rc) rc = run_backward(e, e->d_grad);
+        cudaError_t ce = cudaStreamEndCapture(cap, &g);
+        if (!rc && ce != cudaSuccess) rc = e->fail(AEGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(ce));
+    }
+    if (!rc && cudaGraphInstantiate(&e->grad_graph, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cap);
+    e->stream = saved;
+    e->graph_launches = e->launches - l0;
+    e->launches = l0;
+    cudaGetLastError();
+    return rc;
+}
+
 int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream)
 {
     if (!e || !angles_dev || !grad_dev) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    const int nops = (int)e->excs.size();
+    if (e->use_graph && !e->timing) {
+        if (!e->grad_graph) {
+            int rc = capture_grad_graph(e);
+            if (rc) return rc;
+        }
+        cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+        cudaMemcpyAsync(e->d_ang, angles_dev, nops * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (cudaGraphLaunch(e->grad_graph, st) != cudaSuccess) return e->cuda_check("graph launch");
+        e->launches += e->graph_launches;
+        if (energy_dev) cudaMemcpyAsync(energy_dev, e->d_scalar, sizeof(double), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(grad_dev, e->d_grad, nops * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        e->psi_valid = e->h_valid = false;
+        return e->cuda_check("gradient_dev");
+    }
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
     std::array<cudaEvent_t, 4> ev{};
@@ -1488,6 +1837,13 @@ int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy
     e->stream = saved;
     e->psi_valid = e->h_valid = false;
     return rc;
+}
+
+int aegpu_use_graphs(aegpu_engine *e, int enable)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    e->use_graph = enable != 0;
+    return AEGPU_OK;
 }
 
 int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, void *stream)
@@ -1695,9 +2051,10 @@ int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double 
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
-    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr);
+    int np = 0;
+    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, &np);
     if (!rc && energy_dev) {
-        k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, e->spmv_grid, energy_dev, 1.0);
+        k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0);
         e->launches += 1;
         rc = e->cuda_check("apply_dev");
     }
@@ -1735,7 +2092,8 @@ int aegpu_phase_times(aegpu_engine *e, double *ms, int64_t *count)
 
 int aegpu_problem_info(const aegpu_engine *e, int64_t *info)
 {
-    // D, nops, blocks, ham kind, ham entries, ell width, active (touched) amplitudes summed over blocks
+    // D, nops, blocks, ham kind, stored H entries, stored row width, amplitudes touched per
+    // sweep over all blocks, nonzeros of H (without row padding)
     if (!e || !info) return AEGPU_ERR_ARG;
     info[0] = (int64_t)e->B.D;
     info[1] = (int64_t)e->excs.size();
@@ -1746,6 +2104,7 @@ int aegpu_problem_info(const aegpu_engine *e, int64_t *info)
     int64_t act = 0;
     for (auto &b : e->dblocks) act += b.diagonal ? (int64_t)e->B.D : (int64_t)b.active;
     info[6] = act;
+    info[7] = e->ham_kind == 1 ? e->ham_entries : (e->ham_kind ? (int64_t)e->B.D * e->ints.width : 0);
     return AEGPU_OK;
 }
 

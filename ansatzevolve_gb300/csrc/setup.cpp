@@ -124,6 +124,29 @@ std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std:
     return out;
 }
 
+std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass)
+{
+    std::vector<Block> out;
+    for (const auto &b : blocks) {
+        const int n = (int)b.ops.size();
+        if (b.diagonal || n <= max_pass) {
+            out.push_back(b);
+            continue;
+        }
+        const int parts = (n + max_pass - 1) / max_pass;
+        int start = 0;
+        for (int p = 0; p < parts; ++p) {
+            const int len = n / parts + (p < n % parts ? 1 : 0);
+            Block c;
+            c.diagonal = false;
+            c.ops.assign(b.ops.begin() + start, b.ops.begin() + start + len);
+            start += len;
+            out.push_back(std::move(c));
+        }
+    }
+    return out;
+}
+
 OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int nthreads)
 {
     const int nb = (int)codes.size();
@@ -195,6 +218,16 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
             t.n_orbits = std::min(per_tile, g.n_orbits - o);
             t.elem_off = g.idx_off + o * osz;
             T.tiles.push_back(t);
+        }
+        if (g.k <= (uint32_t)kMaxWarpLayers) {
+            const uint32_t per_task = (uint32_t)kWarpElems / osz;
+            for (uint32_t o = 0; o < g.n_orbits; o += per_task) {
+                WarpTask w{};
+                w.group = (uint32_t)T.groups.size();
+                w.elem_off = g.idx_off + o * osz;
+                w.n = std::min(per_task, g.n_orbits - o) * osz;
+                T.wtasks.push_back(w);
+            }
         }
         T.groups.push_back(g);
         T.active += nroots * osz;

@@ -53,6 +53,10 @@ struct Block {
     std::vector<int> ops;   // operator indices (original order) in application order
 };
 
+// Cut every block into passes of at most max_pass excitations (commuting, so any
+// cut gives the same product); orbits of a pass then have at most 2^max_pass members.
+std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass);
+
 // Greedy commuting-block grouping with forward moves, restating
 // FusedEvolve::regenCache (fusedevolve.cpp:1797-1967): a block grows while the next
 // operator commutes with all members (diagonal only with diagonal); later operators
@@ -91,10 +95,24 @@ struct OrbitTile {
     uint32_t elem_off;   // first entry in the block's rank list
 };
 
+// A warp task is a run of whole orbits of one group with at most 64 members (the
+// orbits of a pass of <= 6 excitations): one warp holds it in registers, two
+// amplitudes per lane, and runs every butterfly layer with shuffles.
+constexpr int kWarpElems = 64;
+constexpr int kMaxWarpLayers = 6;
+
+struct WarpTask {
+    uint32_t group;
+    uint32_t elem_off;   // first entry in the block's rank list
+    uint32_t n;          // members (<= 64)
+    uint32_t pad;
+};
+
 struct OrbitTables {
     std::vector<uint32_t> idx;        // ranks, grouped / ordered as described
     std::vector<OrbitGroup> groups;
     std::vector<OrbitTile> tiles;
+    std::vector<WarpTask> wtasks;     // only when every orbit has <= 64 members
     uint64_t active = 0;              // number of determinants touched by the block
     bool ok = true;                   // false if an excitation leaves the sector
 };

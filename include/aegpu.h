@@ -87,6 +87,9 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y);
  * grad_dev[nops].  Enqueued on `stream`; nothing is synchronised. */
 int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream);
 int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, void *stream);
+/* aegpu_gradient_dev replays one captured CUDA graph of the whole evaluation
+ * (default; phase timing uses the stream path instead).  enable = 0 disables it. */
+int aegpu_use_graphs(aegpu_engine *e, int enable);
 /* y_dev = H x_dev on device vectors; energy_dev (nullable) receives <x|H x>. */
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 /* CUDA-event timing of the phases of aegpu_gradient_dev (evolve, H*psi + energy,
@@ -94,8 +97,8 @@ int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double 
  * evaluations) -- reading resets the accumulators. */
 int aegpu_phase_timing(aegpu_engine *e, int enable);
 int aegpu_phase_times(aegpu_engine *e, double *ms3, int64_t *count);
-/* info[7]: D, operators, fused blocks, Hamiltonian kind, stored H entries, ELL width,
- * amplitudes touched per full sweep over all blocks. */
+/* info[8]: D, operators, fused blocks, Hamiltonian kind, stored H entries, stored row
+ * width (padded), amplitudes touched per sweep over all blocks, nonzeros of H. */
 int aegpu_problem_info(const aegpu_engine *e, int64_t *info);
 /* Device pointers of the current state and of H*state (D or 2D doubles). */
 int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi);
