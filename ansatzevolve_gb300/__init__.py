@@ -69,6 +69,7 @@ def lib(build_if_missing=True):
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64)]),
         "aegpu_apply_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
         "aegpu_use_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
+        "aegpu_csr_energy_noalloc": (ctypes.c_int, [i64, _P, _P, _P, _P, _P, _P, _P]),
         "aegpu_phase_timing": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
         "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),

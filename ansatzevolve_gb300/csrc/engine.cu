@@ -43,6 +43,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1435,6 +1436,23 @@ int stream_sync(aegpu_engine *e, const char *where)
 
 }  // namespace
 
+// ------------------------------------------------- allocation-free H * x --
+// For callers that cannot allocate device memory: the entry point
+// aegpu_csr_energy_noalloc keeps the per-block partial sums of <x|H x> in this
+// fixed device array instead of engine-owned scratch.  Every device that loads the
+// library holds it until the process exits.  One partial sum per 256-row block:
+// at most kNoAllocMaxPartials blocks, i.e. kNoAllocMaxRows rows.
+constexpr int kNoAllocMaxPartials = 16384;
+constexpr int64_t kNoAllocRowsPerPartial = 256;
+constexpr int64_t kNoAllocMaxRows = kNoAllocMaxPartials * kNoAllocRowsPerPartial;  // 4,194,304
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxPartials];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+double *g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+}  // namespace
+
 // ==================================================================== C ABI ==
 extern "C" {
 
@@ -2110,5 +2128,45 @@ int aegpu_problem_info(const aegpu_engine *e, int64_t *info)
 
 int64_t aegpu_device_bytes(const aegpu_engine *e) { return e ? e->dev_bytes : -1; }
 int64_t aegpu_launch_count(const aegpu_engine *e) { return e ? e->launches : -1; }
+
+// No counterpart in the reference (see include/aegpu.h for the contract).
+int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t *col_dev, const double *val_dev,
+                             const double *x_dev, double *y_dev, double *energy_dev, void *stream)
+{
+    if (D < 1 || !rowptr_dev || !col_dev || !val_dev || !x_dev || !y_dev || !energy_dev) return AEGPU_ERR_ARG;
+    if (D > kNoAllocMaxRows) {
+        fprintf(stderr, "aegpu_csr_energy_noalloc: %lld rows exceed the fixed scratch limit of %lld rows\n",
+                (long long)D, (long long)kNoAllocMaxRows);
+        return AEGPU_ERR_TOO_LARGE;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        cudaGetLastError();
+        return AEGPU_ERR_CUDA;
+    }
+    double *scratch = nullptr;
+    {
+        // first call on this device: resolve the array's device address (host code may
+        // not use the symbol itself); this set-up must happen outside any stream capture
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return AEGPU_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = (double *)p;
+        }
+        scratch = g_noalloc_addr[dev];
+    }
+    // every partial sum the reduction reads is written by this call first, so the
+    // array needs no clearing between calls
+    const int grid = (int)((D + kNoAllocRowsPerPartial - 1) / kNoAllocRowsPerPartial);
+    cudaStream_t s = (cudaStream_t)stream;
+    k_spmv<1, false><<<grid, kSpmvThreads, 0, s>>>(rowptr_dev, 0, col_dev, val_dev, x_dev, y_dev, D, scratch);
+    k_reduce_sum<<<1, 256, 0, s>>>(scratch, grid, energy_dev, 1.0);
+    const cudaError_t rc = cudaGetLastError();
+    return rc == cudaSuccess ? AEGPU_OK : AEGPU_ERR_CUDA;
+}
 
 }  // extern "C"

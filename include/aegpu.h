@@ -32,6 +32,7 @@ extern "C" {
 #define AEGPU_ERR_CUDA 3         /* CUDA runtime failure (message in aegpu_last_error) */
 #define AEGPU_ERR_NOMEM 4        /* device allocation failed */
 #define AEGPU_ERR_UNSUPPORTED 5  /* input outside what the engine implements */
+#define AEGPU_ERR_TOO_LARGE 6    /* input larger than a fixed-size buffer allows */
 
 #define AEGPU_BASIS_FULL 0
 #define AEGPU_BASIS_NUMBER 1
@@ -111,6 +112,26 @@ int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi);
 int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *block_sizes, int *n_blocks);
 int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int nops, const int *ops,
                       uint32_t *idx, int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles);
+
+/* Allocation-free H * x (no counterpart in the reference).
+ * For callers that cannot allocate device memory at all -- code running inside a
+ * CUDA memory-pool or allocator callback, a library whose device memory is owned and
+ * budgeted by a host framework, or a context with no free memory left -- this entry
+ * point computes y = H x and <x|H x> for a sector CSR matrix that the caller already
+ * holds in device memory (rowptr[D+1], col[nnz], val[nnz]; row = output), without any
+ * cudaMalloc, cudaFree or allocating library call.  Its only scratch (one partial sum
+ * per 256 rows) lives in a fixed 128 KiB device array that every GPU loading this
+ * library keeps until the process exits, so D is limited to 4,194,304 rows; larger
+ * inputs return AEGPU_ERR_TOO_LARGE (and print why) without launching anything.
+ * The first call on a device looks up that array's device address with the device
+ * current; make that first call before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (different streams, or host threads, without
+ * ordering between them) race and give wrong sums; calls ordered on one stream are
+ * safe.  Nothing needs clearing between calls -- each call writes every partial sum
+ * it reads.  x, y, energy are device pointers; stream is a cudaStream_t (NULL = the
+ * default stream).  The work is enqueued, not synchronised. */
+int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t *col_dev, const double *val_dev,
+                             const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 
 /* Bytes of HBM held by the engine, and kernel launches issued since creation. */
 int64_t aegpu_device_bytes(const aegpu_engine *e);
