@@ -12,12 +12,14 @@
 //                      and H*tangents in [D][W][P+1] layout
 //
 // Kernels (all FP64; bandwidth- or FP64-pipe-bound, no tensor cores):
-//   k_block_rot      one fused block of commuting excitations on 1..n vectors; a CTA
-//                    stages whole orbits (<= 4096 amplitudes) in shared memory and
-//                    applies every butterfly layer there (reference RunFuseN,
-//                    fusedevolve.cpp:917-1774)
-//   k_block_bwd      the adjoint sweep of one block on (psi, H psi) with the gradient
-//                    partial sums of every excitation (fusedevolve.cpp:461-485)
+//   k_block_rot      one pass on many vectors at once (Hessian tangents); a CTA stages
+//                    whole orbits (<= 4096 amplitudes) in shared memory and applies
+//                    every butterfly layer there (reference RunFuseN, fusedevolve.cpp:917-1774)
+//   k_warp_rot       a pass of <= 6 commuting excitations with the orbits in warp
+//                    registers (shuffles, one FMA per amplitude per layer); writes the
+//                    pass's output amplitudes as the adjoint sweep's checkpoint
+//   k_warp_adj       checkpointed adjoint pass: gradient of every excitation from the
+//                    checkpoint and H psi, then H psi rotated back (fusedevolve.cpp:461-485)
 //   k_block_tangent  forward block + tangents T_op = G_op psi (fusedevolve.cpp:492-518)
 //   k_block_hess     backward sweep of many tangents against H psi for the second-
 //                    derivative term of the Hessian (fusedevolve.cpp:2670-2761)
@@ -27,11 +29,13 @@
 //   k_spmm_*         H on P+1 vectors at once for the Hessian (matrix read once)
 //   k_ell_build      fixed-width rows of H generated from h_pq/(pq|rs): diagonal,
 //                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
-//   k_otf_apply      y = H x with the rows regenerated on the fly (no stored matrix)
+//   k_otf_strings    y = H x with no stored matrix: CTA per alpha string, thread per
+//                    determinant, one FP64 FMA per matrix element (otf_tables.cpp)
 // All reductions are two-stage and in a fixed order, so results are bit-identical
 // from run to run.
 #include "../../include/aegpu.h"
 #include "exc_rule.h"
+#include "otf_tables.h"
 #include "setup.h"
 
 #include <cublas_v2.h>
@@ -250,55 +254,6 @@ __global__ void __launch_bounds__(kRotThreads) k_block_rot(BlockArgs a, double *
     }
 }
 
-// Adjoint sweep of one block: rotates psi and h = H psi by -theta and accumulates
-// g_slot += s (h_x y - h_y x) with the values before each layer (fusedevolve.cpp:470-483).
-template <int W>
-__global__ void __launch_bounds__(kRotThreads) k_block_bwd(BlockArgs a, double *psi, double *h, double *partials)
-{
-    extern __shared__ double sm[];
-    double *v = sm, *hv = sm + kTileElems * W;
-    uint32_t *bits = (uint32_t *)(sm + 2 * kTileElems * W);
-    __shared__ ExcCode code[kMaxSlots];
-    __shared__ double C[kMaxSlots], S[kMaxSlots];
-    __shared__ int slot[kMaxSlots];
-    __shared__ double red[kRotThreads / 32];
-    __shared__ double acc[kMaxSlots];
-    if (threadIdx.x < kMaxSlots) acc[threadIdx.x] = 0;
-    const TileCtx c = load_tile(a, bits, code, C, S, slot);
-    gather<W>(v, psi, c);
-    gather<W>(hv, h, c);
-    __syncthreads();
-    for (int i = 0; i < c.k; ++i) {
-        const uint32_t half = c.n >> 1;
-        const double Ci = C[i], Si = S[i];
-        double g = 0;
-        for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
-            const uint32_t lo = insert_zero_bit(p, i), hi = lo | (1u << i);
-            const double s = exc_sign(code[i], bits[lo]);
-            const double sS = s * Si;
-            double t = 0;
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const double x = v[lo * W + w], y = v[hi * W + w];
-                const double hx = hv[lo * W + w], hy = hv[hi * W + w];
-                t = fma(hx, y, t);
-                t = fma(-hy, x, t);
-                v[lo * W + w] = fma(sS, y, Ci * x);
-                v[hi * W + w] = fma(-sS, x, Ci * y);
-                hv[lo * W + w] = fma(sS, hy, Ci * hx);
-                hv[hi * W + w] = fma(-sS, hx, Ci * hy);
-            }
-            g = fma(s, t, g);
-        }
-        g = block_sum(g, red);
-        if (threadIdx.x == 0) acc[slot[i]] = g;
-        __syncthreads();
-    }
-    scatter<W>(v, psi, c);
-    scatter<W>(hv, h, c);
-    if (threadIdx.x < kMaxSlots) partials[(size_t)blockIdx.x * kMaxSlots + threadIdx.x] = acc[threadIdx.x];
-}
-
 // Forward block that also writes the tangents T_slot = G_slot psi (after the block,
 // which equals G psi before it because the block's excitations commute).
 template <int W>
@@ -421,9 +376,38 @@ __device__ __forceinline__ double flip(double x, int s)
     return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)(s < 0) << 63));
 }
 
+// One DFMA whatever the form: the operands are chosen with integer selects, so the
+// compiler cannot evaluate both forms on the FP64 pipe.
 __device__ __forceinline__ double rot_scaled(const PassConst &q, double v, double vp, int s)
 {
-    return q.tan_form ? fma(flip(q.m, s), vp, v) : fma(q.m, v, flip(vp, s));
+    const double a = q.tan_form ? flip(q.m, s) : q.m;
+    const double b = q.tan_form ? vp : v;
+    const double c = q.tan_form ? v : flip(vp, s);
+    return fma(a, b, c);
+}
+
+// Per-CTA tables over the <= 64 active masks of a pass: sigma[m] = product of the
+// layer scales of m, pre2[m][j] = squared product of the scales of the layers of m
+// applied before layer j.  Keeps those products off the per-amplitude FP64 path.
+struct PassTables {
+    double sigma[1 << kMaxWarpLayers];
+    double pre2[1 << kMaxWarpLayers][kMaxWarpLayers];
+};
+
+__device__ __forceinline__ void pass_tables(const PassConst *pc, int nslots, PassTables *t)
+{
+    for (int m = threadIdx.x; m < (1 << nslots); m += blockDim.x) {
+        double sg = 1.0, s2 = 1.0;
+        for (int j = 0; j < nslots; ++j) {
+            t->pre2[m][j] = s2;
+            if (m & (1 << j)) {
+                sg *= pc[j].f;
+                s2 *= pc[j].f2;
+            }
+        }
+        t->sigma[m] = sg;
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ void pass_consts(const BlockArgs &a, PassConst *pc)
@@ -448,12 +432,17 @@ __device__ __forceinline__ void pass_consts(const BlockArgs &a, PassConst *pc)
     __syncthreads();
 }
 
+// ckpt (nullable, single vector only): the pass's amplitudes after rotation, stored in
+// the pass's orbit order (same index as the rank list), for the adjoint sweep.
 template <int W>
 __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
-                                                           double *vecs, size_t vstride, int nvec)
+                                                           double *vecs, size_t vstride, int nvec,
+                                                           double *__restrict__ ckpt)
 {
     __shared__ PassConst pc[kMaxWarpLayers];
+    __shared__ PassTables tab;
     pass_consts(a, pc);
+    pass_tables(pc, a.nslots, &tab);
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
@@ -463,10 +452,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
         const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
-        double sigma = 1.0;
-#pragma unroll
-        for (int j = 0; j < kMaxWarpLayers; ++j)
-            if (mask & (1u << j)) sigma *= pc[j].f;
+        const double sigma = tab.sigma[mask];
         for (int vec = 0; vec < nvec; ++vec) {
             double *psi = vecs + vec * vstride;
             double v0[W], v1[W];
@@ -497,21 +483,35 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
             }
 #pragma unroll
             for (int w = 0; w < W; ++w) {
-                if (ok0) psi[(size_t)z0 * W + w] = sigma * v0[w];
-                if (ok1) psi[(size_t)z1 * W + w] = sigma * v1[w];
+                const double t0 = sigma * v0[w], t1 = sigma * v1[w];
+                if (ok0) psi[(size_t)z0 * W + w] = t0;
+                if (ok1) psi[(size_t)z1 * W + w] = t1;
+                if (ckpt) {
+                    if (ok0) ckpt[((size_t)task.elem_off + lane) * W + w] = t0;
+                    if (ok1) ckpt[((size_t)task.elem_off + lane + 32) * W + w] = t1;
+                }
             }
         }
     }
 }
 
+// Checkpointed adjoint pass.  psi after this pass comes from the forward sweep's
+// checkpoint (orbit order, coalesced), h = H psi back-propagated to the same point is
+// gathered; since every excitation of the pass commutes with the others, the gradient
+// of excitation j is <h|G_j psi> evaluated right there: sum_z h_z s_j(z) psi_p(z),
+// one FP64 FMA per amplitude and layer.  Only h is then rotated back (-theta) through
+// the pass, again one FMA per amplitude and layer, and scattered.  psi is not touched.
 template <int W>
-__global__ void __launch_bounds__(kWarpThreads) k_warp_bwd(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
-                                                           double *psi, double *h, double *partials)
+__global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
+                                                           const double *__restrict__ ckpt, double *h,
+                                                           double *partials)
 {
     __shared__ PassConst pc[kMaxWarpLayers];
-    __shared__ double red[kWarpThreads / 32][kMaxWarpLayers];
+    __shared__ PassTables tab;
+    __shared__ double red[kMaxWarpLayers][kWarpThreads];
     pass_consts(a, pc);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    pass_tables(pc, a.nslots, &tab);
+    const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double accS[kMaxWarpLayers];
 #pragma unroll
@@ -523,69 +523,72 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_bwd(BlockArgs a, const Wa
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
         const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
+        const double *cp = ckpt + (size_t)task.elem_off * W;
         double v0[W], v1[W], h0[W], h1[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
-            v0[w] = ok0 ? psi[(size_t)z0 * W + w] : 0.0;
-            v1[w] = ok1 ? psi[(size_t)z1 * W + w] : 0.0;
+            v0[w] = ok0 ? cp[lane * W + w] : 0.0;
+            v1[w] = ok1 ? cp[(lane + 32) * W + w] : 0.0;
             h0[w] = ok0 ? h[(size_t)z0 * W + w] : 0.0;
             h1[w] = ok1 ? h[(size_t)z1 * W + w] : 0.0;
         }
-        double sig2 = 1.0, sigma = 1.0;  // stored = true / sigma
+        // gradient terms at the pass's output point
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j) {
+            if (!(mask & (1u << j))) continue;
+            const int i = __popc(mask & ((1u << j) - 1u));
+            const int s0 = exc_sign(pc[j].code, b0), s1 = exc_sign(pc[j].code, b1);
+            double g = 0.0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double p0, p1;
+                if (i < 5) {
+                    p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                    p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                } else {
+                    p0 = v1[w];
+                    p1 = v0[w];
+                }
+                g = fma(h0[w], flip(p0, s0), g);
+                g = fma(h1[w], flip(p1, s1), g);
+            }
+            accS[j] += g;
+        }
+        // h back through the pass (scaled form, one FMA per amplitude and layer)
 #pragma unroll
         for (int j = 0; j < kMaxWarpLayers; ++j) {
             if (!(mask & (1u << j))) continue;
             const int i = __popc(mask & ((1u << j) - 1u));
             const PassConst &q = pc[j];
             const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
-            double g = 0.0;
 #pragma unroll
             for (int w = 0; w < W; ++w) {
-                double pv0, pv1, ph0, ph1;
+                double p0, p1;
                 if (i < 5) {
-                    pv0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
-                    pv1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
-                    ph0 = __shfl_xor_sync(0xffffffffu, h0[w], 1 << i);
-                    ph1 = __shfl_xor_sync(0xffffffffu, h1[w], 1 << i);
+                    p0 = __shfl_xor_sync(0xffffffffu, h0[w], 1 << i);
+                    p1 = __shfl_xor_sync(0xffffffffu, h1[w], 1 << i);
                 } else {
-                    pv0 = v1[w];
-                    pv1 = v0[w];
-                    ph0 = h1[w];
-                    ph1 = h0[w];
+                    p0 = h1[w];
+                    p1 = h0[w];
                 }
-                g = fma(h0[w], flip(pv0, s0), g);
-                g = fma(h1[w], flip(pv1, s1), g);
-                v0[w] = rot_scaled(q, v0[w], pv0, s0);
-                v1[w] = rot_scaled(q, v1[w], pv1, s1);
-                h0[w] = rot_scaled(q, h0[w], ph0, s0);
-                h1[w] = rot_scaled(q, h1[w], ph1, s1);
+                h0[w] = rot_scaled(q, h0[w], p0, s0);
+                h1[w] = rot_scaled(q, h1[w], p1, s1);
             }
-            accS[j] = fma(g, sig2, accS[j]);
-            sig2 *= q.f2;
-            sigma *= q.f;
         }
+        const double sigma = tab.sigma[mask];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
-            if (ok0) {
-                psi[(size_t)z0 * W + w] = sigma * v0[w];
-                h[(size_t)z0 * W + w] = sigma * h0[w];
-            }
-            if (ok1) {
-                psi[(size_t)z1 * W + w] = sigma * v1[w];
-                h[(size_t)z1 * W + w] = sigma * h1[w];
-            }
+            if (ok0) h[(size_t)z0 * W + w] = sigma * h0[w];
+            if (ok1) h[(size_t)z1 * W + w] = sigma * h1[w];
         }
     }
 #pragma unroll
-    for (int j = 0; j < kMaxWarpLayers; ++j) {
-        const double v = warp_sum(accS[j]);
-        if (lane == 0) red[warp][j] = v;
-    }
+    for (int j = 0; j < kMaxWarpLayers; ++j) red[j][threadIdx.x] = accS[j];
     __syncthreads();
     if (threadIdx.x < kMaxSlots) {
         double s = 0.0;
         if (threadIdx.x < kMaxWarpLayers)
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+            for (int w = 0; w < (int)blockDim.x; ++w) s += red[threadIdx.x][w];
         partials[(size_t)blockIdx.x * kMaxSlots + threadIdx.x] = s;
     }
 }
@@ -626,7 +629,8 @@ __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
     return m;
 }
 
-__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec)
+// ckpt (nullable, single vector): the amplitudes after the pass, for the adjoint sweep.
+__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, double *__restrict__ ckpt)
 {
     const uint64_t D = a.basis.D;
     for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
@@ -638,11 +642,18 @@ __global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec)
             const double re = p[0], im = p[1];
             p[0] = c * re - s * im;
             p[1] = s * re + c * im;
+            if (ckpt) {
+                ckpt[2 * z] = p[0];
+                ckpt[2 * z + 1] = p[1];
+            }
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_diag_bwd(DiagArgs a, double *psi, double *h, double *partials)
+// Checkpointed adjoint of a diagonal pass: gradient <h|i n psi> at the pass output
+// (psi from the checkpoint), then h rotated back; psi untouched.
+__global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__restrict__ ckpt, double *h,
+                                                  double *partials)
 {
     __shared__ double red[8];
     double acc[kMaxSlots];
@@ -652,15 +663,13 @@ __global__ void __launch_bounds__(256) k_diag_bwd(DiagArgs a, double *psi, doubl
     for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
         if (!m) continue;
-        double *x = psi + 2 * z, *y = h + 2 * z;
-        const double xr = x[0], xi = x[1], hr = y[0], hi = y[1];
+        double *y = h + 2 * z;
+        const double xr = ckpt[2 * z], xi = ckpt[2 * z + 1], hr = y[0], hi = y[1];
         const double q = hi * xr - hr * xi;
 #pragma unroll
         for (int i = 0; i < kMaxSlots; ++i)
             if (m & (1u << i)) acc[i] += q;
         const double c = a.table[2 * m], s = a.table[2 * m + 1];
-        x[0] = c * xr - s * xi;
-        x[1] = s * xr + c * xi;
         y[0] = c * hr - s * hi;
         y[1] = s * hr + c * hi;
     }
@@ -1048,41 +1057,137 @@ __global__ void k_ell_build(IntArgs a, int32_t *__restrict__ col, double *__rest
     }
 }
 
-// y = H x with rows regenerated on the fly (no stored matrix), fused with <x|y>.
-template <int W>
-__global__ void __launch_bounds__(kSpmvThreads) k_otf_apply(IntArgs a, const double *__restrict__ x,
-                                                            double *__restrict__ y, double *__restrict__ epart)
+// Diagonal of H, one thread per determinant (setup of the on-the-fly path).
+__global__ void k_diag_build(IntArgs a, double *__restrict__ diag)
 {
-    __shared__ double red[kSpmvThreads / 32];
-    const int lane = threadIdx.x & 31;
-    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    const int64_t D = a.basis.D;
+    const int64_t D = (int64_t)a.basis.D;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < D; r += (int64_t)gridDim.x * blockDim.x)
+        diag[r] = diag_val(a, a.basis.bits((uint32_t)r));
+}
+
+// ------------------------------------------------- H * psi on the fly (strings) --
+// One CTA per (alpha string, chunk of beta strings), one thread per determinant.
+// Every matrix element costs one FP64 FMA: the alpha string's excitation lists,
+// their values and the alpha-beta integral slices of its singles sit in shared
+// memory; the beta string's lists come from the precomputed tables (otf_tables.cpp).
+// x reads: alpha excitations hit contiguous rows of x across the CTA (coalesced),
+// beta excitations stay inside the CTA's own row of x.  Fused with <x|y>.
+struct OtfArgs {
+    int N, P2, nA, nB;
+    int nsa, nda, nsb, ndb;
+    const int32_t *sa_rank, *sa_code, *da_rank, *da_code;
+    const int32_t *sb_rank, *sb_code, *db_rank, *db_code;
+    const double *vss, *vab, *a_alpha, *b_alpha, *a_beta, *b_beta, *diag;
+};
+
+__host__ __device__ inline size_t otf_smem_bytes(int N, int P2, int nsa, int nda)
+{
+    return sizeof(double) * ((size_t)P2 * P2 + (size_t)nsa * N * N + nsa + nda) + sizeof(int32_t) * (2 * (size_t)nsa + nda);
+}
+
+__device__ __forceinline__ double flipc(double v, int32_t code)
+{
+    return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)((uint32_t)code >> 31) << 63));
+}
+
+template <int W>
+__global__ void __launch_bounds__(512) k_otf_strings(OtfArgs a, const double *__restrict__ x, double *__restrict__ y,
+                                                     double *__restrict__ epart)
+{
+    extern __shared__ double sm[];
+    __shared__ double red[16];
+    const int N = a.N, NN = a.N * a.N, nsa = a.nsa, nda = a.nda;
+    const int ra = blockIdx.x;
+    double *vss = sm;
+    double *vsl = vss + (size_t)a.P2 * a.P2;
+    double *sa_val = vsl + (size_t)nsa * NN;
+    double *da_val = sa_val + nsa;
+    int32_t *sa_rank = (int32_t *)(da_val + nda);
+    int32_t *sa_code = sa_rank + nsa;
+    int32_t *da_rank = sa_code + nsa;
+    for (int i = threadIdx.x; i < a.P2 * a.P2; i += blockDim.x) vss[i] = a.vss[i];
+    for (int i = threadIdx.x; i < nsa; i += blockDim.x) {
+        const int32_t code = a.sa_code[(size_t)ra * nsa + i];
+        sa_rank[i] = a.sa_rank[(size_t)ra * nsa + i];
+        sa_code[i] = code;
+        sa_val[i] = a.a_alpha[(size_t)ra * NN + (code & 31) * N + ((code >> 5) & 31)];
+    }
+    for (int i = threadIdx.x; i < nsa * NN; i += blockDim.x) {
+        const int sidx = i / NN, k = i - sidx * NN;
+        const int32_t code = a.sa_code[(size_t)ra * nsa + sidx];
+        vsl[i] = a.vab[((size_t)((code & 31) * N + ((code >> 5) & 31))) * NN + k];
+    }
+    for (int i = threadIdx.x; i < nda; i += blockDim.x) {
+        const int32_t code = a.da_code[(size_t)ra * nda + i];
+        da_rank[i] = a.da_rank[(size_t)ra * nda + i];
+        da_val[i] = flipc(a.vss[code & 0x7fffffff], code);
+    }
+    __syncthreads();
+    const int nB = a.nB;
+    const int rb = blockIdx.y * blockDim.x + threadIdx.x;
     double en = 0;
-    for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < D; r += warps) {
-        const uint32_t J = a.basis.bits((uint32_t)r);
+    if (rb < nB) {
+        const size_t row = (size_t)ra * nB + rb;
+        const double dg = a.diag[row];
         double acc[W];
 #pragma unroll
-        for (int w = 0; w < W; ++w) acc[w] = 0;
-        for (int64_t e = lane; e < a.width; e += 32) {
-            uint32_t I;
-            double v;
-            row_entry(a, J, e, I, v);
-            const size_t c = (size_t)a.basis.rank_of(I);
+        for (int w = 0; w < W; ++w) acc[w] = dg * x[row * W + w];
+        // alpha singles: sign * (A_alpha[ra] + B_alpha[rb])
+        const double *bal = a.b_alpha + (size_t)rb * NN;
+        for (int s = 0; s < nsa; ++s) {
+            const int32_t code = sa_code[s];
+            const double v = flipc(sa_val[s] + bal[(code & 31) * N + ((code >> 5) & 31)], code);
+            const size_t c = (size_t)sa_rank[s] * nB + rb;
 #pragma unroll
-            for (int w = 0; w < W; ++w) acc[w] = fma(v, __ldg(x + c * W + w), acc[w]);
+            for (int w = 0; w < W; ++w) acc[w] = fma(v, x[c * W + w], acc[w]);
+        }
+        // alpha-alpha doubles
+        for (int d = 0; d < nda; ++d) {
+            const size_t c = (size_t)da_rank[d] * nB + rb;
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] = fma(da_val[d], x[c * W + w], acc[w]);
+        }
+        const size_t rowA = (size_t)ra * nB;
+        const int32_t *sbr = a.sb_rank + (size_t)rb * a.nsb, *sbc = a.sb_code + (size_t)rb * a.nsb;
+        const double *abe = a.a_beta + (size_t)rb * NN, *bbe = a.b_beta + (size_t)ra * NN;
+        // beta singles: sign * (A_beta[rb] + B_beta[ra])
+        for (int t = 0; t < a.nsb; ++t) {
+            const int32_t code = sbc[t];
+            const int k = (code & 31) * N + ((code >> 5) & 31);
+            const double v = flipc(abe[k] + bbe[k], code);
+            const size_t c = rowA + sbr[t];
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] = fma(v, x[c * W + w], acc[w]);
+        }
+        // beta-beta doubles
+        const int32_t *dbr = a.db_rank + (size_t)rb * a.ndb, *dbc = a.db_code + (size_t)rb * a.ndb;
+        for (int d = 0; d < a.ndb; ++d) {
+            const int32_t code = dbc[d];
+            const double v = flipc(vss[code & 0x7fffffff], code);
+            const size_t c = rowA + dbr[d];
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[w] = fma(v, x[c * W + w], acc[w]);
+        }
+        // alpha-beta doubles: (pa ra|pb rb), sign = product of the two single signs
+        for (int t = 0; t < a.nsb; ++t) {
+            const int32_t tc = sbc[t];
+            const int kb = (tc & 31) * N + ((tc >> 5) & 31);
+            const size_t ct = (size_t)sbr[t];
+            for (int s = 0; s < nsa; ++s) {
+                const double v = flipc(vsl[s * NN + kb], sa_code[s] ^ tc);
+                const size_t c = (size_t)sa_rank[s] * nB + ct;
+#pragma unroll
+                for (int w = 0; w < W; ++w) acc[w] = fma(v, x[c * W + w], acc[w]);
+            }
         }
 #pragma unroll
-        for (int w = 0; w < W; ++w) acc[w] = warp_sum(acc[w]);
-        if (lane == 0) {
-#pragma unroll
-            for (int w = 0; w < W; ++w) {
-                y[r * W + w] = acc[w];
-                en = fma(acc[w], x[r * W + w], en);
-            }
+        for (int w = 0; w < W; ++w) {
+            y[row * W + w] = acc[w];
+            en = fma(acc[w], x[row * W + w], en);
         }
     }
     en = block_sum(en, red);
-    if (threadIdx.x == 0 && epart) epart[blockIdx.x] = en;
+    if (threadIdx.x == 0 && epart) epart[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = en;
 }
 
 // ------------------------------------------------------------------ host --
@@ -1128,6 +1233,7 @@ struct aegpu_engine {
         int wgrid = 0;            // CTAs of the warp kernels; also partial-sum rows
         WarpTask *wtasks = nullptr;
         int64_t part_off = 0;     // offset of this block's gradient partials
+        int64_t ckpt_off = 0;     // offset (doubles) of this pass's checkpoint
         uint32_t *idx = nullptr;
         OrbitGroup *groups = nullptr;
         OrbitTile *tiles = nullptr;
@@ -1148,6 +1254,7 @@ struct aegpu_engine {
     double *d_ang = nullptr, *d_sc = nullptr, *d_diag_table = nullptr;
     double *d_start = nullptr, *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
     double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
+    double *d_ckpt = nullptr;  // per pass: amplitudes after the pass (adjoint sweep input)
     int64_t n_partials = 0;
     int spmv_grid = 0;
 
@@ -1160,6 +1267,8 @@ struct aegpu_engine {
     IntArgs ints{};
     double *d_h1 = nullptr, *d_g2 = nullptr;
     int ell_width = 0;
+    OtfArgs otf{};
+    int otf_threads = 0, otf_chunks = 0;
 
     // optional CUDA-event timing of the phases of *_dev evaluations
     bool timing = false;
@@ -1298,10 +1407,15 @@ int set_smem_limits(int dev)
     bad += set_smem(k_block_rot<2>, need(1, 2), optin);
     bad += set_smem(k_block_tangent<1>, need(1, 1), optin);
     bad += set_smem(k_block_tangent<2>, need(1, 2), optin);
-    bad += set_smem(k_block_bwd<1>, need(2, 1), optin);
-    bad += set_smem(k_block_bwd<2>, need(2, 2), optin);
     bad += set_smem(k_block_hess<1>, need(3, 1), optin);
     bad += set_smem(k_block_hess<2>, need(3, 2), optin);
+    // the on-the-fly kernel's need depends on N (<= 150 KB at 14 orbitals): allow the most
+    for (int W = 1; W <= 2; ++W) {
+        cudaFuncAttributes fa{};
+        auto kern = W == 1 ? (const void *)k_otf_strings<1> : (const void *)k_otf_strings<2>;
+        if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess)
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    }
     cudaGetLastError();
     return bad;
 }
@@ -1315,14 +1429,15 @@ int run_evolve(aegpu_engine *e)
         if (b.diagonal) {
             k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, 1.0,
                                                                               e->d_diag_table);
-            k_diag_rot<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1);
+            k_diag_rot<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1, e->d_ckpt + b.ckpt_off);
             e->launches += 2;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(b, 1.0);
+            double *ck = e->d_ckpt + b.ckpt_off;
             if (e->W == 1)
-                k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1);
+                k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1, ck);
             else
-                k_warp_rot<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1);
+                k_warp_rot<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1, ck);
             e->launches += 1;
         }
     }
@@ -1359,10 +1474,13 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int *n
             k_spmv_sell<2><<<sg, kSpmvThreads, 0, e->stream>>>(e->ell_width >> 2, e->d_col, e->d_val, x, y, D, epart);
         if (nparts) *nparts = sg;
     } else if (e->ham_kind == 3) {
+        dim3 g(e->otf.nA, e->otf_chunks);
+        const size_t smem = otf_smem_bytes(e->otf.N, e->otf.P2, e->otf.nsa, e->otf.nda);
         if (e->W == 1)
-            k_otf_apply<1><<<grid, kSpmvThreads, 0, e->stream>>>(e->ints, x, y, epart);
+            k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(e->otf, x, y, epart);
         else
-            k_otf_apply<2><<<grid, kSpmvThreads, 0, e->stream>>>(e->ints, x, y, epart);
+            k_otf_strings<2><<<g, e->otf_threads, smem, e->stream>>>(e->otf, x, y, epart);
+        if (nparts) *nparts = e->otf.nA * e->otf_chunks;
     } else {
         return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     }
@@ -1389,14 +1507,15 @@ int run_backward(aegpu_engine *e, double *grad_dev)
         if (b.diagonal) {
             k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, -1.0,
                                                                               e->d_diag_table);
-            k_diag_bwd<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, e->d_h, part);
+            k_diag_adj<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_ckpt + b.ckpt_off, e->d_h, part);
             e->launches += 2;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(b, -1.0);
+            const double *ck = e->d_ckpt + b.ckpt_off;
             if (e->W == 1)
-                k_warp_bwd<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, e->d_h, part);
+                k_warp_adj<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->d_h, part);
             else
-                k_warp_bwd<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, e->d_h, part);
+                k_warp_adj<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->d_h, part);
             e->launches += 1;
         } else {
             cudaMemsetAsync(part, 0, (size_t)b.wgrid * kMaxSlots * sizeof(double), e->stream);
@@ -1555,7 +1674,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->block_pos0.clear();
     e->op_block.assign(nops, 0);
     e->op_slot.assign(nops, 0);
-    int64_t part_off = 0;
+    int64_t part_off = 0, ckpt_off = 0;
     int pos = 0;
     for (size_t bi = 0; bi < e->blocks.size(); ++bi) {
         const Block &b = e->blocks[bi];
@@ -1588,6 +1707,8 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
         }
         d.part_off = part_off;
         part_off += (int64_t)d.wgrid * kMaxSlots;
+        d.ckpt_off = ckpt_off;
+        ckpt_off += (int64_t)(d.diagonal ? e->B.D : d.active) * (e->cplx ? 2 : 1);
         e->dblocks.push_back(d);
     }
     e->n_partials = part_off;
@@ -1617,7 +1738,8 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->d_epart = e->alloc<double>(std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D + kSpmvThreads - 1) / kSpmvThreads));
     e->d_scalar = e->alloc<double>(4);
     e->d_grad = e->alloc<double>(nops);
-    if (!e->d_tmp || !e->d_partials || !e->d_grad) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
+    e->d_ckpt = e->alloc<double>(std::max<int64_t>(ckpt_off, 1));
+    if (!e->d_tmp || !e->d_partials || !e->d_grad || !e->d_ckpt) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
     cudaMemset(e->d_start, 0, n * sizeof(double));
     e->psi_valid = e->h_valid = false;
     // setup copies ran on the legacy stream: finish them before any engine-stream work
@@ -1725,6 +1847,52 @@ int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2,
         e->ham_kind = 2;
         e->ham_entries = D * a.stride;
     } else {
+        // on the fly: host-built string tables, diagonal on the GPU
+        OtfTables T;
+        std::vector<double> hv(h1, h1 + (size_t)N * N), gv(g2, g2 + (size_t)N * N * N * N);
+        build_otf_tables(e->B, hv, gv, T);
+        OtfArgs o{};
+        o.N = N;
+        o.P2 = T.P2;
+        o.nA = (int)e->B.nA;
+        o.nB = (int)e->B.nB;
+        o.nsa = T.nsa;
+        o.nda = T.nda;
+        o.nsb = T.nsb;
+        o.ndb = T.ndb;
+        o.sa_rank = e->upload(T.sa_rank);
+        o.sa_code = e->upload(T.sa_code);
+        o.da_rank = e->upload(T.da_rank);
+        o.da_code = e->upload(T.da_code);
+        o.sb_rank = e->upload(T.sb_rank);
+        o.sb_code = e->upload(T.sb_code);
+        o.db_rank = e->upload(T.db_rank);
+        o.db_code = e->upload(T.db_code);
+        o.vss = e->upload(T.vss);
+        o.vab = e->upload(T.vab);
+        o.a_alpha = e->upload(T.a_alpha);
+        o.b_alpha = e->upload(T.b_alpha);
+        o.a_beta = e->upload(T.a_beta);
+        o.b_beta = e->upload(T.b_beta);
+        double *diag = e->alloc<double>(D);
+        if (!diag || !o.vab || !o.b_beta) return e->fail(AEGPU_ERR_NOMEM, "on-the-fly table allocation failed");
+        o.diag = diag;
+        cudaDeviceSynchronize();
+        k_diag_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, diag);
+        e->launches += 1;
+        const size_t smem = otf_smem_bytes(N, T.P2, T.nsa, T.nda);
+        int optin = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (smem + 1024 > (size_t)optin) return e->fail(AEGPU_ERR_UNSUPPORTED, "too many orbitals for the on-the-fly kernel");
+        e->otf = o;
+        e->otf_threads = (int)std::min<int64_t>(512, ((int64_t)o.nB + 31) / 32 * 32);
+        e->otf_chunks = (o.nB + e->otf_threads - 1) / e->otf_threads;
+        const int64_t nparts = (int64_t)o.nA * e->otf_chunks;
+        if (nparts > (int64_t)std::max<int64_t>(e->spmv_grid, (D + kSpmvThreads - 1) / kSpmvThreads)) {
+            e->d_epart = e->alloc<double>(nparts);
+            if (!e->d_epart) return e->fail(AEGPU_ERR_NOMEM, "partial-sum allocation failed");
+        }
         e->ham_kind = 3;
         e->ham_entries = 0;
     }
@@ -1776,12 +1944,9 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
         rc = run_energy(e, e->d_scalar);
         if (rc) return rc;
     }
-    // the sweep destroys psi / hpsi: keep the evolved state for later calls
-    const size_t n = (size_t)e->B.D * e->W;
-    cudaMemcpyAsync(e->d_tmp, e->d_psi, n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
+    // the checkpointed sweep consumes H psi and leaves psi as it is
     rc = run_backward(e, e->d_grad);
     if (rc) return rc;
-    std::swap(e->d_tmp, e->d_psi);
     e->h_valid = false;
     if (energy) cudaMemcpyAsync(energy, e->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
@@ -1967,7 +2132,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         const int p0 = e->block_pos0[bi];
         if (b.diagonal) {
             k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table);
-            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0);
+            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0, nullptr);
             k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_psi, T, n, e->d_tpos);
             e->launches += 3;
         } else if (b.ntiles) {
@@ -2024,7 +2189,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
             k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
                                                                             b.ops, p0, Hops, nops);
-            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1);
+            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1, nullptr);
             e->launches += 4;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args(b, -1.0);

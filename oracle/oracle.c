@@ -416,6 +416,37 @@ static void ham_apply(const or_ctx *c, const double *x, double *y, int w)
     }
 }
 
+/* (H x) on a subset of rows only -- a spot check that stays cheap at sizes where a
+ * full operator-list apply (hamiltonianmatrix.cpp:915-1009) would take minutes. */
+int or_apply_h_rows(void *p, const double *x, const int64_t *rows, int n, double *y)
+{
+    or_ctx *c = (or_ctx *)p;
+    if (c->ham_kind != 2) return 1;
+    int w = c->cplx ? 2 : 1;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < n; ++k) {
+        int64_t j = rows[k];
+        uint32_t js = c->states[j];
+        double a0 = 0, a1 = 0;
+        for (int o = 0; o < c->nhops; ++o) {
+            const or_hop *h = &c->hops[o];
+            uint32_t de = js ^ h->create;
+            if (de & h->create) continue;
+            if (de & h->destroy) continue;
+            uint32_t i = de | h->destroy;
+            int sg = popc32(js & h->signmask) & 1;
+            int32_t ri = c->rank[i];
+            if (ri < 0) continue;
+            double v = sg ? -c->hvals[o] : c->hvals[o];
+            a0 += x[(size_t)ri * w] * v;
+            if (w == 2) a1 += x[(size_t)ri * w + 1] * v;
+        }
+        y[(size_t)k * w] = a0;
+        if (w == 2) y[(size_t)k * w + 1] = a1;
+    }
+    return 0;
+}
+
 int or_apply_h(void *p, const double *x, double *y)
 {
     or_ctx *c = (or_ctx *)p;

@@ -43,6 +43,7 @@ def lib():
         L.or_ham_nops.argtypes = [P]
         L.or_ham_csr.argtypes = [P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32), dp]
         L.or_apply_h.argtypes = [P, dp, dp]
+        L.or_apply_h_rows.argtypes = [P, dp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int, dp]
         L.or_evolve.argtypes = [P, dp, dp]
         L.or_energy_gradient.argtypes = [P, dp, dp, dp]
         L.or_gradient_comp.argtypes = [P, dp, dp, dp]
@@ -135,6 +136,13 @@ class Oracle:
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros_like(x)
         assert self.L.or_apply_h(self.h, _d(x), _d(y)) == 0
+        return y
+
+    def apply_h_rows(self, x, rows):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        rows = np.ascontiguousarray(rows, dtype=np.int64)
+        y = np.zeros(len(rows) * self._w())
+        assert self.L.or_apply_h_rows(self.h, _d(x), rows.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(rows), _d(y)) == 0
         return y
 
     def evolve_ops(self, ang_ops):
