@@ -54,6 +54,22 @@ def lib(build_if_missing=True):
         "aegpu_set_initial": (ctypes.c_int, [_P, _DP]),
         "aegpu_set_ham_csr": (ctypes.c_int, [_P, i64, ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int32), _DP]),
         "aegpu_set_ham_integrals": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
+        "aegpu_set_ham_integrals_batch": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
+        "aegpu_set_batch": (ctypes.c_int, [_P, ctypes.c_int]),
+        "aegpu_batch_size": (ctypes.c_int, [_P]),
+        "aegpu_io_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+        "aegpu_io_put_angles": (ctypes.c_int, [_P, _DP, _P]),
+        "aegpu_io_get_results": (ctypes.c_int, [_P, _DP, _DP, _P]),
+        "aegpu_launch_io": (ctypes.c_int, [_P, _P]),
+        "aegpu_optimise_newton": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, _DP, _DP,
+                                                 ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "aegpu_optimise_batch": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, ctypes.c_int,
+                                                ctypes.c_double, _DP, _DP, _IP, ctypes.POINTER(i64)]),
+        "aegpu_group_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.c_int]),
+        "aegpu_group_launch": (ctypes.c_int, [_P, _P]),
+        "aegpu_group_launch_count": (i64, [_P]),
+        "aegpu_group_sync": (ctypes.c_int, [_P]),
+        "aegpu_group_destroy": (None, [_P]),
         "aegpu_ham_info": (ctypes.c_int, [_P, _IP, ctypes.POINTER(i64)]),
         "aegpu_evolve": (ctypes.c_int, [_P, _DP, _DP]),
         "aegpu_energy": (ctypes.c_int, [_P, _DP, _DP]),
@@ -134,6 +150,7 @@ class Engine:
         self._check(self.L.aegpu_set_problem(h, nq, basis_kind, n_elec, n_alpha, n_beta, int(complex_mode), self.nops,
                                              iptr(ops.reshape(-1))))
         self.D = int(self.L.aegpu_dim(h))
+        self.nb = 1
 
     def _check(self, rc):
         if rc:
@@ -175,6 +192,23 @@ class Engine:
         a, b = _f64(h1), _f64(g2)
         self._check(self.L.aegpu_set_ham_integrals(self.h, dptr(a), dptr(b), mode))
 
+    def set_batch(self, nb):
+        """Evaluate nb instances per call (angles [nb, nops] -> energies [nb], gradients [nb, nops])."""
+        self._check(self.L.aegpu_set_batch(self.h, int(nb)))
+        self.nb = int(self.L.aegpu_batch_size(self.h))
+
+    def set_ham_integrals_batch(self, h1s, g2s, mode=HAM_AUTO):
+        """One Hamiltonian per instance: h1s [nb, N, N], g2s [nb, N, N, N, N]."""
+        a, b = _f64(h1s), _f64(g2s)
+        N2 = a.size // self.nb
+        assert a.size == self.nb * N2 and b.size == self.nb * N2 * N2
+        self._check(self.L.aegpu_set_ham_integrals_batch(self.h, dptr(a), dptr(b), mode))
+
+    def _angles(self, angles_ops):
+        a = _f64(angles_ops)
+        assert a.size == self.nb * self.nops, "expected %d x %d angles" % (self.nb, self.nops)
+        return a
+
     def ham_info(self):
         k = ctypes.c_int()
         n = ctypes.c_int64()
@@ -182,23 +216,25 @@ class Engine:
         return k.value, n.value
 
     def evolve(self, angles_ops):
-        a = _f64(angles_ops)
-        out = np.zeros(self.D * self.W)
+        a = self._angles(angles_ops)
+        out = np.zeros(self.nb * self.D * self.W)
         self._check(self.L.aegpu_evolve(self.h, dptr(a), dptr(out)))
-        return out
+        return out if self.nb == 1 else out.reshape(self.nb, -1)
 
     def energy(self, angles_ops):
-        a = _f64(angles_ops)
-        E = np.zeros(1)
+        a = self._angles(angles_ops)
+        E = np.zeros(self.nb)
         self._check(self.L.aegpu_energy(self.h, dptr(a), dptr(E)))
-        return E[0]
+        return E[0] if self.nb == 1 else E
 
     def gradient(self, angles_ops):
-        a = _f64(angles_ops)
-        E = np.zeros(1)
-        g = np.zeros(self.nops)
+        a = self._angles(angles_ops)
+        E = np.zeros(self.nb)
+        g = np.zeros(self.nb * self.nops)
         self._check(self.L.aegpu_gradient(self.h, dptr(a), dptr(E), dptr(g)))
-        return E[0], g
+        if self.nb == 1:
+            return E[0], g
+        return E, g.reshape(self.nb, self.nops)
 
     def hessian(self, angles_ops, param0, scale):
         a = _f64(angles_ops)
@@ -213,6 +249,7 @@ class Engine:
 
     def apply_h(self, x):
         x = _f64(x)
+        assert x.size == self.nb * self.D * self.W
         y = np.zeros_like(x)
         self._check(self.L.aegpu_apply_h(self.h, dptr(x), dptr(y)))
         return y
@@ -225,6 +262,49 @@ class Engine:
 
     def apply_dev(self, x_ptr, y_ptr, energy_ptr=None, stream=0):
         self._check(self.L.aegpu_apply_dev(self.h, x_ptr, y_ptr, energy_ptr, stream or None))
+
+    def io_dev(self):
+        """Device addresses (angles [nb, nops], energies [nb], gradients [nb, nops]) that
+        the captured evaluation graph reads and writes."""
+        a, e, g = _P(), _P(), _P()
+        self._check(self.L.aegpu_io_dev(self.h, ctypes.byref(a), ctypes.byref(e), ctypes.byref(g)))
+        return a.value, e.value, g.value
+
+    def io_put_angles(self, angles_ops, stream=0):
+        a = self._angles(angles_ops)
+        self._io_keep = a  # the copy is asynchronous: keep the host array alive
+        self._check(self.L.aegpu_io_put_angles(self.h, dptr(a), stream or None))
+
+    def io_get_results(self, stream=0):
+        E = np.zeros(self.nb)
+        g = np.zeros(self.nb * self.nops)
+        self._check(self.L.aegpu_io_get_results(self.h, dptr(E), dptr(g), stream or None))
+        return E, g.reshape(self.nb, self.nops)
+
+    def launch_io(self, stream=0):
+        self._check(self.L.aegpu_launch_io(self.h, stream or None))
+
+    def optimise_newton(self, x0, param0, scale, gtol=1e-6):
+        """The reference's Newton method on this (batch-of-1) engine: (x, E, |g|, hessian evals, energy evals)."""
+        x = _f64(x0).copy()
+        p, s = _i32(param0), _f64(scale)
+        E, gn = np.zeros(1), np.zeros(1)
+        nh, ne = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.L.aegpu_optimise_newton(self.h, len(x), iptr(p), dptr(s), dptr(x), gtol, dptr(E), dptr(gn),
+                                                 ctypes.byref(nh), ctypes.byref(ne)))
+        return x, E[0], gn[0], nh.value, ne.value
+
+    def optimise_batch(self, x0, param0, scale, gtol=1e-6, max_rounds=2000, max_step=1.0):
+        """Lockstep BFGS of all instances from x0 [nb, P]: (x, E [nb], |g| [nb], iterations [nb], rounds)."""
+        x = _f64(x0).reshape(self.nb, -1).copy()
+        P = x.shape[1]
+        p, s = _i32(param0), _f64(scale)
+        E, gn = np.zeros(self.nb), np.zeros(self.nb)
+        it = np.zeros(self.nb, dtype=np.int32)
+        r = ctypes.c_int64()
+        self._check(self.L.aegpu_optimise_batch(self.h, P, iptr(p), dptr(s), dptr(x), gtol, int(max_rounds), max_step,
+                                                dptr(E), dptr(gn), iptr(it), ctypes.byref(r)))
+        return x, E, gn, it, r.value
 
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))
@@ -249,6 +329,42 @@ class Engine:
 
     def launch_count(self):
         return int(self.L.aegpu_launch_count(self.h))
+
+
+class Group:
+    """Several engines evaluated by one CUDA graph launch (aegpu_group_*)."""
+
+    def __init__(self, engines):
+        self.L = lib()
+        self.engines = list(engines)
+        arr = (_P * len(self.engines))(*[e.h for e in self.engines])
+        h = _P()
+        rc = self.L.aegpu_group_create(ctypes.byref(h), arr, len(self.engines))
+        if rc:
+            msgs = "; ".join(self.L.aegpu_last_error(e.h).decode() for e in self.engines)
+            raise AegpuError("aegpu_group_create failed (%d): %s" % (rc, msgs))
+        self.h = h
+
+    def launch(self, stream=0):
+        rc = self.L.aegpu_group_launch(self.h, stream or None)
+        if rc:
+            msgs = "; ".join(self.L.aegpu_last_error(e.h).decode() for e in self.engines)
+            raise AegpuError("aegpu_group_launch failed (%d): %s" % (rc, msgs))
+
+    def sync(self):
+        if self.L.aegpu_group_sync(self.h):
+            raise AegpuError("aegpu_group_sync failed")
+
+    def launch_count(self):
+        return int(self.L.aegpu_group_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aegpu_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def host_block_layout(nq, ops0):

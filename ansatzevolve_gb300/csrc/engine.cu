@@ -43,6 +43,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -50,6 +51,8 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 using namespace ae;
@@ -95,6 +98,14 @@ struct DevBasis {
     }
 };
 
+struct PassConst {
+    ExcCode code;
+    double f;      // layer scale (C or dir*S)
+    double m;      // S/C (tan form) or C/S (cot form), with dir applied to S
+    int tan_form;
+    int pad;
+};
+
 struct BlockArgs {
     const uint32_t *idx;
     const OrbitGroup *groups;
@@ -105,6 +116,9 @@ struct BlockArgs {
     const double *sc;        // per operator: sin, cos
     double dir;              // +1 forward, -1 backward
     DevBasis basis;
+    const PassConst *pc;     // this pass's layer constants for this direction (instance 0)
+    const double *sigma;     // this pass's scale products per active mask (instance 0)
+    int64_t pc_stride, sig_stride;  // per-instance strides of pc / sigma
 };
 
 __device__ __forceinline__ uint32_t insert_zero_bit(uint32_t p, int i)
@@ -122,15 +136,12 @@ __device__ __forceinline__ size_t ell_pos(int64_t r, int64_t e, int64_t q)
 }
 
 // ---------------------------------------------------------------- utilities --
-__global__ void k_sincos(const double *__restrict__ ang, double *__restrict__ sc, int n)
+// dst[b * n + i] = src[i] for every instance b = blockIdx.y (the shared start vector)
+__global__ void k_broadcast(const double *__restrict__ src, double *__restrict__ dst, int64_t n)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        double s, c;
-        sincos(ang[i], &s, &c);
-        sc[2 * i] = s;
-        sc[2 * i + 1] = c;
-    }
+    dst += (size_t)blockIdx.y * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -154,13 +165,15 @@ __device__ __forceinline__ double block_sum(double v, double *red)
     return s;
 }
 
+// One CTA per instance: out[b] = scale * sum of parts[b * n .. b * n + n).
 __global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__restrict__ out, double scale)
 {
     __shared__ double red[32];
+    parts += (size_t)blockIdx.x * n;
     double s = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += parts[i];
     s = block_sum(s, red);
-    if (threadIdx.x == 0) out[0] = s * scale;
+    if (threadIdx.x == 0) out[blockIdx.x] = s * scale;
 }
 
 // -------------------------------------------------------- block rotations --
@@ -363,14 +376,6 @@ __global__ void __launch_bounds__(kRotThreads) k_block_hess(BlockArgs a, const d
 // fusedevolve.cpp:461-483.)
 constexpr int kWarpThreads = 256;
 
-struct PassConst {
-    ExcCode code;
-    double f;      // layer scale (C or dir*S)
-    double m;      // S/C (tan form) or C/S (cot form), with dir applied to S
-    double f2;     // f^2
-    int tan_form;
-};
-
 __device__ __forceinline__ double flip(double x, int s)
 {
     return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)(s < 0) << 63));
@@ -386,64 +391,76 @@ __device__ __forceinline__ double rot_scaled(const PassConst &q, double v, doubl
     return fma(a, b, c);
 }
 
-// Per-CTA tables over the <= 64 active masks of a pass: sigma[m] = product of the
-// layer scales of m, pre2[m][j] = squared product of the scales of the layers of m
-// applied before layer j.  Keeps those products off the per-amplitude FP64 path.
-struct PassTables {
-    double sigma[1 << kMaxWarpLayers];
-    double pre2[1 << kMaxWarpLayers][kMaxWarpLayers];
+// Per-evaluation preparation, one CTA per (pass, instance): sin / cos of the pass's
+// angles (kept for the Hessian and diagonal kernels), the scaled-Givens constants of
+// every layer for both directions, and for every active mask the product of its
+// layer scales.  The pass kernels then only read these (no FP64 division, no
+// per-CTA set-up barrier on the hot path).
+struct PrepArgs {
+    const int *pass_ops;    // operators of all passes, concatenated
+    const int *pass_off;    // first operator of each pass
+    const int *pass_n;      // operators per pass
+    const int *pass_diag;   // 1 for diagonal passes (no scaled-Givens constants)
+    const ExcCode *codes;
+    int nops, npass;
 };
 
-__device__ __forceinline__ void pass_tables(const PassConst *pc, int nslots, PassTables *t)
+__global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *__restrict__ sc,
+                            PassConst *__restrict__ pc, double *__restrict__ sig)
 {
-    for (int m = threadIdx.x; m < (1 << nslots); m += blockDim.x) {
-        double sg = 1.0, s2 = 1.0;
-        for (int j = 0; j < nslots; ++j) {
-            t->pre2[m][j] = s2;
-            if (m & (1 << j)) {
-                sg *= pc[j].f;
-                s2 *= pc[j].f2;
+    const int pass = blockIdx.x, b = blockIdx.y;
+    const int ns = a.pass_n[pass];
+    const int *ops = a.pass_ops + a.pass_off[pass];
+    __shared__ double f[2][kMaxWarpLayers];
+    const bool paired = !a.pass_diag[pass] && ns <= kMaxWarpLayers;
+    if (threadIdx.x < (unsigned)ns) {
+        const int op = ops[threadIdx.x];
+        double S0, C;
+        sincos(ang[(size_t)b * a.nops + op], &S0, &C);
+        sc[(size_t)b * 2 * a.nops + 2 * op] = S0;
+        sc[(size_t)b * 2 * a.nops + 2 * op + 1] = C;
+        if (paired)
+            for (int d = 0; d < 2; ++d) {
+                const double S = d == 0 ? S0 : -S0;
+                PassConst q;
+                q.code = a.codes[op];
+                q.pad = 0;
+                if (fabs(C) >= fabs(S)) {
+                    q.tan_form = 1;
+                    q.f = C;
+                    q.m = S / C;
+                } else {
+                    q.tan_form = 0;
+                    q.f = S;
+                    q.m = C / S;
+                }
+                f[d][threadIdx.x] = q.f;
+                pc[(((size_t)b * a.npass + pass) * 2 + d) * kMaxWarpLayers + threadIdx.x] = q;
             }
-        }
-        t->sigma[m] = sg;
     }
     __syncthreads();
-}
-
-__device__ __forceinline__ void pass_consts(const BlockArgs &a, PassConst *pc)
-{
-    if (threadIdx.x < (unsigned)a.nslots) {
-        const int op = a.ops[threadIdx.x];
-        const double S = a.dir * a.sc[2 * op], C = a.sc[2 * op + 1];
-        PassConst q;
-        q.code = a.codes[op];
-        if (fabs(C) >= fabs(S)) {
-            q.tan_form = 1;
-            q.f = C;
-            q.m = S / C;
-        } else {
-            q.tan_form = 0;
-            q.f = S;
-            q.m = C / S;
+    if (!paired) return;
+    for (int m = threadIdx.x; m < (1 << ns); m += blockDim.x)
+        for (int d = 0; d < 2; ++d) {
+            double prod = 1.0;
+            for (int j = 0; j < ns; ++j)
+                if (m & (1 << j)) prod *= f[d][j];
+            sig[(((size_t)b * a.npass + pass) * 2 + d) * (1 << kMaxWarpLayers) + m] = prod;
         }
-        q.f2 = q.f * q.f;
-        pc[threadIdx.x] = q;
-    }
-    __syncthreads();
 }
 
-// ckpt (nullable, single vector only): the pass's amplitudes after rotation, stored in
-// the pass's orbit order (same index as the rank list), for the adjoint sweep.
+// Instance b = blockIdx.y.  ckpt (nullable): the pass's amplitudes after rotation,
+// stored in the pass's orbit order (same index as the rank list), for the adjoint.
 template <int W>
 __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
-                                                           double *vecs, size_t vstride, int nvec,
-                                                           double *__restrict__ ckpt)
+                                                           double *vecs, int64_t inst_stride, double *__restrict__ ckpt,
+                                                           int64_t ckpt_stride)
 {
-    __shared__ PassConst pc[kMaxWarpLayers];
-    __shared__ PassTables tab;
-    pass_consts(a, pc);
-    pass_tables(pc, a.nslots, &tab);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, b = blockIdx.y;
+    const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
+    const double *sig = a.sigma + (size_t)b * a.sig_stride;
+    double *psi = vecs + (size_t)b * inst_stride;
+    if (ckpt) ckpt += (size_t)b * ckpt_stride;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
         const WarpTask task = tasks[t];
@@ -452,66 +469,64 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
         const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
-        const double sigma = tab.sigma[mask];
-        for (int vec = 0; vec < nvec; ++vec) {
-            double *psi = vecs + vec * vstride;
-            double v0[W], v1[W];
+        double v0[W], v1[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            v0[w] = ok0 ? psi[(size_t)z0 * W + w] : 0.0;
+            v1[w] = ok1 ? psi[(size_t)z1 * W + w] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j) {
+            if (!(mask & (1u << j))) continue;
+            const int i = __popc(mask & ((1u << j) - 1u));
+            const PassConst q = pc[j];
+            const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
 #pragma unroll
             for (int w = 0; w < W; ++w) {
-                v0[w] = ok0 ? psi[(size_t)z0 * W + w] : 0.0;
-                v1[w] = ok1 ? psi[(size_t)z1 * W + w] : 0.0;
-            }
-#pragma unroll
-            for (int j = 0; j < kMaxWarpLayers; ++j) {
-                if (!(mask & (1u << j))) continue;
-                const int i = __popc(mask & ((1u << j) - 1u));
-                const PassConst &q = pc[j];
-                const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
-#pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    double p0, p1;
-                    if (i < 5) {
-                        p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
-                        p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
-                    } else {
-                        p0 = v1[w];
-                        p1 = v0[w];
-                    }
-                    v0[w] = rot_scaled(q, v0[w], p0, s0);
-                    v1[w] = rot_scaled(q, v1[w], p1, s1);
+                double p0, p1;
+                if (i < 5) {
+                    p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                    p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                } else {
+                    p0 = v1[w];
+                    p1 = v0[w];
                 }
+                v0[w] = rot_scaled(q, v0[w], p0, s0);
+                v1[w] = rot_scaled(q, v1[w], p1, s1);
             }
+        }
+        const double sigma = sig[mask];
 #pragma unroll
-            for (int w = 0; w < W; ++w) {
-                const double t0 = sigma * v0[w], t1 = sigma * v1[w];
-                if (ok0) psi[(size_t)z0 * W + w] = t0;
-                if (ok1) psi[(size_t)z1 * W + w] = t1;
-                if (ckpt) {
-                    if (ok0) ckpt[((size_t)task.elem_off + lane) * W + w] = t0;
-                    if (ok1) ckpt[((size_t)task.elem_off + lane + 32) * W + w] = t1;
-                }
+        for (int w = 0; w < W; ++w) {
+            const double t0 = sigma * v0[w], t1 = sigma * v1[w];
+            if (ok0) psi[(size_t)z0 * W + w] = t0;
+            if (ok1) psi[(size_t)z1 * W + w] = t1;
+            if (ckpt) {
+                if (ok0) ckpt[((size_t)task.elem_off + lane) * W + w] = t0;
+                if (ok1) ckpt[((size_t)task.elem_off + lane + 32) * W + w] = t1;
             }
         }
     }
 }
 
-// Checkpointed adjoint pass.  psi after this pass comes from the forward sweep's
-// checkpoint (orbit order, coalesced), h = H psi back-propagated to the same point is
-// gathered; since every excitation of the pass commutes with the others, the gradient
-// of excitation j is <h|G_j psi> evaluated right there: sum_z h_z s_j(z) psi_p(z),
-// one FP64 FMA per amplitude and layer.  Only h is then rotated back (-theta) through
-// the pass, again one FMA per amplitude and layer, and scattered.  psi is not touched.
+// Checkpointed adjoint pass (instance b = blockIdx.y).  psi after this pass comes
+// from the forward sweep's checkpoint (orbit order, coalesced), h = H psi
+// back-propagated to the same point is gathered; since the pass's excitations
+// commute, the gradient of excitation j is <h|G_j psi> evaluated right there:
+// sum_z h_z s_j(z) psi_p(z), one FP64 FMA per amplitude and layer.  Only h is then
+// rotated back (-theta) through the pass, one FMA per amplitude and layer.
 template <int W>
 __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
-                                                           const double *__restrict__ ckpt, double *h,
-                                                           double *partials)
+                                                           const double *__restrict__ ckpt, int64_t ckpt_stride,
+                                                           double *hv, int64_t inst_stride, double *partials,
+                                                           int64_t part_stride)
 {
-    __shared__ PassConst pc[kMaxWarpLayers];
-    __shared__ PassTables tab;
     __shared__ double red[kMaxWarpLayers][kWarpThreads];
-    pass_consts(a, pc);
-    pass_tables(pc, a.nslots, &tab);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, b = blockIdx.y;
+    const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
+    const double *sig = a.sigma + (size_t)b * a.sig_stride;
+    double *h = hv + (size_t)b * inst_stride;
+    ckpt += (size_t)b * ckpt_stride;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double accS[kMaxWarpLayers];
 #pragma unroll
@@ -532,12 +547,12 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
             h0[w] = ok0 ? h[(size_t)z0 * W + w] : 0.0;
             h1[w] = ok1 ? h[(size_t)z1 * W + w] : 0.0;
         }
-        // gradient terms at the pass's output point
 #pragma unroll
         for (int j = 0; j < kMaxWarpLayers; ++j) {
             if (!(mask & (1u << j))) continue;
             const int i = __popc(mask & ((1u << j) - 1u));
-            const int s0 = exc_sign(pc[j].code, b0), s1 = exc_sign(pc[j].code, b1);
+            const PassConst q = pc[j];
+            const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
             double g = 0.0;
 #pragma unroll
             for (int w = 0; w < W; ++w) {
@@ -554,12 +569,11 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
             }
             accS[j] += g;
         }
-        // h back through the pass (scaled form, one FMA per amplitude and layer)
 #pragma unroll
         for (int j = 0; j < kMaxWarpLayers; ++j) {
             if (!(mask & (1u << j))) continue;
             const int i = __popc(mask & ((1u << j) - 1u));
-            const PassConst &q = pc[j];
+            const PassConst q = pc[j];
             const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
 #pragma unroll
             for (int w = 0; w < W; ++w) {
@@ -575,21 +589,22 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
                 h1[w] = rot_scaled(q, h1[w], p1, s1);
             }
         }
-        const double sigma = tab.sigma[mask];
+        const double sigma = sig[mask];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
             if (ok0) h[(size_t)z0 * W + w] = sigma * h0[w];
             if (ok1) h[(size_t)z1 * W + w] = sigma * h1[w];
         }
     }
+    // fixed-order CTA sum through shared memory
 #pragma unroll
     for (int j = 0; j < kMaxWarpLayers; ++j) red[j][threadIdx.x] = accS[j];
     __syncthreads();
     if (threadIdx.x < kMaxSlots) {
-        double s = 0.0;
+        double sum = 0.0;
         if (threadIdx.x < kMaxWarpLayers)
-            for (int w = 0; w < (int)blockDim.x; ++w) s += red[threadIdx.x][w];
-        partials[(size_t)blockIdx.x * kMaxSlots + threadIdx.x] = s;
+            for (int w = 0; w < (int)blockDim.x; ++w) sum += red[threadIdx.x][w];
+        partials[(size_t)b * part_stride + (size_t)blockIdx.x * kMaxSlots + threadIdx.x] = sum;
     }
 }
 
@@ -598,10 +613,12 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
 // amplitude by exp(+i * sum of the active angles) (RunFuseNDiagonal,
 // fusedevolve.cpp:625-717).  table[m] = (cos, sin) of dir * sum_{i in m} theta_i.
 __global__ void k_diag_table(const double *__restrict__ ang, const int *__restrict__ ops, int nslots, double dir,
-                             double *__restrict__ table)
+                             double *__restrict__ table, int nops)
 {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= (1u << nslots)) return;
+    ang += (size_t)blockIdx.y * nops;                          // instance blockIdx.y
+    table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
     double th = 0;
     for (int i = 0; i < nslots; ++i)
         if (m & (1u << i)) th += ang[ops[i]];
@@ -615,7 +632,7 @@ struct DiagArgs {
     const int *ops;
     int nslots;
     const ExcCode *codes;
-    const double *table;
+    const double *table;  // instance 0; instance b at + b * 2 * 2^kMaxSlots
     DevBasis basis;
 };
 
@@ -630,9 +647,13 @@ __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
 }
 
 // ckpt (nullable, single vector): the amplitudes after the pass, for the adjoint sweep.
-__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, double *__restrict__ ckpt)
+__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, double *__restrict__ ckpt,
+                           int64_t inst_stride, int64_t ckpt_stride)
 {
     const uint64_t D = a.basis.D;
+    a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
+    vecs += (size_t)blockIdx.y * inst_stride;
+    if (ckpt) ckpt += (size_t)blockIdx.y * ckpt_stride;
     for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
         if (!m) continue;
@@ -652,10 +673,14 @@ __global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, d
 
 // Checkpointed adjoint of a diagonal pass: gradient <h|i n psi> at the pass output
 // (psi from the checkpoint), then h rotated back; psi untouched.
-__global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__restrict__ ckpt, double *h,
-                                                  double *partials)
+__global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__restrict__ ckpt, int64_t ckpt_stride,
+                                                  double *h, int64_t inst_stride, double *partials, int64_t part_stride)
 {
     __shared__ double red[8];
+    a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
+    ckpt += (size_t)blockIdx.y * ckpt_stride;
+    h += (size_t)blockIdx.y * inst_stride;
+    partials += (size_t)blockIdx.y * part_stride;
     double acc[kMaxSlots];
 #pragma unroll
     for (int i = 0; i < kMaxSlots; ++i) acc[i] = 0;
@@ -730,13 +755,16 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
 
 // ------------------------------------------------------------ reductions --
 // grad[op] = scale * sum over the tiles of op's block of partials[tile][slot].
+// warp per (instance, operator); instance b's partial sums start at b * part_stride.
 __global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t *__restrict__ op_part_off,
                               const int *__restrict__ op_ntiles, const int *__restrict__ op_slot, int nops, double scale,
-                              double *__restrict__ grad)
+                              double *__restrict__ grad, int nb, int64_t part_stride)
 {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= nops) return;
-    const double *p = partials + op_part_off[warp];
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (gw >= nops * nb) return;
+    const int b = gw / nops, warp = gw - b * nops;
+    grad += (size_t)b * nops;
+    const double *p = partials + (size_t)b * part_stride + op_part_off[warp];
     const int nt = op_ntiles[warp], sl = op_slot[warp];
     double s = 0;
     for (int t = lane; t < nt; t += 32) s += p[(size_t)t * kMaxSlots + sl];
@@ -774,6 +802,9 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(const int64_t *__restrict
     __shared__ double red[kSpmvThreads / 32];
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    x += (size_t)blockIdx.y * D * W;  // instance blockIdx.y, same matrix
+    y += (size_t)blockIdx.y * D * W;
+    if (epart) epart += (size_t)blockIdx.y * gridDim.x;
     double e = 0;
     for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < D; r += warps) {
         const int64_t b = ELL ? r * ell_width : rowptr[r], end = ELL ? b + ell_width : rowptr[r + 1];
@@ -807,10 +838,16 @@ template <int W>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int32_t *__restrict__ col,
                                                             const double *__restrict__ val,
                                                             const double *__restrict__ x, double *__restrict__ y,
-                                                            int64_t D, double *__restrict__ epart)
+                                                            int64_t D, double *__restrict__ epart, int64_t mat_stride)
 {
     __shared__ double red[kSpmvThreads / 32];
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // instance blockIdx.y: its vectors, and its matrix (mat_stride = 0 when shared)
+    col += (size_t)blockIdx.y * mat_stride;
+    val += (size_t)blockIdx.y * mat_stride;
+    x += (size_t)blockIdx.y * D * W;
+    y += (size_t)blockIdx.y * D * W;
+    if (epart) epart += (size_t)blockIdx.y * gridDim.x;
     double e = 0;
     if (r < D) {
         const size_t base = ell_pos(r, 0, q);  // group g of this row starts at base + 128 g
@@ -1077,7 +1114,10 @@ struct OtfArgs {
     int nsa, nda, nsb, ndb;
     const int32_t *sa_rank, *sa_code, *da_rank, *da_code;
     const int32_t *sb_rank, *sb_code, *db_rank, *db_code;
+    // integral-dependent tables of instance 0; instance b at + b * (its size), or
+    // shared by every instance when `shared` is set
     const double *vss, *vab, *a_alpha, *b_alpha, *a_beta, *b_beta, *diag;
+    int shared;
 };
 
 __host__ __device__ inline size_t otf_smem_bytes(int N, int P2, int nsa, int nda)
@@ -1098,6 +1138,20 @@ __global__ void __launch_bounds__(512) k_otf_strings(OtfArgs a, const double *__
     __shared__ double red[16];
     const int N = a.N, NN = a.N * a.N, nsa = a.nsa, nda = a.nda;
     const int ra = blockIdx.x;
+    {
+        // instance blockIdx.z: its vectors and (unless shared) its integral tables
+        const size_t b = blockIdx.z, D = (size_t)a.nA * a.nB, bt = a.shared ? 0 : b;
+        x += b * D * W;
+        y += b * D * W;
+        if (epart) epart += b * gridDim.x * gridDim.y;
+        a.vss += bt * a.P2 * a.P2;
+        a.vab += bt * NN * NN;
+        a.a_alpha += bt * a.nA * NN;
+        a.b_alpha += bt * a.nB * NN;
+        a.a_beta += bt * a.nB * NN;
+        a.b_beta += bt * a.nA * NN;
+        a.diag += bt * D;
+    }
     double *vss = sm;
     double *vsl = vss + (size_t)a.P2 * a.P2;
     double *sa_val = vsl + (size_t)nsa * NN;
@@ -1251,16 +1305,31 @@ struct aegpu_engine {
     int *d_pos_op = nullptr;        // application position -> op
     int64_t *d_op_part_off = nullptr;
     int *d_op_ntiles = nullptr, *d_op_slot = nullptr;
-    double *d_ang = nullptr, *d_sc = nullptr, *d_diag_table = nullptr;
-    double *d_start = nullptr, *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
-    double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
-    double *d_ckpt = nullptr;  // per pass: amplitudes after the pass (adjoint sweep input)
-    int64_t n_partials = 0;
+    PrepArgs prep{};                // pass lists for k_pass_prep
+    double *d_start = nullptr;      // start vector, shared by every instance
+    int64_t n_partials = 0;         // gradient partial sums per instance
+    int64_t n_ckpt = 0;             // checkpoint doubles per instance
+    int64_t n_epart = 0;            // H psi partial sums per instance
     int spmv_grid = 0;
 
-    // Hamiltonian
+    // Per-instance buffers, instance b at b * (per-instance size).  An engine evaluates
+    // nb instances per call: nb angle vectors over one problem, with one shared
+    // Hamiltonian or one Hamiltonian per instance.
+    int nb = 1;
+    double *d_ang = nullptr, *d_sc = nullptr, *d_diag_table = nullptr, *d_sig = nullptr;
+    PassConst *d_pc = nullptr;
+    double *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
+    double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
+    double *d_ckpt = nullptr;  // per pass: amplitudes after the pass (adjoint sweep input)
+    std::vector<std::pair<void *, size_t>> inst_allocs;
+
+    // Hamiltonian (its device arrays, released when it is replaced)
+    std::vector<void *> ham_allocs;
+    std::unordered_map<void *, size_t> ham_alloc_bytes;
     int ham_kind = 0;  // 1 CSR, 2 ELL, 3 on the fly
+    bool ham_per_instance = false;
     int64_t ham_entries = 0;
+    int64_t ell_stride_inst = 0;  // doubles between instances' stored matrices (0 = shared)
     int64_t *d_rowptr = nullptr;
     int32_t *d_col = nullptr;
     double *d_val = nullptr;
@@ -1291,7 +1360,9 @@ struct aegpu_engine {
     // CUDA graph of one energy + gradient evaluation (angles from d_ang, results in
     // d_scalar / d_grad), captured on first use of aegpu_gradient_dev
     cudaGraphExec_t grad_graph = nullptr;
+    cudaGraph_t grad_graph_def = nullptr;  // its definition (child node of group graphs)
     int64_t graph_launches = 0;  // kernels inside the graph
+    int64_t generation = 0;      // bumped whenever device buffers or the Hamiltonian change
     bool use_graph = true;
 
     // state caching: psi / hpsi valid for these angles
@@ -1304,7 +1375,7 @@ struct aegpu_engine {
         for (auto &m : ev_marks)
             for (auto ev : m) cudaEventDestroy(ev);
         for (auto ev : ev_pool) cudaEventDestroy(ev);
-        if (grad_graph) cudaGraphExecDestroy(grad_graph);
+        drop_graph();
         if (cublas) cublasDestroy(cublas);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -1350,8 +1421,12 @@ struct aegpu_engine {
         return p;
     }
 
-    BlockArgs block_args(const DevBlock &b, double dir) const
+    // Arguments of pass bi in direction dir (+1 forward, -1 adjoint).
+    BlockArgs block_args(int bi, double dir) const
     {
+        const DevBlock &b = dblocks[bi];
+        const int d = dir > 0 ? 0 : 1;
+        const int npass = (int)dblocks.size();
         BlockArgs a;
         a.idx = b.idx;
         a.groups = b.groups;
@@ -1362,7 +1437,81 @@ struct aegpu_engine {
         a.sc = d_sc;
         a.dir = dir;
         a.basis = db;
+        a.pc = d_pc + ((size_t)bi * 2 + d) * kMaxWarpLayers;
+        a.sigma = d_sig + ((size_t)bi * 2 + d) * (1 << kMaxWarpLayers);
+        a.pc_stride = (int64_t)npass * 2 * kMaxWarpLayers;
+        a.sig_stride = (int64_t)npass * 2 * (1 << kMaxWarpLayers);
         return a;
+    }
+    size_t vec_elems() const { return (size_t)B.D * W; }
+
+    template <typename T>
+    T *ham_alloc(size_t n)
+    {
+        T *p = alloc<T>(n);
+        if (p) {
+            ham_allocs.push_back((void *)p);
+            ham_alloc_bytes[(void *)p] = std::max<size_t>(n, 1) * sizeof(T);
+        }
+        return p;
+    }
+    // Release the current Hamiltonian (and the graph that reads it).
+    void drop_ham()
+    {
+        for (void *p : ham_allocs) release(p, ham_alloc_bytes[p]);
+        ham_allocs.clear();
+        ham_alloc_bytes.clear();
+        ham_kind = 0;
+        ham_per_instance = false;
+        ell_stride_inst = 0;
+        d_rowptr = nullptr;
+        d_col = nullptr;
+        d_val = nullptr;
+        d_h1 = d_g2 = nullptr;
+        drop_graph();
+        h_valid = false;
+    }
+    void drop_graph()
+    {
+        ++generation;
+        if (grad_graph) cudaGraphExecDestroy(grad_graph);
+        if (grad_graph_def) cudaGraphDestroy(grad_graph_def);
+        grad_graph = nullptr;
+        grad_graph_def = nullptr;
+    }
+
+    // (Re)allocate the per-instance buffers for nb instances.
+    int alloc_instances(int n_inst)
+    {
+        for (auto &pa : inst_allocs) release(pa.first, pa.second);
+        inst_allocs.clear();
+        nb = n_inst;
+        const size_t nops = excs.size(), npass = dblocks.size(), n = vec_elems(), B_ = (size_t)nb;
+        bool ok = true;
+        auto get = [&](auto *&ptr, size_t count) {
+            using T = std::remove_reference_t<decltype(*ptr)>;
+            ptr = alloc<T>(count);
+            ok = ok && ptr;
+            inst_allocs.push_back({(void *)ptr, std::max<size_t>(count, 1) * sizeof(T)});
+        };
+        get(d_ang, B_ * nops);
+        get(d_sc, B_ * 2 * nops);
+        get(d_pc, B_ * npass * 2 * kMaxWarpLayers);
+        get(d_sig, B_ * npass * 2 * (1 << kMaxWarpLayers));
+        get(d_diag_table, B_ * 2 * (1 << kMaxSlots));
+        get(d_psi, B_ * n);
+        get(d_h, B_ * n);
+        get(d_tmp, B_ * n);
+        get(d_partials, B_ * std::max<int64_t>(n_partials, 1));
+        get(d_epart, B_ * std::max<int64_t>(n_epart, 1));
+        get(d_scalar, std::max<size_t>(B_, 4));
+        get(d_grad, B_ * nops);
+        get(d_ckpt, B_ * std::max<int64_t>(n_ckpt, 1));
+        drop_graph();
+        cached_angles.clear();
+        psi_valid = h_valid = false;
+        if (!ok) return fail(AEGPU_ERR_NOMEM, "device allocation of the instance buffers failed");
+        return AEGPU_OK;
     }
     DiagArgs diag_args(const DevBlock &b) const
     {
@@ -1420,61 +1569,75 @@ int set_smem_limits(int dev)
     return bad;
 }
 
-// Forward evolution of psi from the start vector (angles already in d_sc / d_ang).
-int run_evolve(aegpu_engine *e)
+// Forward evolution of the first ninst instances from the start vector (pass
+// constants already prepared from d_ang).
+int run_evolve(aegpu_engine *e, int ninst)
 {
-    const size_t n = (size_t)e->B.D * e->W;
-    cudaMemcpyAsync(e->d_psi, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
-    for (auto &b : e->dblocks) {
+    const int64_t n = (int64_t)e->vec_elems();
+    k_broadcast<<<dim3((unsigned)std::min<int64_t>((n + 255) / 256, e->sm_count * 4), ninst), 256, 0, e->stream>>>(
+        e->d_start, e->d_psi, n);
+    e->launches += 1;
+    for (int bi = 0; bi < (int)e->dblocks.size(); ++bi) {
+        auto &b = e->dblocks[bi];
+        double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, 1.0,
-                                                                              e->d_diag_table);
-            k_diag_rot<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1, e->d_ckpt + b.ckpt_off);
+            k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
+                e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table, (int)e->excs.size());
+            k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1, ck, n, e->n_ckpt);
             e->launches += 2;
         } else if (b.nwtasks) {
-            BlockArgs a = e->block_args(b, 1.0);
-            double *ck = e->d_ckpt + b.ckpt_off;
+            BlockArgs a = e->block_args(bi, 1.0);
+            const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
-                k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1, ck);
+                k_warp_rot<1><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             else
-                k_warp_rot<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, 0, 1, ck);
+                k_warp_rot<2><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             e->launches += 1;
         }
     }
     return e->cuda_check("evolve");
 }
 
-int upload_angles(aegpu_engine *e, const double *angles, bool host)
+// Pass constants of the first ninst instances from their angles in d_ang.
+int run_prep(aegpu_engine *e, int ninst)
 {
-    const int n = (int)e->excs.size();
-    cudaMemcpyAsync(e->d_ang, angles, n * sizeof(double), host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
-                    e->stream);
-    k_sincos<<<(n + 127) / 128, 128, 0, e->stream>>>(e->d_ang, e->d_sc, n);
+    k_pass_prep<<<dim3((unsigned)e->dblocks.size(), ninst), 64, 0, e->stream>>>(e->prep, e->d_ang, e->d_sc, e->d_pc,
+                                                                             e->d_sig);
     e->launches += 1;
-    return e->cuda_check("angles");
+    return e->cuda_check("pass constants");
 }
 
-// y = H x on device vectors, with <x|y> partial sums into epart (nullable); *nparts
-// receives how many partial sums the launch wrote.
-int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int *nparts = nullptr)
+int upload_angles(aegpu_engine *e, const double *angles, bool host, int ninst)
+{
+    const size_t n = e->excs.size() * (size_t)ninst;
+    cudaMemcpyAsync(e->d_ang, angles, n * sizeof(double), host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                    e->stream);
+    return run_prep(e, ninst);
+}
+
+// y = H x for the first ninst instances (vectors at stride D*W), with <x|y> partial
+// sums into epart (nullable; *nparts partial sums per instance).
+int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ninst, int *nparts = nullptr)
 {
     if (nparts) *nparts = e->spmv_grid;
     const int64_t D = (int64_t)e->B.D;
-    const int grid = e->spmv_grid;
     if (e->ham_kind == 1) {
+        const dim3 g(e->spmv_grid, ninst);
         if (e->W == 1)
-            k_spmv<1, false><<<grid, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv<1, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
         else
-            k_spmv<2, false><<<grid, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv<2, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
     } else if (e->ham_kind == 2) {
         const int sg = (int)((D + kSpmvThreads - 1) / kSpmvThreads);
+        const dim3 g(sg, ninst);
+        const int64_t q = e->ell_width >> 2, ms = e->ell_stride_inst;
         if (e->W == 1)
-            k_spmv_sell<1><<<sg, kSpmvThreads, 0, e->stream>>>(e->ell_width >> 2, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv_sell<1><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms);
         else
-            k_spmv_sell<2><<<sg, kSpmvThreads, 0, e->stream>>>(e->ell_width >> 2, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv_sell<2><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms);
         if (nparts) *nparts = sg;
     } else if (e->ham_kind == 3) {
-        dim3 g(e->otf.nA, e->otf_chunks);
+        const dim3 g(e->otf.nA, e->otf_chunks, ninst);
         const size_t smem = otf_smem_bytes(e->otf.N, e->otf.P2, e->otf.nsa, e->otf.nda);
         if (e->W == 1)
             k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(e->otf, x, y, epart);
@@ -1488,59 +1651,70 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int *n
     return e->cuda_check("apply H");
 }
 
-int run_energy(aegpu_engine *e, double *E_dev)
+// E_dev[b] = <psi_b|H psi_b> for the first ninst instances (H psi left in d_h).
+int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 {
     int np = 0;
-    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, &np);
+    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np);
     if (rc) return rc;
-    k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0);
+    k_reduce_sum<<<ninst, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0);
     e->launches += 1;
     return e->cuda_check("energy");
 }
 
-// Adjoint sweep over all blocks (psi, h updated in place), per-op gradient in grad_dev.
-int run_backward(aegpu_engine *e, double *grad_dev)
+// Adjoint sweep over all passes for the first ninst instances (h updated in place,
+// psi taken from the checkpoints), per-op gradients in grad_dev[b * nops + op].
+int run_backward(aegpu_engine *e, double *grad_dev, int ninst)
 {
+    const int64_t n = (int64_t)e->vec_elems();
+    const int nops = (int)e->excs.size();
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
         auto &b = e->dblocks[bi];
         double *part = e->d_partials + b.part_off;
+        const double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, e->stream>>>(e->d_ang, b.ops, b.nslots, -1.0,
-                                                                              e->d_diag_table);
-            k_diag_adj<<<kDiagGrid, 256, 0, e->stream>>>(e->diag_args(b), e->d_ckpt + b.ckpt_off, e->d_h, part);
+            k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
+                e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table, nops);
+            k_diag_adj<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h, n, part,
+                                                                     e->n_partials);
             e->launches += 2;
         } else if (b.nwtasks) {
-            BlockArgs a = e->block_args(b, -1.0);
-            const double *ck = e->d_ckpt + b.ckpt_off;
+            BlockArgs a = e->block_args(bi, -1.0);
+            const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
-                k_warp_adj<1><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->d_h, part);
+                k_warp_adj<1><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n, part,
+                                                                 e->n_partials);
             else
-                k_warp_adj<2><<<b.wgrid, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->d_h, part);
+                k_warp_adj<2><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n, part,
+                                                                 e->n_partials);
             e->launches += 1;
         } else {
-            cudaMemsetAsync(part, 0, (size_t)b.wgrid * kMaxSlots * sizeof(double), e->stream);
+            cudaMemset2DAsync(part, e->n_partials * sizeof(double), 0, (size_t)b.wgrid * kMaxSlots * sizeof(double),
+                              ninst, e->stream);
         }
     }
-    const int nops = (int)e->excs.size();
-    k_grad_reduce<<<(nops * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
-                                                                  e->d_op_slot, nops, 2.0, grad_dev);
+    const int warps = nops * ninst;
+    k_grad_reduce<<<(warps * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
+                                                                   e->d_op_slot, nops, 2.0, grad_dev, ninst,
+                                                                   e->n_partials);
     e->launches += 1;
     return e->cuda_check("backward");
 }
 
 bool same_angles(const aegpu_engine *e, const double *angles)
 {
-    return e->psi_valid && e->cached_angles.size() == e->excs.size() &&
+    return e->psi_valid && e->cached_angles.size() == e->excs.size() * (size_t)e->nb &&
            std::equal(e->cached_angles.begin(), e->cached_angles.end(), angles);
 }
 
+// psi of every instance evolved to these host angles ([nb][nops]), unless it already is.
 int ensure_state(aegpu_engine *e, const double *angles)
 {
     if (same_angles(e, angles)) return AEGPU_OK;
-    int rc = upload_angles(e, angles, true);
-    if (!rc) rc = run_evolve(e);
+    int rc = upload_angles(e, angles, true, e->nb);
+    if (!rc) rc = run_evolve(e, e->nb);
     if (rc) return rc;
-    e->cached_angles.assign(angles, angles + e->excs.size());
+    e->cached_angles.assign(angles, angles + e->excs.size() * (size_t)e->nb);
     e->psi_valid = true;
     e->h_valid = false;
     return AEGPU_OK;
@@ -1726,22 +1900,32 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->d_tpos = e->upload(e->pos_of_op);
     e->d_pos_op = e->upload(e->perm);
 
-    const size_t n = (size_t)e->B.D * e->W;
-    e->d_ang = e->alloc<double>(nops);
-    e->d_sc = e->alloc<double>(2 * nops);
-    e->d_diag_table = e->alloc<double>(2 * (1 << kMaxSlots));
+    // pass lists for the per-evaluation constant preparation
+    std::vector<int> pops, poff, pn, pdiag;
+    for (const Block &b : e->blocks) {
+        poff.push_back((int)pops.size());
+        pn.push_back((int)b.ops.size());
+        pdiag.push_back(b.diagonal ? 1 : 0);
+        pops.insert(pops.end(), b.ops.begin(), b.ops.end());
+    }
+    PrepArgs pa{};
+    pa.pass_ops = e->upload(pops);
+    pa.pass_off = e->upload(poff);
+    pa.pass_n = e->upload(pn);
+    pa.pass_diag = e->upload(pdiag);
+    pa.codes = e->d_codes;
+    pa.nops = nops;
+    pa.npass = (int)e->blocks.size();
+    e->prep = pa;
+
+    const size_t n = e->vec_elems();
+    e->n_ckpt = ckpt_off;
+    e->n_epart = std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D + kSpmvThreads - 1) / kSpmvThreads);
     e->d_start = e->alloc<double>(n);
-    e->d_psi = e->alloc<double>(n);
-    e->d_h = e->alloc<double>(n);
-    e->d_tmp = e->alloc<double>(n);
-    e->d_partials = e->alloc<double>(std::max<int64_t>(part_off, 1));
-    e->d_epart = e->alloc<double>(std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D + kSpmvThreads - 1) / kSpmvThreads));
-    e->d_scalar = e->alloc<double>(4);
-    e->d_grad = e->alloc<double>(nops);
-    e->d_ckpt = e->alloc<double>(std::max<int64_t>(ckpt_off, 1));
-    if (!e->d_tmp || !e->d_partials || !e->d_grad || !e->d_ckpt) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
+    if (!e->d_start || !pa.pass_ops || !pa.pass_diag) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
+    int rc = e->alloc_instances(e->nb);
+    if (rc) return rc;
     cudaMemset(e->d_start, 0, n * sizeof(double));
-    e->psi_valid = e->h_valid = false;
     // setup copies ran on the legacy stream: finish them before any engine-stream work
     if (cudaDeviceSynchronize() != cudaSuccess) return e->cuda_check("set_problem");
     return e->cuda_check("set_problem");
@@ -1785,9 +1969,10 @@ int aegpu_set_ham_csr(aegpu_engine *e, int64_t nnz, const int64_t *rowptr, const
     if (rowptr[0] != 0 || rowptr[D] != nnz) return e->fail(AEGPU_ERR_ARG, "inconsistent CSR row pointers");
     for (int64_t k = 0; k < nnz; ++k)
         if (col[k] < 0 || col[k] >= D) return e->fail(AEGPU_ERR_ARG, "CSR column out of range");
-    e->d_rowptr = e->alloc<int64_t>(D + 1);
-    e->d_col = e->alloc<int32_t>(nnz);
-    e->d_val = e->alloc<double>(nnz);
+    e->drop_ham();
+    e->d_rowptr = e->ham_alloc<int64_t>(D + 1);
+    e->d_col = e->ham_alloc<int32_t>(nnz);
+    e->d_val = e->ham_alloc<double>(nnz);
     if (!e->d_rowptr || !e->d_col || !e->d_val) return e->fail(AEGPU_ERR_NOMEM, "CSR allocation failed");
     cudaMemcpy(e->d_rowptr, rowptr, (D + 1) * sizeof(int64_t), cudaMemcpyHostToDevice);
     if (nnz) {
@@ -1795,18 +1980,26 @@ int aegpu_set_ham_csr(aegpu_engine *e, int64_t nnz, const int64_t *rowptr, const
         cudaMemcpy(e->d_val, val, nnz * sizeof(double), cudaMemcpyHostToDevice);
     }
     e->ham_kind = 1;
+    e->ham_per_instance = false;
+    e->ell_stride_inst = 0;
     e->ham_entries = nnz;
     e->h_valid = false;
     cudaDeviceSynchronize();
     return e->cuda_check("set_ham_csr");
 }
 
-int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2, int mode)
+}  // extern "C"
+
+namespace {
+
+// Hamiltonian from integrals for ntab table sets: ntab = 1 shares one Hamiltonian
+// between all instances, ntab = nb gives instance b the integrals h1s[b], g2s[b].
+int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int ntab, int mode)
 {
-    if (!e || !h1 || !g2) return AEGPU_ERR_ARG;
     if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
     if (e->B.kind != BASIS_SZ) return e->fail(AEGPU_ERR_UNSUPPORTED, "integral Hamiltonians need the Sz sector");
     const int N = e->B.N;
+    const size_t NN = (size_t)N * N, N4 = NN * NN;
     IntArgs a{};
     a.N = N;
     a.nq = e->B.nq;
@@ -1818,69 +2011,109 @@ int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2,
     auto c2 = [](int64_t n) { return n * (n - 1) / 2; };
     a.width = 1 + (int64_t)a.nOa * a.nVa + (int64_t)a.nOb * a.nVb + c2(a.nOa) * c2(a.nVa) + c2(a.nOb) * c2(a.nVb) +
               (int64_t)a.nOa * a.nVa * a.nOb * a.nVb;
-    e->d_h1 = e->alloc<double>((size_t)N * N);
-    e->d_g2 = e->alloc<double>((size_t)N * N * N * N);
-    if (!e->d_h1 || !e->d_g2) return e->fail(AEGPU_ERR_NOMEM, "integral allocation failed");
-    cudaMemcpy(e->d_h1, h1, sizeof(double) * N * N, cudaMemcpyHostToDevice);
-    cudaMemcpy(e->d_g2, g2, sizeof(double) * N * N * N * N, cudaMemcpyHostToDevice);
+    a.stride = (a.width + 3) & ~(int64_t)3;
+    e->drop_ham();
+    auto ham_alloc = [&](auto *&ptr, size_t count) {
+        using T = std::remove_reference_t<decltype(*ptr)>;
+        ptr = e->ham_alloc<T>(count);
+        return ptr != nullptr;
+    };
+    auto ham_upload = [&](auto *&ptr, const auto &v) {
+        using T = std::remove_const_t<std::remove_reference_t<decltype(*ptr)>>;
+        T *p = e->ham_alloc<T>(v.size());
+        ptr = p;
+        if (!p) return false;
+        if (!v.empty()) cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return true;
+    };
+    if (!ham_alloc(e->d_h1, NN * ntab) || !ham_alloc(e->d_g2, N4 * ntab))
+        return e->fail(AEGPU_ERR_NOMEM, "integral allocation failed");
+    cudaMemcpy(e->d_h1, h1s, sizeof(double) * NN * ntab, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_g2, g2s, sizeof(double) * N4 * ntab, cudaMemcpyHostToDevice);
     cudaDeviceSynchronize();
     a.h1 = e->d_h1;
     a.g2 = e->d_g2;
-    a.stride = (a.width + 3) & ~(int64_t)3;
     e->ints = a;
     e->ell_width = (int)a.stride;
     const int64_t D = (int64_t)e->B.D;
-    const double ell_bytes = (double)((D + 31) & ~(int64_t)31) * a.stride * 12.0;
+    const int64_t Dpad = (D + 31) & ~(int64_t)31;
+    const double ell_bytes = (double)Dpad * a.stride * 12.0 * ntab;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     if (mode == AEGPU_HAM_AUTO) mode = ell_bytes < 0.6 * (double)free_b ? AEGPU_HAM_STORED : AEGPU_HAM_ON_THE_FLY;
+    e->ham_per_instance = ntab > 1;
     if (mode == AEGPU_HAM_STORED) {
-        const int64_t Dpad = (D + 31) & ~(int64_t)31;
-        e->d_col = e->alloc<int32_t>((size_t)Dpad * a.stride);
-        e->d_val = e->alloc<double>((size_t)Dpad * a.stride);
-        if (!e->d_col || !e->d_val) return e->fail(AEGPU_ERR_NOMEM, "ELL allocation failed");
+        const size_t per = (size_t)Dpad * a.stride;
+        if (!ham_alloc(e->d_col, per * ntab) || !ham_alloc(e->d_val, per * ntab))
+            return e->fail(AEGPU_ERR_NOMEM, "ELL allocation failed");
         const int64_t chunk = 1 << 16;
-        for (int64_t r0 = 0; r0 < Dpad; r0 += chunk) {
-            k_ell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, e->d_col, e->d_val, r0, std::min(Dpad, r0 + chunk));
-            e->launches += 1;
+        for (int t = 0; t < ntab; ++t) {
+            IntArgs ai = a;
+            ai.h1 = e->d_h1 + NN * t;
+            ai.g2 = e->d_g2 + N4 * t;
+            for (int64_t r0 = 0; r0 < Dpad; r0 += chunk) {
+                k_ell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(ai, e->d_col + per * t, e->d_val + per * t, r0,
+                                                                    std::min(Dpad, r0 + chunk));
+                e->launches += 1;
+            }
         }
         e->ham_kind = 2;
         e->ham_entries = D * a.stride;
+        e->ell_stride_inst = ntab > 1 ? (int64_t)per : 0;
     } else {
-        // on the fly: host-built string tables, diagonal on the GPU
-        OtfTables T;
-        std::vector<double> hv(h1, h1 + (size_t)N * N), gv(g2, g2 + (size_t)N * N * N * N);
-        build_otf_tables(e->B, hv, gv, T);
+        // on the fly: host-built string tables (the string lists do not depend on the
+        // integrals; the integral tables are one set per instance), diagonal on the GPU
+        std::vector<OtfTables> T(ntab);
+        {
+            const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+            std::vector<std::thread> pool;
+            std::atomic<int> next{0};
+            for (int w = 0; w < std::min(hw, ntab); ++w)
+                pool.emplace_back([&]() {
+                    for (int t; (t = next.fetch_add(1)) < ntab;) {
+                        std::vector<double> hv(h1s + NN * t, h1s + NN * (t + 1)), gv(g2s + N4 * t, g2s + N4 * (t + 1));
+                        build_otf_tables(e->B, hv, gv, T[t], t == 0);
+                    }
+                });
+            for (auto &th : pool) th.join();
+        }
+        auto cat = [&](std::vector<double> OtfTables::*m) {
+            std::vector<double> all;
+            all.reserve((T[0].*m).size() * ntab);
+            for (auto &x : T) all.insert(all.end(), (x.*m).begin(), (x.*m).end());
+            return all;
+        };
+        const OtfTables &T0 = T[0];
         OtfArgs o{};
         o.N = N;
-        o.P2 = T.P2;
+        o.P2 = T0.P2;
         o.nA = (int)e->B.nA;
         o.nB = (int)e->B.nB;
-        o.nsa = T.nsa;
-        o.nda = T.nda;
-        o.nsb = T.nsb;
-        o.ndb = T.ndb;
-        o.sa_rank = e->upload(T.sa_rank);
-        o.sa_code = e->upload(T.sa_code);
-        o.da_rank = e->upload(T.da_rank);
-        o.da_code = e->upload(T.da_code);
-        o.sb_rank = e->upload(T.sb_rank);
-        o.sb_code = e->upload(T.sb_code);
-        o.db_rank = e->upload(T.db_rank);
-        o.db_code = e->upload(T.db_code);
-        o.vss = e->upload(T.vss);
-        o.vab = e->upload(T.vab);
-        o.a_alpha = e->upload(T.a_alpha);
-        o.b_alpha = e->upload(T.b_alpha);
-        o.a_beta = e->upload(T.a_beta);
-        o.b_beta = e->upload(T.b_beta);
-        double *diag = e->alloc<double>(D);
-        if (!diag || !o.vab || !o.b_beta) return e->fail(AEGPU_ERR_NOMEM, "on-the-fly table allocation failed");
+        o.nsa = T0.nsa;
+        o.nda = T0.nda;
+        o.nsb = T0.nsb;
+        o.ndb = T0.ndb;
+        bool ok = ham_upload(o.sa_rank, T0.sa_rank) && ham_upload(o.sa_code, T0.sa_code) &&
+                  ham_upload(o.da_rank, T0.da_rank) && ham_upload(o.da_code, T0.da_code) &&
+                  ham_upload(o.sb_rank, T0.sb_rank) && ham_upload(o.sb_code, T0.sb_code) &&
+                  ham_upload(o.db_rank, T0.db_rank) && ham_upload(o.db_code, T0.db_code) &&
+                  ham_upload(o.vss, cat(&OtfTables::vss)) && ham_upload(o.vab, cat(&OtfTables::vab)) &&
+                  ham_upload(o.a_alpha, cat(&OtfTables::a_alpha)) && ham_upload(o.b_alpha, cat(&OtfTables::b_alpha)) &&
+                  ham_upload(o.a_beta, cat(&OtfTables::a_beta)) && ham_upload(o.b_beta, cat(&OtfTables::b_beta));
+        double *diag = nullptr;
+        ok = ok && ham_alloc(diag, (size_t)D * ntab);
+        if (!ok) return e->fail(AEGPU_ERR_NOMEM, "on-the-fly table allocation failed");
         o.diag = diag;
+        o.shared = ntab == 1;
         cudaDeviceSynchronize();
-        k_diag_build<<<e->sm_count * 8, 256, 0, e->stream>>>(a, diag);
-        e->launches += 1;
-        const size_t smem = otf_smem_bytes(N, T.P2, T.nsa, T.nda);
+        for (int t = 0; t < ntab; ++t) {
+            IntArgs ai = a;
+            ai.h1 = e->d_h1 + NN * t;
+            ai.g2 = e->d_g2 + N4 * t;
+            k_diag_build<<<e->sm_count * 8, 256, 0, e->stream>>>(ai, diag + (size_t)D * t);
+            e->launches += 1;
+        }
+        const size_t smem = otf_smem_bytes(N, T0.P2, T0.nsa, T0.nda);
         int optin = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
@@ -1889,16 +2122,49 @@ int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2,
         e->otf_threads = (int)std::min<int64_t>(512, ((int64_t)o.nB + 31) / 32 * 32);
         e->otf_chunks = (o.nB + e->otf_threads - 1) / e->otf_threads;
         const int64_t nparts = (int64_t)o.nA * e->otf_chunks;
-        if (nparts > (int64_t)std::max<int64_t>(e->spmv_grid, (D + kSpmvThreads - 1) / kSpmvThreads)) {
-            e->d_epart = e->alloc<double>(nparts);
-            if (!e->d_epart) return e->fail(AEGPU_ERR_NOMEM, "partial-sum allocation failed");
+        if (nparts > e->n_epart) {
+            e->n_epart = nparts;
+            int rc = e->alloc_instances(e->nb);
+            if (rc) return rc;
         }
         e->ham_kind = 3;
         e->ham_entries = 0;
+        e->ell_stride_inst = 0;
     }
     e->h_valid = false;
     return stream_sync(e, "set_ham_integrals");
 }
+
+}  // namespace
+
+extern "C" {
+
+int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2, int mode)
+{
+    if (!e || !h1 || !g2) return AEGPU_ERR_ARG;
+    return set_integrals(e, h1, g2, 1, mode);
+}
+
+int aegpu_set_ham_integrals_batch(aegpu_engine *e, const double *h1s, const double *g2s, int mode)
+{
+    if (!e || !h1s || !g2s) return AEGPU_ERR_ARG;
+    return set_integrals(e, h1s, g2s, e->nb, mode);
+}
+
+int aegpu_set_batch(aegpu_engine *e, int nb)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (nb < 1 || nb > 65535) return e->fail(AEGPU_ERR_ARG, "batch size must be in 1..65535");
+    if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    if (nb == e->nb) return AEGPU_OK;
+    // per-instance Hamiltonians were built for the old batch: they must be set again
+    if (e->ham_per_instance) e->drop_ham();
+    int rc = e->alloc_instances(nb);
+    if (rc) return rc;
+    return e->cuda_check("set_batch");
+}
+
+int aegpu_batch_size(const aegpu_engine *e) { return e ? e->nb : -1; }
 
 int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored)
 {
@@ -1915,7 +2181,7 @@ int aegpu_evolve(aegpu_engine *e, const double *angles, double *state)
     int rc = ensure_state(e, angles);
     if (rc) return rc;
     if (state)
-        cudaMemcpyAsync(state, e->d_psi, (size_t)e->B.D * e->W * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        cudaMemcpyAsync(state, e->d_psi, e->vec_elems() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "evolve");
 }
 
@@ -1926,11 +2192,11 @@ int aegpu_energy(aegpu_engine *e, const double *angles, double *energy)
     int rc = ensure_state(e, angles);
     if (rc) return rc;
     if (!e->h_valid) {
-        rc = run_energy(e, e->d_scalar);
+        rc = run_energy(e, e->d_scalar, e->nb);
         if (rc) return rc;
         e->h_valid = true;
     }
-    cudaMemcpyAsync(energy, e->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "energy");
 }
 
@@ -1941,19 +2207,22 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
     int rc = ensure_state(e, angles);
     if (rc) return rc;
     if (!e->h_valid) {
-        rc = run_energy(e, e->d_scalar);
+        rc = run_energy(e, e->d_scalar, e->nb);
         if (rc) return rc;
     }
     // the checkpointed sweep consumes H psi and leaves psi as it is
-    rc = run_backward(e, e->d_grad);
+    rc = run_backward(e, e->d_grad, e->nb);
     if (rc) return rc;
     e->h_valid = false;
-    if (energy) cudaMemcpyAsync(energy, e->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
-    cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    if (energy) cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "gradient");
 }
 
-// Capture evolve + H psi + adjoint sweep (reading d_ang) into one CUDA graph.
+}  // extern "C"
+
+// Capture pass constants + evolve + H psi + adjoint sweep of all nb instances
+// (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
 static int capture_grad_graph(aegpu_engine *e)
 {
     cudaStream_t cap = nullptr, saved = e->stream;
@@ -1964,16 +2233,19 @@ static int capture_grad_graph(aegpu_engine *e)
     int rc = AEGPU_OK;
     if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = e->cuda_check("begin capture");
     if (!rc) {
-        k_sincos<<<((int)e->excs.size() + 127) / 128, 128, 0, cap>>>(e->d_ang, e->d_sc, (int)e->excs.size());
-        e->launches += 1;
-        rc = run_evolve(e);
-        if (!rc) rc = run_energy(e, e->d_scalar);
-        if (!rc) rc = run_backward(e, e->d_grad);
+        rc = run_prep(e, e->nb);
+        if (!rc) rc = run_evolve(e, e->nb);
+        if (!rc) rc = run_energy(e, e->d_scalar, e->nb);
+        if (!rc) rc = run_backward(e, e->d_grad, e->nb);
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         if (!rc && ce != cudaSuccess) rc = e->fail(AEGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(ce));
     }
     if (!rc && cudaGraphInstantiate(&e->grad_graph, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
-    if (g) cudaGraphDestroy(g);
+    if (!rc) {
+        e->grad_graph_def = g;
+    } else if (g) {
+        cudaGraphDestroy(g);
+    }
     cudaStreamDestroy(cap);
     e->stream = saved;
     e->graph_launches = e->launches - l0;
@@ -1982,22 +2254,24 @@ static int capture_grad_graph(aegpu_engine *e)
     return rc;
 }
 
+extern "C" {
+
 int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream)
 {
     if (!e || !angles_dev || !grad_dev) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
-    const int nops = (int)e->excs.size();
+    const size_t nang = e->excs.size() * (size_t)e->nb;
     if (e->use_graph && !e->timing) {
         if (!e->grad_graph) {
             int rc = capture_grad_graph(e);
             if (rc) return rc;
         }
         cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
-        cudaMemcpyAsync(e->d_ang, angles_dev, nops * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(e->d_ang, angles_dev, nang * sizeof(double), cudaMemcpyDeviceToDevice, st);
         if (cudaGraphLaunch(e->grad_graph, st) != cudaSuccess) return e->cuda_check("graph launch");
         e->launches += e->graph_launches;
-        if (energy_dev) cudaMemcpyAsync(energy_dev, e->d_scalar, sizeof(double), cudaMemcpyDeviceToDevice, st);
-        cudaMemcpyAsync(grad_dev, e->d_grad, nops * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (energy_dev) cudaMemcpyAsync(energy_dev, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(grad_dev, e->d_grad, nang * sizeof(double), cudaMemcpyDeviceToDevice, st);
         e->psi_valid = e->h_valid = false;
         return e->cuda_check("gradient_dev");
     }
@@ -2007,12 +2281,12 @@ int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy
     if (e->timing)
         for (auto &x : ev) x = e->next_event();
     if (e->timing) cudaEventRecord(ev[0], e->stream);
-    int rc = upload_angles(e, angles_dev, false);
-    if (!rc) rc = run_evolve(e);
+    int rc = upload_angles(e, angles_dev, false, e->nb);
+    if (!rc) rc = run_evolve(e, e->nb);
     if (e->timing) cudaEventRecord(ev[1], e->stream);
-    if (!rc) rc = run_energy(e, energy_dev ? energy_dev : e->d_scalar);
+    if (!rc) rc = run_energy(e, energy_dev ? energy_dev : e->d_scalar, e->nb);
     if (e->timing) cudaEventRecord(ev[2], e->stream);
-    if (!rc) rc = run_backward(e, grad_dev);
+    if (!rc) rc = run_backward(e, grad_dev, e->nb);
     if (e->timing) {
         cudaEventRecord(ev[3], e->stream);
         e->ev_marks.push_back(ev);
@@ -2021,6 +2295,150 @@ int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy
     e->psi_valid = e->h_valid = false;
     return rc;
 }
+
+int aegpu_io_dev(aegpu_engine *e, double **angles_dev, double **energy_dev, double **grad_dev)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (!e->d_ang) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    if (angles_dev) *angles_dev = e->d_ang;
+    if (energy_dev) *energy_dev = e->d_scalar;
+    if (grad_dev) *grad_dev = e->d_grad;
+    return AEGPU_OK;
+}
+
+// Evaluate every instance at the angles already in the io buffer (graph replay).
+int aegpu_launch_io(aegpu_engine *e, void *stream)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (!e->grad_graph) {
+        int rc = capture_grad_graph(e);
+        if (rc) return rc;
+    }
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    if (cudaGraphLaunch(e->grad_graph, st) != cudaSuccess) return e->cuda_check("graph launch");
+    e->launches += e->graph_launches;
+    e->psi_valid = e->h_valid = false;
+    return e->cuda_check("launch_io");
+}
+
+// Host <-> io buffer copies on `stream` (NULL: the engine's stream); the get
+// synchronises that stream.
+int aegpu_io_put_angles(aegpu_engine *e, const double *angles, void *stream)
+{
+    if (!e || !angles) return AEGPU_ERR_ARG;
+    if (!e->d_ang) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    cudaMemcpyAsync(e->d_ang, angles, e->excs.size() * e->nb * sizeof(double), cudaMemcpyHostToDevice, st);
+    return e->cuda_check("io_put_angles");
+}
+
+int aegpu_io_get_results(aegpu_engine *e, double *energy, double *grad, void *stream)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (!e->d_ang) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    if (energy) cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (grad) cudaMemcpyAsync(grad, e->d_grad, e->excs.size() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, st);
+    cudaError_t rc = cudaStreamSynchronize(st);
+    if (rc != cudaSuccess) return e->fail(AEGPU_ERR_CUDA, std::string("io_get_results: ") + cudaGetErrorString(rc));
+    return e->cuda_check("io_get_results");
+}
+
+}  // extern "C"
+
+struct aegpu_group {
+    std::vector<aegpu_engine *> engines;
+    std::vector<int64_t> generations;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;  // used when the caller passes none
+    cudaStream_t last = nullptr;    // stream of the latest launch
+    int64_t launches = 0;
+    ~aegpu_group()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" {
+
+int aegpu_group_create(aegpu_group **out, aegpu_engine *const *engines, int n)
+{
+    if (!out || !engines || n < 1) return AEGPU_ERR_ARG;
+    *out = nullptr;
+    auto *g = new aegpu_group();
+    cudaGraph_t parent = nullptr;
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaGraphCreate(&parent, 0) != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return AEGPU_ERR_CUDA;
+    }
+    int rc = AEGPU_OK;
+    for (int i = 0; i < n && !rc; ++i) {
+        aegpu_engine *e = engines[i];
+        if (!e || !e->ham_kind) {
+            rc = e ? e->fail(AEGPU_ERR_STATE, "no Hamiltonian set") : AEGPU_ERR_ARG;
+            break;
+        }
+        if (!e->grad_graph_def) rc = capture_grad_graph(e);
+        if (rc) break;
+        // independent child graphs: the engines' evaluations may run concurrently
+        cudaGraphNode_t node;
+        if (cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, e->grad_graph_def) != cudaSuccess) {
+            cudaGetLastError();
+            rc = AEGPU_ERR_CUDA;
+            break;
+        }
+        g->engines.push_back(e);
+        g->generations.push_back(e->generation);
+        g->launches += e->graph_launches;
+    }
+    if (!rc && cudaGraphInstantiate(&g->exec, parent, 0) != cudaSuccess) {
+        cudaGetLastError();
+        rc = AEGPU_ERR_CUDA;
+    }
+    cudaGraphDestroy(parent);
+    if (rc) {
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return AEGPU_OK;
+}
+
+int aegpu_group_launch(aegpu_group *g, void *stream)
+{
+    if (!g) return AEGPU_ERR_ARG;
+    for (size_t i = 0; i < g->engines.size(); ++i)
+        if (g->engines[i]->generation != g->generations[i])
+            return g->engines[i]->fail(AEGPU_ERR_STATE, "engine changed since the group was created");
+    g->last = stream ? (cudaStream_t)stream : g->stream;
+    if (cudaGraphLaunch(g->exec, g->last) != cudaSuccess) {
+        cudaGetLastError();
+        return AEGPU_ERR_CUDA;
+    }
+    for (auto *e : g->engines) {
+        e->launches += e->graph_launches;
+        e->psi_valid = e->h_valid = false;
+    }
+    return AEGPU_OK;
+}
+
+int aegpu_group_sync(aegpu_group *g)
+{
+    if (!g) return AEGPU_ERR_ARG;
+    if (g->last && cudaStreamSynchronize(g->last) != cudaSuccess) {
+        cudaGetLastError();
+        return AEGPU_ERR_CUDA;
+    }
+    return AEGPU_OK;
+}
+
+int64_t aegpu_group_launch_count(const aegpu_group *g) { return g ? g->launches : -1; }
+
+void aegpu_group_destroy(aegpu_group *g) { delete g; }
 
 int aegpu_use_graphs(aegpu_engine *e, int enable)
 {
@@ -2035,9 +2453,9 @@ int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_d
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
-    int rc = upload_angles(e, angles_dev, false);
-    if (!rc) rc = run_evolve(e);
-    if (!rc) rc = run_energy(e, energy_dev);
+    int rc = upload_angles(e, angles_dev, false, e->nb);
+    if (!rc) rc = run_evolve(e, e->nb);
+    if (!rc) rc = run_energy(e, energy_dev, e->nb);
     e->stream = saved;
     e->psi_valid = e->h_valid = false;
     return rc;
@@ -2055,11 +2473,15 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
 {
     if (!e || !x || !y) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
-    const size_t n = (size_t)e->B.D * e->W;
+    const size_t n = e->vec_elems() * e->nb;
     double *dx = e->alloc<double>(n), *dy = e->alloc<double>(n);
-    if (!dx || !dy) return e->fail(AEGPU_ERR_NOMEM, "apply_h scratch");
+    if (!dx || !dy) {
+        e->release(dx, n * sizeof(double));
+        e->release(dy, n * sizeof(double));
+        return e->fail(AEGPU_ERR_NOMEM, "apply_h scratch");
+    }
     cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, e->stream);
-    int rc = run_apply(e, dx, dy, nullptr);
+    int rc = run_apply(e, dx, dy, nullptr, e->nb);
     if (!rc) {
         cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
         rc = stream_sync(e, "apply_h");
@@ -2074,6 +2496,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
 {
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the Hessian needs a batch size of 1");
     const int nops = (int)e->excs.size();
     const int W = e->W;
     const int64_t D = (int64_t)e->B.D;
@@ -2120,7 +2543,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         cleanup();
         return e->fail(AEGPU_ERR_NOMEM, "Hessian scratch allocation failed");
     }
-    int rc = upload_angles(e, angles, true);
+    int rc = upload_angles(e, angles, true, 1);
     if (rc) { cleanup(); return rc; }
     cudaStream_t s = e->stream;
     cudaMemsetAsync(T, 0, n * nops * sizeof(double), s);
@@ -2131,12 +2554,13 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         auto &b = e->dblocks[bi];
         const int p0 = e->block_pos0[bi];
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table);
-            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0, nullptr);
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table,
+                                                                       nops);
+            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0, nullptr, 0, 0);
             k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_psi, T, n, e->d_tpos);
             e->launches += 3;
         } else if (b.ntiles) {
-            BlockArgs a = e->block_args(b, 1.0);
+            BlockArgs a = e->block_args((int)bi, 1.0);
             if (W == 1) {
                 if (p0 > 0) k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
                 k_block_tangent<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
@@ -2159,7 +2583,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         for (int v = 0; v < V; ++v) {
             cudaMemcpy2DAsync(e->d_tmp, sizeof(double), TC + v, (size_t)V * sizeof(double), sizeof(double), n,
                               cudaMemcpyDeviceToDevice, s);
-            run_apply(e, e->d_tmp, e->d_h, nullptr);
+            run_apply(e, e->d_tmp, e->d_h, nullptr, 1);
             cudaMemcpy2DAsync(HTC + v, (size_t)V * sizeof(double), e->d_h, sizeof(double), sizeof(double), n,
                               cudaMemcpyDeviceToDevice, s);
         }
@@ -2184,15 +2608,16 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         const int p0 = e->block_pos0[bi];
         const int nvec = p0 + b.nslots;
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table);
+            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table,
+                                                                       nops);
             dim3 g(kDiagGrid, nvec);
             k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
                                                                             b.ops, p0, Hops, nops);
-            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1, nullptr);
+            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1, nullptr, 0, 0);
             e->launches += 4;
         } else if (b.ntiles) {
-            BlockArgs a = e->block_args(b, -1.0);
+            BlockArgs a = e->block_args(bi, -1.0);
             const int vchunk = 8;
             dim3 g(b.ntiles, (nvec + vchunk - 1) / vchunk);
             if (W == 1) {
@@ -2235,9 +2660,9 @@ int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double 
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
     int np = 0;
-    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, &np);
+    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, e->nb, &np);
     if (!rc && energy_dev) {
-        k_reduce_sum<<<1, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0);
+        k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0);
         e->launches += 1;
         rc = e->cuda_check("apply_dev");
     }

@@ -133,14 +133,17 @@ void single_tables(const TwoE &V, const std::vector<double> &h1, int N, int off_
 
 }  // namespace
 
-void build_otf_tables(const Basis &B, const std::vector<double> &h1, const std::vector<double> &g2, OtfTables &T)
+void build_otf_tables(const Basis &B, const std::vector<double> &h1, const std::vector<double> &g2, OtfTables &T,
+                      bool with_strings)
 {
     const int N = B.N;
     T.N = N;
     T.P2 = N * (N - 1) / 2;
     TwoE V{N, g2.data()};
-    string_lists(B.strA, B.rankA, N, B.na, T.sa_rank, T.sa_code, T.da_rank, T.da_code, T.nsa, T.nda);
-    string_lists(B.strB, B.rankB, N, B.nb, T.sb_rank, T.sb_code, T.db_rank, T.db_code, T.nsb, T.ndb);
+    if (with_strings) {
+        string_lists(B.strA, B.rankA, N, B.na, T.sa_rank, T.sa_code, T.da_rank, T.da_code, T.nsa, T.nda);
+        string_lists(B.strB, B.rankB, N, B.nb, T.sb_rank, T.sb_code, T.db_rank, T.db_code, T.nsb, T.ndb);
+    }
     // same-spin doubles (pairs of orbitals inside one spin block; identical for both spins)
     T.vss.assign((size_t)T.P2 * T.P2, 0.0);
     for (int p1 = 0; p1 < N; ++p1)

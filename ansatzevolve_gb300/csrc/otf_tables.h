@@ -20,6 +20,9 @@ struct OtfTables {
     std::vector<double> a_beta, b_beta;      // [beta string][p*N+r],  [alpha string][p*N+r]
 };
 
-void build_otf_tables(const Basis &B, const std::vector<double> &h1, const std::vector<double> &g2, OtfTables &T);
+// with_strings = false skips the per-string excitation lists (they depend only on the
+// basis), for the second and later instances of a batch that share them.
+void build_otf_tables(const Basis &B, const std::vector<double> &h1, const std::vector<double> &g2, OtfTables &T,
+                      bool with_strings = true);
 
 }  // namespace ae

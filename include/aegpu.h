@@ -70,6 +70,18 @@ int aegpu_set_ham_csr(aegpu_engine *e, int64_t nnz, const int64_t *rowptr, const
  * (the layout of <prefix>_oneEInts.bin / _twoEInts.bin, hamiltonianmatrix.cpp:402-554).
  * Needs the Sz sector. */
 int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2, int mode);
+
+/* Batches (no counterpart in the reference, which evaluates one angle vector per
+ * call).  After aegpu_set_batch(e, nb) every evaluation below works on nb instances
+ * of the problem at once: angles[nb][nops], energy[nb], grad[nb][nops],
+ * state / x / y [nb][D*(1+complex)].  All instances start from the same initial
+ * state.  A Hamiltonian set by aegpu_set_ham_csr / aegpu_set_ham_integrals is shared
+ * by all instances; aegpu_set_ham_integrals_batch gives instance b its own integrals
+ * h1s[b][N*N], g2s[b][N^4] (set the batch size first: changing it drops them).
+ * nb is 1..65535; the Hessian needs nb = 1. */
+int aegpu_set_batch(aegpu_engine *e, int nb);
+int aegpu_batch_size(const aegpu_engine *e);
+int aegpu_set_ham_integrals_batch(aegpu_engine *e, const double *h1s, const double *g2s, int mode);
 /* Which representation is in use: 1 CSR, 2 stored ELL, 3 on the fly; and its stored entries. */
 int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored_entries);
 
@@ -84,13 +96,48 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
                   double *energy, double *grad_comp, double *hess_comp);
 int aegpu_apply_h(aegpu_engine *e, const double *x, double *y);
 
-/* Device-resident variants (inputs already in HBM): angles_dev[nops], energy_dev[1],
- * grad_dev[nops].  Enqueued on `stream`; nothing is synchronised. */
+/* Device-resident variants (inputs already in HBM): angles_dev[nb][nops],
+ * energy_dev[nb], grad_dev[nb][nops].  Enqueued on `stream`; nothing is synchronised. */
 int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream);
 int aegpu_energy_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, void *stream);
 /* aegpu_gradient_dev replays one captured CUDA graph of the whole evaluation
  * (default; phase timing uses the stream path instead).  enable = 0 disables it. */
 int aegpu_use_graphs(aegpu_engine *e, int enable);
+/* The engine's own device buffers that its captured evaluation graph reads (angles
+ * [nb][nops]) and writes (energies [nb], gradients [nb][nops]).  Valid until the
+ * batch size or the problem changes. */
+int aegpu_io_dev(aegpu_engine *e, double **angles_dev, double **energy_dev, double **grad_dev);
+/* Copies between host arrays and those buffers, enqueued on `stream` (NULL: the
+ * engine's own stream); aegpu_io_get_results synchronises the stream. */
+int aegpu_io_put_angles(aegpu_engine *e, const double *angles, void *stream);
+int aegpu_io_get_results(aegpu_engine *e, double *energy, double *grad, void *stream);
+/* Energy + gradient of every instance at the angles in the io buffer, written to
+ * the io result buffers: one replay of the captured graph on `stream`. */
+int aegpu_launch_io(aegpu_engine *e, void *stream);
+/* A group evaluates several engines (e.g. batches of different determinant-space
+ * sizes) with ONE graph launch: each member's captured energy + gradient graph is a
+ * child node with no dependencies, reading and writing the member's aegpu_io_dev
+ * buffers.  Launching fails with AEGPU_ERR_STATE once a member's batch size or
+ * Hamiltonian has changed.  No counterpart in the reference. */
+typedef struct aegpu_group aegpu_group;
+int aegpu_group_create(aegpu_group **out, aegpu_engine *const *engines, int n);
+/* stream NULL: the group's own stream.  aegpu_group_sync waits for the latest launch. */
+int aegpu_group_launch(aegpu_group *g, void *stream);
+int aegpu_group_sync(aegpu_group *g);
+int64_t aegpu_group_launch_count(const aegpu_group *g);
+void aegpu_group_destroy(aegpu_group *g);
+/* Optimisers.  Compressed parameters x[P]: theta_op = scale[op] * x[param[op]].
+ * aegpu_optimise_newton: the reference's Newton method (TUPSQuantities::OptimiseTups,
+ * tupsquantities.cpp:1940-2011) for a batch of 1, with the analytic Hessian; x is the
+ * start on entry and the optimum on return.
+ * aegpu_optimise_batch: all nb instances (x[nb][P]) by lockstep BFGS, one batched
+ * energy + gradient evaluation per round, until |g| < gtol for every instance or
+ * max_rounds rounds; max_step bounds each trial step's length (<= 0: 1.0).
+ * No counterpart in the reference for the batched optimiser. */
+int aegpu_optimise_newton(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
+                          double *energy, double *gnorm, int64_t *hessian_evals, int64_t *energy_evals);
+int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
+                         int max_rounds, double max_step, double *energy, double *gnorm, int *iters, int64_t *rounds);
 /* y_dev = H x_dev on device vectors; energy_dev (nullable) receives <x|H x>. */
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 /* CUDA-event timing of the phases of aegpu_gradient_dev (evolve, H*psi + energy,

@@ -1,0 +1,204 @@
+"""Batched evaluation (nb instances per call) against one-at-a-time evaluation and the
+oracle.  A batch runs the same kernels with an instance index, so every instance's
+energy, gradient and state must be bit-identical to evaluating it alone."""
+import numpy as np
+import pytest
+
+import ansatzevolve_gb300 as ae
+from ansatzevolve_gb300.synthetic import family_integrals
+from tests.fixtures import oracle_synthetic, sector_of, synthetic_problem
+
+pytestmark = pytest.mark.gpu
+TOL_E, TOL_G = 1e-10, 1e-9
+
+
+def make_engine(pb, nb=1):
+    ops0 = np.asarray(pb["ops_1b"]) - 1
+    N = pb["N"]
+    eng = ae.Engine(2 * N, ae.BASIS_SZ, pb["na"] + pb["nb"], pb["na"], pb["nb"], ops0)
+    init = np.zeros(eng.D)
+    init[np.searchsorted(eng.states(), pb["hf"])] = 1.0
+    eng.set_initial(init)
+    if nb > 1:
+        eng.set_batch(nb)
+    return eng
+
+
+@pytest.mark.parametrize("mode", [ae.HAM_STORED, ae.HAM_ON_THE_FLY])
+def test_batch_shared_hamiltonian_bit_identical(mode):
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    nb = 6
+    rng = np.random.default_rng(21)
+    nops = len(pb["ops_1b"])
+    ang = rng.uniform(-0.3, 0.3, (nb, nops))
+    one = make_engine(pb)
+    one.set_ham_integrals(pb["h1"], pb["g2"], mode)
+    bat = make_engine(pb, nb)
+    assert bat.nb == nb
+    bat.set_ham_integrals(pb["h1"], pb["g2"], mode)
+    Eb, gb = bat.gradient(ang)
+    psib = bat.evolve(ang)
+    assert gb.shape == (nb, nops) and psib.shape == (nb, one.D)
+    for b in range(nb):
+        E, g = one.gradient(ang[b])
+        assert Eb[b] == E
+        assert np.array_equal(gb[b], g)
+        assert np.array_equal(psib[b], one.evolve(ang[b]))
+    assert np.array_equal(bat.energy(ang), Eb)
+    # one instance against the oracle
+    o = oracle_synthetic(pb, csr=False)
+    Eo, go = o.energy_gradient_ops(ang[3])
+    assert abs(Eb[3] - Eo) < TOL_E
+    np.testing.assert_allclose(gb[3], go, atol=TOL_G, rtol=0)
+    one.close()
+    bat.close()
+
+
+@pytest.mark.parametrize("mode", [ae.HAM_STORED, ae.HAM_ON_THE_FLY])
+def test_batch_per_instance_integrals(mode):
+    """Instance b carries its own integrals (a Hamiltonian family): each must agree
+    bit for bit with an engine holding only that Hamiltonian."""
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    nb = 5
+    s = np.linspace(0.0, 1.0, nb)
+    fam = [family_integrals(8, float(si), seed=3) for si in s]
+    h1s = np.stack([f[0] for f in fam])
+    g2s = np.stack([f[1] for f in fam])
+    rng = np.random.default_rng(5)
+    ang = rng.uniform(-0.3, 0.3, (nb, len(pb["ops_1b"])))
+    bat = make_engine(pb, nb)
+    bat.set_ham_integrals_batch(h1s, g2s, mode)
+    Eb, gb = bat.gradient(ang)
+    one = make_engine(pb)
+    for b in range(nb):
+        one.set_ham_integrals(h1s[b], g2s[b], mode)
+        E, g = one.gradient(ang[b])
+        assert Eb[b] == E, (b, Eb[b], E)
+        assert np.array_equal(gb[b], g)
+    # the last instance against the oracle
+    pb_last = dict(pb, h1=h1s[-1], g2=g2s[-1])
+    Eo, go = oracle_synthetic(pb_last, csr=False).energy_gradient_ops(ang[-1])
+    assert abs(Eb[-1] - Eo) < TOL_E
+    np.testing.assert_allclose(gb[-1], go, atol=TOL_G, rtol=0)
+    # changing the batch size drops per-instance Hamiltonians
+    bat.set_batch(nb + 1)
+    with pytest.raises(ae.AegpuError, match="no Hamiltonian"):
+        bat.energy(np.zeros((nb + 1, len(pb["ops_1b"]))))
+    one.close()
+    bat.close()
+
+
+def test_batch_10_orbital_family_on_the_fly_vs_oracle():
+    pb = synthetic_problem(10, 5, 5, 3, 0)
+    nb = 3
+    fam = [family_integrals(10, si, seed=11) for si in (0.1, 0.5, 0.9)]
+    bat = make_engine(pb, nb)
+    bat.set_ham_integrals_batch(np.stack([f[0] for f in fam]), np.stack([f[1] for f in fam]), ae.HAM_ON_THE_FLY)
+    rng = np.random.default_rng(3)
+    ang = rng.uniform(-0.3, 0.3, (nb, len(pb["ops_1b"])))
+    Eb, gb = bat.gradient(ang)
+    b = 1
+    Eo, go = oracle_synthetic(dict(pb, h1=fam[b][0], g2=fam[b][1]), csr=False).energy_gradient_ops(ang[b])
+    assert abs(Eb[b] - Eo) < TOL_E
+    np.testing.assert_allclose(gb[b], go, atol=TOL_G, rtol=0)
+    bat.close()
+
+
+def test_batch_graph_path_matches_host_path():
+    torch = pytest.importorskip("torch")
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    nb = 7
+    nops = len(pb["ops_1b"])
+    bat = make_engine(pb, nb)
+    fam = [family_integrals(8, float(si), seed=4) for si in np.linspace(0, 1, nb)]
+    bat.set_ham_integrals_batch(np.stack([f[0] for f in fam]), np.stack([f[1] for f in fam]), ae.HAM_STORED)
+    rng = np.random.default_rng(17)
+    for k in range(3):
+        ang = rng.uniform(-0.3, 0.3, (nb, nops))
+        E, g = bat.gradient(ang)
+        a = torch.tensor(ang, dtype=torch.float64, device="cuda")
+        Ed = torch.zeros(nb, dtype=torch.float64, device="cuda")
+        gd = torch.zeros((nb, nops), dtype=torch.float64, device="cuda")
+        bat.gradient_dev(a.data_ptr(), Ed.data_ptr(), gd.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        assert np.array_equal(Ed.cpu().numpy(), E)
+        assert np.array_equal(gd.cpu().numpy(), g)
+    bat.close()
+
+
+def test_batch_complex_with_number_operators(golden):
+    """Complex mode with diagonal (number) passes, one Hamiltonian shared by the batch."""
+    fx = golden("h4c")
+    nq = int(fx["nq"])
+    ops0 = np.asarray(fx["ops_1b"]) - 1
+    kind, ne, na, nbe = sector_of(nq, fx["init_idx"], ops0)
+    assert kind == ae.BASIS_SZ
+    order = np.asarray(fx["order_1b"]) - 1
+    scale = np.asarray(fx["scale"])
+
+    def build(nb):
+        eng = ae.Engine(nq, kind, ne, na, nbe, ops0, complex_mode=True)
+        init = np.zeros(2 * eng.D)
+        pos = np.searchsorted(eng.states(), np.asarray(fx["init_idx"]))
+        init[2 * pos] = fx["init_re"]
+        init[2 * pos + 1] = fx["init_im"]
+        eng.set_initial(init)
+        if nb > 1:
+            eng.set_batch(nb)
+        eng.set_ham_integrals(fx["h1"], fx["g2"], ae.HAM_STORED)
+        return eng
+
+    nb = 4
+    rng = np.random.default_rng(2)
+    P = int(order.max()) + 1
+    xs = rng.uniform(-0.5, 0.5, (nb, P))
+    ang = scale * xs[:, order]
+    one, bat = build(1), build(nb)
+    Eb, gb = bat.gradient(ang)
+    for b in range(nb):
+        E, g = one.gradient(ang[b])
+        assert Eb[b] == E
+        assert np.array_equal(gb[b], g)
+    # every instance at the fixture's angles reproduces the reference energy
+    for k in range(len(fx["angles"])):
+        angk = np.tile(scale * np.asarray(fx["angles"][k])[:P][order], (nb, 1))
+        np.testing.assert_allclose(bat.energy(angk), fx["E"][k] - float(fx["nuclear"]), atol=TOL_E, rtol=0)
+    one.close()
+    bat.close()
+
+
+def test_group_launch_mixed_sizes():
+    """Two batches of different determinant-space sizes evaluated by one graph launch
+    give the same results as each engine's own evaluation."""
+    p8 = synthetic_problem(8, 4, 4, 2, 0)
+    p6 = synthetic_problem(6, 3, 3, 2, 1)
+    e8 = make_engine(p8, 3)
+    fam = [family_integrals(8, float(si), seed=6) for si in (0.0, 0.4, 0.8)]
+    e8.set_ham_integrals_batch(np.stack([f[0] for f in fam]), np.stack([f[1] for f in fam]), ae.HAM_ON_THE_FLY)
+    e6 = make_engine(p6, 2)
+    e6.set_ham_integrals(p6["h1"], p6["g2"], ae.HAM_STORED)
+    grp = ae.Group([e8, e6])
+    assert grp.launch_count() > 0
+    rng = np.random.default_rng(23)
+    for k in range(2):
+        a8 = rng.uniform(-0.3, 0.3, (3, e8.nops))
+        a6 = rng.uniform(-0.3, 0.3, (2, e6.nops))
+        e8.io_put_angles(a8)
+        e6.io_put_angles(a6)
+        for e in (e8, e6):  # uploads ran on the engines' streams: finish them
+            e.io_get_results()
+        grp.launch()
+        grp.sync()
+        E8, g8 = e8.io_get_results()
+        E6, g6 = e6.io_get_results()
+        R8, G8 = e8.gradient(a8)
+        R6, G6 = e6.gradient(a6)
+        assert np.array_equal(E8, R8) and np.array_equal(g8, G8)
+        assert np.array_equal(E6, R6) and np.array_equal(g6, G6)
+    # a member that changes invalidates the group
+    e6.set_batch(3)
+    with pytest.raises(ae.AegpuError):
+        grp.launch()
+    grp.close()
+    e8.close()
+    e6.close()
