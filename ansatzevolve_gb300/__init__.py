@@ -24,6 +24,7 @@ BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 _P = ctypes.c_void_p
 _DP = ctypes.POINTER(ctypes.c_double)
 _IP = ctypes.POINTER(ctypes.c_int)
+_FP = ctypes.POINTER(ctypes.c_float)
 
 
 class AegpuError(RuntimeError):
@@ -65,6 +66,19 @@ def lib(build_if_missing=True):
                                                  ctypes.POINTER(i64), ctypes.POINTER(i64)]),
         "aegpu_optimise_batch": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, ctypes.c_int,
                                                 ctypes.c_double, _DP, _DP, _IP, ctypes.POINTER(i64)]),
+        "aegpu_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_uint64]),
+        "aegpu_mlp_destroy": (None, [_P]),
+        "aegpu_mlp_last_error": (ctypes.c_char_p, [_P]),
+        "aegpu_mlp_num_params": (i64, [_P]),
+        "aegpu_mlp_set_scaling": (ctypes.c_int, [_P, _FP, _FP, _FP, _FP]),
+        "aegpu_mlp_get_params": (ctypes.c_int, [_P, _FP]),
+        "aegpu_mlp_set_params": (ctypes.c_int, [_P, _FP]),
+        "aegpu_mlp_train": (ctypes.c_int, [_P, _FP, _FP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                           ctypes.c_uint64, _FP]),
+        "aegpu_mlp_loss_grad": (ctypes.c_int, [_P, _FP, _FP, ctypes.c_int, _FP, _FP]),
+        "aegpu_mlp_predict": (ctypes.c_int, [_P, _FP, ctypes.c_int, _FP]),
+        "aegpu_mlp_predict_dev": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P]),
         "aegpu_group_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.c_int]),
         "aegpu_group_launch": (ctypes.c_int, [_P, _P]),
         "aegpu_group_launch_count": (i64, [_P]),

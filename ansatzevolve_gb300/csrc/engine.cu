@@ -1365,6 +1365,15 @@ struct aegpu_engine {
     int64_t generation = 0;      // bumped whenever device buffers or the Hamiltonian change
     bool use_graph = true;
 
+    // Hessian scratch, kept between calls with the same parameter count
+    struct HessScratch {
+        int V = 0;
+        double *T = nullptr, *TC = nullptr, *HTC = nullptr, *THT = nullptr, *Hops = nullptr, *hpart = nullptr;
+        int *pptr = nullptr, *ppos = nullptr;
+        double *pscale = nullptr;
+        std::vector<std::pair<void *, size_t>> allocs;
+    } hess;
+
     // state caching: psi / hpsi valid for these angles
     std::vector<double> cached_angles;
     bool psi_valid = false, h_valid = false;
@@ -2504,15 +2513,6 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
     for (int o = 0; o < nops; ++o)
         if (param[o] < 0 || param[o] >= nparams) return e->fail(AEGPU_ERR_ARG, "parameter index out of range");
     const int V = nparams + 1;
-    // scratch: tangents by application position, compressed tangents and H * them
-    double *T = e->alloc<double>(n * nops);
-    double *TC = e->alloc<double>(n * V);
-    double *HTC = e->alloc<double>(n * V);
-    double *THT = e->alloc<double>((size_t)V * V);
-    double *Hops = e->alloc<double>((size_t)nops * nops);
-    int64_t maxpart = 0;
-    for (auto &b : e->dblocks) maxpart = std::max<int64_t>(maxpart, (int64_t)b.ntiles * nops * kMaxSlots);
-    double *hpart = e->alloc<double>(maxpart);
     // parameter -> (application position, scale) lists
     std::vector<int> pptr(nparams + 1, 0), ppos, pcnt(nparams, 0);
     std::vector<double> pscale;
@@ -2525,27 +2525,39 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         ppos[fill[param[o]]] = e->pos_of_op[o];
         pscale[fill[param[o]]++] = scale[o];
     }
-    int *d_pptr = e->upload(pptr), *d_ppos = e->upload(ppos);
-    double *d_pscale = e->upload(pscale);
-    cudaDeviceSynchronize();
-    auto cleanup = [&]() {
-        e->release(T, n * nops * 8);
-        e->release(TC, n * V * 8);
-        e->release(HTC, n * V * 8);
-        e->release(THT, (size_t)V * V * 8);
-        e->release(Hops, (size_t)nops * nops * 8);
-        e->release(hpart, maxpart * 8);
-        e->release(d_pptr, pptr.size() * 4);
-        e->release(d_ppos, ppos.size() * 4);
-        e->release(d_pscale, pscale.size() * 8);
-    };
-    if (!T || !TC || !HTC || !THT || !Hops || !hpart || !d_pptr || !d_ppos || !d_pscale) {
-        cleanup();
-        return e->fail(AEGPU_ERR_NOMEM, "Hessian scratch allocation failed");
+    // scratch (kept between calls for the same parameter count): tangents by
+    // application position, compressed tangents and H * them, Gram matrices
+    auto &hs = e->hess;
+    if (hs.V != V) {
+        for (auto &pa : hs.allocs) e->release(pa.first, pa.second);
+        hs = aegpu_engine::HessScratch{};
+        int64_t maxpart = 0;
+        for (auto &b : e->dblocks) maxpart = std::max<int64_t>(maxpart, (int64_t)b.ntiles * nops * kMaxSlots);
+        auto get = [&](auto *&ptr, size_t count) {
+            using T = std::remove_reference_t<decltype(*ptr)>;
+            ptr = e->alloc<T>(count);
+            hs.allocs.push_back({(void *)ptr, std::max<size_t>(count, 1) * sizeof(T)});
+            return ptr != nullptr;
+        };
+        bool ok = get(hs.T, n * nops) && get(hs.TC, n * V) && get(hs.HTC, n * V) && get(hs.THT, (size_t)V * V) &&
+                  get(hs.Hops, (size_t)nops * nops) && get(hs.hpart, maxpart) && get(hs.pptr, (size_t)nparams + 1) &&
+                  get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops);
+        if (!ok) {
+            for (auto &pa : hs.allocs) e->release(pa.first, pa.second);
+            hs = aegpu_engine::HessScratch{};
+            return e->fail(AEGPU_ERR_NOMEM, "Hessian scratch allocation failed");
+        }
+        hs.V = V;
     }
-    int rc = upload_angles(e, angles, true, 1);
-    if (rc) { cleanup(); return rc; }
+    double *T = hs.T, *TC = hs.TC, *HTC = hs.HTC, *THT = hs.THT, *Hops = hs.Hops, *hpart = hs.hpart;
+    int *d_pptr = hs.pptr, *d_ppos = hs.ppos;
+    double *d_pscale = hs.pscale;
     cudaStream_t s = e->stream;
+    cudaMemcpyAsync(d_pptr, pptr.data(), pptr.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_ppos, ppos.data(), ppos.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_pscale, pscale.data(), pscale.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    int rc = upload_angles(e, angles, true, 1);
+    if (rc) return rc;
     cudaMemsetAsync(T, 0, n * nops * sizeof(double), s);
     cudaMemsetAsync(Hops, 0, (size_t)nops * nops * sizeof(double), s);
     cudaMemcpyAsync(e->d_psi, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
@@ -2590,10 +2602,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
     }
     e->launches += 2;
     if (!e->cublas) {
-        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) {
-            cleanup();
-            return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
-        }
+        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
     }
     cublasSetStream(e->cublas, s);
     const double two = 2.0, zero = 0.0;
@@ -2638,7 +2647,6 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
     cudaMemcpyAsync(hops.data(), Hops, hops.size() * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(tht.data(), THT, tht.size() * 8, cudaMemcpyDeviceToHost, s);
     rc = stream_sync(e, "hessian");
-    cleanup();
     e->psi_valid = e->h_valid = false;
     if (rc) return rc;
     // Hessian = C Hops C^T + THT (fusedevolve.cpp:2762-2763); THT column-major V x V

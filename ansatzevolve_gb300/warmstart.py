@@ -1,0 +1,168 @@
+"""Learned warm start for the TUPS optimiser.
+
+A small MLP maps a Hamiltonian's integrals to starting angles.  Features are the
+flattened one-electron integrals h_pq and the Coulomb-like diagonal g_ppqq; targets
+are converged compressed angles produced by the engine itself.  The network is
+trained and run by the project's CUDA kernels (aegpu_mlp_*: BF16 weights, FP32
+accumulation, Adam, MSE).  Every proposal is judged by the engine: an instance starts
+from the proposal only if its energy there is below the energy at the plain start,
+so the optimiser's converged answer is decided by the engine, not by the network.
+No counterpart in the reference.
+"""
+import ctypes
+
+import numpy as np
+
+from . import AegpuError, _FP, _P, lib
+
+
+def features(h1, g2):
+    """[h_pq flattened, g_ppqq flattened] for one Hamiltonian (N*N + N*N values)."""
+    h1 = np.asarray(h1, dtype=np.float64)
+    g2 = np.asarray(g2, dtype=np.float64)
+    N = h1.shape[0]
+    g = g2.reshape(N, N, N, N)
+    diag = g[np.arange(N)[:, None], np.arange(N)[:, None], np.arange(N)[None, :], np.arange(N)[None, :]]
+    return np.concatenate([h1.reshape(-1), diag.reshape(-1)])
+
+
+def _fp(a):
+    return a.ctypes.data_as(_FP)
+
+
+class Mlp:
+    """The aegpu_mlp C ABI: n_in -> hidden -> hidden -> n_out, GELU."""
+
+    def __init__(self, n_in, n_out, hidden=512, seed=0):
+        self.L = lib()
+        h = _P()
+        rc = self.L.aegpu_mlp_create(ctypes.byref(h), int(n_in), int(hidden), int(n_out), int(seed))
+        if rc:
+            raise AegpuError("aegpu_mlp_create failed (%d)" % rc)
+        self.h = h
+        self.n_in, self.n_out, self.hidden = int(n_in), int(n_out), int(hidden)
+
+    def _check(self, rc):
+        if rc:
+            raise AegpuError("aegpu mlp error %d: %s" % (rc, self.L.aegpu_mlp_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aegpu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def num_params(self):
+        return int(self.L.aegpu_mlp_num_params(self.h))
+
+    def set_scaling(self, in_mean, in_scale, out_mean, out_scale):
+        arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (in_mean, in_scale, out_mean, out_scale)]
+        self._check(self.L.aegpu_mlp_set_scaling(self.h, *[_fp(a) for a in arrs]))
+
+    def fit_scaling(self, X, T):
+        """Standardise inputs and targets by their training-set mean and spread."""
+        X = np.asarray(X, dtype=np.float64)
+        T = np.asarray(T, dtype=np.float64)
+        xs = X.std(axis=0)
+        ts = T.std(axis=0)
+        self.set_scaling(X.mean(axis=0), np.where(xs > 1e-8, xs, 1.0), T.mean(axis=0), np.where(ts > 1e-8, ts, 1.0))
+
+    def get_params(self):
+        p = np.zeros(self.num_params(), dtype=np.float32)
+        self._check(self.L.aegpu_mlp_get_params(self.h, _fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params()
+        self._check(self.L.aegpu_mlp_set_params(self.h, _fp(p)))
+
+    def train(self, X, T, epochs, batch=128, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        n = X.shape[0]
+        assert X.shape == (n, self.n_in) and T.shape == (n, self.n_out)
+        loss = np.zeros(max(1, epochs), dtype=np.float32)
+        self._check(self.L.aegpu_mlp_train(self.h, _fp(X), _fp(T), n, int(epochs), int(batch), float(lr), int(seed),
+                                           _fp(loss)))
+        return loss[:epochs]
+
+    def loss_grad(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        g = np.zeros(self.num_params(), dtype=np.float32)
+        self._check(self.L.aegpu_mlp_loss_grad(self.h, _fp(X), _fp(T), X.shape[0], _fp(loss), _fp(g)))
+        return float(loss[0]), g
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros((X.shape[0], self.n_out), dtype=np.float32)
+        self._check(self.L.aegpu_mlp_predict(self.h, _fp(X), X.shape[0], _fp(Y)))
+        return Y
+
+
+def judged_starts(engine, proposals, param0, scale, plain=None):
+    """Per instance of a batched engine, the start to optimise from: the network's
+    proposal where the engine finds a lower energy there than at the plain start
+    (zeros unless given), else the plain start.  Returns (starts, used_proposal)."""
+    proposals = np.asarray(proposals, dtype=np.float64)
+    nb, P = proposals.shape
+    plain = np.zeros((nb, P)) if plain is None else np.asarray(plain, dtype=np.float64)
+    p0 = np.asarray(param0)
+    sc = np.asarray(scale, dtype=np.float64)
+    Ep = engine.energy(sc * proposals[:, p0])
+    Ez = engine.energy(sc * plain[:, p0])
+    Ep, Ez = np.atleast_1d(Ep), np.atleast_1d(Ez)
+    use = Ep < Ez
+    return np.where(use[:, None], proposals, plain), use
+
+
+# ------------------------------------------------------------------ pipeline --
+def family_engine(n_orb, n_alpha, layers, nb, integrals=None, mode=None):
+    """A batched engine for the TUPS ansatz on a Hamiltonian family: nb instances with
+    their own integrals (list of (h1, g2)), Hartree-Fock start, compressed
+    parameters (param0, scale).  Returns (engine, param0, scale)."""
+    from . import BASIS_SZ, HAM_ON_THE_FLY, Engine
+    from .synthetic import hartree_fock_index, tups_operators
+    ops, param, scale = tups_operators(n_orb, layers)
+    e = Engine(2 * n_orb, BASIS_SZ, 2 * n_alpha, n_alpha, n_alpha, np.asarray(ops) - 1)
+    init = np.zeros(e.D)
+    init[np.searchsorted(e.states(), hartree_fock_index(n_orb, n_alpha, n_alpha))] = 1.0
+    e.set_initial(init)
+    if nb > 1:
+        e.set_batch(nb)
+    if integrals is not None:
+        e.set_ham_integrals_batch(np.stack([h for h, _ in integrals]), np.stack([g for _, g in integrals]),
+                                  HAM_ON_THE_FLY if mode is None else mode)
+    return e, np.asarray(param) - 1, np.asarray(scale, dtype=np.float64)
+
+
+def converge_batch(n_orb, n_alpha, layers, integrals, starts=None, gtol=1e-6, chunk=256, mode=None):
+    """Converged compressed angles for every Hamiltonian in `integrals`, optimised in
+    batches of `chunk` instances by the lockstep BFGS (zero start unless given).
+    Returns (x [n, P], E [n], |g| [n])."""
+    xs, Es, gs = [], [], []
+    for c0 in range(0, len(integrals), chunk):
+        part = integrals[c0:c0 + chunk]
+        e, p0, sc = family_engine(n_orb, n_alpha, layers, len(part), part, mode)
+        P = int(p0.max()) + 1
+        x0 = np.zeros((len(part), P)) if starts is None else np.asarray(starts[c0:c0 + chunk], dtype=np.float64)
+        x, E, gn, _, _ = e.optimise_batch(x0.reshape(len(part), P), p0, sc, gtol=gtol)
+        xs.append(x.reshape(len(part), P))
+        Es.append(np.atleast_1d(E))
+        gs.append(np.atleast_1d(gn))
+        e.close()
+    return np.concatenate(xs), np.concatenate(Es), np.concatenate(gs)
+
+
+def train_warmstart(feats, targets, hidden=512, epochs=400, batch=128, lr=1e-3, seed=0):
+    """Train the MLP features -> converged angles on the GPU; returns (model, loss history)."""
+    feats = np.asarray(feats, dtype=np.float64)
+    targets = np.asarray(targets, dtype=np.float64)
+    m = Mlp(feats.shape[1], targets.shape[1], hidden=hidden, seed=seed)
+    m.fit_scaling(feats, targets)
+    hist = m.train(feats, targets, epochs=epochs, batch=batch, lr=lr, seed=seed + 1)
+    return m, hist

@@ -138,6 +138,27 @@ int aegpu_optimise_newton(aegpu_engine *e, int nparams, const int *param, const 
                           double *energy, double *gnorm, int64_t *hessian_evals, int64_t *energy_evals);
 int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
                          int max_rounds, double max_step, double *energy, double *gnorm, int *iters, int64_t *rounds);
+/* Learned warm start (no counterpart in the reference): an MLP
+ * n_in -> n_hidden -> n_hidden -> n_out with GELU activations, BF16 weights in every
+ * product, FP32 accumulation, FP32 master weights trained by Adam on the mean squared
+ * error of standardised targets.  Inputs are standardised with (x - in_mean) /
+ * in_scale and outputs returned as y * out_scale + out_mean (identity by default).
+ * Parameters (aegpu_mlp_get_params / set_params / loss_grad gradients), FP32:
+ * W1[H][n_in], b1[H], W2[H][H], b2[H], W3[n_out][H], b3[n_out]. */
+typedef struct aegpu_mlp aegpu_mlp;
+int aegpu_mlp_create(aegpu_mlp **out, int n_in, int n_hidden, int n_out, uint64_t seed);
+void aegpu_mlp_destroy(aegpu_mlp *m);
+const char *aegpu_mlp_last_error(const aegpu_mlp *m);
+int64_t aegpu_mlp_num_params(const aegpu_mlp *m);
+int aegpu_mlp_set_scaling(aegpu_mlp *m, const float *in_mean, const float *in_scale, const float *out_mean,
+                          const float *out_scale);
+int aegpu_mlp_get_params(aegpu_mlp *m, float *params);
+int aegpu_mlp_set_params(aegpu_mlp *m, const float *params);
+int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epochs, int batch, float lr,
+                    uint64_t seed, float *epoch_loss);
+int aegpu_mlp_loss_grad(aegpu_mlp *m, const float *X, const float *T, int n, float *loss, float *grads);
+int aegpu_mlp_predict(aegpu_mlp *m, const float *X, int n, float *Y);
+int aegpu_mlp_predict_dev(aegpu_mlp *m, const float *X_dev, int n, float *Y_dev, void *stream);
 /* y_dev = H x_dev on device vectors; energy_dev (nullable) receives <x|H x>. */
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 /* CUDA-event timing of the phases of aegpu_gradient_dev (evolve, H*psi + energy,
