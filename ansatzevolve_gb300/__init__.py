@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
 _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
+TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS = 1, 2, 3
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 
 _P = ctypes.c_void_p
@@ -58,6 +59,8 @@ def lib(build_if_missing=True):
         "aegpu_set_ham_integrals_batch": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
         "aegpu_set_batch": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_batch_size": (ctypes.c_int, [_P]),
+        "aegpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+        "aegpu_get_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_io_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
         "aegpu_io_put_angles": (ctypes.c_int, [_P, _DP, _P]),
         "aegpu_io_get_results": (ctypes.c_int, [_P, _DP, _DP, _P]),
@@ -65,7 +68,7 @@ def lib(build_if_missing=True):
         "aegpu_optimise_newton": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, _DP, _DP,
                                                  ctypes.POINTER(i64), ctypes.POINTER(i64)]),
         "aegpu_optimise_batch": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, ctypes.c_int,
-                                                ctypes.c_double, _DP, _DP, _IP, ctypes.POINTER(i64)]),
+                                                ctypes.c_double, _DP, _DP, _DP, _IP, ctypes.POINTER(i64)]),
         "aegpu_mlp_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             ctypes.c_uint64]),
         "aegpu_mlp_destroy": (None, [_P]),
@@ -151,13 +154,19 @@ def _i32(a):
 class Engine:
     """The aegpu C ABI for one problem (sector basis + excitations + Hamiltonian)."""
 
-    def __init__(self, nq, basis_kind, n_elec, n_alpha, n_beta, ops0, complex_mode=False):
+    def __init__(self, nq, basis_kind, n_elec, n_alpha, n_beta, ops0, complex_mode=False, tuning=None):
         self.L = lib()
         h = _P()
         rc = self.L.aegpu_create(ctypes.byref(h))
         if rc:
             raise AegpuError("aegpu_create failed (%d): no usable CUDA device" % rc)
         self.h = h
+        # launch-shape knobs that must precede the problem set-up
+        for knob in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM):
+            if tuning and knob in tuning:
+                self._check(self.L.aegpu_set_tuning(h, knob, int(tuning[knob])))
+        if tuning and TUNE_OTF_THREADS in tuning:
+            self._check(self.L.aegpu_set_tuning(h, TUNE_OTF_THREADS, int(tuning[TUNE_OTF_THREADS])))
         ops = _i32(ops0).reshape(-1, 4)
         self.nops = len(ops)
         self.W = 2 if complex_mode else 1
@@ -308,17 +317,25 @@ class Engine:
                                                  ctypes.byref(nh), ctypes.byref(ne)))
         return x, E[0], gn[0], nh.value, ne.value
 
-    def optimise_batch(self, x0, param0, scale, gtol=1e-6, max_rounds=2000, max_step=1.0):
-        """Lockstep BFGS of all instances from x0 [nb, P]: (x, E [nb], |g| [nb], iterations [nb], rounds)."""
+    def optimise_batch(self, x0, param0, scale, gtol=1e-6, max_rounds=2000, max_step=1.0, hinv=None):
+        """Lockstep BFGS of all instances from x0 [nb, P]: (x, E [nb], |g| [nb], iterations [nb], rounds).
+        hinv [nb, P, P] (optional): initial inverse Hessians, overwritten with the final ones."""
         x = _f64(x0).reshape(self.nb, -1).copy()
         P = x.shape[1]
         p, s = _i32(param0), _f64(scale)
         E, gn = np.zeros(self.nb), np.zeros(self.nb)
         it = np.zeros(self.nb, dtype=np.int32)
         r = ctypes.c_int64()
+        hp = None
+        if hinv is not None:
+            assert hinv.dtype == np.float64 and hinv.flags.c_contiguous and hinv.size == self.nb * P * P
+            hp = dptr(hinv)
         self._check(self.L.aegpu_optimise_batch(self.h, P, iptr(p), dptr(s), dptr(x), gtol, int(max_rounds), max_step,
-                                                dptr(E), dptr(gn), iptr(it), ctypes.byref(r)))
+                                                hp, dptr(E), dptr(gn), iptr(it), ctypes.byref(r)))
         return x, E, gn, it, r.value
+
+    def tuning(self):
+        return {k: int(self.L.aegpu_get_tuning(self.h, k)) for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS)}
 
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))

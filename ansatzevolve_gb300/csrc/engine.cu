@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(kRotThreads) k_block_rot(BlockArgs a, double *
     __shared__ double C[kMaxSlots], S[kMaxSlots];
     __shared__ int slot[kMaxSlots];
     const TileCtx c = load_tile(a, bits, code, C, S, slot);
-    for (int vec = 0; vec < nvec; ++vec) {
+    for (int vec = blockIdx.y; vec < nvec; vec += gridDim.y) {  // vectors spread over grid.y
         double *psi = vecs + vec * vstride;
         gather<W>(v, psi, c);
         __syncthreads();
@@ -1339,6 +1339,12 @@ struct aegpu_engine {
     OtfArgs otf{};
     int otf_threads = 0, otf_chunks = 0;
 
+    // launch-shape knobs (aegpu_set_tuning): excitations per pass (<= kMaxWarpLayers),
+    // CTAs per SM of the pass kernels, threads per CTA of the on-the-fly H kernel
+    int tune_pass_ops = kMaxWarpLayers;
+    int tune_ctas_per_sm = 8;
+    int tune_otf_threads = 512;
+
     // optional CUDA-event timing of the phases of *_dev evaluations
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -1817,7 +1823,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     }
     // the reference's commuting blocks, cut into passes of <= 6 excitations so that
     // every orbit fits one warp's registers
-    e->blocks = split_passes(group_blocks(e->excs, kMaxSlots, e->perm), kMaxWarpLayers);
+    e->blocks = split_passes(group_blocks(e->excs, kMaxSlots, e->perm), e->tune_pass_ops);
     e->pos_of_op.assign(nops, 0);
     for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;
 
@@ -1882,7 +1888,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             d.ntiles = (int)T.tiles.size();
             d.wtasks = e->upload(T.wtasks);
             d.nwtasks = (int)T.wtasks.size();
-            d.wgrid = std::max(1, std::min(e->sm_count * 8, (d.nwtasks + 7) / 8));
+            d.wgrid = std::max(1, std::min(e->sm_count * e->tune_ctas_per_sm, (d.nwtasks + 7) / 8));
             d.active = T.active;
         } else {
             d.ntiles = kDiagGrid;
@@ -2128,7 +2134,7 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (smem + 1024 > (size_t)optin) return e->fail(AEGPU_ERR_UNSUPPORTED, "too many orbitals for the on-the-fly kernel");
         e->otf = o;
-        e->otf_threads = (int)std::min<int64_t>(512, ((int64_t)o.nB + 31) / 32 * 32);
+        e->otf_threads = (int)std::min<int64_t>(e->tune_otf_threads, ((int64_t)o.nB + 31) / 32 * 32);
         e->otf_chunks = (o.nB + e->otf_threads - 1) / e->otf_threads;
         const int64_t nparts = (int64_t)o.nA * e->otf_chunks;
         if (nparts > e->n_epart) {
@@ -2174,6 +2180,41 @@ int aegpu_set_batch(aegpu_engine *e, int nb)
 }
 
 int aegpu_batch_size(const aegpu_engine *e) { return e ? e->nb : -1; }
+
+int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    switch (knob) {
+    case AEGPU_TUNE_PASS_OPS:
+        if (value < 1 || value > kMaxWarpLayers) return e->fail(AEGPU_ERR_ARG, "pass size must be 1..6");
+        if (e->d_start) return e->fail(AEGPU_ERR_STATE, "set the pass size before the problem");
+        e->tune_pass_ops = value;
+        return AEGPU_OK;
+    case AEGPU_TUNE_CTAS_PER_SM:
+        if (value < 1 || value > 64) return e->fail(AEGPU_ERR_ARG, "CTAs per SM must be 1..64");
+        if (e->d_start) return e->fail(AEGPU_ERR_STATE, "set the CTAs per SM before the problem");
+        e->tune_ctas_per_sm = value;
+        return AEGPU_OK;
+    case AEGPU_TUNE_OTF_THREADS:
+        if (value < 64 || value > 512 || value % 32) return e->fail(AEGPU_ERR_ARG, "threads must be 64..512, x32");
+        if (e->ham_kind) return e->fail(AEGPU_ERR_STATE, "set the thread count before the Hamiltonian");
+        e->tune_otf_threads = value;
+        return AEGPU_OK;
+    default:
+        return e->fail(AEGPU_ERR_ARG, "unknown tuning knob");
+    }
+}
+
+int aegpu_get_tuning(const aegpu_engine *e, int knob)
+{
+    if (!e) return -1;
+    switch (knob) {
+    case AEGPU_TUNE_PASS_OPS: return e->tune_pass_ops;
+    case AEGPU_TUNE_CTAS_PER_SM: return e->tune_ctas_per_sm;
+    case AEGPU_TUNE_OTF_THREADS: return e->tune_otf_threads;
+    default: return -1;
+    }
+}
 
 int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored)
 {
@@ -2573,11 +2614,13 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
             e->launches += 3;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args((int)bi, 1.0);
+            // earlier tangents carried through the block: one CTA per (tile, vector)
+            const dim3 gv(b.ntiles, std::min(p0, 4096));
             if (W == 1) {
-                if (p0 > 0) k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                if (p0 > 0) k_block_rot<1><<<gv, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
                 k_block_tangent<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             } else {
-                if (p0 > 0) k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                if (p0 > 0) k_block_rot<2><<<gv, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
                 k_block_tangent<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             }
             e->launches += 2;
@@ -2627,7 +2670,9 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
             e->launches += 4;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args(bi, -1.0);
-            const int vchunk = 8;
+            // vectors per CTA: enough CTAs to fill the GPU (about 4 per SM), at most 8
+            const int vchunk =
+                std::max(1, std::min(8, (int)(((int64_t)b.ntiles * nvec) / ((int64_t)e->sm_count * 4))));
             dim3 g(b.ntiles, (nvec + vchunk - 1) / vchunk);
             if (W == 1) {
                 k_block_hess<1><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);

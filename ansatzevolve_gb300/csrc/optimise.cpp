@@ -71,7 +71,8 @@ void start_trial(BfgsInstance &s, int P, double max_step)
 extern "C" {
 
 int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
-                         int max_rounds, double max_step, double *energy, double *gnorm, int *iters, int64_t *rounds)
+                         int max_rounds, double max_step, double *hinv, double *energy, double *gnorm, int *iters,
+                         int64_t *rounds)
 {
     if (!e || nparams < 1 || !param || !scale || !x || !(gtol > 0) || max_rounds < 1) return AEGPU_ERR_ARG;
     const int nb = aegpu_batch_size(e);
@@ -86,7 +87,13 @@ int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const d
     for (int b = 0; b < nb; ++b) {
         st[b].x.assign(x + (size_t)b * P, x + (size_t)(b + 1) * P);
         st[b].xt = st[b].x;
-        set_identity(st[b].Hinv, P, 1.0);
+        if (hinv) {
+            // caller's initial inverse Hessian (e.g. from a nearby instance): no rescaling
+            st[b].Hinv.assign(hinv + (size_t)b * P * P, hinv + (size_t)(b + 1) * P * P);
+            st[b].scaled = true;
+        } else {
+            set_identity(st[b].Hinv, P, 1.0);
+        }
     }
     std::vector<double> ang((size_t)nb * nops), E(nb), gops((size_t)nb * nops), gc(P), s(P), y(P), Hy(P);
     int64_t round = 0;
@@ -184,6 +191,7 @@ int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const d
         if (energy) energy[b] = st[b].f;
         if (gnorm) gnorm[b] = st[b].g.empty() ? -1.0 : std::sqrt(dot(st[b].g.data(), st[b].g.data(), P));
         if (iters) iters[b] = st[b].iters;
+        if (hinv) std::copy(st[b].Hinv.begin(), st[b].Hinv.end(), hinv + (size_t)b * P * P);
     }
     if (rounds) *rounds = round;
     return AEGPU_OK;

@@ -166,3 +166,124 @@ def train_warmstart(feats, targets, hidden=512, epochs=400, batch=128, lr=1e-3, 
     m.fit_scaling(feats, targets)
     hist = m.train(feats, targets, epochs=epochs, batch=batch, lr=lr, seed=seed + 1)
     return m, hist
+
+
+# ------------------------------------------------------------- family scans --
+class FamilySpec:
+    """A TUPS ansatz over a Hamiltonian family h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1
+    (synthetic.family_integrals with a fixed seed)."""
+
+    def __init__(self, n_orb=10, n_alpha=5, layers=3, seed=0):
+        from .synthetic import tups_operators
+        self.n_orb, self.n_alpha, self.layers, self.seed = n_orb, n_alpha, layers, seed
+        ops, param, scale = tups_operators(n_orb, layers)
+        self.param0 = np.asarray(param) - 1
+        self.scale = np.asarray(scale, dtype=np.float64)
+        self.P = int(self.param0.max()) + 1
+
+    def integrals(self, s):
+        from .synthetic import family_integrals
+        return family_integrals(self.n_orb, float(s), seed=self.seed)
+
+    def features(self, svals):
+        return np.stack([features(*self.integrals(s)) for s in svals])
+
+    def engine(self, nb=1, integrals=None, mode=None):
+        e, _, _ = family_engine(self.n_orb, self.n_alpha, self.layers, nb, integrals, mode)
+        return e
+
+
+def scan_newton(spec, svals, x_start, gtol=1e-6, mode=None):
+    """The plain path of a family scan: one instance at a time in the given order,
+    each optimised by the reference's Newton method from the previous instance's
+    converged angles (x_start for the first).  Returns (x [M, P], E [M], seconds of
+    optimisation, Hessian evaluations, energy evaluations)."""
+    import time
+    from . import HAM_STORED
+    e = spec.engine(1)
+    x = np.asarray(x_start, dtype=np.float64).copy()
+    xs, Es, t, nh, ne = [], [], 0.0, 0, 0
+    for s in svals:
+        e.set_ham_integrals(*spec.integrals(s), HAM_STORED if mode is None else mode)
+        t0 = time.perf_counter()
+        x, E, gn, h, n = e.optimise_newton(x, spec.param0, spec.scale, gtol=gtol)
+        t += time.perf_counter() - t0
+        xs.append(x.copy())
+        Es.append(E)
+        nh += h
+        ne += n
+    e.close()
+    return np.array(xs), np.array(Es), t, nh, ne
+
+
+def scan_bfgs_chain(spec, svals, x_start, gtol=1e-8, mode=None):
+    """Training targets: a continuation chain over the given order, each instance
+    optimised by BFGS from the previous converged angles and inverse Hessian (the
+    first from x_start with the inverse of the analytic Hessian there)."""
+    from . import HAM_STORED
+    e = spec.engine(1)
+    x = np.asarray(x_start, dtype=np.float64).reshape(1, -1).copy()
+    hinv = None
+    xs, Es, gs, its = [], [], [], []
+    for s in svals:
+        e.set_ham_integrals(*spec.integrals(s), HAM_STORED if mode is None else mode)
+        if hinv is None:
+            hinv = np.ascontiguousarray(inverse_hessian(e, x[0], spec)[None])
+        x, E, gn, it, r = e.optimise_batch(x, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=hinv)
+        xs.append(x[0].copy())
+        Es.append(float(np.atleast_1d(E)[0]))
+        gs.append(float(np.atleast_1d(gn)[0]))
+        its.append(int(it[0]))
+    e.close()
+    return np.array(xs), np.array(Es), np.array(gs), np.array(its)
+
+
+def inverse_hessian(engine, x, spec, floor=1e-3):
+    """|H|^-1 over the eigenpairs of the analytic Hessian at x (eigenvalues below
+    floor * max |lambda| raised to it): the initial inverse Hessian of warm BFGS."""
+    _, _, H = engine.hessian(spec.scale * np.asarray(x)[spec.param0], spec.param0, spec.scale)
+    H = 0.5 * (H + H.T)
+    w, V = np.linalg.eigh(H)
+    a = np.maximum(np.abs(w), floor * np.abs(w).max())
+    return (V / a) @ V.T
+
+
+def scan_batched_warm(spec, svals, model, x_fallback, gtol=1e-6, n_anchor=4, mode=None, max_rounds=3000):
+    """The batched, warm-started path: every instance at once, each starting from the
+    network's proposal where the engine finds it lower in energy than the fallback
+    start, then lockstep BFGS from an inverse Hessian taken at the nearest of n_anchor
+    anchor instances.  Returns a dict with x, E, |g|, rounds, used proposal flags
+    and the seconds spent (set-up excluded)."""
+    import time
+    from . import HAM_ON_THE_FLY, HAM_STORED
+    svals = np.asarray(svals, dtype=np.float64)
+    M = len(svals)
+    ints = [spec.integrals(s) for s in svals]
+    feats = np.stack([features(*i) for i in ints])
+    e = spec.engine(M, ints, HAM_ON_THE_FLY if mode is None else mode)
+    anchors = np.argsort(svals)[(np.arange(n_anchor) * M + M // 2) // n_anchor] if n_anchor else []
+    ea = spec.engine(1)
+    t0 = time.perf_counter()
+    prop = model.predict(feats).astype(np.float64)
+    starts, used = judged_starts(e, prop, spec.param0, spec.scale, np.tile(np.asarray(x_fallback, float), (M, 1)))
+    hinv = None
+    t_anchor = t_setup = 0.0
+    if n_anchor:
+        hs = []
+        for a in anchors:
+            t1 = time.perf_counter()
+            ea.set_ham_integrals(*ints[a], HAM_STORED)  # set-up of the anchor engine, not timed
+            t2 = time.perf_counter()
+            hs.append(inverse_hessian(ea, starts[a], spec))
+            t_anchor += time.perf_counter() - t2
+            t_setup += t2 - t1
+        near = np.abs(svals[:, None] - svals[anchors][None, :]).argmin(axis=1)
+        hinv = np.ascontiguousarray(np.stack([hs[k] for k in near]))
+    t_pre = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    x, E, gn, it, rounds = e.optimise_batch(starts, spec.param0, spec.scale, gtol=gtol, max_rounds=max_rounds, hinv=hinv)
+    t_opt = time.perf_counter() - t1
+    e.close()
+    ea.close()
+    return dict(x=x, E=np.atleast_1d(E), gnorm=np.atleast_1d(gn), iters=it, rounds=rounds, used=used,
+                seconds=t_opt + t_pre - t_setup, t_opt=t_opt, t_pre=t_pre - t_setup, t_anchor=t_anchor)

@@ -80,6 +80,14 @@ int aegpu_set_ham_integrals(aegpu_engine *e, const double *h1, const double *g2,
  * h1s[b][N*N], g2s[b][N^4] (set the batch size first: changing it drops them).
  * nb is 1..65535; the Hessian needs nb = 1. */
 int aegpu_set_batch(aegpu_engine *e, int nb);
+/* Launch-shape knobs (picked by the autotuner, ansatzevolve_gb300/autotune.py):
+ * excitations fused per pass (1..6; before aegpu_set_problem), CTAs per SM of the
+ * pass kernels (1..64; before aegpu_set_problem), threads per CTA of the on-the-fly
+ * H kernel (64..512, multiple of 32; before the Hamiltonian).  No counterpart in the
+ * reference. */
+enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3 };
+int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
+int aegpu_get_tuning(const aegpu_engine *e, int knob);
 int aegpu_batch_size(const aegpu_engine *e);
 int aegpu_set_ham_integrals_batch(aegpu_engine *e, const double *h1s, const double *g2s, int mode);
 /* Which representation is in use: 1 CSR, 2 stored ELL, 3 on the fly; and its stored entries. */
@@ -132,12 +140,15 @@ void aegpu_group_destroy(aegpu_group *g);
  * start on entry and the optimum on return.
  * aegpu_optimise_batch: all nb instances (x[nb][P]) by lockstep BFGS, one batched
  * energy + gradient evaluation per round, until |g| < gtol for every instance or
- * max_rounds rounds; max_step bounds each trial step's length (<= 0: 1.0).
+ * max_rounds rounds; max_step bounds each trial step's length (<= 0: 1.0).  hinv
+ * (nullable, [nb][P][P]): each instance's initial inverse Hessian on entry (else a
+ * scaled identity), its final BFGS approximation on return.
  * No counterpart in the reference for the batched optimiser. */
 int aegpu_optimise_newton(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
                           double *energy, double *gnorm, int64_t *hessian_evals, int64_t *energy_evals);
 int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
-                         int max_rounds, double max_step, double *energy, double *gnorm, int *iters, int64_t *rounds);
+                         int max_rounds, double max_step, double *hinv, double *energy, double *gnorm, int *iters,
+                         int64_t *rounds);
 /* Learned warm start (no counterpart in the reference): an MLP
  * n_in -> n_hidden -> n_hidden -> n_out with GELU activations, BF16 weights in every
  * product, FP32 accumulation, FP32 master weights trained by Adam on the mean squared
