@@ -16,6 +16,11 @@ Under torchrun every rank runs an independent replica (the path does not shard),
 timing is the max over ranks and `value` sums all ranks' evaluations.
 `--impl reference` times the reference algorithm's CPU implementation (the C
 restatement in oracle/, all host threads) on the same workload.
+
+Two more objects on the same line: `batched` (512 instances of 8, 10 and 12 orbitals
+with their own integrals, one graph launch per step) and `time_to_converge` (a
+10-orbital Hamiltonian family scan: the reference's Newton method one instance at a
+time against the batched, network-warm-started path).
 """
 import argparse
 import json
@@ -34,9 +39,15 @@ METRIC = "TUPS energy+gradient evals/s (12 orb, FP64) and time-to-converge vs pl
 N_ORB, N_A, N_B, LAYERS, SEED = 12, 6, 6, 3, 0
 
 
+def set_orbitals(n):
+    """Smaller or larger cases of the same workload for profiling (default 12)."""
+    global N_ORB, N_A, N_B, LAYERS
+    N_ORB, N_A, N_B, LAYERS = n, n // 2, n // 2, 2 if n <= 8 else 3
+
+
 def workload_desc(D, P, nops, ham):
-    return {"workload": "tUPS 12 orbitals, 6a+6b electrons (D=%d), 3 layers (%d parameters, %d excitations), "
-                        "synthetic random integrals seed 0, H %s" % (D, P, nops, ham),
+    return {"workload": "tUPS %d orbitals, %da+%db electrons (D=%d), %d layers (%d parameters, %d excitations), "
+                        "synthetic random integrals seed 0, H %s" % (N_ORB, N_A, N_B, D, LAYERS, P, nops, ham),
             "global_batch": 1, "parallelism": "replicas", "l2": "inputs larger than L2 (H rows stream from HBM every step)"}
 
 
@@ -130,8 +141,8 @@ def cpu_baseline(pb, max_seconds=30.0):
             break
     t = float(np.median(times[1:])) if len(times) > 1 else times[0]
     return {"value": 1.0 / t, "unit": "evals/s", "cores": int(olib().or_num_threads()), "kind": "port",
-            "sample": "%d energy+gradient evaluations of the same 12-orbital workload (%s), operator-list H*psi "
-                      "as the reference picks for this size" % (len(times), "median of all but the first"
+            "sample": "%d energy+gradient evaluations of the same %d-orbital workload (%s), operator-list H*psi "
+                      "as the reference picks for this size" % (len(times), N_ORB, "median of all but the first"
                                                                   if len(times) > 1 else "single evaluation")}, E, g
 
 
@@ -159,7 +170,7 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1),
             "ms_per_step": 1e3 * dt / done, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": workload_desc(853776, pb["P"], len(pb["ops0"]), "applied from the operator list on the fly"),
+            "config": workload_desc(int(o.D), pb["P"], len(pb["ops0"]), "applied from the operator list on the fly"),
             "cpu_baseline": {"value": v, "unit": "evals/s", "cores": int(olib().or_num_threads()), "kind": "port",
                              "sample": "%d of %d requested steps within the %.0f s budget" % (done, args.steps, budget)},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -189,6 +200,127 @@ def e2e_c_abi(pb, steps, warmup):
             "ms_per_step": 1e3 * dt / steps, "api": "getEnergy + getGradient_COMP (H*psi cached between the pair)"}
 
 
+def tuned(key):
+    """Knob settings for a problem class: the local autotuner cache, else the table
+    tuned on GB300 that ships with the package, else the defaults."""
+    from ansatzevolve_gb300 import autotune
+    t = autotune.lookup(key)
+    if not t:
+        t = autotune.lookup(key, os.path.join(ROOT, "ansatzevolve_gb300", "tuned_gb300.json"))
+    return t
+
+
+def batched_bench(stream, steps=10, warmup=3):
+    """512 instances with their own seeded integrals and U(-0.3, 0.3) angles, evaluated
+    by ONE graph launch: 256 x 8 orbitals (4a+4b, 2 layers), 192 x 10 orbitals (5a+5b,
+    3 layers), 64 x 12 orbitals (6a+6b, 3 layers); instance i uses integral seed i."""
+    import torch
+    import ansatzevolve_gb300 as ae
+    from ansatzevolve_gb300 import autotune
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
+    classes = [(8, 4, 2, 256, 0, ae.HAM_STORED), (10, 5, 3, 192, 256, ae.HAM_ON_THE_FLY),
+               (12, 6, 3, 64, 448, ae.HAM_ON_THE_FLY)]
+    rng = np.random.default_rng(SEED)
+    engines, per_class = [], []
+    t0 = time.perf_counter()
+    for N, na, L, nb, s0, mode in classes:
+        key = autotune.problem_key(N, na, na, L, nb, mode, True)
+        tuning = tuned(key)
+        ops, _, _ = tups_operators(N, L)
+        e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1, tuning=tuning or None)
+        init = np.zeros(e.D)
+        init[np.searchsorted(e.states(), hartree_fock_index(N, na, na))] = 1.0
+        e.set_initial(init)
+        e.set_batch(nb)
+        ints = [synthetic_integrals(N, s) for s in range(s0, s0 + nb)]
+        e.set_ham_integrals_batch(np.stack([i[0] for i in ints]), np.stack([i[1] for i in ints]), mode)
+        e.io_put_angles(rng.uniform(-0.3, 0.3, (nb, e.nops)))
+        e.io_get_results()
+        engines.append(e)
+        per_class.append({"orbitals": N, "instances": nb, "D": e.D, "ham": "stored" if mode == ae.HAM_STORED else
+                          "on the fly", "tuning": {str(k): v for k, v in e.tuning().items()},
+                          "tuned": bool(tuning)})
+    setup_s = time.perf_counter() - t0
+    grp = ae.Group(engines)
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        grp.launch(sp)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        grp.launch(sp)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    # each class alone, for the breakdown
+    for e, pc in zip(engines, per_class):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e.launch_io(sp)
+        a.record(stream)
+        for _ in range(3):
+            e.launch_io(sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        pc["ms_per_batch"] = a.elapsed_time(b) / 3
+        pc["evals_per_s"] = pc["instances"] / (pc["ms_per_batch"] / 1e3)
+    E, g = engines[0].io_get_results()
+    out = {"value": 512 / (ms / 1e3), "unit": "instance energy+gradient evals/s", "instances": 512,
+           "ms_per_step": ms, "steps": steps, "warmup": warmup, "graph_launches_per_step": 1,
+           "gpu_launches_per_step": grp.launch_count(), "classes": per_class, "setup_s": setup_s,
+           "finite": bool(np.all(np.isfinite(E)) and np.all(np.isfinite(g)))}
+    grp.close()
+    for e in engines:
+        e.close()
+    return out
+
+
+def ttc_bench(n_train=2000, n_heldout=200, n_plain=24, epochs=400):
+    """Time to converge over a 10-orbital Hamiltonian family scan (5a+5b, 3 layers,
+    81 parameters): h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1.  Both paths start the scan
+    from the converged s = 0 member (the reference's Newton method from zero angles).
+    Plain: one instance at a time in increasing s, the reference's Newton method from
+    the previous converged angles (timed on the first n_plain held-out values, mean
+    per instance).  Batched + warm-started: all n_heldout instances in one batch,
+    network proposals judged by the engine against the s = 0 angles, then lockstep
+    BFGS from anchor inverse Hessians.  The network is trained once per family on
+    n_train converged angle sets from a continuation chain (reported separately)."""
+    from ansatzevolve_gb300 import warmstart as ws
+    spec = ws.FamilySpec(10, 5, 3, seed=0)
+    t0 = time.perf_counter()
+    x0, E0, _, _, _ = ws.scan_newton(spec, [0.0], np.zeros(spec.P))
+    x0 = x0[0]
+    t_origin = time.perf_counter() - t0
+    s_tr = np.sort(np.random.default_rng(2024).uniform(0, 1, n_train))
+    s_ho = np.sort(np.random.default_rng(77).uniform(0, 1, n_heldout))
+    t0 = time.perf_counter()
+    xtr, Etr, gtr, its = ws.scan_bfgs_chain(spec, s_tr, x0, gtol=1e-8)
+    t_chain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    model, hist = ws.train_warmstart(spec.features(s_tr), xtr, epochs=epochs, batch=128, lr=1e-3)
+    t_train = time.perf_counter() - t0
+    r = ws.scan_batched_warm(spec, s_ho, model, x0, gtol=1e-6, n_anchor=4)
+    xp, Ep, tp, nh, ne = ws.scan_newton(spec, s_ho[:n_plain], x0, gtol=1e-6)
+    plain_per = tp / n_plain
+    batched_per = r["seconds"] / n_heldout
+    dE = r["E"][:n_plain] - Ep
+    model.close()
+    return {"speedup": plain_per / batched_per, "unit": "x (plain seconds per instance / batched seconds per instance)",
+            "plain_s_per_instance": plain_per, "plain_instances_timed": n_plain,
+            "plain_hessians": nh, "plain_energy_evals": ne,
+            "batched_s_total": r["seconds"], "batched_instances": n_heldout, "batched_s_per_instance": batched_per,
+            "batched_rounds": int(r["rounds"]), "batched_iters_median": float(np.median(r["iters"])),
+            "batched_iters_max": int(r["iters"].max()), "proposals_used": int(r["used"].sum()),
+            "anchor_hessian_s": r["t_anchor"], "max_gnorm": float(r["gnorm"].max()), "gtol": 1e-6,
+            "energy_match_1e-8": int(np.sum(np.abs(dE) < 1e-8)), "energy_compared": n_plain,
+            "max_abs_dE": float(np.abs(dE).max()),
+            "training": {"instances": n_train, "chain_s": t_chain, "chain_iters_median": float(np.median(its)),
+                         "mlp_train_s": t_train, "epochs": epochs, "loss_first": float(hist[0]),
+                         "loss_last": float(hist[-1]), "origin_newton_s": t_origin},
+            "workload": "10 orbitals 5a+5b, 3 layers (81 parameters), family h(s)=h0+s h1, L(s)=L0+s L1, seed 0; "
+                        "%d training / %d held-out s ~ U(0,1)" % (n_train, n_heldout)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -198,8 +330,16 @@ def main():
     ap.add_argument("--ham", default="stored", choices=["stored", "otf"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--orbitals", type=int, default=12, choices=[8, 10, 12, 14],
+                    help="workload size (the metric is quoted at 12; others are profiling cases)")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-ttc", action="store_true")
+    ap.add_argument("--ttc-train", type=int, default=2000)
+    ap.add_argument("--ttc-heldout", type=int, default=200)
+    ap.add_argument("--ttc-plain", type=int, default=24)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
+    set_orbitals(args.orbitals)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -220,7 +360,9 @@ def main():
     if not args.no_e2e:
         e2e = e2e_c_abi(pb, max(10, args.steps // 10), 2)
 
-    eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"])
+    from ansatzevolve_gb300 import autotune
+    tuning = tuned(autotune.problem_key(N_ORB, N_A, N_B, LAYERS, 1, mode, False))
+    eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"], tuning=tuning or None)
     init = np.zeros(eng.D)
     init[np.searchsorted(eng.states(), pb["hf"])] = 1.0
     eng.set_initial(init)
@@ -298,11 +440,17 @@ def main():
                           "phase_ms": {"evolve": phase_ms[0] / max(nph, 1), "hpsi_energy": phase_ms[1] / max(nph, 1),
                                        "adjoint": phase_ms[2] / max(nph, 1)}},
         "gpu_launches": int(launches),
+        "tuning": {"settings": {str(k): v for k, v in eng.tuning().items()}, "tuned": bool(tuning)},
         "clocks": clk.summary(),
         "setup_s": setup_s,
     }
     if e2e:
         line["e2e"] = e2e
+    eng.close()
+    if not args.no_batched:
+        line["batched"] = batched_bench(stream)
+    if not args.no_ttc:
+        line["time_to_converge"] = ttc_bench(args.ttc_train, args.ttc_heldout, args.ttc_plain)
     if not args.no_cpu:
         cb, Eo, go = cpu_baseline(pb)
         line["cpu_baseline"] = cb
