@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
 _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
-TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS = 1, 2, 3
+TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR = 1, 2, 3, 4
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 
 _P = ctypes.c_void_p
@@ -93,6 +93,8 @@ def lib(build_if_missing=True):
         "aegpu_gradient": (ctypes.c_int, [_P, _DP, _DP, _DP]),
         "aegpu_hessian": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, _DP, _DP, _DP]),
         "aegpu_apply_h": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_gradient_proj": (ctypes.c_int, [_P, _DP, _DP, _DP, _DP]),
+        "aegpu_hessian_proj": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, _DP, _DP, _DP, _DP]),
         "aegpu_gradient_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
         "aegpu_energy_dev": (ctypes.c_int, [_P, _P, _P, _P]),
         "aegpu_state_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
@@ -165,8 +167,9 @@ class Engine:
         for knob in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM):
             if tuning and knob in tuning:
                 self._check(self.L.aegpu_set_tuning(h, knob, int(tuning[knob])))
-        if tuning and TUNE_OTF_THREADS in tuning:
-            self._check(self.L.aegpu_set_tuning(h, TUNE_OTF_THREADS, int(tuning[TUNE_OTF_THREADS])))
+        for knob in (TUNE_OTF_THREADS, TUNE_SPMV_TPR):
+            if tuning and knob in tuning:
+                self._check(self.L.aegpu_set_tuning(h, knob, int(tuning[knob])))
         ops = _i32(ops0).reshape(-1, 4)
         self.nops = len(ops)
         self.W = 2 if complex_mode else 1
@@ -259,6 +262,18 @@ class Engine:
             return E[0], g
         return E, g.reshape(self.nb, self.nops)
 
+    def gradient_proj(self, angles_ops, proj):
+        """(<proj|psi>, d<proj|psi>/dtheta_op) per instance (evolveDerivativeProj)."""
+        a = self._angles(angles_ops)
+        pr = _f64(proj)
+        assert pr.size == self.nb * self.D * self.W
+        ov = np.zeros(self.nb)
+        g = np.zeros(self.nb * self.nops)
+        self._check(self.L.aegpu_gradient_proj(self.h, dptr(a), dptr(pr), dptr(ov), dptr(g)))
+        if self.nb == 1:
+            return ov[0], g
+        return ov, g.reshape(self.nb, self.nops)
+
     def hessian(self, angles_ops, param0, scale):
         a = _f64(angles_ops)
         p = _i32(param0)
@@ -269,6 +284,21 @@ class Engine:
         H = np.zeros((P, P))
         self._check(self.L.aegpu_hessian(self.h, dptr(a), iptr(p), dptr(s), P, dptr(E), dptr(g), dptr(H)))
         return E[0], g, H
+
+    def hessian_proj(self, angles_ops, param0, scale, proj):
+        """(<proj|psi>, gradient, Hessian) of the overlap in the compressed parameters."""
+        a = _f64(angles_ops)
+        p = _i32(param0)
+        s = _f64(scale)
+        pr = _f64(proj)
+        assert pr.size == self.D * self.W
+        P = int(p.max()) + 1
+        ov = np.zeros(1)
+        g = np.zeros(P)
+        H = np.zeros((P, P))
+        self._check(self.L.aegpu_hessian_proj(self.h, dptr(a), iptr(p), dptr(s), P, dptr(pr), dptr(ov), dptr(g),
+                                              dptr(H)))
+        return ov[0], g, H
 
     def apply_h(self, x):
         x = _f64(x)
@@ -335,7 +365,8 @@ class Engine:
         return x, E, gn, it, r.value
 
     def tuning(self):
-        return {k: int(self.L.aegpu_get_tuning(self.h, k)) for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS)}
+        return {k: int(self.L.aegpu_get_tuning(self.h, k))
+                for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR)}
 
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))

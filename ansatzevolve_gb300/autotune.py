@@ -8,7 +8,8 @@ knobs and keeps the fastest:
   pass means fewer sweeps over HBM, but fewer commuting excitations to fill a pass);
 * TUNE_CTAS_PER_SM: CTAs per SM of the pass kernels (occupancy against tail effects);
 * TUNE_OTF_THREADS: threads per CTA of the on-the-fly H*psi kernel (one CTA per alpha
-  string and chunk of beta strings).
+  string and chunk of beta strings);
+* TUNE_SPMV_TPR: threads per row of the stored-H product (0 = chosen by size).
 
 The search is greedy, one knob at a time in that order.  Results are cached in a JSON
 file (AEGPU_TUNE_CACHE, default ~/.cache/ansatzevolve_gb300/autotune.json) under a key
@@ -21,14 +22,15 @@ import time
 
 import numpy as np
 
-from . import HAM_ON_THE_FLY, HAM_STORED, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_PASS_OPS
+from . import HAM_ON_THE_FLY, HAM_STORED, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_PASS_OPS, TUNE_SPMV_TPR
 
 CANDIDATES = {
     TUNE_CTAS_PER_SM: (2, 4, 8, 16),
     TUNE_PASS_OPS: (4, 5, 6),
     TUNE_OTF_THREADS: (128, 256, 512),
+    TUNE_SPMV_TPR: (1, 2, 4, 8),
 }
-DEFAULT = {TUNE_PASS_OPS: 6, TUNE_CTAS_PER_SM: 8, TUNE_OTF_THREADS: 512}
+DEFAULT = {TUNE_PASS_OPS: 6, TUNE_CTAS_PER_SM: 8, TUNE_OTF_THREADS: 512, TUNE_SPMV_TPR: 0}
 
 
 def cache_path():
@@ -83,8 +85,9 @@ def time_config(build, tuning, reps=5):
 
 
 def tune(key, build, knobs=(TUNE_CTAS_PER_SM, TUNE_PASS_OPS, TUNE_OTF_THREADS), reps=5, path=None, log=None):
-    """Greedy search; build(tuning) -> an engine with its Hamiltonian and angles in
-    its io buffer.  Stores and returns the best settings."""
+    """Greedy search over `knobs` in order (add TUNE_SPMV_TPR for stored Hamiltonians);
+    build(tuning) -> an engine with its Hamiltonian and angles in its io buffer.
+    Stores and returns the best settings."""
     best = dict(DEFAULT)
     trials = []
     t_best = time_config(build, best, reps)

@@ -108,6 +108,7 @@ struct PassConst {
 
 struct BlockArgs {
     const uint32_t *idx;
+    const uint32_t *obits;   // bitstrings parallel to idx (warp kernels)
     const OrbitGroup *groups;
     const OrbitTile *tiles;
     const int *ops;          // slot -> operator
@@ -174,6 +175,20 @@ __global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += parts[i];
     s = block_sum(s, red);
     if (threadIdx.x == 0) out[blockIdx.x] = s * scale;
+}
+
+// Per-CTA partial sums of <a|b> over instance blockIdx.y (vectors at stride n):
+// parts[blockIdx.y * gridDim.x + blockIdx.x].
+__global__ void k_dot(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ parts)
+{
+    __shared__ double red[32];
+    a += (size_t)blockIdx.y * n;
+    b += (size_t)blockIdx.y * n;
+    double s = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) parts[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
 }
 
 // -------------------------------------------------------- block rotations --
@@ -464,11 +479,11 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
     const int nw = (gridDim.x * blockDim.x) >> 5;
     for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
         const WarpTask task = tasks[t];
-        const uint32_t mask = a.groups[task.group].mask;
-        const uint32_t *idx = a.idx + task.elem_off;
+        const uint32_t mask = task.mask;
+        const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
-        const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
+        const uint32_t b0 = ok0 ? obits[lane] : 0u, b1 = ok1 ? obits[lane + 32] : 0u;
         double v0[W], v1[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
@@ -521,7 +536,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
                                                            double *hv, int64_t inst_stride, double *partials,
                                                            int64_t part_stride)
 {
-    __shared__ double red[kMaxWarpLayers][kWarpThreads];
+    __shared__ double red[kMaxWarpLayers][kWarpThreads / 32];
     const int lane = threadIdx.x & 31, b = blockIdx.y;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
@@ -533,11 +548,11 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
     for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
     for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
         const WarpTask task = tasks[t];
-        const uint32_t mask = a.groups[task.group].mask;
-        const uint32_t *idx = a.idx + task.elem_off;
+        const uint32_t mask = task.mask;
+        const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
-        const uint32_t b0 = ok0 ? a.basis.bits(z0) : 0u, b1 = ok1 ? a.basis.bits(z1) : 0u;
+        const uint32_t b0 = ok0 ? obits[lane] : 0u, b1 = ok1 ? obits[lane + 32] : 0u;
         const double *cp = ckpt + (size_t)task.elem_off * W;
         double v0[W], v1[W], h0[W], h1[W];
 #pragma unroll
@@ -596,14 +611,20 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
             if (ok1) h[(size_t)z1 * W + w] = sigma * h1[w];
         }
     }
-    // fixed-order CTA sum through shared memory
+    // fixed-order CTA sum: a butterfly over each warp's lanes, then the warps in order
+    const int warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int j = 0; j < kMaxWarpLayers; ++j) red[j][threadIdx.x] = accS[j];
+    for (int j = 0; j < kMaxWarpLayers; ++j) {
+        double v = accS[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[j][warp] = v;
+    }
     __syncthreads();
     if (threadIdx.x < kMaxSlots) {
         double sum = 0.0;
         if (threadIdx.x < kMaxWarpLayers)
-            for (int w = 0; w < (int)blockDim.x; ++w) sum += red[threadIdx.x][w];
+            for (int w = 0; w < kWarpThreads / 32; ++w) sum += red[threadIdx.x][w];
         partials[(size_t)b * part_stride + (size_t)blockIdx.x * kMaxSlots + threadIdx.x] = sum;
     }
 }
@@ -775,7 +796,7 @@ __global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t
 // Hessian second-derivative partials of one block -> Hops (nops x nops, row-major).
 __global__ void k_hess_reduce(const double *__restrict__ partials, int ntiles, int nvec, int nslots,
                               const int *__restrict__ pos_op, const int *__restrict__ block_ops, int block_pos0,
-                              double *__restrict__ Hops, int nops)
+                              double *__restrict__ Hops, int nops, double factor)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= nvec * nslots) return;
@@ -786,8 +807,8 @@ __global__ void k_hess_reduce(const double *__restrict__ partials, int ntiles, i
     s = warp_sum(s);
     if (lane == 0) {
         const int i = pos_op[vec], j = block_ops[sl];
-        Hops[(size_t)i * nops + j] += 2.0 * s;
-        if (i != j) Hops[(size_t)j * nops + i] += 2.0 * s;
+        Hops[(size_t)i * nops + j] += factor * s;
+        if (i != j) Hops[(size_t)j * nops + i] += factor * s;
     }
 }
 
@@ -834,14 +855,19 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv(const int64_t *__restrict
 // Sliced-ELL product, one thread per row: 4 independent FP64 accumulators, no
 // cross-lane reduction (its shuffles and adds would cost FP64 issue slots, the
 // binding pipe of this kernel on GB300), fused with the partial sums of <x|y>.
-template <int W>
+template <int W, int T>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int32_t *__restrict__ col,
                                                             const double *__restrict__ val,
                                                             const double *__restrict__ x, double *__restrict__ y,
                                                             int64_t D, double *__restrict__ epart, int64_t mat_stride)
 {
+    // T threads per row: a warp covers 32/T consecutive rows of one 32-row slab; lane
+    // (sub, k) takes row k's groups sub, sub+T, ... (each group read by 32/T lanes is
+    // one contiguous run), and the T partial sums meet in a fixed butterfly.
+    constexpr int RPW = 32 / T;
     __shared__ double red[kSpmvThreads / 32];
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, sub = lane / RPW;
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane) / T + lane % RPW;
     // instance blockIdx.y: its vectors, and its matrix (mat_stride = 0 when shared)
     col += (size_t)blockIdx.y * mat_stride;
     val += (size_t)blockIdx.y * mat_stride;
@@ -849,14 +875,14 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int
     y += (size_t)blockIdx.y * D * W;
     if (epart) epart += (size_t)blockIdx.y * gridDim.x;
     double e = 0;
+    double a0[W], a1[W], a2[W], a3[W];
+#pragma unroll
+    for (int w = 0; w < W; ++w) a0[w] = a1[w] = a2[w] = a3[w] = 0.0;
     if (r < D) {
         const size_t base = ell_pos(r, 0, q);  // group g of this row starts at base + 128 g
         const int4 *c4 = reinterpret_cast<const int4 *>(col + base);
         const double2 *v2 = reinterpret_cast<const double2 *>(val + base);
-        double a0[W], a1[W], a2[W], a3[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) a0[w] = a1[w] = a2[w] = a3[w] = 0.0;
-        for (int64_t g = 0; g < q; ++g) {
+        for (int64_t g = sub; g < q; g += T) {
             const int4 c = __ldg(c4 + 32 * g);
             const double2 h01 = __ldg(v2 + 64 * g), h23 = __ldg(v2 + 64 * g + 1);
 #pragma unroll
@@ -867,9 +893,13 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int
                 a3[w] = fma(h23.y, __ldg(x + (size_t)c.w * W + w), a3[w]);
             }
         }
+    }
 #pragma unroll
-        for (int w = 0; w < W; ++w) {
-            const double acc = (a0[w] + a1[w]) + (a2[w] + a3[w]);
+    for (int w = 0; w < W; ++w) {
+        double acc = (a0[w] + a1[w]) + (a2[w] + a3[w]);
+#pragma unroll
+        for (int o = RPW; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (r < D && sub == 0) {
             y[r * W + w] = acc;
             e = fma(acc, x[r * W + w], e);
         }
@@ -1288,7 +1318,7 @@ struct aegpu_engine {
         WarpTask *wtasks = nullptr;
         int64_t part_off = 0;     // offset of this block's gradient partials
         int64_t ckpt_off = 0;     // offset (doubles) of this pass's checkpoint
-        uint32_t *idx = nullptr;
+        uint32_t *idx = nullptr, *bits = nullptr;
         OrbitGroup *groups = nullptr;
         OrbitTile *tiles = nullptr;
         int *ops = nullptr;
@@ -1344,6 +1374,14 @@ struct aegpu_engine {
     int tune_pass_ops = kMaxWarpLayers;
     int tune_ctas_per_sm = 8;
     int tune_otf_threads = 512;
+    int tune_spmv_tpr = 0;  // threads per stored-H row: 0 = by size (>= 4 CTAs per SM)
+    int spmv_tpr() const
+    {
+        if (tune_spmv_tpr) return tune_spmv_tpr;
+        int t = 1;
+        while (t < 8 && (int64_t)B.D * t < (int64_t)sm_count * 4 * kSpmvThreads) t *= 2;
+        return t;
+    }
 
     // optional CUDA-event timing of the phases of *_dev evaluations
     bool timing = false;
@@ -1444,6 +1482,7 @@ struct aegpu_engine {
         const int npass = (int)dblocks.size();
         BlockArgs a;
         a.idx = b.idx;
+        a.obits = b.bits;
         a.groups = b.groups;
         a.tiles = b.tiles;
         a.ops = b.ops;
@@ -1643,13 +1682,18 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         else
             k_spmv<2, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
     } else if (e->ham_kind == 2) {
-        const int sg = (int)((D + kSpmvThreads - 1) / kSpmvThreads);
+        const int T = e->spmv_tpr();
+        const int64_t rows_per_cta = kSpmvThreads / T;
+        const int sg = (int)((D + rows_per_cta - 1) / rows_per_cta);
         const dim3 g(sg, ninst);
         const int64_t q = e->ell_width >> 2, ms = e->ell_stride_inst;
-        if (e->W == 1)
-            k_spmv_sell<1><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms);
-        else
-            k_spmv_sell<2><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms);
+#define AE_SELL(WW, TT) k_spmv_sell<WW, TT><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms)
+        if (e->W == 1) {
+            if (T == 1) AE_SELL(1, 1); else if (T == 2) AE_SELL(1, 2); else if (T == 4) AE_SELL(1, 4); else AE_SELL(1, 8);
+        } else {
+            if (T == 1) AE_SELL(2, 1); else if (T == 2) AE_SELL(2, 2); else if (T == 4) AE_SELL(2, 4); else AE_SELL(2, 8);
+        }
+#undef AE_SELL
         if (nparts) *nparts = sg;
     } else if (e->ham_kind == 3) {
         const dim3 g(e->otf.nA, e->otf_chunks, ninst);
@@ -1678,8 +1722,9 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 }
 
 // Adjoint sweep over all passes for the first ninst instances (h updated in place,
-// psi taken from the checkpoints), per-op gradients in grad_dev[b * nops + op].
-int run_backward(aegpu_engine *e, double *grad_dev, int ninst)
+// psi taken from the checkpoints), per-op gradients scale * <h|G_op psi> in
+// grad_dev[b * nops + op] (scale 2 for the energy gradient, 1 for a projection).
+int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.0)
 {
     const int64_t n = (int64_t)e->vec_elems();
     const int nops = (int)e->excs.size();
@@ -1710,7 +1755,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst)
     }
     const int warps = nops * ninst;
     k_grad_reduce<<<(warps * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
-                                                                   e->d_op_slot, nops, 2.0, grad_dev, ninst,
+                                                                   e->d_op_slot, nops, scale, grad_dev, ninst,
                                                                    e->n_partials);
     e->launches += 1;
     return e->cuda_check("backward");
@@ -1883,6 +1928,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             OrbitTables T = build_orbits(e->B, bc, (int)hw);
             if (!T.ok) return e->fail(AEGPU_ERR_UNSUPPORTED, "an excitation leaves the determinant sector");
             d.idx = e->upload(T.idx);
+            d.bits = e->upload(T.bits);
             d.groups = e->upload(T.groups);
             d.tiles = e->upload(T.tiles);
             d.ntiles = (int)T.tiles.size();
@@ -1935,7 +1981,9 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
 
     const size_t n = e->vec_elems();
     e->n_ckpt = ckpt_off;
-    e->n_epart = std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D + kSpmvThreads - 1) / kSpmvThreads);
+    // partial sums per instance: the CSR grid, or one per CTA of the stored-H product at
+    // up to 8 threads per row
+    e->n_epart = std::max<int64_t>(e->spmv_grid, ((int64_t)e->B.D * 8 + kSpmvThreads - 1) / kSpmvThreads);
     e->d_start = e->alloc<double>(n);
     if (!e->d_start || !pa.pass_ops || !pa.pass_diag) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
     int rc = e->alloc_instances(e->nb);
@@ -2200,6 +2248,12 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         if (e->ham_kind) return e->fail(AEGPU_ERR_STATE, "set the thread count before the Hamiltonian");
         e->tune_otf_threads = value;
         return AEGPU_OK;
+    case AEGPU_TUNE_SPMV_TPR:
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+            return e->fail(AEGPU_ERR_ARG, "threads per row must be 0 (by size), 1, 2, 4 or 8");
+        if (e->grad_graph) return e->fail(AEGPU_ERR_STATE, "set the threads per row before the first evaluation");
+        e->tune_spmv_tpr = value;
+        return AEGPU_OK;
     default:
         return e->fail(AEGPU_ERR_ARG, "unknown tuning knob");
     }
@@ -2212,6 +2266,7 @@ int aegpu_get_tuning(const aegpu_engine *e, int knob)
     case AEGPU_TUNE_PASS_OPS: return e->tune_pass_ops;
     case AEGPU_TUNE_CTAS_PER_SM: return e->tune_ctas_per_sm;
     case AEGPU_TUNE_OTF_THREADS: return e->tune_otf_threads;
+    case AEGPU_TUNE_SPMV_TPR: return e->spmv_tpr();
     default: return -1;
     }
 }
@@ -2250,10 +2305,32 @@ int aegpu_energy(aegpu_engine *e, const double *angles, double *energy)
     return stream_sync(e, "energy");
 }
 
+static int capture_grad_graph(aegpu_engine *e);
+
 int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double *grad_ops)
 {
     if (!e || !angles || !grad_ops) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    const size_t nang = e->excs.size() * (size_t)e->nb;
+    if (e->use_graph && !e->timing && !(same_angles(e, angles) && e->h_valid)) {
+        // the whole evaluation as one graph replay (H psi is not cached for these angles)
+        if (!e->grad_graph) {
+            int rc = capture_grad_graph(e);
+            if (rc) return rc;
+        }
+        cudaMemcpyAsync(e->d_ang, angles, nang * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+        if (cudaGraphLaunch(e->grad_graph, e->stream) != cudaSuccess) return e->cuda_check("graph launch");
+        e->launches += e->graph_launches;
+        if (energy) cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        cudaMemcpyAsync(grad_ops, e->d_grad, nang * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        int rc = stream_sync(e, "gradient");
+        if (rc) return rc;
+        // psi is left evolved to these angles (the adjoint sweep reads checkpoints only)
+        e->cached_angles.assign(angles, angles + nang);
+        e->psi_valid = true;
+        e->h_valid = false;
+        return AEGPU_OK;
+    }
     int rc = ensure_state(e, angles);
     if (rc) return rc;
     if (!e->h_valid) {
@@ -2269,11 +2346,33 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
     return stream_sync(e, "gradient");
 }
 
+// Projected sweep (FusedEvolve::evolveDerivativeProj, fusedevolve.cpp:2814-2880):
+// overlap[b] = <proj_b|psi_b(theta_b)>, grad[b][op] = d overlap / d theta_op.
+int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *proj, double *overlap, double *grad_ops)
+{
+    if (!e || !angles || !proj || !grad_ops) return AEGPU_ERR_ARG;
+    if (!e->d_psi) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    int rc = ensure_state(e, angles);
+    if (rc) return rc;
+    const int64_t n = (int64_t)e->vec_elems();
+    cudaMemcpyAsync(e->d_h, proj, (size_t)n * e->nb * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+    e->h_valid = false;
+    const int grid = (int)std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), e->n_epart);
+    k_dot<<<dim3(grid, e->nb), 256, 0, e->stream>>>(e->d_h, e->d_psi, n, e->d_epart);
+    k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, grid, e->d_scalar, 1.0);
+    e->launches += 2;
+    rc = run_backward(e, e->d_grad, e->nb, 1.0);
+    if (rc) return rc;
+    if (overlap) cudaMemcpyAsync(overlap, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    return stream_sync(e, "gradient_proj");
+}
+
 }  // extern "C"
 
 // Capture pass constants + evolve + H psi + adjoint sweep of all nb instances
 // (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
-static int capture_grad_graph(aegpu_engine *e)
+int capture_grad_graph(aegpu_engine *e)
 {
     cudaStream_t cap = nullptr, saved = e->stream;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return e->cuda_check("graph stream");
@@ -2541,8 +2640,14 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
     return rc;
 }
 
-int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
-                  double *energy, double *grad_comp, double *hess_comp)
+}  // extern "C"
+
+// Energy Hessian (proj = nullptr; FusedEvolve::evolveHessian, fusedevolve.cpp:2437-2780)
+// or projected Hessian of <proj|psi(theta)> (FusedEvolve::evolveHessianProj,
+// fusedevolve.cpp:2882-3183: no T^T H T term, second-derivative sweeps against the
+// fixed bra, factor 1); energy receives <psi|H psi> or <proj|psi>.
+static int hessian_impl(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                        const double *proj, double *energy, double *grad_comp, double *hess_comp)
 {
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
@@ -2629,7 +2734,16 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
     // 2. compressed tangents, H on all of them, Gram matrix 2 T_C^T H T_C
     k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
     const int VW = V * W;
-    if (e->ham_kind == 1)
+    if (!e->cublas) {
+        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
+    }
+    cublasSetStream(e->cublas, s);
+    if (proj) {
+        // projected: <proj|T_C v> for every column (the last is <proj|psi>), bra for the sweeps
+        cudaMemcpyAsync(e->d_h, proj, n * sizeof(double), cudaMemcpyHostToDevice, s);
+        const double one = 1.0, zero = 0.0;
+        cublasDgemv(e->cublas, CUBLAS_OP_N, V, (int)(D * W), &one, TC, V, e->d_h, 1, &zero, THT, 1);
+    } else if (e->ham_kind == 1)
         k_spmm<false><<<e->sm_count * 16, 128, 0, s>>>(e->d_rowptr, 0, e->d_col, e->d_val, TC, HTC, VW, D);
     else if (e->ham_kind == 2)
         k_spmm<true><<<e->sm_count * 16, 128, 0, s>>>(nullptr, e->ell_width, e->d_col, e->d_val, TC, HTC, VW, D);
@@ -2644,16 +2758,14 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         }
     }
     e->launches += 2;
-    if (!e->cublas) {
-        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
+    if (!proj) {
+        const double two = 2.0, zero = 0.0;
+        // TC, HTC are row-major (D*W) x V == column-major V x (D*W)
+        cublasDgemm(e->cublas, CUBLAS_OP_N, CUBLAS_OP_T, V, V, (int)(D * W), &two, TC, V, HTC, V, &zero, THT, V);
+        // H psi for the backward sweeps: last column of HTC
+        cudaMemcpy2DAsync(e->d_h, sizeof(double), HTC + nparams, (size_t)V * sizeof(double), sizeof(double), n,
+                          cudaMemcpyDeviceToDevice, s);
     }
-    cublasSetStream(e->cublas, s);
-    const double two = 2.0, zero = 0.0;
-    // TC, HTC are row-major (D*W) x V == column-major V x (D*W)
-    cublasDgemm(e->cublas, CUBLAS_OP_N, CUBLAS_OP_T, V, V, (int)(D * W), &two, TC, V, HTC, V, &zero, THT, V);
-    // H psi for the backward sweeps: last column of HTC
-    cudaMemcpy2DAsync(e->d_h, sizeof(double), HTC + nparams, (size_t)V * sizeof(double), sizeof(double), n,
-                      cudaMemcpyDeviceToDevice, s);
     // 3. second-derivative sweeps
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
         auto &b = e->dblocks[bi];
@@ -2665,7 +2777,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
             dim3 g(kDiagGrid, nvec);
             k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
-                                                                            b.ops, p0, Hops, nops);
+                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
             k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1, nullptr, 0, 0);
             e->launches += 4;
         } else if (b.ntiles) {
@@ -2680,7 +2792,7 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
                 k_block_hess<2><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);
             }
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, b.ntiles, nvec, b.nslots, e->d_pos_op,
-                                                                            b.ops, p0, Hops, nops);
+                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
             if (W == 1)
                 k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_h, 0, 1);
             else
@@ -2690,10 +2802,21 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
     }
     std::vector<double> hops((size_t)nops * nops), tht((size_t)V * V);
     cudaMemcpyAsync(hops.data(), Hops, hops.size() * 8, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(tht.data(), THT, tht.size() * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(tht.data(), THT, (proj ? (size_t)V : tht.size()) * 8, cudaMemcpyDeviceToHost, s);
     rc = stream_sync(e, "hessian");
     e->psi_valid = e->h_valid = false;
     if (rc) return rc;
+    if (proj) {
+        // Hessian = C Hops C^T (fusedevolve.cpp:3171); gradient and overlap from <proj|T_C>
+        for (size_t k = 0; k < (size_t)nparams * nparams; ++k) hess_comp[k] = 0.0;
+        for (int a = 0; a < nops; ++a)
+            for (int b = 0; b < nops; ++b)
+                hess_comp[(size_t)param[a] * nparams + param[b]] += scale[a] * scale[b] * hops[(size_t)a * nops + b];
+        if (grad_comp)
+            for (int i = 0; i < nparams; ++i) grad_comp[i] = tht[i];
+        if (energy) *energy = tht[nparams];
+        return AEGPU_OK;
+    }
     // Hessian = C Hops C^T + THT (fusedevolve.cpp:2762-2763); THT column-major V x V
     for (int i = 0; i < nparams; ++i)
         for (int j = 0; j < nparams; ++j) hess_comp[(size_t)i * nparams + j] = tht[(size_t)j * V + i];
@@ -2704,6 +2827,21 @@ int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const
         for (int i = 0; i < nparams; ++i) grad_comp[i] = tht[(size_t)nparams * V + i];
     if (energy) *energy = tht[(size_t)nparams * V + nparams] / 2.0;
     return AEGPU_OK;
+}
+
+extern "C" {
+
+int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                  double *energy, double *grad_comp, double *hess_comp)
+{
+    return hessian_impl(e, angles, param, scale, nparams, nullptr, energy, grad_comp, hess_comp);
+}
+
+int aegpu_hessian_proj(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                       const double *proj, double *overlap, double *grad_comp, double *hess_comp)
+{
+    if (!proj) return AEGPU_ERR_ARG;
+    return hessian_impl(e, angles, param, scale, nparams, proj, overlap, grad_comp, hess_comp);
 }
 
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream)

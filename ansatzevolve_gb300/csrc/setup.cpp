@@ -192,6 +192,7 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
             if (m & (1u << i)) g.slot[g.k++] = (int8_t)i;
         const uint32_t osz = 1u << g.k;
         T.idx.reserve(T.idx.size() + nroots * osz);
+        T.bits.reserve(T.bits.size() + nroots * osz);
         std::vector<uint32_t> orb(osz);
         for (auto &c : chunks)
             for (uint32_t root : c.roots[m]) {
@@ -208,6 +209,7 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
                     int64_t r = B.rank_of(orb[q]);
                     if (r < 0) T.ok = false;
                     T.idx.push_back((uint32_t)(r < 0 ? 0 : r));
+                    T.bits.push_back(orb[q]);
                 }
             }
         const uint32_t per_tile = osz >= (uint32_t)kTileElems ? 1u : (uint32_t)kTileElems / osz;
@@ -226,6 +228,7 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
                 w.group = (uint32_t)T.groups.size();
                 w.elem_off = g.idx_off + o * osz;
                 w.n = std::min(per_task, g.n_orbits - o) * osz;
+                w.mask = m;
                 T.wtasks.push_back(w);
             }
         }

@@ -105,11 +105,12 @@ struct WarpTask {
     uint32_t group;
     uint32_t elem_off;   // first entry in the block's rank list
     uint32_t n;          // members (<= 64)
-    uint32_t pad;
+    uint32_t mask;       // the group's active-excitation mask
 };
 
 struct OrbitTables {
     std::vector<uint32_t> idx;        // ranks, grouped / ordered as described
+    std::vector<uint32_t> bits;       // the determinants' bitstrings, parallel to idx
     std::vector<OrbitGroup> groups;
     std::vector<OrbitTile> tiles;
     std::vector<WarpTask> wtasks;     // only when every orbit has <= 64 members

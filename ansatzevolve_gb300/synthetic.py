@@ -30,19 +30,20 @@ def synthetic_integrals(n_orb, seed=0, n_factors=None):
     return np.ascontiguousarray(h), np.ascontiguousarray(g)
 
 
-def family_integrals(n_orb, s, seed=0, n_factors=None):
-    """h(s) = h0 + s*h1 and L^k(s) = L^k0 + s*L^k1 for a Hamiltonian family scan."""
+def family_integrals(n_orb, s, seed=0, n_factors=None, pert=1.0):
+    """h(s) = h0 + s*h1 and L^k(s) = L^k0 + s*L^k1 for a Hamiltonian family scan; the
+    perturbation tensors h1, L^k1 are drawn at `pert` times the base tensors' scale."""
     rng = np.random.default_rng(seed)
     k = n_orb if n_factors is None else n_factors
     p = np.arange(n_orb)
     damp = np.exp(-np.abs(p[:, None] - p[None, :]) / 2.0)
     a0 = rng.normal(0.0, 1.0, (n_orb, n_orb))
-    a1 = rng.normal(0.0, 1.0, (n_orb, n_orb))
+    a1 = rng.normal(0.0, pert, (n_orb, n_orb))
     h = 0.5 * ((a0 + s * a1) + (a0 + s * a1).T) * damp
     g = np.zeros((n_orb,) * 4)
     for _ in range(k):
         l0 = rng.normal(0.0, 0.3, (n_orb, n_orb))
-        l1 = rng.normal(0.0, 0.3, (n_orb, n_orb))
+        l1 = rng.normal(0.0, 0.3 * pert, (n_orb, n_orb))
         l = l0 + s * l1
         l = 0.5 * (l + l.T)
         g += np.einsum("pq,rs->pqrs", l, l)

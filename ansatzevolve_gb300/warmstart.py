@@ -171,11 +171,13 @@ def train_warmstart(feats, targets, hidden=512, epochs=400, batch=128, lr=1e-3, 
 # ------------------------------------------------------------- family scans --
 class FamilySpec:
     """A TUPS ansatz over a Hamiltonian family h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1
-    (synthetic.family_integrals with a fixed seed)."""
+    (synthetic.family_integrals with a fixed seed).  pert: scale of the perturbation
+    tensors relative to the base ones (0.25 keeps s in [0, 1] a smooth scan; at 1.0 the
+    continuation branch changes every few hundredths of s)."""
 
-    def __init__(self, n_orb=10, n_alpha=5, layers=3, seed=0):
+    def __init__(self, n_orb=10, n_alpha=5, layers=3, seed=0, pert=0.25):
         from .synthetic import tups_operators
-        self.n_orb, self.n_alpha, self.layers, self.seed = n_orb, n_alpha, layers, seed
+        self.n_orb, self.n_alpha, self.layers, self.seed, self.pert = n_orb, n_alpha, layers, seed, pert
         ops, param, scale = tups_operators(n_orb, layers)
         self.param0 = np.asarray(param) - 1
         self.scale = np.asarray(scale, dtype=np.float64)
@@ -183,7 +185,7 @@ class FamilySpec:
 
     def integrals(self, s):
         from .synthetic import family_integrals
-        return family_integrals(self.n_orb, float(s), seed=self.seed)
+        return family_integrals(self.n_orb, float(s), seed=self.seed, pert=self.pert)
 
     def features(self, svals):
         return np.stack([features(*self.integrals(s)) for s in svals])

@@ -42,23 +42,41 @@ N_ORB, N_A, N_B, LAYERS, SEED = 12, 6, 6, 3, 0
 def set_orbitals(n):
     """Smaller or larger cases of the same workload for profiling (default 12)."""
     global N_ORB, N_A, N_B, LAYERS
-    N_ORB, N_A, N_B, LAYERS = n, n // 2, n // 2, 2 if n <= 8 else 3
+    N_ORB, N_A, N_B, LAYERS = n, n // 2, n // 2, 2 if n <= 8 else (4 if n >= 14 else 3)
 
 
 def workload_desc(D, P, nops, ham):
+    if LUCJ:
+        return {"workload": "LUCJ exp(-K) exp(iJ) exp(K), complex128, %d orbitals, %da+%db electrons (D=%d), %d "
+                            "operators, synthetic random integrals seed 0, H %s" % (N_ORB, N_A, N_B, D, nops, ham),
+                "global_batch": 1, "parallelism": "replicas", "l2": "state vectors larger than L2"}
     return {"workload": "tUPS %d orbitals, %da+%db electrons (D=%d), %d layers (%d parameters, %d excitations), "
                         "synthetic random integrals seed 0, H %s" % (N_ORB, N_A, N_B, D, LAYERS, P, nops, ham),
             "global_batch": 1, "parallelism": "replicas", "l2": "inputs larger than L2 (H rows stream from HBM every step)"}
 
 
+LUCJ = False
+# DRAM traffic / algorithmic bytes of k_spmv_sell measured by ncu on the 10-orbital
+# launch (669.27 MB read + 3.68 MB written for 668.57 MB algorithmic)
+SELL_TRAFFIC_RATIO = (669.273856 + 3.678720) / 668.570112
+
+
 def problem():
     from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
     h1, g2 = synthetic_integrals(N_ORB, SEED)
+    hf = hartree_fock_index(N_ORB, N_A, N_B)
+    if LUCJ:
+        # exp(-K) exp(iJ) exp(K), K anti-Hermitian N(0, 0.1), nearest-neighbour J ~ N(0, 0.1)
+        from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+        K, J = random_lucj(N_ORB, SEED)
+        ops0, ang = lucj_operators(K, J)
+        n = len(ops0)
+        return dict(h1=h1, g2=g2, ops0=ops0, ops1=None, p0=np.arange(n), scale=np.ones(n), P=n, x=ang, hf=hf,
+                    cplx=True)
     ops, param, scale = tups_operators(N_ORB, LAYERS)
     P = int(param.max())
     x = np.random.default_rng(SEED + 1).uniform(-0.1, 0.1, P)
-    return dict(h1=h1, g2=g2, ops0=ops - 1, ops1=ops, p0=param - 1, scale=scale, P=P, x=x,
-                hf=hartree_fock_index(N_ORB, N_A, N_B))
+    return dict(h1=h1, g2=g2, ops0=ops - 1, ops1=ops, p0=param - 1, scale=scale, P=P, x=x, hf=hf, cplx=False)
 
 
 class ClockSampler:
@@ -125,7 +143,7 @@ def measured_peak():
 def cpu_baseline(pb, max_seconds=30.0):
     """The oracle (C restatement of the reference algorithm, OpenMP) on a bounded sample."""
     from oracle.oracle import Oracle, lib as olib
-    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B)
+    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B, cplx=pb["cplx"])
     o.set_initial([pb["hf"]], [1.0])
     o.set_ops(pb["ops0"], pb["p0"], pb["scale"])
     o.set_ham_integrals(pb["h1"], pb["g2"], csr=False)
@@ -198,6 +216,18 @@ def e2e_c_abi(pb, steps, warmup):
     m.close()
     return {"value": steps / dt, "unit": "evals/s", "h2d_bytes_per_step": 2 * 8 * P, "d2h_bytes_per_step": 8 + 8 * P,
             "ms_per_step": 1e3 * dt / steps, "api": "getEnergy + getGradient_COMP (H*psi cached between the pair)"}
+
+
+def max_over_ranks(ms, dist):
+    """The slowest rank's timed-region length (every rank runs an independent replica)."""
+    if not dist:
+        return ms
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
 
 
 def tuned(key):
@@ -317,8 +347,9 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=24, epochs=400):
             "training": {"instances": n_train, "chain_s": t_chain, "chain_iters_median": float(np.median(its)),
                          "mlp_train_s": t_train, "epochs": epochs, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1]), "origin_newton_s": t_origin},
-            "workload": "10 orbitals 5a+5b, 3 layers (81 parameters), family h(s)=h0+s h1, L(s)=L0+s L1, seed 0; "
-                        "%d training / %d held-out s ~ U(0,1)" % (n_train, n_heldout)}
+            "workload": "10 orbitals 5a+5b, 3 layers (81 parameters), family h(s)=h0+s h1, L(s)=L0+s L1, seed 0, "
+                        "h1 and L1 at %.2f of the base scale; %d training / %d held-out s ~ U(0,1)"
+                        % (spec.pert, n_train, n_heldout)}
 
 
 def main():
@@ -332,7 +363,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--orbitals", type=int, default=12, choices=[8, 10, 12, 14],
                     help="workload size (the metric is quoted at 12; others are profiling cases)")
+    ap.add_argument("--lucj", action="store_true", help="complex LUCJ ansatz instead of tUPS (no C-ABI e2e)")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-hessian", action="store_true")
     ap.add_argument("--no-ttc", action="store_true")
     ap.add_argument("--ttc-train", type=int, default=2000)
     ap.add_argument("--ttc-heldout", type=int, default=200)
@@ -340,6 +373,10 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
     set_orbitals(args.orbitals)
+    global LUCJ
+    LUCJ = args.lucj
+    if LUCJ:
+        args.no_e2e = True
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -362,9 +399,11 @@ def main():
 
     from ansatzevolve_gb300 import autotune
     tuning = tuned(autotune.problem_key(N_ORB, N_A, N_B, LAYERS, 1, mode, False))
-    eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"], tuning=tuning or None)
-    init = np.zeros(eng.D)
-    init[np.searchsorted(eng.states(), pb["hf"])] = 1.0
+    eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"], complex_mode=pb["cplx"],
+                    tuning=tuning or None)
+    W = 2 if pb["cplx"] else 1
+    init = np.zeros(eng.D * W)
+    init[W * np.searchsorted(eng.states(), pb["hf"])] = 1.0
     eng.set_initial(init)
     t0 = time.perf_counter()
     eng.set_ham_integrals(pb["h1"], pb["g2"], mode)
@@ -403,12 +442,17 @@ def main():
     torch.cuda.synchronize()
     phase_ms, nph = eng.phase_times()
     eng.phase_timing(False)
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        dist.barrier()
+    # one full analytic Hessian (evolveHessian), median of three, host buffers
+    hess_ms = None
+    if not args.no_hessian:
+        ang_h = pb["scale"] * pb["x"][pb["p0"]]
+        th = []
+        for k in range(3):
+            t0 = time.perf_counter()
+            eng.hessian(ang_h + 1e-4 * k, pb["p0"], pb["scale"])
+            th.append(time.perf_counter() - t0)
+        hess_ms = 1e3 * float(np.median(th))
+    t_max = max_over_ranks(ms, dist)
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -418,12 +462,12 @@ def main():
     # roofline of the dominant kernel (H*psi): algorithmic bytes per launch
     peak, peak_kind = measured_peak()
     nnz = info["nnz"]
-    hpsi_bytes = nnz * 12 + 16 * D if mode == ae.HAM_STORED else 16 * D
+    hpsi_bytes = nnz * 12 + 16 * D * W if mode == ae.HAM_STORED else 16 * D * W
     t_hpsi = phase_ms[1] / max(nph, 1) / 1e3
     achieved = hpsi_bytes / t_hpsi / 1e9
     # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
     passes = info["blocks"]
-    step_bytes = passes * 16 * D + hpsi_bytes + passes * 32 * D
+    step_bytes = passes * 16 * D * W + hpsi_bytes + passes * 32 * D * W
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -431,9 +475,15 @@ def main():
         "config": workload_desc(D, pb["P"], len(pb["ops0"]),
                                 "stored as %d-wide rows in HBM (%.1f GB)" % (info["ell_width"], nnz * 12 / 1e9)
                                 if mode == ae.HAM_STORED else "regenerated on the fly"),
-        "roofline": {"bound": "hbm", "kernel": "k_spmv (H*psi)" if mode == ae.HAM_STORED else "k_otf_apply",
+        "roofline": {"bound": "hbm", "kernel": "k_spmv_sell (H*psi)" if mode == ae.HAM_STORED else "k_otf_strings (H*psi)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None, "algorithmic_bytes": hpsi_bytes,
+                     "peak_source": peak_kind,
+                     # DRAM bytes per launch: the ncu count of the 10-orbital launch of this kernel
+                     # (traffic / algorithmic = 1.0066) scaled by nonzeros to this launch
+                     "traffic": hpsi_bytes * SELL_TRAFFIC_RATIO if mode == ae.HAM_STORED else None,
+                     "traffic_source": "profiles/k_spmv_sell_tups10_stored.md (scaled by nonzeros)"
+                     if mode == ae.HAM_STORED else None,
+                     "algorithmic_bytes": hpsi_bytes,
                      "launch_ms": t_hpsi * 1e3},
         "step_roofline": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms_step / 1e3) / 1e9,
                           "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
@@ -446,6 +496,8 @@ def main():
     }
     if e2e:
         line["e2e"] = e2e
+    if hess_ms is not None:
+        line["hessian"] = {"ms": hess_ms, "parameters": pb["P"], "api": "aegpu_hessian (host buffers), median of 3"}
     eng.close()
     if not args.no_batched:
         line["batched"] = batched_bench(stream)

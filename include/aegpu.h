@@ -83,9 +83,10 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
 /* Launch-shape knobs (picked by the autotuner, ansatzevolve_gb300/autotune.py):
  * excitations fused per pass (1..6; before aegpu_set_problem), CTAs per SM of the
  * pass kernels (1..64; before aegpu_set_problem), threads per CTA of the on-the-fly
- * H kernel (64..512, multiple of 32; before the Hamiltonian).  No counterpart in the
- * reference. */
-enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3 };
+ * H kernel (64..512, multiple of 32; before the Hamiltonian), threads per row of the
+ * stored-H product (1, 2, 4, 8; 0 = chosen by size; before the first evaluation).
+ * No counterpart in the reference. */
+enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4 };
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
 int aegpu_batch_size(const aegpu_engine *e);
@@ -103,6 +104,15 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
 int aegpu_hessian(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
                   double *energy, double *grad_comp, double *hess_comp);
 int aegpu_apply_h(aegpu_engine *e, const double *x, double *y);
+/* Projected Hessian (FusedEvolve::evolveHessianProj, fusedevolve.cpp:2882-3183):
+ * d^2 <proj|psi> / dx_i dx_j in the compressed parameters, with the gradient
+ * d<proj|psi>/dx and overlap <proj|psi>; proj[D*(1+complex)], batch of 1. */
+int aegpu_hessian_proj(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                       const double *proj, double *overlap, double *grad_comp, double *hess_comp);
+/* Projected sweep (FusedEvolve::evolveDerivativeProj, fusedevolve.cpp:2814-2880):
+ * overlap[b] = <proj_b|psi_b(theta_b)> and grad[b][op] = d overlap / d theta_op for a
+ * fixed bra proj[nb][D*(1+complex)] (no factor 2, unlike the energy gradient). */
+int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *proj, double *overlap, double *grad_ops);
 
 /* Device-resident variants (inputs already in HBM): angles_dev[nb][nops],
  * energy_dev[nb], grad_dev[nb][nops].  Enqueued on `stream`; nothing is synchronised. */

@@ -565,6 +565,31 @@ int or_energy_gradient(void *p, const double *angles, double *E, double *grad_op
     return 0;
 }
 
+/* Projected variant (FusedEvolve::evolveDerivativeProj, fusedevolve.cpp:2814-2880):
+ * overlap = <proj|psi(theta)> and grad_op = d<proj|psi>/dtheta_op (no factor 2), the
+ * same backward sweep with the fixed bra proj in place of H psi. */
+int or_gradient_proj(void *p, const double *angles, const double *proj, double *overlap, double *grad_op)
+{
+    or_ctx *c = (or_ctx *)p;
+    int w = c->cplx ? 2 : 1;
+    size_t n = (size_t)c->D * w;
+    double *psi = (double *)malloc(sizeof(double) * n), *h = (double *)malloc(sizeof(double) * n);
+    or_evolve(p, angles, psi);
+    memcpy(h, proj, sizeof(double) * n);
+    if (overlap) *overlap = rdot(h, psi, (int64_t)n);
+    if (grad_op) {
+        for (int o = c->nops - 1; o >= 0; --o) {
+            const int8_t *e = c->ops + 4 * o;
+            grad_op[o] = braket_gen(c, e, h, psi, w);
+            rotate_op(c, e, -angles[o], psi, w);
+            rotate_op(c, e, -angles[o], h, w);
+        }
+    }
+    free(psi);
+    free(h);
+    return 0;
+}
+
 /* Full second derivative d^2E/dtheta_i dtheta_j over operator angles:
  * 2 Re<T_i|H|T_j> + 2 Re<Hpsi| d_i d_j psi>, fusedevolve.cpp:2437-2780. */
 int or_hessian_ops(void *p, const double *angles, double *Hops)

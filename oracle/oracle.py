@@ -48,6 +48,7 @@ def lib():
         L.or_energy_gradient.argtypes = [P, dp, dp, dp]
         L.or_gradient_comp.argtypes = [P, dp, dp, dp]
         L.or_hessian_comp.argtypes = [P, dp, dp]
+        L.or_gradient_proj.argtypes = [P, dp, dp, dp, dp]
         L.or_hessian_ops.argtypes = [P, dp, dp]
         L.or_exc_apply.argtypes = [ctypes.c_uint32] + [ctypes.c_int] * 4 + [ctypes.POINTER(ctypes.c_uint32), ip]
         L.or_basis_size.restype = ctypes.c_int64
@@ -157,6 +158,16 @@ class Oracle:
         g = np.zeros(self.nops)
         self.L.or_energy_gradient(self.h, _d(a), _d(E), _d(g))
         return E[0], g
+
+    def gradient_proj_ops(self, ang_ops, proj):
+        """(<proj|psi>, d<proj|psi>/dtheta_op): the projected sweep (evolveDerivativeProj)."""
+        a = np.ascontiguousarray(ang_ops, dtype=np.float64)
+        pr = np.ascontiguousarray(proj, dtype=np.float64)
+        assert pr.size == self.D * self._w()
+        ov = np.zeros(1)
+        g = np.zeros(self.nops)
+        self.L.or_gradient_proj(self.h, _d(a), _d(pr), _d(ov), _d(g))
+        return ov[0], g
 
     def gradient_comp(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

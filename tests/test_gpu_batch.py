@@ -202,3 +202,26 @@ def test_group_launch_mixed_sizes():
     grp.close()
     e8.close()
     e6.close()
+
+
+@pytest.mark.parametrize("tpr", [1, 2, 4, 8])
+def test_stored_product_threads_per_row(tpr):
+    """Every threads-per-row shape of the stored-H product gives H x (against the
+    oracle's operator-list product) and the same energy."""
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    ops0 = np.asarray(pb["ops_1b"]) - 1
+    e = ae.Engine(16, ae.BASIS_SZ, 8, 4, 4, ops0, tuning={ae.TUNE_SPMV_TPR: tpr})
+    init = np.zeros(e.D)
+    init[np.searchsorted(e.states(), pb["hf"])] = 1.0
+    e.set_initial(init)
+    e.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    assert e.tuning()[ae.TUNE_SPMV_TPR] == tpr
+    o = oracle_synthetic(pb, csr=False)
+    x = np.random.default_rng(tpr).normal(size=e.D)
+    np.testing.assert_allclose(e.apply_h(x), o.apply_h(x), atol=1e-11, rtol=1e-12)
+    ang = np.random.default_rng(1).uniform(-0.3, 0.3, len(ops0))
+    E, g = e.gradient(ang)
+    Eo, go = o.energy_gradient_ops(ang)
+    assert abs(E - Eo) < TOL_E
+    np.testing.assert_allclose(g, go, atol=TOL_G, rtol=0)
+    e.close()

@@ -95,3 +95,24 @@ def test_synthetic_tups_matches_reference(golden):
     o = oracle_synthetic(pb, csr=True)
     H = o.hessian_comp(fx["angles"][0])
     np.testing.assert_allclose(H, fx["H"][0], atol=1e-9, rtol=0)
+
+
+def test_projected_gradient_is_the_derivative_of_the_overlap():
+    """The oracle's projected sweep (evolveDerivativeProj) against central differences
+    of <proj|psi(theta)>, real and complex."""
+    import numpy as np
+    from oracle.oracle import Oracle
+    from tests.fixtures import oracle_synthetic, synthetic_problem
+    pb = synthetic_problem(6, 3, 3, 2, 4)
+    o = oracle_synthetic(pb)
+    rng = np.random.default_rng(3)
+    ang = rng.uniform(-0.4, 0.4, o.nops)
+    proj = rng.normal(size=o.D)
+    ov, g = o.gradient_proj_ops(ang, proj)
+    assert abs(ov - proj @ o.evolve_ops(ang)) < 1e-13
+    h = 1e-6
+    for k in range(0, o.nops, 5):
+        d = np.zeros(o.nops)
+        d[k] = h
+        fd = (proj @ o.evolve_ops(ang + d) - proj @ o.evolve_ops(ang - d)) / (2 * h)
+        assert abs(fd - g[k]) < 1e-8
