@@ -109,6 +109,8 @@ def lib(build_if_missing=True):
         "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
         "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
         "aegpu_device_bytes": (i64, [_P]),
+        "aegpu_fp64_work": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
+        "aegpu_fp64_peak": (ctypes.c_int, [_DP]),
         "aegpu_launch_count": (i64, [_P]),
         # reference C ABI
         "init": (_P, []),
@@ -386,6 +388,12 @@ class Engine:
         keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active", "nnz")
         return dict(zip(keys, map(int, out)))
 
+    def fp64_work(self):
+        """FP64 instructions per evaluation and instance: (H psi, forward, adjoint)."""
+        w = np.zeros(3, dtype=np.int64)
+        self._check(self.L.aegpu_fp64_work(self.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return tuple(int(x) for x in w)
+
     def device_bytes(self):
         return int(self.L.aegpu_device_bytes(self.h))
 
@@ -427,6 +435,15 @@ class Group:
 
     def __del__(self):
         self.close()
+
+
+def fp64_peak():
+    """Measured DFMA throughput of the current CUDA device in TFLOP/s."""
+    t = ctypes.c_double()
+    rc = lib().aegpu_fp64_peak(ctypes.byref(t))
+    if rc:
+        raise AegpuError("aegpu_fp64_peak failed (%d)" % rc)
+    return t.value
 
 
 def host_block_layout(nq, ops0):

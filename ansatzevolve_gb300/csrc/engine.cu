@@ -1323,6 +1323,7 @@ struct aegpu_engine {
         OrbitTile *tiles = nullptr;
         int *ops = nullptr;
         uint64_t active = 0;
+        uint64_t amp_layers = 0;  // touched amplitudes x their active layers
     };
     std::vector<DevBlock> dblocks;
     std::vector<void *> allocs;
@@ -1806,6 +1807,23 @@ constexpr int kNoAllocMaxDevices = 64;
 double *g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_scratch, per device
 }  // namespace
 
+// FP64 pipe probe: every thread runs 8 independent DFMA chains (enough independent
+// work to hide the pipe latency); out receives a value that depends on every chain.
+__global__ void k_fp64_probe(double *out, int iters, double a, double b)
+{
+    double r[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) r[k] = threadIdx.x * 1e-3 + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) r[k] = fma(r[k], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += r[k];
+    if (s == 12345.678) out[0] = s;  // keeps the chains live; practically never taken
+}
+
 // ==================================================================== C ABI ==
 extern "C" {
 
@@ -1936,6 +1954,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             d.nwtasks = (int)T.wtasks.size();
             d.wgrid = std::max(1, std::min(e->sm_count * e->tune_ctas_per_sm, (d.nwtasks + 7) / 8));
             d.active = T.active;
+            d.amp_layers = T.amp_layers;
         } else {
             d.ntiles = kDiagGrid;
             d.wgrid = kDiagGrid;
@@ -2904,6 +2923,60 @@ int aegpu_problem_info(const aegpu_engine *e, int64_t *info)
     for (auto &b : e->dblocks) act += b.diagonal ? (int64_t)e->B.D : (int64_t)b.active;
     info[6] = act;
     info[7] = e->ham_kind == 1 ? e->ham_entries : (e->ham_kind ? (int64_t)e->B.D * e->ints.width : 0);
+    return AEGPU_OK;
+}
+
+int aegpu_fp64_work(const aegpu_engine *e, int64_t *work)
+{
+    // FP64 instructions of one energy + gradient evaluation per instance:
+    // [0] H psi (one DFMA per stored / regenerated matrix element + the energy FMA),
+    // [1] forward passes (one DFMA per amplitude-layer + one DMUL per amplitude),
+    // [2] adjoint passes (two DFMA per amplitude-layer + one DMUL per amplitude + one
+    //     DADD per lane-layer for the gradient sums)
+    if (!e || !work) return AEGPU_ERR_ARG;
+    int64_t al = 0, act = 0;
+    for (auto &b : e->dblocks) {
+        if (b.diagonal) continue;
+        al += (int64_t)b.amp_layers;
+        act += (int64_t)b.active;
+    }
+    const int64_t D = (int64_t)e->B.D, W = e->W;
+    const int64_t elems = e->ham_kind == 1 ? e->ham_entries : (e->ham_kind ? D * e->ints.width : 0);
+    work[0] = (elems + D) * W;
+    work[1] = (al + act) * W;
+    work[2] = (2 * al + act) * W + al / 2;
+    return AEGPU_OK;
+}
+
+// Measured DFMA throughput of this device (TFLOP/s, an FMA counted as 2 flops): a
+// ~50 ms probe over every SM.
+int aegpu_fp64_peak(double *tflops)
+{
+    if (!tflops) return AEGPU_ERR_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return AEGPU_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    double *out = nullptr;
+    if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return AEGPU_ERR_NOMEM;
+    }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_fp64_probe<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);  // warm-up
+    cudaEventRecord(e0);
+    k_fp64_probe<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess || ms <= 0) return AEGPU_ERR_CUDA;
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
     return AEGPU_OK;
 }
 

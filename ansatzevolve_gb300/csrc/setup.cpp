@@ -234,6 +234,7 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
         }
         T.groups.push_back(g);
         T.active += nroots * osz;
+        T.amp_layers += nroots * osz * g.k;
     }
     return T;
 }

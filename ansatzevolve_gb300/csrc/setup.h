@@ -115,6 +115,7 @@ struct OrbitTables {
     std::vector<OrbitTile> tiles;
     std::vector<WarpTask> wtasks;     // only when every orbit has <= 64 members
     uint64_t active = 0;              // number of determinants touched by the block
+    uint64_t amp_layers = 0;          // sum over touched determinants of their active layers
     bool ok = true;                   // false if an excitation leaves the sector
 };
 

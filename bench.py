@@ -305,7 +305,7 @@ def batched_bench(stream, steps=10, warmup=3):
     return out
 
 
-def ttc_bench(n_train=2000, n_heldout=200, n_plain=24, epochs=400):
+def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     """Time to converge over a 10-orbital Hamiltonian family scan (5a+5b, 3 layers,
     81 parameters): h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1.  Both paths start the scan
     from the converged s = 0 member (the reference's Newton method from zero angles).
@@ -313,7 +313,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=24, epochs=400):
     the previous converged angles (timed on the first n_plain held-out values, mean
     per instance).  Batched + warm-started: all n_heldout instances in one batch,
     network proposals judged by the engine against the s = 0 angles, then lockstep
-    BFGS from anchor inverse Hessians.  The network is trained once per family on
+    BFGS from the inverse Hessians at 8 anchors.  The network is trained once per family on
     n_train converged angle sets from a continuation chain (reported separately)."""
     from ansatzevolve_gb300 import warmstart as ws
     spec = ws.FamilySpec(10, 5, 3, seed=0)
@@ -329,7 +329,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=24, epochs=400):
     t0 = time.perf_counter()
     model, hist = ws.train_warmstart(spec.features(s_tr), xtr, epochs=epochs, batch=128, lr=1e-3)
     t_train = time.perf_counter() - t0
-    r = ws.scan_batched_warm(spec, s_ho, model, x0, gtol=1e-6, n_anchor=4)
+    r = ws.scan_batched_warm(spec, s_ho, model, x0, gtol=1e-6, n_anchor=8)
     xp, Ep, tp, nh, ne = ws.scan_newton(spec, s_ho[:n_plain], x0, gtol=1e-6)
     plain_per = tp / n_plain
     batched_per = r["seconds"] / n_heldout
@@ -369,7 +369,7 @@ def main():
     ap.add_argument("--no-ttc", action="store_true")
     ap.add_argument("--ttc-train", type=int, default=2000)
     ap.add_argument("--ttc-heldout", type=int, default=200)
-    ap.add_argument("--ttc-plain", type=int, default=24)
+    ap.add_argument("--ttc-plain", type=int, default=48)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
     set_orbitals(args.orbitals)
@@ -468,6 +468,17 @@ def main():
     # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
     passes = info["blocks"]
     step_bytes = passes * 16 * D * W + hpsi_bytes + passes * 32 * D * W
+    # FP64-pipe roofline of the same step: FP64 instructions per evaluation against the
+    # DFMA throughput measured on this device right now
+    fw = eng.fp64_work()
+    peak_t = ae.fp64_peak() / 2.0  # T DFMA/s
+    ph = [phase_ms[k] / max(nph, 1) / 1e3 for k in range(3)]
+    fp64 = {"unit": "T FP64 instr/s", "peak": peak_t, "peak_source": "measured (aegpu_fp64_peak)",
+            "instructions_per_step": int(sum(fw)),
+            "achieved": sum(fw) / (ms_step / 1e3) / 1e12, "frac": sum(fw) / (ms_step / 1e3) / 1e12 / peak_t,
+            "phase_frac": {"evolve": fw[1] / ph[0] / 1e12 / peak_t if ph[0] else None,
+                           "hpsi_energy": fw[0] / ph[1] / 1e12 / peak_t if ph[1] else None,
+                           "adjoint": fw[2] / ph[2] / 1e12 / peak_t if ph[2] else None}}
     line = {
         "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -489,6 +500,7 @@ def main():
                           "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
                           "phase_ms": {"evolve": phase_ms[0] / max(nph, 1), "hpsi_energy": phase_ms[1] / max(nph, 1),
                                        "adjoint": phase_ms[2] / max(nph, 1)}},
+        "fp64_roofline": fp64,
         "gpu_launches": int(launches),
         "tuning": {"settings": {str(k): v for k, v in eng.tuning().items()}, "tuned": bool(tuning)},
         "clocks": clk.summary(),

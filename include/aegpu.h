@@ -224,6 +224,12 @@ int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t
 
 /* Bytes of HBM held by the engine, and kernel launches issued since creation. */
 int64_t aegpu_device_bytes(const aegpu_engine *e);
+/* FP64 instructions of one energy + gradient evaluation per instance: work[0] H psi
+ * (one DFMA per matrix element + the energy FMA), work[1] forward passes, work[2]
+ * adjoint passes (complex mode counts each real part). */
+int aegpu_fp64_work(const aegpu_engine *e, int64_t *work);
+/* Measured DFMA throughput of the current device, TFLOP/s (FMA = 2 flops). */
+int aegpu_fp64_peak(double *tflops);
 int64_t aegpu_launch_count(const aegpu_engine *e);
 
 #ifdef __cplusplus

@@ -237,3 +237,19 @@ def test_14_orbital_on_the_fly_rows_and_gradient():
     Em = eng.energy(pb["scale"] * (th - h * d)[p0])
     assert abs((Ep - Em) / (2 * h) - g @ d) < 1e-7 * max(1.0, abs(g @ d))
     eng.close()
+
+
+def test_fp64_work_and_peak_probe():
+    """The FP64 work model counts one DFMA per stored element (the stored H's
+    nonzeros) and the DFMA probe reports a plausible GB300 rate."""
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    ops0 = np.asarray(pb["ops_1b"]) - 1
+    eng = ae.Engine(16, ae.BASIS_SZ, 8, 4, 4, ops0)
+    eng.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    w = eng.fp64_work()
+    info = eng.info()
+    assert w[0] == info["nnz"] + info["D"]
+    assert w[1] > info["active"] and w[2] > 2 * (w[1] - info["active"])
+    t = ae.fp64_peak()
+    assert 0.2 < t < 20.0, t
+    eng.close()
