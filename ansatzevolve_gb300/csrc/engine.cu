@@ -1762,6 +1762,39 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
     return e->cuda_check("backward");
 }
 
+// Capture pass constants + evolve + H psi + adjoint sweep of all nb instances
+// (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
+int capture_grad_graph(aegpu_engine *e)
+{
+    cudaStream_t cap = nullptr, saved = e->stream;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return e->cuda_check("graph stream");
+    const int64_t l0 = e->launches;
+    e->stream = cap;
+    cudaGraph_t g = nullptr;
+    int rc = AEGPU_OK;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = e->cuda_check("begin capture");
+    if (!rc) {
+        rc = run_prep(e, e->nb);
+        if (!rc) rc = run_evolve(e, e->nb);
+        if (!rc) rc = run_energy(e, e->d_scalar, e->nb);
+        if (!rc) rc = run_backward(e, e->d_grad, e->nb);
+        cudaError_t ce = cudaStreamEndCapture(cap, &g);
+        if (!rc && ce != cudaSuccess) rc = e->fail(AEGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(ce));
+    }
+    if (!rc && cudaGraphInstantiate(&e->grad_graph, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
+    if (!rc) {
+        e->grad_graph_def = g;
+    } else if (g) {
+        cudaGraphDestroy(g);
+    }
+    cudaStreamDestroy(cap);
+    e->stream = saved;
+    e->graph_launches = e->launches - l0;
+    e->launches = l0;
+    cudaGetLastError();
+    return rc;
+}
+
 bool same_angles(const aegpu_engine *e, const double *angles)
 {
     return e->psi_valid && e->cached_angles.size() == e->excs.size() * (size_t)e->nb &&
@@ -1860,6 +1893,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
                       int nops, const int *ops)
 {
     if (!e) return AEGPU_ERR_ARG;
+    if (e->d_start) return e->fail(AEGPU_ERR_STATE, "the problem is already set (create a new engine)");
     if (nops < 1 || !ops) return e->fail(AEGPU_ERR_ARG, "no excitations");
     if (!e->B.init(nq, basis_kind, n_elec, n_alpha, n_beta, e->err)) return AEGPU_ERR_ARG;
     e->cplx = complex_mode != 0;
@@ -2014,6 +2048,8 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
 }
 
 int64_t aegpu_dim(const aegpu_engine *e) { return e ? (int64_t)e->B.D : -1; }
+
+int aegpu_amplitude_width(const aegpu_engine *e) { return e ? e->W : -1; }
 
 int aegpu_basis_states(const aegpu_engine *e, uint32_t *out)
 {
@@ -2324,8 +2360,6 @@ int aegpu_energy(aegpu_engine *e, const double *angles, double *energy)
     return stream_sync(e, "energy");
 }
 
-static int capture_grad_graph(aegpu_engine *e);
-
 int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double *grad_ops)
 {
     if (!e || !angles || !grad_ops) return AEGPU_ERR_ARG;
@@ -2386,43 +2420,6 @@ int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *pro
     cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "gradient_proj");
 }
-
-}  // extern "C"
-
-// Capture pass constants + evolve + H psi + adjoint sweep of all nb instances
-// (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
-int capture_grad_graph(aegpu_engine *e)
-{
-    cudaStream_t cap = nullptr, saved = e->stream;
-    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return e->cuda_check("graph stream");
-    const int64_t l0 = e->launches;
-    e->stream = cap;
-    cudaGraph_t g = nullptr;
-    int rc = AEGPU_OK;
-    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = e->cuda_check("begin capture");
-    if (!rc) {
-        rc = run_prep(e, e->nb);
-        if (!rc) rc = run_evolve(e, e->nb);
-        if (!rc) rc = run_energy(e, e->d_scalar, e->nb);
-        if (!rc) rc = run_backward(e, e->d_grad, e->nb);
-        cudaError_t ce = cudaStreamEndCapture(cap, &g);
-        if (!rc && ce != cudaSuccess) rc = e->fail(AEGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(ce));
-    }
-    if (!rc && cudaGraphInstantiate(&e->grad_graph, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
-    if (!rc) {
-        e->grad_graph_def = g;
-    } else if (g) {
-        cudaGraphDestroy(g);
-    }
-    cudaStreamDestroy(cap);
-    e->stream = saved;
-    e->graph_launches = e->launches - l0;
-    e->launches = l0;
-    cudaGetLastError();
-    return rc;
-}
-
-extern "C" {
 
 int aegpu_gradient_dev(aegpu_engine *e, const double *angles_dev, double *energy_dev, double *grad_dev, void *stream)
 {
@@ -2669,7 +2666,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
                         const double *proj, double *energy, double *grad_comp, double *hess_comp)
 {
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
-    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (!proj && !e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the Hessian needs a batch size of 1");
     const int nops = (int)e->excs.size();
     const int W = e->W;

@@ -207,4 +207,121 @@ bool optimise_newton(NewtonProblem &p, std::vector<double> &th, NewtonStats &st,
     return true;
 }
 
+// runNewtonMethodProjected (tupsquantities.cpp:1238-1465, the active branch: no
+// overlap normalisation, |1/lambda| steps, cubic line search with forward steps, at
+// most 6 trial points, stop at |g| < 1e-10 or after 500 Hessians).
+static bool run_newton_projected(ProjectedProblem &p, std::vector<double> &th, const std::vector<double> &psiH,
+                                 NewtonStats &st)
+{
+    const int P = p.nparams;
+    const double zeroThreshold = 1e-10;
+    std::vector<double> g, H, w, V, gt;
+    NewtonProblem np;  // for step()
+    np.param = p.param;
+    np.scale = p.scale;
+    for (int count = 0; count < 500; ++count) {
+        double E;
+        if (!p.proj_hess(th, psiH, E, g, H)) return false;
+        st.hessian_evals++;
+        st.energy_evals++;
+        sym_eig(P, H, w, V);
+        std::vector<double> vg(P, 0.0), dx(P, 0.0);
+        for (int k = 0; k < P; ++k) {
+            double s = 0;
+            for (int i = 0; i < P; ++i) s += V[(size_t)i * P + k] * g[i];
+            vg[k] = std::abs(w[k]) >= zeroThreshold ? s * std::abs(1.0 / w[k]) : 0.0;
+        }
+        for (int i = 0; i < P; ++i) {
+            double s = 0;
+            for (int k = 0; k < P; ++k) s += V[(size_t)i * P + k] * vg[k];
+            dx[i] = -s;
+        }
+        const double gnorm = norm2(g);
+        long double bH = 0, cg = 0;
+        for (int i = 0; i < P; ++i) {
+            double s = 0;
+            for (int j = 0; j < P; ++j) s += H[(size_t)i * P + j] * dx[j];
+            bH += (long double)dx[i] * s;
+            cg += (long double)dx[i] * g[i];
+        }
+        const std::vector<double> base = th;
+        const size_t maxSearch = 5;
+        size_t searchCount = 0;
+        long double tMax = 1.5, t = 1, newT = 1, lastGood = newT;
+        bool forward = false;
+        step(th, base, np, dx, t);
+        while (true) {
+            searchCount++;
+            double Et;
+            if (!p.proj_grad(th, psiH, Et, gt)) return false;
+            st.energy_evals++;
+            long double b = bH, c = cg, found = 0;
+            for (int i = 0; i < P; ++i) found += (long double)gt[i] * dx[i];
+            long double a = (found - (b + c)) / (t * t);
+            b /= t;
+            if (Et < E && gnorm > 1e-5) forward = true;
+            const long double disc = b * b - 4 * a * c;
+            if (a >= 0) {
+                newT = (-b + std::sqrt(disc)) / (2 * a);
+            } else if (disc >= 0) {
+                const long double t1 = (-b + std::sqrt(disc)) / (2 * a);
+                const long double E1 = a * t1 * t1 * t1 / 3 + b * t1 * t1 / 2 + c * t1 + E;
+                const long double E2 = a * tMax * tMax * tMax / 3 + b * tMax * tMax / 2 + c * tMax + E;
+                newT = E2 < E1 ? tMax : t1;
+            } else {
+                newT = tMax;
+            }
+            if (newT > tMax) newT = tMax;
+            step(th, base, np, dx, newT);
+            if (searchCount > maxSearch) break;
+            if (Et > E && gnorm > 1e-5) {
+                if (forward) {
+                    if (lastGood > tMax / 2) lastGood = tMax / 2;
+                    t = t / 2;
+                    tMax = tMax / 2;
+                    newT = lastGood;
+                    step(th, base, np, dx, newT);
+                    break;
+                }
+                forward = false;
+                t = t / 2;
+                tMax = tMax / 2;
+                step(th, base, np, dx, t);
+            } else {
+                if (forward) {
+                    t = 2 * t;
+                    tMax = 2 * tMax;
+                    step(th, base, np, dx, t);
+                    lastGood = newT;
+                } else {
+                    if (newT > tMax) newT = tMax;
+                    step(th, base, np, dx, newT);
+                    break;
+                }
+            }
+        }
+        if (gnorm < 1e-10) break;
+    }
+    return true;
+}
+
+bool optimise_projected(ProjectedProblem &p, std::vector<double> &th, NewtonStats &st, int &outer_iters)
+{
+    std::vector<double> psiH, g;
+    if (!p.bra(th, psiH)) return false;
+    outer_iters = 0;
+    double E = 0, gnorm = 0;
+    while (outer_iters++ < p.max_outer) {
+        if (!run_newton_projected(p, th, psiH, st)) return false;
+        if (!p.bra(th, psiH)) return false;
+        if (!p.proj_grad(th, psiH, E, g)) return false;
+        st.energy_evals++;
+        gnorm = norm2(g);
+        if (gnorm < p.gtol) break;
+    }
+    st.energy = E;
+    st.gnorm = gnorm;
+    return true;
+}
+
 }  // namespace ae

@@ -24,4 +24,26 @@ struct NewtonStats {
 void sym_eig(int n, const std::vector<double> &A, std::vector<double> &w, std::vector<double> &V);
 bool optimise_newton(NewtonProblem &p, std::vector<double> &theta, NewtonStats &st, bool verbose);
 
+// The projected iteration (TUPSQuantities::iterativeTups, tupsquantities.cpp:2044-2145,
+// with runNewtonMethodProjected, :1238-1465): the bra psiH = H psi(theta_prev) is frozen,
+// <psiH|psi(theta)> is minimised by Newton steps with the projected Hessian, then psiH is
+// renewed; stops when the projected gradient at the renewed bra is below gtol.
+struct ProjectedProblem {
+    int nparams = 0;
+    std::vector<int> param;
+    std::vector<double> scale;
+    double gtol = 1e-5;             // tupsquantities.cpp:2096
+    int max_outer = 3000;           // :2076
+    // psiH = H psi(theta) (device-size vector on the host)
+    std::function<bool(const std::vector<double> &theta, std::vector<double> &psiH)> bra;
+    // overlap <psiH|psi(theta)> and its compressed gradient
+    std::function<bool(const std::vector<double> &theta, const std::vector<double> &psiH, double &ov,
+                       std::vector<double> &g)> proj_grad;
+    // overlap, compressed gradient and compressed Hessian (row-major)
+    std::function<bool(const std::vector<double> &theta, const std::vector<double> &psiH, double &ov,
+                       std::vector<double> &g, std::vector<double> &H)> proj_hess;
+};
+
+bool optimise_projected(ProjectedProblem &p, std::vector<double> &theta, NewtonStats &st, int &outer_iters);
+
 }  // namespace ae

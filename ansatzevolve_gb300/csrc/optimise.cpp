@@ -244,4 +244,64 @@ int aegpu_optimise_newton(aegpu_engine *e, int nparams, const int *param, const 
     return AEGPU_OK;
 }
 
+int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x,
+                             double gtol, int max_outer, double *energy, double *gnorm, int64_t *hessian_evals,
+                             int64_t *energy_evals, int *outer_iters)
+{
+    if (!e || nparams < 1 || !param || !scale || !x || !(gtol > 0) || max_outer < 1) return AEGPU_ERR_ARG;
+    if (aegpu_batch_size(e) != 1) return AEGPU_ERR_UNSUPPORTED;
+    int64_t info[8];
+    int rc = aegpu_problem_info(e, info);
+    if (rc) return rc;
+    const int nops = (int)info[1], P = nparams;
+    const size_t n = (size_t)aegpu_dim(e) * (size_t)aegpu_amplitude_width(e);
+    for (int o = 0; o < nops; ++o)
+        if (param[o] < 0 || param[o] >= P) return AEGPU_ERR_ARG;
+    ae::ProjectedProblem p;
+    p.nparams = P;
+    p.param.assign(param, param + nops);
+    p.scale.assign(scale, scale + nops);
+    p.gtol = gtol;
+    p.max_outer = max_outer;
+    int err = AEGPU_OK;
+    std::vector<double> psi(n);
+    p.bra = [&](const std::vector<double> &th, std::vector<double> &psiH) {
+        psiH.assign(n, 0.0);
+        return (err = aegpu_evolve(e, th.data(), psi.data())) == AEGPU_OK &&
+               (err = aegpu_apply_h(e, psi.data(), psiH.data())) == AEGPU_OK;
+    };
+    p.proj_grad = [&](const std::vector<double> &th, const std::vector<double> &psiH, double &ov,
+                      std::vector<double> &g) {
+        std::vector<double> gops(nops);
+        if ((err = aegpu_gradient_proj(e, th.data(), psiH.data(), &ov, gops.data()))) return false;
+        g.assign(P, 0.0);
+        for (int i = 0; i < nops; ++i) g[param[i]] += scale[i] * gops[i];
+        return true;
+    };
+    p.proj_hess = [&](const std::vector<double> &th, const std::vector<double> &psiH, double &ov,
+                      std::vector<double> &g, std::vector<double> &H) {
+        g.assign(P, 0.0);
+        H.assign((size_t)P * P, 0.0);
+        return (err = aegpu_hessian_proj(e, th.data(), param, scale, P, psiH.data(), &ov, g.data(), H.data())) ==
+               AEGPU_OK;
+    };
+    std::vector<double> th(nops);
+    for (int o = 0; o < nops; ++o) th[o] = scale[o] * x[param[o]];
+    ae::NewtonStats st;
+    int outer = 0;
+    if (!ae::optimise_projected(p, th, st, outer)) return err ? err : AEGPU_ERR_CUDA;
+    std::vector<bool> seen(P, false);
+    for (int o = 0; o < nops; ++o)
+        if (!seen[param[o]] && scale[o] != 0) {
+            x[param[o]] = th[o] / scale[o];
+            seen[param[o]] = true;
+        }
+    if (energy) *energy = st.energy;
+    if (gnorm) *gnorm = st.gnorm;
+    if (hessian_evals) *hessian_evals = st.hessian_evals;
+    if (energy_evals) *energy_evals = st.energy_evals;
+    if (outer_iters) *outer_iters = outer;
+    return AEGPU_OK;
+}
+
 }  // extern "C"

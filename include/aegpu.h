@@ -54,6 +54,8 @@ const char *aegpu_last_error(const aegpu_engine *e);
 int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n_alpha, int n_beta,
                       int complex_mode, int nops, const int *ops);
 int64_t aegpu_dim(const aegpu_engine *e);
+/* doubles per amplitude: 1 real, 2 complex (re, im interleaved) */
+int aegpu_amplitude_width(const aegpu_engine *e);
 int aegpu_basis_states(const aegpu_engine *e, uint32_t *out);
 int aegpu_num_blocks(const aegpu_engine *e);
 /* Operator application order (the reference's m_excPerm) and the size of every pass. */
@@ -159,6 +161,14 @@ int aegpu_optimise_newton(aegpu_engine *e, int nparams, const int *param, const 
 int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x, double gtol,
                          int max_rounds, double max_step, double *hinv, double *energy, double *gnorm, int *iters,
                          int64_t *rounds);
+/* The reference's projected iteration (TUPSQuantities::iterativeTups with
+ * runNewtonMethodProjected, tupsquantities.cpp:2044-2145, 1238-1465) on a batch-of-1
+ * engine: freeze psiH = H psi, minimise <psiH|psi(x)> by projected Newton steps, renew
+ * psiH; stop when the projected gradient is below gtol (the reference uses 1e-5) or
+ * after max_outer renewals.  x: start on entry, result on return. */
+int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x,
+                             double gtol, int max_outer, double *energy, double *gnorm, int64_t *hessian_evals,
+                             int64_t *energy_evals, int *outer_iters);
 /* Learned warm start (no counterpart in the reference): an MLP
  * n_in -> n_hidden -> n_hidden -> n_out with GELU activations, BF16 weights in every
  * product, FP32 accumulation, FP32 master weights trained by Adam on the mean squared

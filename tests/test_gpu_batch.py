@@ -225,3 +225,23 @@ def test_stored_product_threads_per_row(tpr):
     assert abs(E - Eo) < TOL_E
     np.testing.assert_allclose(g, go, atol=TOL_G, rtol=0)
     e.close()
+
+
+def test_out_of_order_calls_are_refused():
+    """A second problem on one engine, a batch size out of range, a Hessian of a batch
+    and a group launch without a Hamiltonian return status codes (no trap)."""
+    pb = synthetic_problem(6, 3, 3, 1, 0)
+    ops0 = np.ascontiguousarray(np.asarray(pb["ops_1b"]) - 1, dtype=np.int32)
+    e = ae.Engine(12, ae.BASIS_SZ, 6, 3, 3, ops0)
+    rc = e.L.aegpu_set_problem(e.h, 12, ae.BASIS_SZ, 6, 3, 3, 0, len(ops0), ae.iptr(ops0.reshape(-1)))
+    assert rc == 2 and "already set" in e.L.aegpu_last_error(e.h).decode()
+    assert e.L.aegpu_set_batch(e.h, 0) == 1
+    assert e.L.aegpu_set_batch(e.h, 70000) == 1
+    with pytest.raises(ae.AegpuError):
+        ae.Group([e])  # no Hamiltonian yet
+    e.set_batch(2)
+    e.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    p0 = np.asarray(pb["order_1b"]) - 1
+    with pytest.raises(ae.AegpuError, match="batch size of 1"):
+        e.hessian(np.zeros(len(ops0)), p0, np.asarray(pb["scale"]))
+    e.close()

@@ -53,3 +53,35 @@ def test_batched_bfgs_and_newton_share_minima_on_a_family():
     np.testing.assert_allclose(bat.energy(scale * xb[:, p0]), Eb, atol=1e-12, rtol=0)
     one.close()
     bat.close()
+
+
+def test_projected_iteration_reaches_a_stationary_point(golden):
+    """The reference's iterativeTups on the H4 L1 fixture (integrals from the
+    reference's own Hams/ inputs): it stops at a projected gradient below 1e-5, which is
+    half the energy gradient at a renewed bra, so the energy gradient there is below
+    2e-5, and the reported energy is the engine's energy at the returned angles; Newton
+    from there stays at that energy."""
+    from tests.fixtures import sector_of
+    fx = golden("h4")
+    nq = int(fx["nq"])
+    ops0 = np.asarray(fx["ops_1b"]) - 1
+    kind, ne, na, nbe = sector_of(nq, fx["init_idx"], ops0)
+    p0 = np.asarray(fx["order_1b"]) - 1
+    scale = np.asarray(fx["scale"])
+    P = int(p0.max()) + 1
+    e = ae.Engine(nq, kind, ne, na, nbe, ops0)
+    init = np.zeros(e.D)
+    init[np.searchsorted(e.states(), np.asarray(fx["init_idx"]))] = fx["init_re"]
+    e.set_initial(init)
+    e.set_ham_integrals(fx["h1"], fx["g2"], ae.HAM_STORED)
+    x0 = np.asarray(fx["angles"][1])[:P]
+    x, E, gp, nh, nev, outer = e.optimise_projected(x0, p0, scale, gtol=1e-5)
+    assert gp < 1e-5 and nh > 0 and outer >= 1
+    Ee, gops = e.gradient(scale * x[p0])
+    g = np.zeros(P)
+    np.add.at(g, p0, scale * gops)
+    assert abs(Ee - E) < 1e-12
+    assert np.linalg.norm(g) < 2.0001e-5
+    xn, En, gn, _, _ = e.optimise_newton(x, p0, scale, gtol=1e-10)
+    assert abs(En - E) < 1e-8
+    e.close()
