@@ -1,15 +1,18 @@
 // GB300 statevector engine: the CUDA side of the aegpu C ABI (include/aegpu.h).
 //
-// Data layout in HBM (one problem per engine):
-//   psi, hpsi          FP64[D*W]      W = 1 (real) or 2 (complex, re/im interleaved)
+// Data layout in HBM (one problem per engine, nb instances of it per evaluation):
+//   psi, hpsi          FP64[nb][D*W]  W = 1 (real) or 2 (complex, re/im interleaved)
+//   checkpoints        per pass, the amplitudes after it in orbit order, per instance
 //   basis tables       Sz sector: alpha/beta strings + 2^N rank tables (a few KB);
 //                      other sectors: D bitstrings + 2^nq rank table
-//   orbit tables       per fused block: uint32 ranks of every touched determinant,
-//                      grouped into orbits (hypercubes of the active excitations),
-//                      plus group/tile descriptors (setup.cpp)
-//   Hamiltonian        CSR (general) or fixed-width ELL rows built from integrals
+//   orbit tables       per pass: uint32 ranks and bitstrings of every touched
+//                      determinant, grouped into orbits (hypercubes of the active
+//                      excitations), plus group/tile/warp-task descriptors (setup.cpp)
+//   Hamiltonian        CSR (general), sliced-ELL rows built from integrals, or the
+//                      string tables of the on-the-fly product (one set per instance
+//                      for a Hamiltonian family)
 //   Hessian scratch    per-operator tangents FP64[nops][D*W], compressed tangents
-//                      and H*tangents in [D][W][P+1] layout
+//                      and H*tangents column-major [P+1][D*W]
 //
 // Kernels (all FP64; bandwidth- or FP64-pipe-bound, no tensor cores):
 //   k_block_rot      one pass on many vectors at once (Hessian tangents); a CTA stages
@@ -25,8 +28,11 @@
 //                    derivative term of the Hessian (fusedevolve.cpp:2670-2761)
 //   k_diag_*         the same four for diagonal (number / density-density) blocks,
 //                    complex mode (fusedevolve.cpp:625-717)
-//   k_spmv_csr/_ell  warp-per-row y = H x fused with the <x|y> partial sums
-//   k_spmm_*         H on P+1 vectors at once for the Hessian (matrix read once)
+//   k_pass_prep      per evaluation: sin/cos and the scaled-Givens constants of every
+//                    pass and direction, and the scale products of every active mask
+//   k_spmv           warp-per-row CSR y = H x fused with the <x|y> partial sums
+//   k_spmv_sell      sliced-ELL y = H x (1-8 threads per row) fused with <x|y>; the
+//                    Hessian applies it to its P+1 compressed tangents as a batch
 //   k_ell_build      fixed-width rows of H generated from h_pq/(pq|rs): diagonal,
 //                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
 //   k_otf_strings    y = H x with no stored matrix: CTA per alpha string, thread per
@@ -908,25 +914,6 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int
     if (threadIdx.x == 0 && epart) epart[blockIdx.x] = e;
 }
 
-// H applied to V interleaved vectors X[D][W][V] -> Y[D][W][V] (one CTA per row).
-template <bool ELL>
-__global__ void k_spmm(const int64_t *__restrict__ rowptr, int ell_width, const int32_t *__restrict__ col,
-                       const double *__restrict__ val, const double *__restrict__ X, double *__restrict__ Y, int VW,
-                       int64_t D)
-{
-    const int64_t q = ell_width >> 2;
-    for (int64_t r = blockIdx.x; r < D; r += gridDim.x) {
-        const int64_t b = ELL ? 0 : rowptr[r], end = ELL ? ell_width : rowptr[r + 1];
-        for (int t = threadIdx.x; t < VW; t += blockDim.x) {
-            double acc = 0;
-            for (int64_t k = b; k < end; ++k) {
-                const size_t p = ELL ? ell_pos(r, k, q) : (size_t)k;
-                acc = fma(__ldg(val + p), __ldg(X + (size_t)__ldg(col + p) * VW + t), acc);
-            }
-            Y[(size_t)r * VW + t] = acc;
-        }
-    }
-}
 
 // Compressed tangents T_C[j][w][mu] = sum_{op: param(op)=mu} scale_op T[pos(op)][j][w];
 // column P holds psi (fusedevolve.cpp:2609-2612, m_compressMatrixPsi).
@@ -946,7 +933,7 @@ __global__ void k_tc_build(const double *__restrict__ T, size_t tstride, const d
             s = 0;
             for (int k = prm_ptr[mu]; k < prm_ptr[mu + 1]; ++k) s += prm_scale[k] * T[(size_t)prm_pos[k] * tstride + jw];
         }
-        TC[t] = s;
+        TC[(size_t)mu * D * W + jw] = s;  // column-major: column mu is a contiguous vector
     }
 }
 
@@ -2638,21 +2625,15 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
 {
     if (!e || !x || !y) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    // the engine's own scratch vectors (the cached H psi is given up)
     const size_t n = e->vec_elems() * e->nb;
-    double *dx = e->alloc<double>(n), *dy = e->alloc<double>(n);
-    if (!dx || !dy) {
-        e->release(dx, n * sizeof(double));
-        e->release(dy, n * sizeof(double));
-        return e->fail(AEGPU_ERR_NOMEM, "apply_h scratch");
-    }
-    cudaMemcpyAsync(dx, x, n * sizeof(double), cudaMemcpyHostToDevice, e->stream);
-    int rc = run_apply(e, dx, dy, nullptr, e->nb);
+    e->h_valid = false;
+    cudaMemcpyAsync(e->d_tmp, x, n * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+    int rc = run_apply(e, e->d_tmp, e->d_h, nullptr, e->nb);
     if (!rc) {
-        cudaMemcpyAsync(y, dy, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        cudaMemcpyAsync(y, e->d_h, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
         rc = stream_sync(e, "apply_h");
     }
-    e->release(dx, n * sizeof(double));
-    e->release(dy, n * sizeof(double));
     return rc;
 }
 
@@ -2747,40 +2728,28 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             e->launches += 2;
         }
     }
-    // 2. compressed tangents, H on all of them, Gram matrix 2 T_C^T H T_C
+    // 2. compressed tangents (column-major: column v is T_C v, column P is psi), H on all
+    //    of them as one batched product, Gram matrix 2 T_C^T H T_C
     k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
-    const int VW = V * W;
+    e->launches += 1;
     if (!e->cublas) {
         if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
     }
     cublasSetStream(e->cublas, s);
+    const int DW = (int)(D * W);
     if (proj) {
         // projected: <proj|T_C v> for every column (the last is <proj|psi>), bra for the sweeps
         cudaMemcpyAsync(e->d_h, proj, n * sizeof(double), cudaMemcpyHostToDevice, s);
         const double one = 1.0, zero = 0.0;
-        cublasDgemv(e->cublas, CUBLAS_OP_N, V, (int)(D * W), &one, TC, V, e->d_h, 1, &zero, THT, 1);
-    } else if (e->ham_kind == 1)
-        k_spmm<false><<<e->sm_count * 16, 128, 0, s>>>(e->d_rowptr, 0, e->d_col, e->d_val, TC, HTC, VW, D);
-    else if (e->ham_kind == 2)
-        k_spmm<true><<<e->sm_count * 16, 128, 0, s>>>(nullptr, e->ell_width, e->d_col, e->d_val, TC, HTC, VW, D);
-    else {
-        // on the fly: one column at a time through strided copies
-        for (int v = 0; v < V; ++v) {
-            cudaMemcpy2DAsync(e->d_tmp, sizeof(double), TC + v, (size_t)V * sizeof(double), sizeof(double), n,
-                              cudaMemcpyDeviceToDevice, s);
-            run_apply(e, e->d_tmp, e->d_h, nullptr, 1);
-            cudaMemcpy2DAsync(HTC + v, (size_t)V * sizeof(double), e->d_h, sizeof(double), sizeof(double), n,
-                              cudaMemcpyDeviceToDevice, s);
-        }
-    }
-    e->launches += 2;
-    if (!proj) {
+        cublasDgemv(e->cublas, CUBLAS_OP_T, DW, V, &one, TC, DW, e->d_h, 1, &zero, THT, 1);
+    } else {
+        // the V columns as V instances of the H product (the matrix or tables are shared)
+        rc = run_apply(e, TC, HTC, nullptr, V);
+        if (rc) return rc;
         const double two = 2.0, zero = 0.0;
-        // TC, HTC are row-major (D*W) x V == column-major V x (D*W)
-        cublasDgemm(e->cublas, CUBLAS_OP_N, CUBLAS_OP_T, V, V, (int)(D * W), &two, TC, V, HTC, V, &zero, THT, V);
-        // H psi for the backward sweeps: last column of HTC
-        cudaMemcpy2DAsync(e->d_h, sizeof(double), HTC + nparams, (size_t)V * sizeof(double), sizeof(double), n,
-                          cudaMemcpyDeviceToDevice, s);
+        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, V, V, DW, &two, TC, DW, HTC, DW, &zero, THT, V);
+        // H psi for the backward sweeps: the last column
+        cudaMemcpyAsync(e->d_h, HTC + (size_t)nparams * DW, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     }
     // 3. second-derivative sweeps
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
