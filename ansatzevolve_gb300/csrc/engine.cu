@@ -1280,6 +1280,7 @@ struct DevBuf {
 struct aegpu_engine {
     std::string err;
     int64_t dev_bytes = 0;
+    bool alloc_failed = false;  // a set-up allocation failed (checked at the end of set-up)
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
     cublasHandle_t cublas = nullptr;
@@ -1429,6 +1430,7 @@ struct aegpu_engine {
         cudaError_t rc = cudaMalloc(&p, n * sizeof(T));
         if (rc != cudaSuccess) {
             cudaGetLastError();
+            alloc_failed = true;
             return nullptr;
         }
         allocs.push_back(p);
@@ -2019,6 +2021,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     pa.npass = (int)e->blocks.size();
     e->prep = pa;
 
+    if (e->alloc_failed) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed while building the passes");
     const size_t n = e->vec_elems();
     e->n_ckpt = ckpt_off;
     // partial sums per instance: the CSR grid, or one per CTA of the stored-H product at
@@ -2028,6 +2031,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     if (!e->d_start || !pa.pass_ops || !pa.pass_diag) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
     int rc = e->alloc_instances(e->nb);
     if (rc) return rc;
+    if (e->alloc_failed) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
     cudaMemset(e->d_start, 0, n * sizeof(double));
     // setup copies ran on the legacy stream: finish them before any engine-stream work
     if (cudaDeviceSynchronize() != cudaSuccess) return e->cuda_check("set_problem");
