@@ -515,6 +515,18 @@ def main():
         line["batched"] = batched_bench(stream)
     if not args.no_ttc:
         line["time_to_converge"] = ttc_bench(args.ttc_train, args.ttc_heldout, args.ttc_plain)
+    # parity of this very run against the reference's own output for the same inputs
+    # (tests/golden/ref<N>.npz, produced by the reference build)
+    ref = os.path.join(ROOT, "tests", "golden", "ref%d.npz" % N_ORB)
+    if os.path.exists(ref) and not LUCJ:
+        fx = np.load(ref)
+        if np.allclose(fx["x"], pb["x"]):
+            g_ops = g_d.cpu().numpy()
+            g = np.zeros(pb["P"])
+            np.add.at(g, pb["p0"], pb["scale"] * g_ops)
+            line["parity_reference"] = {"dE": abs(float(E_d.item()) - float(fx["E"])),
+                                        "max_dg": float(np.max(np.abs(g - fx["G"]))),
+                                        "source": "tests/golden/ref%d.npz" % N_ORB}
     if not args.no_cpu:
         cb, Eo, go = cpu_baseline(pb)
         line["cpu_baseline"] = cb

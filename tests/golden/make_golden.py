@@ -12,6 +12,12 @@ Sources of the inputs:
   h4c      -- Hams/H4_Complex/L1 (complex build, diagonal U3 operators)
   syn8     -- synthetic 8-orbital TUPS, seed 0 (ansatzevolve_gb300.synthetic)
   syn6     -- synthetic 6-orbital TUPS, seed 3, plus the excitation rule table
+  ref10    -- the benchmark's 10-orbital inputs (seed 0, 3 layers): E, gradient, Hessian,
+              sampled final-state amplitudes
+  ref12    -- the benchmark's 12-orbital inputs (seed 0, 3 layers): E, gradient,
+              sampled final-state amplitudes (the reference's Hessian takes minutes here)
+Only the ref10 / ref12 cases can be regenerated alone:
+    python tests/golden/make_golden.py ref10 ref12
 """
 import os
 import re
@@ -31,13 +37,13 @@ DRV = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
-def run(spec_lines, cplx=False):
+def run(spec_lines, cplx=False, threads=4):
     with tempfile.TemporaryDirectory() as td:
         sp, op = os.path.join(td, "spec"), os.path.join(td, "out")
         open(sp, "w").write("\n".join(spec_lines) + "\nend\n")
         drv = DRV + ("_cplx" if cplx else "")
         subprocess.run([drv, sp, op], check=True, stderr=subprocess.DEVNULL, stdout=subprocess.DEVNULL,
-                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
         return np.fromfile(op, dtype="<f8")
 
 
@@ -207,10 +213,46 @@ def synthetic_case(tag, N, na, nb, layers, seed, pairs=False, hess=True):
     print(tag, res["E"])
 
 
+def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
+    """The benchmark's own inputs at 10 / 12 orbitals (integrals of `seed`, angles
+    default_rng(seed + 1).uniform(-0.1, 0.1)): energy, gradient, (Hessian), and a seeded
+    sample of the final state's sector amplitudes with the state's norm."""
+    h, g = synthetic_integrals(N, seed)
+    ops, param, scale = tups_operators(N, layers)
+    P = int(param.max())
+    x = np.random.default_rng(seed + 1).uniform(-0.1, 0.1, P)
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, "syn")
+        write_integrals(prefix, h, g)
+        hf = hartree_fock_index(N, na, nb)
+        want = (1, 1, int(hess), 1)
+        d = run(spec(2 * N, [(hf, 1.0, 0.0)], ops - 1, param - 1, scale, [f"ham ints {prefix}"], [x], want=want),
+                threads=8)
+    res, _ = split_outputs(d, 1, P, 1 << (2 * N), want)
+    state = res["S"][0]
+    allst = np.arange(1 << (2 * N), dtype=np.uint32)
+    pc = np.array([bin(v).count("1") for v in range(1 << N)], dtype=np.int64)
+    sect = np.flatnonzero((pc[allst >> N] == na) & (pc[allst & ((1 << N) - 1)] == nb)).astype(np.uint32)
+    pick = np.sort(np.random.default_rng(seed + 7).choice(len(sect), nsample, replace=False))
+    fx = dict(N=N, na=na, nb=nb, layers=layers, seed=seed, hf=hf, ops_1b=ops, order_1b=param, scale=scale,
+              x=x, E=res["E"][0], G=res["G"][0], sample_rank=pick.astype(np.int64), sample_bits=sect[pick],
+              sample_amp=state[sect[pick]], norm=float(np.dot(state, state)))
+    if hess:
+        fx["H"] = res["H"][0]
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), **fx)
+    print(tag, fx["E"])
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 1:
+        for t in sys.argv[1:]:
+            large_case(t, int(t[3:]), int(t[3:]) // 2, int(t[3:]) // 2, 3, 0, hess=t == "ref10")
+        sys.exit(0)
     fortran_case()
     hams_case("TestFermionic", None, tag="ferm")
     hams_case("H4", "L1", optimise=True, tag="h4")
     hams_case("H4_Complex", "L1", cplx=True, tag="h4c")
     synthetic_case("syn6", 6, 3, 3, 2, 3, pairs=True)
     synthetic_case("syn8", 8, 4, 4, 2, 0)
+    large_case("ref10", 10, 5, 5, 3, 0, hess=True)
+    large_case("ref12", 12, 6, 6, 3, 0, hess=False)

@@ -116,3 +116,25 @@ def test_projected_gradient_is_the_derivative_of_the_overlap():
         d[k] = h
         fd = (proj @ o.evolve_ops(ang + d) - proj @ o.evolve_ops(ang - d)) / (2 * h)
         assert abs(fd - g[k]) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["ref10", "ref12"])
+def test_oracle_matches_reference_at_benchmark_sizes(golden, name):
+    """The benchmark's own 10- and 12-orbital inputs: the oracle's energy, gradient and
+    sampled final-state amplitudes against the reference's (tests/golden/ref*.npz)."""
+    import numpy as np
+    from tests.fixtures import oracle_synthetic
+    fx = golden(name)
+    N = int(fx["N"])
+    pb = dict(N=N, nq=2 * N, na=int(fx["na"]), nb=int(fx["nb"]), hf=int(fx["hf"]), ops_1b=fx["ops_1b"],
+              order_1b=fx["order_1b"], scale=fx["scale"])
+    from ansatzevolve_gb300.synthetic import synthetic_integrals
+    pb["h1"], pb["g2"] = synthetic_integrals(N, int(fx["seed"]))
+    o = oracle_synthetic(pb, csr=False)
+    E, g = o.gradient_comp(fx["x"])
+    assert abs(E - float(fx["E"])) < 1e-10
+    np.testing.assert_allclose(g, fx["G"], atol=1e-9, rtol=0)
+    p0 = np.asarray(fx["order_1b"]) - 1
+    psi = o.evolve_ops(np.asarray(fx["scale"]) * np.asarray(fx["x"])[p0])
+    np.testing.assert_allclose(psi[fx["sample_rank"]], fx["sample_amp"], atol=1e-12, rtol=0)
+    assert abs(np.dot(psi, psi) - float(fx["norm"])) < 1e-12
