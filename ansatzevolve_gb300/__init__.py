@@ -59,6 +59,7 @@ def lib(build_if_missing=True):
         "aegpu_set_ham_integrals_batch": (ctypes.c_int, [_P, _DP, _DP, ctypes.c_int]),
         "aegpu_set_batch": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_batch_size": (ctypes.c_int, [_P]),
+        "aegpu_set_active": (ctypes.c_int, [_P, _IP]),
         "aegpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
         "aegpu_get_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_io_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
@@ -227,6 +228,15 @@ class Engine:
         """Evaluate nb instances per call (angles [nb, nops] -> energies [nb], gradients [nb, nops])."""
         self._check(self.L.aegpu_set_batch(self.h, int(nb)))
         self.nb = int(self.L.aegpu_batch_size(self.h))
+
+    def set_active(self, mask=None):
+        """Skip instances with mask[b] == 0 in batched evaluations (None: all active)."""
+        if mask is None:
+            self._check(self.L.aegpu_set_active(self.h, None))
+        else:
+            m = _i32(mask)
+            assert m.size == self.nb
+            self._check(self.L.aegpu_set_active(self.h, iptr(m)))
 
     def set_ham_integrals_batch(self, h1s, g2s, mode=HAM_AUTO):
         """One Hamiltonian per instance: h1s [nb, N, N], g2s [nb, N, N, N, N]."""

@@ -126,6 +126,7 @@ struct BlockArgs {
     const PassConst *pc;     // this pass's layer constants for this direction (instance 0)
     const double *sigma;     // this pass's scale products per active mask (instance 0)
     int64_t pc_stride, sig_stride;  // per-instance strides of pc / sigma
+    const int *active;       // instance mask of the warp kernels (nullable)
 };
 
 __device__ __forceinline__ uint32_t insert_zero_bit(uint32_t p, int i)
@@ -143,9 +144,15 @@ __device__ __forceinline__ size_t ell_pos(int64_t r, int64_t e, int64_t q)
 }
 
 // ---------------------------------------------------------------- utilities --
+// Instance b of a batched launch is skipped when the engine's mask says so (the mask
+// pointer is null for launches that are not per instance, e.g. the Hessian's columns).
+__device__ __forceinline__ bool skip_instance(const int *active, int b) { return active && !active[b]; }
+
 // dst[b * n + i] = src[i] for every instance b = blockIdx.y (the shared start vector)
-__global__ void k_broadcast(const double *__restrict__ src, double *__restrict__ dst, int64_t n)
+__global__ void k_broadcast(const double *__restrict__ src, double *__restrict__ dst, int64_t n,
+                            const int *__restrict__ active)
 {
+    if (skip_instance(active, blockIdx.y)) return;
     dst += (size_t)blockIdx.y * n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         dst[i] = src[i];
@@ -173,9 +180,11 @@ __device__ __forceinline__ double block_sum(double v, double *red)
 }
 
 // One CTA per instance: out[b] = scale * sum of parts[b * n .. b * n + n).
-__global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__restrict__ out, double scale)
+__global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__restrict__ out, double scale,
+                             const int *__restrict__ active)
 {
     __shared__ double red[32];
+    if (skip_instance(active, blockIdx.x)) return;
     parts += (size_t)blockIdx.x * n;
     double s = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += parts[i];
@@ -185,9 +194,11 @@ __global__ void k_reduce_sum(const double *__restrict__ parts, int n, double *__
 
 // Per-CTA partial sums of <a|b> over instance blockIdx.y (vectors at stride n):
 // parts[blockIdx.y * gridDim.x + blockIdx.x].
-__global__ void k_dot(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ parts)
+__global__ void k_dot(const double *__restrict__ a, const double *__restrict__ b, int64_t n, double *__restrict__ parts,
+                      const int *__restrict__ active)
 {
     __shared__ double red[32];
+    if (skip_instance(active, blockIdx.y)) return;
     a += (size_t)blockIdx.y * n;
     b += (size_t)blockIdx.y * n;
     double s = 0;
@@ -424,12 +435,14 @@ struct PrepArgs {
     const int *pass_diag;   // 1 for diagonal passes (no scaled-Givens constants)
     const ExcCode *codes;
     int nops, npass;
+    const int *active;      // instance mask (nullable)
 };
 
 __global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *__restrict__ sc,
                             PassConst *__restrict__ pc, double *__restrict__ sig)
 {
     const int pass = blockIdx.x, b = blockIdx.y;
+    if (skip_instance(a.active, b)) return;
     const int ns = a.pass_n[pass];
     const int *ops = a.pass_ops + a.pass_off[pass];
     __shared__ double f[2][kMaxWarpLayers];
@@ -478,6 +491,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
                                                            int64_t ckpt_stride)
 {
     const int lane = threadIdx.x & 31, b = blockIdx.y;
+    if (skip_instance(a.active, b)) return;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
     double *psi = vecs + (size_t)b * inst_stride;
@@ -544,6 +558,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
 {
     __shared__ double red[kMaxWarpLayers][kWarpThreads / 32];
     const int lane = threadIdx.x & 31, b = blockIdx.y;
+    if (skip_instance(a.active, b)) return;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
     double *h = hv + (size_t)b * inst_stride;
@@ -640,8 +655,9 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
 // amplitude by exp(+i * sum of the active angles) (RunFuseNDiagonal,
 // fusedevolve.cpp:625-717).  table[m] = (cos, sin) of dir * sum_{i in m} theta_i.
 __global__ void k_diag_table(const double *__restrict__ ang, const int *__restrict__ ops, int nslots, double dir,
-                             double *__restrict__ table, int nops)
+                             double *__restrict__ table, int nops, const int *__restrict__ active)
 {
+    if (skip_instance(active, blockIdx.y)) return;
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= (1u << nslots)) return;
     ang += (size_t)blockIdx.y * nops;                          // instance blockIdx.y
@@ -661,6 +677,7 @@ struct DiagArgs {
     const ExcCode *codes;
     const double *table;  // instance 0; instance b at + b * 2 * 2^kMaxSlots
     DevBasis basis;
+    const int *active;    // instance mask (nullable)
 };
 
 __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
@@ -678,6 +695,7 @@ __global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, d
                            int64_t inst_stride, int64_t ckpt_stride)
 {
     const uint64_t D = a.basis.D;
+    if (skip_instance(a.active, blockIdx.y)) return;
     a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
     vecs += (size_t)blockIdx.y * inst_stride;
     if (ckpt) ckpt += (size_t)blockIdx.y * ckpt_stride;
@@ -704,6 +722,7 @@ __global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__re
                                                   double *h, int64_t inst_stride, double *partials, int64_t part_stride)
 {
     __shared__ double red[8];
+    if (skip_instance(a.active, blockIdx.y)) return;
     a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
     ckpt += (size_t)blockIdx.y * ckpt_stride;
     h += (size_t)blockIdx.y * inst_stride;
@@ -785,11 +804,12 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
 // warp per (instance, operator); instance b's partial sums start at b * part_stride.
 __global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t *__restrict__ op_part_off,
                               const int *__restrict__ op_ntiles, const int *__restrict__ op_slot, int nops, double scale,
-                              double *__restrict__ grad, int nb, int64_t part_stride)
+                              double *__restrict__ grad, int nb, int64_t part_stride, const int *__restrict__ active)
 {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (gw >= nops * nb) return;
     const int b = gw / nops, warp = gw - b * nops;
+    if (skip_instance(active, b)) return;
     grad += (size_t)b * nops;
     const double *p = partials + (size_t)b * part_stride + op_part_off[warp];
     const int nt = op_ntiles[warp], sl = op_slot[warp];
@@ -824,9 +844,10 @@ template <int W, bool ELL>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv(const int64_t *__restrict__ rowptr, int ell_width,
                                                        const int32_t *__restrict__ col, const double *__restrict__ val,
                                                        const double *__restrict__ x, double *__restrict__ y, int64_t D,
-                                                       double *__restrict__ epart)
+                                                       double *__restrict__ epart, const int *__restrict__ active)
 {
     __shared__ double red[kSpmvThreads / 32];
+    if (skip_instance(active, blockIdx.y)) return;
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     x += (size_t)blockIdx.y * D * W;  // instance blockIdx.y, same matrix
@@ -865,8 +886,10 @@ template <int W, int T>
 __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int32_t *__restrict__ col,
                                                             const double *__restrict__ val,
                                                             const double *__restrict__ x, double *__restrict__ y,
-                                                            int64_t D, double *__restrict__ epart, int64_t mat_stride)
+                                                            int64_t D, double *__restrict__ epart, int64_t mat_stride,
+                                                            const int *__restrict__ active)
 {
+    if (skip_instance(active, blockIdx.y)) return;
     // T threads per row: a warp covers 32/T consecutive rows of one 32-row slab; lane
     // (sub, k) takes row k's groups sub, sub+T, ... (each group read by 32/T lanes is
     // one contiguous run), and the T partial sums meet in a fixed butterfly.
@@ -1135,6 +1158,7 @@ struct OtfArgs {
     // shared by every instance when `shared` is set
     const double *vss, *vab, *a_alpha, *b_alpha, *a_beta, *b_beta, *diag;
     int shared;
+    const int *active;  // instance mask (nullable)
 };
 
 __host__ __device__ inline size_t otf_smem_bytes(int N, int P2, int nsa, int nda)
@@ -1155,6 +1179,7 @@ __global__ void __launch_bounds__(512) k_otf_strings(OtfArgs a, const double *__
     __shared__ double red[16];
     const int N = a.N, NN = a.N * a.N, nsa = a.nsa, nda = a.nda;
     const int ra = blockIdx.x;
+    if (skip_instance(a.active, blockIdx.z)) return;
     {
         // instance blockIdx.z: its vectors and (unless shared) its integral tables
         const size_t b = blockIdx.z, D = (size_t)a.nA * a.nB, bt = a.shared ? 0 : b;
@@ -1340,6 +1365,7 @@ struct aegpu_engine {
     double *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
     double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
     double *d_ckpt = nullptr;  // per pass: amplitudes after the pass (adjoint sweep input)
+    int *d_active = nullptr;   // per instance: 0 = skip it in batched launches
     std::vector<std::pair<void *, size_t>> inst_allocs;
 
     // Hamiltonian (its device arrays, released when it is replaced)
@@ -1485,6 +1511,7 @@ struct aegpu_engine {
         a.sigma = d_sig + ((size_t)bi * 2 + d) * (1 << kMaxWarpLayers);
         a.pc_stride = (int64_t)npass * 2 * kMaxWarpLayers;
         a.sig_stride = (int64_t)npass * 2 * (1 << kMaxWarpLayers);
+        a.active = d_active;
         return a;
     }
     size_t vec_elems() const { return (size_t)B.D * W; }
@@ -1551,15 +1578,22 @@ struct aegpu_engine {
         get(d_scalar, std::max<size_t>(B_, 4));
         get(d_grad, B_ * nops);
         get(d_ckpt, B_ * std::max<int64_t>(n_ckpt, 1));
+        get(d_active, B_);
+        if (d_active) {
+            const std::vector<int> ones(B_, 1);
+            cudaMemcpy(d_active, ones.data(), B_ * sizeof(int), cudaMemcpyHostToDevice);
+        }
+        prep.active = d_active;
         drop_graph();
         cached_angles.clear();
         psi_valid = h_valid = false;
         if (!ok) return fail(AEGPU_ERR_NOMEM, "device allocation of the instance buffers failed");
         return AEGPU_OK;
     }
-    DiagArgs diag_args(const DevBlock &b) const
+    DiagArgs diag_args(const DevBlock &b, bool masked = true) const
     {
         DiagArgs a;
+        a.active = masked ? d_active : nullptr;
         a.ops = b.ops;
         a.nslots = b.nslots;
         a.codes = d_codes;
@@ -1619,14 +1653,14 @@ int run_evolve(aegpu_engine *e, int ninst)
 {
     const int64_t n = (int64_t)e->vec_elems();
     k_broadcast<<<dim3((unsigned)std::min<int64_t>((n + 255) / 256, e->sm_count * 4), ninst), 256, 0, e->stream>>>(
-        e->d_start, e->d_psi, n);
+        e->d_start, e->d_psi, n, e->d_active);
     e->launches += 1;
     for (int bi = 0; bi < (int)e->dblocks.size(); ++bi) {
         auto &b = e->dblocks[bi];
         double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
             k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
-                e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table, (int)e->excs.size());
+                e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table, (int)e->excs.size(), e->d_active);
             k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1, ck, n, e->n_ckpt);
             e->launches += 2;
         } else if (b.nwtasks) {
@@ -1643,41 +1677,48 @@ int run_evolve(aegpu_engine *e, int ninst)
 }
 
 // Pass constants of the first ninst instances from their angles in d_ang.
-int run_prep(aegpu_engine *e, int ninst)
+int run_prep(aegpu_engine *e, int ninst, bool masked = true)
 {
-    k_pass_prep<<<dim3((unsigned)e->dblocks.size(), ninst), 64, 0, e->stream>>>(e->prep, e->d_ang, e->d_sc, e->d_pc,
+    PrepArgs pa = e->prep;
+    pa.active = masked ? e->d_active : nullptr;
+    k_pass_prep<<<dim3((unsigned)e->dblocks.size(), ninst), 64, 0, e->stream>>>(pa, e->d_ang, e->d_sc, e->d_pc,
                                                                              e->d_sig);
     e->launches += 1;
     return e->cuda_check("pass constants");
 }
 
-int upload_angles(aegpu_engine *e, const double *angles, bool host, int ninst)
+int upload_angles(aegpu_engine *e, const double *angles, bool host, int ninst, bool masked = true)
 {
     const size_t n = e->excs.size() * (size_t)ninst;
     cudaMemcpyAsync(e->d_ang, angles, n * sizeof(double), host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
                     e->stream);
-    return run_prep(e, ninst);
+    return run_prep(e, ninst, masked);
 }
 
 // y = H x for the first ninst instances (vectors at stride D*W), with <x|y> partial
 // sums into epart (nullable; *nparts partial sums per instance).
-int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ninst, int *nparts = nullptr)
+int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ninst, int *nparts = nullptr,
+              bool masked = true)
 {
+    const int *act = masked ? e->d_active : nullptr;
     if (nparts) *nparts = e->spmv_grid;
     const int64_t D = (int64_t)e->B.D;
     if (e->ham_kind == 1) {
         const dim3 g(e->spmv_grid, ninst);
         if (e->W == 1)
-            k_spmv<1, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv<1, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart,
+                                                                act);
         else
-            k_spmv<2, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart);
+            k_spmv<2, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart,
+                                                                act);
     } else if (e->ham_kind == 2) {
         const int T = e->spmv_tpr();
         const int64_t rows_per_cta = kSpmvThreads / T;
         const int sg = (int)((D + rows_per_cta - 1) / rows_per_cta);
         const dim3 g(sg, ninst);
         const int64_t q = e->ell_width >> 2, ms = e->ell_stride_inst;
-#define AE_SELL(WW, TT) k_spmv_sell<WW, TT><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms)
+#define AE_SELL(WW, TT) \
+    k_spmv_sell<WW, TT><<<g, kSpmvThreads, 0, e->stream>>>(q, e->d_col, e->d_val, x, y, D, epart, ms, act)
         if (e->W == 1) {
             if (T == 1) AE_SELL(1, 1); else if (T == 2) AE_SELL(1, 2); else if (T == 4) AE_SELL(1, 4); else AE_SELL(1, 8);
         } else {
@@ -1688,10 +1729,12 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
     } else if (e->ham_kind == 3) {
         const dim3 g(e->otf.nA, e->otf_chunks, ninst);
         const size_t smem = otf_smem_bytes(e->otf.N, e->otf.P2, e->otf.nsa, e->otf.nda);
+        OtfArgs o = e->otf;
+        o.active = act;
         if (e->W == 1)
-            k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(e->otf, x, y, epart);
+            k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart);
         else
-            k_otf_strings<2><<<g, e->otf_threads, smem, e->stream>>>(e->otf, x, y, epart);
+            k_otf_strings<2><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart);
         if (nparts) *nparts = e->otf.nA * e->otf_chunks;
     } else {
         return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
@@ -1706,7 +1749,7 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
     int np = 0;
     int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np);
     if (rc) return rc;
-    k_reduce_sum<<<ninst, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0);
+    k_reduce_sum<<<ninst, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0, e->d_active);
     e->launches += 1;
     return e->cuda_check("energy");
 }
@@ -1724,7 +1767,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         const double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
             k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
-                e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table, nops);
+                e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table, nops, e->d_active);
             k_diag_adj<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h, n, part,
                                                                      e->n_partials);
             e->launches += 2;
@@ -1746,7 +1789,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
     const int warps = nops * ninst;
     k_grad_reduce<<<(warps * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
                                                                    e->d_op_slot, nops, scale, grad_dev, ninst,
-                                                                   e->n_partials);
+                                                                   e->n_partials, e->d_active);
     e->launches += 1;
     return e->cuda_check("backward");
 }
@@ -2275,6 +2318,18 @@ int aegpu_set_batch(aegpu_engine *e, int nb)
 
 int aegpu_batch_size(const aegpu_engine *e) { return e ? e->nb : -1; }
 
+int aegpu_set_active(aegpu_engine *e, const int *active)
+{
+    if (!e) return AEGPU_ERR_ARG;
+    if (!e->d_active) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    std::vector<int> m(e->nb, 1);
+    if (active)
+        for (int b = 0; b < e->nb; ++b) m[b] = active[b] != 0;
+    cudaMemcpyAsync(e->d_active, m.data(), m.size() * sizeof(int), cudaMemcpyHostToDevice, e->stream);
+    e->psi_valid = e->h_valid = false;
+    return stream_sync(e, "set_active");
+}
+
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
 {
     if (!e) return AEGPU_ERR_ARG;
@@ -2402,8 +2457,8 @@ int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *pro
     cudaMemcpyAsync(e->d_h, proj, (size_t)n * e->nb * sizeof(double), cudaMemcpyHostToDevice, e->stream);
     e->h_valid = false;
     const int grid = (int)std::min<int64_t>(std::max<int64_t>(1, (n + 255) / 256), e->n_epart);
-    k_dot<<<dim3(grid, e->nb), 256, 0, e->stream>>>(e->d_h, e->d_psi, n, e->d_epart);
-    k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, grid, e->d_scalar, 1.0);
+    k_dot<<<dim3(grid, e->nb), 256, 0, e->stream>>>(e->d_h, e->d_psi, n, e->d_epart, e->d_active);
+    k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, grid, e->d_scalar, 1.0, e->d_active);
     e->launches += 2;
     rc = run_backward(e, e->d_grad, e->nb, 1.0);
     if (rc) return rc;
@@ -2633,7 +2688,7 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
     const size_t n = e->vec_elems() * e->nb;
     e->h_valid = false;
     cudaMemcpyAsync(e->d_tmp, x, n * sizeof(double), cudaMemcpyHostToDevice, e->stream);
-    int rc = run_apply(e, e->d_tmp, e->d_h, nullptr, e->nb);
+    int rc = run_apply(e, e->d_tmp, e->d_h, nullptr, e->nb, nullptr, false);
     if (!rc) {
         cudaMemcpyAsync(y, e->d_h, n * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
         rc = stream_sync(e, "apply_h");
@@ -2703,7 +2758,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     cudaMemcpyAsync(d_pptr, pptr.data(), pptr.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_ppos, ppos.data(), ppos.size() * sizeof(int), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(d_pscale, pscale.data(), pscale.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    int rc = upload_angles(e, angles, true, 1);
+    int rc = upload_angles(e, angles, true, 1, false);
     if (rc) return rc;
     cudaMemsetAsync(T, 0, n * nops * sizeof(double), s);
     cudaMemsetAsync(Hops, 0, (size_t)nops * nops * sizeof(double), s);
@@ -2714,9 +2769,9 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         const int p0 = e->block_pos0[bi];
         if (b.diagonal) {
             k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table,
-                                                                       nops);
-            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), T, n, p0, nullptr, 0, 0);
-            k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_psi, T, n, e->d_tpos);
+                                                                       nops, nullptr);
+            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), T, n, p0, nullptr, 0, 0);
+            k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), e->d_psi, T, n, e->d_tpos);
             e->launches += 3;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args((int)bi, 1.0);
@@ -2748,7 +2803,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         cublasDgemv(e->cublas, CUBLAS_OP_T, DW, V, &one, TC, DW, e->d_h, 1, &zero, THT, 1);
     } else {
         // the V columns as V instances of the H product (the matrix or tables are shared)
-        rc = run_apply(e, TC, HTC, nullptr, V);
+        rc = run_apply(e, TC, HTC, nullptr, V, nullptr, false);
         if (rc) return rc;
         const double two = 2.0, zero = 0.0;
         cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, V, V, DW, &two, TC, DW, HTC, DW, &zero, THT, V);
@@ -2762,12 +2817,12 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         const int nvec = p0 + b.nslots;
         if (b.diagonal) {
             k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table,
-                                                                       nops);
+                                                                       nops, nullptr);
             dim3 g(kDiagGrid, nvec);
-            k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b), e->d_h, T, n, nvec, p0, hpart);
+            k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b, false), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
                                                                             b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
-            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b), e->d_h, 0, 1, nullptr, 0, 0);
+            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), e->d_h, 0, 1, nullptr, 0, 0);
             e->launches += 4;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args(bi, -1.0);
@@ -2840,9 +2895,9 @@ int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double 
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
     int np = 0;
-    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, e->nb, &np);
+    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, e->nb, &np, false);
     if (!rc && energy_dev) {
-        k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0);
+        k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0, nullptr);
         e->launches += 1;
         rc = e->cuda_check("apply_dev");
     }
@@ -2987,8 +3042,8 @@ int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t
     // array needs no clearing between calls
     const int grid = (int)((D + kNoAllocRowsPerPartial - 1) / kNoAllocRowsPerPartial);
     cudaStream_t s = (cudaStream_t)stream;
-    k_spmv<1, false><<<grid, kSpmvThreads, 0, s>>>(rowptr_dev, 0, col_dev, val_dev, x_dev, y_dev, D, scratch);
-    k_reduce_sum<<<1, 256, 0, s>>>(scratch, grid, energy_dev, 1.0);
+    k_spmv<1, false><<<grid, kSpmvThreads, 0, s>>>(rowptr_dev, 0, col_dev, val_dev, x_dev, y_dev, D, scratch, nullptr);
+    k_reduce_sum<<<1, 256, 0, s>>>(scratch, grid, energy_dev, 1.0, nullptr);
     const cudaError_t rc = cudaGetLastError();
     return rc == cudaSuccess ? AEGPU_OK : AEGPU_ERR_CUDA;
 }

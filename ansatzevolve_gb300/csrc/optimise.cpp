@@ -9,8 +9,9 @@
 //   ed., Alg. 6.1 with the initial scaling of eq. 6.20) with a backtracking Armijo
 //   line search.  Every round is ONE batched energy + gradient evaluation: each
 //   instance contributes its current trial point, so line-search points of some
-//   instances and new iterates of others share the launch.  No counterpart in the
-//   reference, which optimises one angle vector at a time.
+//   instances and new iterates of others share the launch, and converged instances
+//   are masked out of it (aegpu_set_active).  No counterpart in the reference, which
+//   optimises one angle vector at a time.
 #include "../../include/aegpu.h"
 #include "newton.h"
 
@@ -96,11 +97,20 @@ int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const d
         }
     }
     std::vector<double> ang((size_t)nb * nops), E(nb), gops((size_t)nb * nops), gc(P), s(P), y(P), Hy(P);
+    std::vector<int> active(nb, 1), last(nb, 1);
     int64_t round = 0;
     for (; round < max_rounds; ++round) {
         bool any = false;
-        for (int b = 0; b < nb; ++b) any = any || st[b].phase != BfgsInstance::kDone;
+        for (int b = 0; b < nb; ++b) {
+            active[b] = st[b].phase != BfgsInstance::kDone;
+            any = any || active[b];
+        }
         if (!any) break;
+        // converged instances drop out of the batched launches
+        if (active != last) {
+            if ((rc = aegpu_set_active(e, active.data()))) return rc;
+            last = active;
+        }
         // theta_op = scale[op] * x[param[op]] for every instance's trial point
         for (int b = 0; b < nb; ++b)
             for (int o = 0; o < nops; ++o) ang[(size_t)b * nops + o] = scale[o] * st[b].xt[param[o]];
@@ -186,6 +196,7 @@ int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const d
             }
         }
     }
+    if ((rc = aegpu_set_active(e, nullptr))) return rc;
     for (int b = 0; b < nb; ++b) {
         std::copy(st[b].x.begin(), st[b].x.end(), x + (size_t)b * P);
         if (energy) energy[b] = st[b].f;

@@ -92,6 +92,10 @@ enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREA
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
 int aegpu_batch_size(const aegpu_engine *e);
+/* Instance mask of batched evaluations: active[b] = 0 skips instance b (its results are
+ * left as they were); NULL makes every instance active.  The Hessian and the H*x
+ * calls ignore the mask. */
+int aegpu_set_active(aegpu_engine *e, const int *active);
 int aegpu_set_ham_integrals_batch(aegpu_engine *e, const double *h1s, const double *g2s, int mode);
 /* Which representation is in use: 1 CSR, 2 stored ELL, 3 on the fly; and its stored entries. */
 int aegpu_ham_info(const aegpu_engine *e, int *kind, int64_t *stored_entries);

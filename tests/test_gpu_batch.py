@@ -245,3 +245,31 @@ def test_out_of_order_calls_are_refused():
     with pytest.raises(ae.AegpuError, match="batch size of 1"):
         e.hessian(np.zeros(len(ops0)), p0, np.asarray(pb["scale"]))
     e.close()
+
+
+def test_instance_mask_skips_and_keeps_results():
+    """Masked instances are skipped (their results stay as they were); the others are
+    bit-identical to the unmasked evaluation, through both the host and graph paths."""
+    pb = synthetic_problem(8, 4, 4, 2, 0)
+    nb = 5
+    e = make_engine(pb, nb)
+    fam = [family_integrals(8, float(si), seed=8) for si in np.linspace(0, 1, nb)]
+    e.set_ham_integrals_batch(np.stack([f[0] for f in fam]), np.stack([f[1] for f in fam]), ae.HAM_ON_THE_FLY)
+    rng = np.random.default_rng(30)
+    a1 = rng.uniform(-0.3, 0.3, (nb, e.nops))
+    a2 = rng.uniform(-0.3, 0.3, (nb, e.nops))
+    E1, g1 = e.gradient(a1)
+    E2, g2 = e.gradient(a2)
+    mask = np.array([1, 0, 1, 0, 1])
+    E1, g1 = e.gradient(a1)  # all active: results at a1
+    e.set_active(mask)
+    Em, gm = e.gradient(a2)
+    for b in range(nb):
+        if mask[b]:
+            assert Em[b] == E2[b] and np.array_equal(gm[b], g2[b])
+        else:
+            assert Em[b] == E1[b] and np.array_equal(gm[b], g1[b])
+    e.set_active(None)
+    Ea, ga = e.gradient(a2)
+    assert np.array_equal(Ea, E2) and np.array_equal(ga, g2)
+    e.close()
