@@ -313,7 +313,9 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     the previous converged angles (timed on the first n_plain held-out values, mean
     per instance).  Batched + warm-started: all n_heldout instances in one batch,
     network proposals judged by the engine against the s = 0 angles, then lockstep
-    BFGS from the inverse Hessians at 8 anchors.  The network is trained once per family on
+    BFGS from the inverse Hessians at 8 anchors (converged instances drop out; those
+    still unconverged after 150 rounds finish with the plain method one at a time,
+    timed).  The network is trained once per family on
     n_train converged angle sets from a continuation chain (reported separately)."""
     from ansatzevolve_gb300 import warmstart as ws
     spec = ws.FamilySpec(10, 5, 3, seed=0)
@@ -341,6 +343,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
             "batched_s_total": r["seconds"], "batched_instances": n_heldout, "batched_s_per_instance": batched_per,
             "batched_rounds": int(r["rounds"]), "batched_iters_median": float(np.median(r["iters"])),
             "batched_iters_max": int(r["iters"].max()), "proposals_used": int(r["used"].sum()),
+            "finished_by_newton": int(r["newton_finished"]), "newton_finish_s": r["t_late"],
             "anchor_hessian_s": r["t_anchor"], "max_gnorm": float(r["gnorm"].max()), "gtol": 1e-6,
             "energy_match_1e-8": int(np.sum(np.abs(dE) < 1e-8)), "energy_compared": n_plain,
             "max_abs_dE": float(np.abs(dE).max()),
