@@ -250,7 +250,7 @@ def inverse_hessian(engine, x, spec, floor=1e-3):
     return (V / a) @ V.T
 
 
-def scan_batched_warm(spec, svals, model, x_fallback, gtol=1e-6, n_anchor=4, mode=None, max_rounds=150):
+def scan_batched_warm(spec, svals, model, x_fallback, gtol=1e-6, n_anchor=4, mode=None, max_rounds=2000):
     """The batched, warm-started path: every instance at once, each starting from the
     network's proposal where the engine finds it lower in energy than the fallback
     start, then lockstep BFGS from an inverse Hessian taken at the nearest of n_anchor

@@ -313,9 +313,9 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     the previous converged angles (timed on the first n_plain held-out values, mean
     per instance).  Batched + warm-started: all n_heldout instances in one batch,
     network proposals judged by the engine against the s = 0 angles, then lockstep
-    BFGS from the inverse Hessians at 8 anchors (converged instances drop out; those
-    still unconverged after 150 rounds finish with the plain method one at a time,
-    timed).  The network is trained once per family on
+    BFGS from the inverse Hessians at 8 anchors (converged instances drop out of the
+    launches; any still unconverged after 2000 rounds would finish with the plain
+    method, timed).  The network is trained once per family on
     n_train converged angle sets from a continuation chain (reported separately)."""
     from ansatzevolve_gb300 import warmstart as ws
     spec = ws.FamilySpec(10, 5, 3, seed=0)
