@@ -4,7 +4,7 @@ A small MLP maps a Hamiltonian's integrals to starting angles.  Features are the
 flattened one-electron integrals h_pq and the Coulomb-like diagonal g_ppqq; targets
 are converged compressed angles produced by the engine itself.  The network is
 trained and run by the project's CUDA kernels (aegpu_mlp_*: BF16 weights, FP32
-accumulation, Adam, MSE).  Every proposal is judged by the engine: an instance starts
+accumulation, Adam, MSE).  Every proposal is screened by the engine: an instance starts
 from the proposal only if its energy there is below the energy at the plain start,
 so the optimiser's converged answer is decided by the engine, not by the network.
 No counterpart in the reference.
@@ -104,7 +104,7 @@ class Mlp:
         return Y
 
 
-def judged_starts(engine, proposals, param0, scale, plain=None):
+def screened_starts(engine, proposals, param0, scale, plain=None):
     """Per instance of a batched engine, the start to optimise from: the network's
     proposal where the engine finds a lower energy there than at the plain start
     (zeros unless given), else the plain start.  Returns (starts, used_proposal)."""
@@ -270,7 +270,7 @@ def scan_batched_warm(spec, svals, model, x_fallback, gtol=1e-6, n_anchor=4, mod
     ea = spec.engine(1)
     t0 = time.perf_counter()
     prop = model.predict(feats).astype(np.float64)
-    starts, used = judged_starts(e, prop, spec.param0, spec.scale, np.tile(np.asarray(x_fallback, float), (M, 1)))
+    starts, used = screened_starts(e, prop, spec.param0, spec.scale, np.tile(np.asarray(x_fallback, float), (M, 1)))
     hinv = None
     t_anchor = t_setup = 0.0
     if n_anchor:

@@ -312,7 +312,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     Plain: one instance at a time in increasing s, the reference's Newton method from
     the previous converged angles (timed on the first n_plain held-out values, mean
     per instance).  Batched + warm-started: all n_heldout instances in one batch,
-    network proposals judged by the engine against the s = 0 angles, then lockstep
+    network proposals screened by the engine against the s = 0 angles, then lockstep
     BFGS from the inverse Hessians at 8 anchors (converged instances drop out of the
     launches; any still unconverged after 2000 rounds would finish with the plain
     method, timed).  The network is trained once per family on

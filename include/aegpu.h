@@ -8,7 +8,7 @@
  * Every call returns AEGPU_OK (0) or a positive status and never traps; the text
  * of the last failure is available from aegpu_last_error().
  *
- * Conventions (the reference's, see SURVEY of AnsatzEvolve):
+ * Conventions (the reference's internal ones: operatorpool.cpp:198-199, 221-230):
  *  - spin orbital k < N is beta (low bits), k >= N is alpha (high bits);
  *  - excitations are 4 signed 0-based orbital indices, -1 = absent, op-major;
  *  - the sector basis is the ascending list of bitstrings in the sector; vectors
@@ -16,6 +16,9 @@
  *    re, im);
  *  - angles are per operator, in the order the operators were given;
  *  - H is applied as y = H x with rows = output determinants.
+ * An engine is not thread-safe: one thread at a time per engine (the reference-
+ * compatible layer serialises its calls per context with a mutex); different
+ * engines may be used from different threads.
  */
 #ifndef AEGPU_H
 #define AEGPU_H
