@@ -1,8 +1,8 @@
 #!/usr/bin/env bash
 # Builds the reference AnsatzEvolve library (real and complex variants) straight from
 # its own sources, plus the pinning driver oracle/ref_driver.cpp, into oracle/_ref/.
-# Test infrastructure only: oracle/_ref/ is the checker for the C restatement in
-# oracle/oracle.c and the source of the golden fixtures under tests/golden/.
+# Test infrastructure only: oracle/_ref/ validates the C restatement in
+# oracle/oracle.c and produces the golden fixtures under tests/golden/.
 # The reference's CMake project needs gfortran, so the translation units are
 # compiled directly.  Needs the reference checkout (default /root/reference).
 set -euo pipefail

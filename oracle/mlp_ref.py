@@ -1,5 +1,5 @@
 """Test infrastructure only: a numpy restatement of the warm-start MLP (the aegpu_mlp_*
-kernels) used as the checker for their forward pass and gradients.  Nothing in the
+kernels) used to check their forward pass and gradients.  Nothing in the
 product imports it.
 
 Model: x' = (x - in_mean) / in_scale; z1 = x' W1^T + b1, a1 = gelu(z1);

@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of AnsatzEvolve's statevector hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA product
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity reference for the CUDA product
  * path and the timed CPU baseline ("port") of bench.py; nothing in the product
  * library links, loads or calls it.  It restates the reference algorithm in plain
  * C (+ OpenMP for the row loops the reference runs on its thread pool), and it is

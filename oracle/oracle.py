@@ -1,5 +1,5 @@
 """ctypes view of oracle/liboracle.so -- the CPU restatement used as the parity
-checker in tests/ and as the timed CPU baseline ("port") of bench.py.
+reference in tests/ and as the timed CPU baseline ("port") of bench.py.
 
 Test infrastructure only; the product library never imports this module.
 """

@@ -1,4 +1,4 @@
-"""The numpy restatement of the warm-start MLP (the checker for its CUDA kernels):
+"""The numpy restatement of the warm-start MLP (the reference for its CUDA kernels):
 gradients against finite differences, bf16 rounding against known values."""
 import numpy as np
 
