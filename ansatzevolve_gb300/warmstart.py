@@ -195,6 +195,27 @@ class FamilySpec:
         return e
 
 
+def scan_origin(spec, n_starts=64, seed=5, s0=0.0, gtol=1e-6):
+    """The scan's starting member: the lowest minimum at s = s0 among a batched BFGS
+    multi-start (zero angles plus n_starts - 1 seeded U(-1, 1) starts), polished by the
+    reference's Newton method.  Following the lowest branch makes the scan smooth where
+    a single Newton run from zero angles lands on a higher branch with jumps.
+    Returns (x0, E0)."""
+    from . import HAM_STORED
+    P = spec.P
+    ints = spec.integrals(s0)
+    e = spec.engine(n_starts, [ints] * n_starts, HAM_STORED)
+    starts = np.vstack([np.zeros(P), np.random.default_rng(seed).uniform(-1.0, 1.0, (n_starts - 1, P))])
+    xs, Es, _, _, _ = e.optimise_batch(starts, spec.param0, spec.scale, gtol=gtol, max_rounds=5000)
+    e.close()
+    best = int(np.argmin(Es))
+    e1 = spec.engine(1)
+    e1.set_ham_integrals(*ints, HAM_STORED)
+    x0, E0, _, _, _ = e1.optimise_newton(xs[best], spec.param0, spec.scale, gtol=gtol)
+    e1.close()
+    return x0, E0
+
+
 def scan_newton(spec, svals, x_start, gtol=1e-6, mode=None):
     """The plain path of a family scan: one instance at a time in the given order,
     each optimised by the reference's Newton method from the previous instance's
