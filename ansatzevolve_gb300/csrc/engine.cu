@@ -46,6 +46,7 @@
 
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <array>
@@ -62,6 +63,14 @@
 #include <vector>
 
 using namespace ae;
+
+namespace {
+// NVTX range over a host-side phase (visible in Nsight timelines; no cost without a tool)
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
 
 namespace {
 
@@ -1651,6 +1660,7 @@ int set_smem_limits(int dev)
 // constants already prepared from d_ang).
 int run_evolve(aegpu_engine *e, int ninst)
 {
+    NvtxRange r("aegpu evolve");
     const int64_t n = (int64_t)e->vec_elems();
     k_broadcast<<<dim3((unsigned)std::min<int64_t>((n + 255) / 256, e->sm_count * 4), ninst), 256, 0, e->stream>>>(
         e->d_start, e->d_psi, n, e->d_active);
@@ -1746,6 +1756,7 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
 // E_dev[b] = <psi_b|H psi_b> for the first ninst instances (H psi left in d_h).
 int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 {
+    NvtxRange r("aegpu H*psi + energy");
     int np = 0;
     int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np);
     if (rc) return rc;
@@ -1759,6 +1770,7 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 // grad_dev[b * nops + op] (scale 2 for the energy gradient, 1 for a projection).
 int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.0)
 {
+    NvtxRange r("aegpu adjoint sweep");
     const int64_t n = (int64_t)e->vec_elems();
     const int nops = (int)e->excs.size();
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
@@ -1798,6 +1810,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
 // (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
 int capture_grad_graph(aegpu_engine *e)
 {
+    NvtxRange r("aegpu capture evaluation graph");
     cudaStream_t cap = nullptr, saved = e->stream;
     if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return e->cuda_check("graph stream");
     const int64_t l0 = e->launches;
@@ -1926,6 +1939,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
 {
     if (!e) return AEGPU_ERR_ARG;
     if (e->d_start) return e->fail(AEGPU_ERR_STATE, "the problem is already set (create a new engine)");
+    NvtxRange r("aegpu set problem");
     if (nops < 1 || !ops) return e->fail(AEGPU_ERR_ARG, "no excitations");
     if (!e->B.init(nq, basis_kind, n_elec, n_alpha, n_beta, e->err)) return AEGPU_ERR_ARG;
     e->cplx = complex_mode != 0;
@@ -2148,6 +2162,7 @@ namespace {
 // between all instances, ntab = nb gives instance b the integrals h1s[b], g2s[b].
 int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int ntab, int mode)
 {
+    NvtxRange r("aegpu set Hamiltonian");
     if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
     if (e->B.kind != BASIS_SZ) return e->fail(AEGPU_ERR_UNSUPPORTED, "integral Hamiltonians need the Sz sector");
     const int N = e->B.N;
@@ -2705,6 +2720,7 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
 static int hessian_impl(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
                         const double *proj, double *energy, double *grad_comp, double *hess_comp)
 {
+    NvtxRange r(proj ? "aegpu projected Hessian" : "aegpu Hessian");
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
     if (!proj && !e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the Hessian needs a batch size of 1");
