@@ -113,6 +113,7 @@ def lib(build_if_missing=True):
         "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
         "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
         "aegpu_device_bytes": (i64, [_P]),
+        "aegpu_debug_fail_alloc_after": (None, [i64]),
         "aegpu_fp64_work": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),
         "aegpu_fp64_peak": (ctypes.c_int, [_DP]),
         "aegpu_launch_count": (i64, [_P]),

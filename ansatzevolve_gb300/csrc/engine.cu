@@ -65,6 +65,10 @@
 using namespace ae;
 
 namespace {
+// Host-side fault injection for tests: after this many further engine allocations,
+// every allocation fails as if the device were out of memory (-1: off).
+std::atomic<int64_t> g_fail_alloc_after{-1};
+
 // NVTX range over a host-side phase (visible in Nsight timelines; no cost without a tool)
 struct NvtxRange {
     explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
@@ -1462,6 +1466,11 @@ struct aegpu_engine {
     {
         void *p = nullptr;
         if (n == 0) n = 1;
+        if (g_fail_alloc_after.load() >= 0 && g_fail_alloc_after.fetch_sub(1) <= 0) {
+            g_fail_alloc_after.store(0);
+            alloc_failed = true;
+            return nullptr;
+        }
         cudaError_t rc = cudaMalloc(&p, n * sizeof(T));
         if (rc != cudaSuccess) {
             cudaGetLastError();
@@ -3022,6 +3031,10 @@ int aegpu_fp64_peak(double *tflops)
 }
 
 int64_t aegpu_device_bytes(const aegpu_engine *e) { return e ? e->dev_bytes : -1; }
+
+// Test hook (no counterpart in the reference): the next n engine allocations succeed,
+// all later ones fail as out of memory, until called again with n < 0.
+void aegpu_debug_fail_alloc_after(int64_t n) { g_fail_alloc_after.store(n < 0 ? -1 : n); }
 int64_t aegpu_launch_count(const aegpu_engine *e) { return e ? e->launches : -1; }
 
 // No counterpart in the reference (see include/aegpu.h for the contract).

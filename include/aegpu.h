@@ -241,6 +241,10 @@ int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t
 
 /* Bytes of HBM held by the engine, and kernel launches issued since creation. */
 int64_t aegpu_device_bytes(const aegpu_engine *e);
+/* Fault injection for tests: the next n engine allocations succeed and every later one
+ * fails as out of memory (AEGPU_ERR_NOMEM is returned, nothing traps); n < 0 turns it
+ * off.  Process-wide. */
+void aegpu_debug_fail_alloc_after(int64_t n);
 /* FP64 instructions of one energy + gradient evaluation per instance: work[0] H psi
  * (one DFMA per matrix element + the energy FMA), work[1] forward passes, work[2]
  * adjoint passes (complex mode counts each real part). */

@@ -273,3 +273,32 @@ def test_instance_mask_skips_and_keeps_results():
     Ea, ga = e.gradient(a2)
     assert np.array_equal(Ea, E2) and np.array_equal(ga, g2)
     e.close()
+
+
+def test_allocation_failures_return_status_codes():
+    """Host-side fault injection: whichever set-up allocation fails, the call returns a
+    status (out of memory) instead of trapping, and a later engine works normally."""
+    pb = synthetic_problem(6, 3, 3, 1, 0)
+    ops0 = np.asarray(pb["ops_1b"]) - 1
+    L = ae.lib()
+    seen_fail = 0
+    try:
+        for n in (0, 2, 5, 9, 14, 20, 30, 45):
+            L.aegpu_debug_fail_alloc_after(n)
+            try:
+                e = ae.Engine(12, ae.BASIS_SZ, 6, 3, 3, ops0)
+                e.set_batch(3)
+                e.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+                e.gradient(np.zeros((3, e.nops)))
+                e.close()
+            except ae.AegpuError as err:
+                assert "error 4" in str(err) or "allocation" in str(err), err
+                seen_fail += 1
+    finally:
+        L.aegpu_debug_fail_alloc_after(-1)
+    assert seen_fail >= 4
+    e = ae.Engine(12, ae.BASIS_SZ, 6, 3, 3, ops0)
+    e.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    E, g = e.gradient(np.zeros(e.nops))
+    assert np.isfinite(E)
+    e.close()
