@@ -1433,6 +1433,10 @@ struct aegpu_engine {
     // d_scalar / d_grad), captured on first use of aegpu_gradient_dev
     cudaGraphExec_t grad_graph = nullptr;
     cudaGraph_t grad_graph_def = nullptr;  // its definition (child node of group graphs)
+    // the same evaluation split in two (host-buffer calls): pass constants + evolve +
+    // H psi + energy, and the adjoint sweep + gradient reduction
+    cudaGraphExec_t energy_graph = nullptr, back_graph = nullptr;
+    int64_t energy_graph_launches = 0, back_graph_launches = 0;
     int64_t graph_launches = 0;  // kernels inside the graph
     int64_t generation = 0;      // bumped whenever device buffers or the Hamiltonian change
     bool use_graph = true;
@@ -1565,8 +1569,11 @@ struct aegpu_engine {
         ++generation;
         if (grad_graph) cudaGraphExecDestroy(grad_graph);
         if (grad_graph_def) cudaGraphDestroy(grad_graph_def);
+        if (energy_graph) cudaGraphExecDestroy(energy_graph);
+        if (back_graph) cudaGraphExecDestroy(back_graph);
         grad_graph = nullptr;
         grad_graph_def = nullptr;
+        energy_graph = back_graph = nullptr;
     }
 
     // (Re)allocate the per-instance buffers for nb instances.
@@ -1817,7 +1824,11 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
 
 // Capture pass constants + evolve + H psi + adjoint sweep of all nb instances
 // (reading d_ang, writing d_scalar / d_grad) into one CUDA graph.
-int capture_grad_graph(aegpu_engine *e)
+// Capture one evaluation phase set of all nb instances into a graph: kind 0 = pass
+// constants + evolve + H psi + energy + adjoint sweep (reading d_ang, writing d_scalar
+// / d_grad), 1 = the first four only, 2 = the adjoint sweep only.  def (nullable)
+// receives the graph's definition.
+int capture_phases(aegpu_engine *e, int kind, cudaGraphExec_t *exec, cudaGraph_t *def, int64_t *nlaunch)
 {
     NvtxRange r("aegpu capture evaluation graph");
     cudaStream_t cap = nullptr, saved = e->stream;
@@ -1828,25 +1839,46 @@ int capture_grad_graph(aegpu_engine *e)
     int rc = AEGPU_OK;
     if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = e->cuda_check("begin capture");
     if (!rc) {
-        rc = run_prep(e, e->nb);
-        if (!rc) rc = run_evolve(e, e->nb);
-        if (!rc) rc = run_energy(e, e->d_scalar, e->nb);
-        if (!rc) rc = run_backward(e, e->d_grad, e->nb);
+        if (kind != 2) {
+            rc = run_prep(e, e->nb);
+            if (!rc) rc = run_evolve(e, e->nb);
+            if (!rc) rc = run_energy(e, e->d_scalar, e->nb);
+        }
+        if (!rc && kind != 1) rc = run_backward(e, e->d_grad, e->nb);
         cudaError_t ce = cudaStreamEndCapture(cap, &g);
         if (!rc && ce != cudaSuccess) rc = e->fail(AEGPU_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(ce));
     }
-    if (!rc && cudaGraphInstantiate(&e->grad_graph, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
-    if (!rc) {
-        e->grad_graph_def = g;
+    if (!rc && cudaGraphInstantiate(exec, g, 0) != cudaSuccess) rc = e->cuda_check("graph instantiate");
+    if (!rc && def) {
+        *def = g;
     } else if (g) {
         cudaGraphDestroy(g);
     }
     cudaStreamDestroy(cap);
     e->stream = saved;
-    e->graph_launches = e->launches - l0;
+    *nlaunch = e->launches - l0;
     e->launches = l0;
     cudaGetLastError();
     return rc;
+}
+
+int capture_grad_graph(aegpu_engine *e)
+{
+    return capture_phases(e, 0, &e->grad_graph, &e->grad_graph_def, &e->graph_launches);
+}
+
+// Replay the energy-phase (1) or adjoint-phase (2) graph on the engine's stream.
+int launch_phases(aegpu_engine *e, int kind)
+{
+    cudaGraphExec_t &g = kind == 1 ? e->energy_graph : e->back_graph;
+    int64_t &nl = kind == 1 ? e->energy_graph_launches : e->back_graph_launches;
+    if (!g) {
+        int rc = capture_phases(e, kind, &g, nullptr, &nl);
+        if (rc) return rc;
+    }
+    if (cudaGraphLaunch(g, e->stream) != cudaSuccess) return e->cuda_check("graph launch");
+    e->launches += nl;
+    return AEGPU_OK;
 }
 
 bool same_angles(const aegpu_engine *e, const double *angles)
@@ -2419,12 +2451,22 @@ int aegpu_energy(aegpu_engine *e, const double *angles, double *energy)
 {
     if (!e || !angles || !energy) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
-    int rc = ensure_state(e, angles);
-    if (rc) return rc;
-    if (!e->h_valid) {
-        rc = run_energy(e, e->d_scalar, e->nb);
+    int rc = AEGPU_OK;
+    if (e->use_graph && !e->timing && !same_angles(e, angles)) {
+        // pass constants + evolve + H psi + energy as one graph replay
+        const size_t nang = e->excs.size() * (size_t)e->nb;
+        cudaMemcpyAsync(e->d_ang, angles, nang * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+        if ((rc = launch_phases(e, 1))) return rc;
+        e->cached_angles.assign(angles, angles + nang);
+        e->psi_valid = e->h_valid = true;
+    } else {
+        rc = ensure_state(e, angles);
         if (rc) return rc;
-        e->h_valid = true;
+        if (!e->h_valid) {
+            rc = run_energy(e, e->d_scalar, e->nb);
+            if (rc) return rc;
+            e->h_valid = true;
+        }
     }
     cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "energy");
@@ -2461,7 +2503,7 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
         if (rc) return rc;
     }
     // the checkpointed sweep consumes H psi and leaves psi as it is
-    rc = run_backward(e, e->d_grad, e->nb);
+    rc = e->use_graph && !e->timing ? launch_phases(e, 2) : run_backward(e, e->d_grad, e->nb);
     if (rc) return rc;
     e->h_valid = false;
     if (energy) cudaMemcpyAsync(energy, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
