@@ -15,17 +15,17 @@
 //                      and H*tangents column-major [P+1][D*W]
 //
 // Kernels (all FP64; bandwidth- or FP64-pipe-bound, no tensor cores):
-//   k_block_rot      one pass on many vectors at once (Hessian tangents); a CTA stages
-//                    whole orbits (<= 4096 amplitudes) in shared memory and applies
-//                    every butterfly layer there (reference RunFuseN, fusedevolve.cpp:917-1774)
 //   k_warp_rot       a pass of <= 6 commuting excitations with the orbits in warp
-//                    registers (shuffles, one FMA per amplitude per layer); writes the
-//                    pass's output amplitudes as the adjoint sweep's checkpoint
+//                    registers (shuffles, one FMA per amplitude per layer; reference
+//                    RunFuseN, fusedevolve.cpp:917-1774); writes the pass's output
+//                    amplitudes as the adjoint sweep's checkpoint; the instance
+//                    dimension also carries the Hessian's tangents through a pass
 //   k_warp_adj       checkpointed adjoint pass: gradient of every excitation from the
 //                    checkpoint and H psi, then H psi rotated back (fusedevolve.cpp:461-485)
-//   k_block_tangent  forward block + tangents T_op = G_op psi (fusedevolve.cpp:492-518)
-//   k_block_hess     backward sweep of many tangents against H psi for the second-
-//                    derivative term of the Hessian (fusedevolve.cpp:2670-2761)
+//   k_block_tangent  forward block + tangents T_op = G_op psi, a CTA staging whole
+//                    orbits (<= 4096 amplitudes) in shared memory (fusedevolve.cpp:492-518)
+//   k_warp_hess      second-derivative sweep of the Hessian: every tangent against the
+//                    back-propagated H psi through a pass (fusedevolve.cpp:2670-2761)
 //   k_diag_*         the same four for diagonal (number / density-density) blocks,
 //                    complex mode (fusedevolve.cpp:625-717)
 //   k_pass_prep      per evaluation: sin/cos and the scaled-Givens constants of every
@@ -289,28 +289,6 @@ __device__ __forceinline__ void layer(double *v, const uint32_t *bits, const Til
     }
 }
 
-template <int W>
-__global__ void __launch_bounds__(kRotThreads) k_block_rot(BlockArgs a, double *vecs, size_t vstride, int nvec)
-{
-    extern __shared__ double sm[];
-    double *v = sm;
-    uint32_t *bits = (uint32_t *)(sm + kTileElems * W);
-    __shared__ ExcCode code[kMaxSlots];
-    __shared__ double C[kMaxSlots], S[kMaxSlots];
-    __shared__ int slot[kMaxSlots];
-    const TileCtx c = load_tile(a, bits, code, C, S, slot);
-    for (int vec = blockIdx.y; vec < nvec; vec += gridDim.y) {  // vectors spread over grid.y
-        double *psi = vecs + vec * vstride;
-        gather<W>(v, psi, c);
-        __syncthreads();
-        for (int i = 0; i < c.k; ++i) {
-            layer<W>(v, bits, c, i, code[i], C[i], S[i]);
-            __syncthreads();
-        }
-        scatter<W>(v, psi, c);
-        __syncthreads();
-    }
-}
 
 // Forward block that also writes the tangents T_slot = G_slot psi (after the block,
 // which equals G psi before it because the block's excitations commute).
@@ -344,66 +322,6 @@ __global__ void __launch_bounds__(kRotThreads) k_block_tangent(BlockArgs a, doub
     }
 }
 
-// Second-derivative sweeps: for every live tangent T_v (vectors [0, nvec) of T),
-// rotate (T_v, h) backward through the block and accumulate <h|G_j T_v> for the
-// block's excitations j whose application position is >= v.  h is read (not
-// written); each vector works on its own copy.  partials[(tile*nvec+v)*12+slot].
-template <int W>
-__global__ void __launch_bounds__(kRotThreads) k_block_hess(BlockArgs a, const double *h, double *T, size_t tstride,
-                                                            int nvec, int vchunk, int block_pos0, double *partials)
-{
-    extern __shared__ double sm[];
-    double *h0 = sm, *hv = sm + kTileElems * W, *v = sm + 2 * kTileElems * W;
-    uint32_t *bits = (uint32_t *)(sm + 3 * kTileElems * W);
-    __shared__ ExcCode code[kMaxSlots];
-    __shared__ double C[kMaxSlots], S[kMaxSlots];
-    __shared__ int slot[kMaxSlots];
-    __shared__ double red[kRotThreads / 32];
-    __shared__ double acc[kMaxSlots];
-    const TileCtx c = load_tile(a, bits, code, C, S, slot);
-    gather<W>(h0, h, c);
-    const int v0 = blockIdx.y * vchunk, v1 = min(nvec, v0 + vchunk);
-    for (int vec = v0; vec < v1; ++vec) {
-        double *t = T + (size_t)vec * tstride;
-        if (threadIdx.x < kMaxSlots) acc[threadIdx.x] = 0;
-        gather<W>(v, t, c);
-        for (uint32_t e = threadIdx.x; e < c.n * W; e += blockDim.x) hv[e] = h0[e];
-        __syncthreads();
-        for (int i = 0; i < c.k; ++i) {
-            const uint32_t half = c.n >> 1;
-            const double Ci = C[i], Si = S[i];
-            const bool want = block_pos0 + slot[i] >= vec;
-            double g = 0;
-            for (uint32_t p = threadIdx.x; p < half; p += blockDim.x) {
-                const uint32_t lo = insert_zero_bit(p, i), hi = lo | (1u << i);
-                const double s = exc_sign(code[i], bits[lo]);
-                const double sS = s * Si;
-                double tt = 0;
-#pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    const double x = v[lo * W + w], y = v[hi * W + w];
-                    const double hx = hv[lo * W + w], hy = hv[hi * W + w];
-                    tt = fma(hx, y, tt);
-                    tt = fma(-hy, x, tt);
-                    v[lo * W + w] = fma(sS, y, Ci * x);
-                    v[hi * W + w] = fma(-sS, x, Ci * y);
-                    hv[lo * W + w] = fma(sS, hy, Ci * hx);
-                    hv[hi * W + w] = fma(-sS, hx, Ci * hy);
-                }
-                g = fma(s, tt, g);
-            }
-            if (want) {
-                g = block_sum(g, red);
-                if (threadIdx.x == 0) acc[slot[i]] = g;
-            }
-            __syncthreads();
-        }
-        scatter<W>(v, t, c);
-        if (threadIdx.x < kMaxSlots)
-            partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + threadIdx.x] = acc[threadIdx.x];
-        __syncthreads();
-    }
-}
 
 // ------------------------------------------------ warp-register passes --
 // A pass holds <= 6 commuting excitations, so every orbit has <= 64 members and a
@@ -660,6 +578,107 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
         if (threadIdx.x < kMaxWarpLayers)
             for (int w = 0; w < kWarpThreads / 32; ++w) sum += red[threadIdx.x][w];
         partials[(size_t)b * part_stride + (size_t)blockIdx.x * kMaxSlots + threadIdx.x] = sum;
+    }
+}
+
+// Second-derivative sweep of the Hessian through one pass (evolveHessian,
+// fusedevolve.cpp:2670-2761), vector v = blockIdx.y of the tangents T: with the bra h
+// (H psi back-propagated to this pass's output, read only) every excitation j of the
+// pass at application position >= v contributes <h|G_j T_v>, taken at the pass output
+// (the pass's excitations commute), then T_v is rotated back through the pass.
+// partials[(blockIdx.x * nvec + v) * kMaxSlots + slot] (fixed-order CTA sums).
+template <int W>
+__global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
+                                                            const double *__restrict__ h, double *T, int64_t tstride,
+                                                            int nvec, int block_pos0, double *__restrict__ partials)
+{
+    __shared__ double red[kMaxWarpLayers][kWarpThreads / 32];
+    const int lane = threadIdx.x & 31, vec = blockIdx.y;
+    const PassConst *pc = a.pc;
+    const double *sig = a.sigma;
+    double *t = T + (size_t)vec * tstride;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double accS[kMaxWarpLayers];
+#pragma unroll
+    for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
+    for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < ntasks; k += nw) {
+        const WarpTask task = tasks[k];
+        const uint32_t mask = task.mask;
+        const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
+        const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
+        const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
+        const uint32_t b0 = ok0 ? obits[lane] : 0u, b1 = ok1 ? obits[lane + 32] : 0u;
+        double v0[W], v1[W], h0[W], h1[W];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            v0[w] = ok0 ? t[(size_t)z0 * W + w] : 0.0;
+            v1[w] = ok1 ? t[(size_t)z1 * W + w] : 0.0;
+            h0[w] = ok0 ? h[(size_t)z0 * W + w] : 0.0;
+            h1[w] = ok1 ? h[(size_t)z1 * W + w] : 0.0;
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j) {
+            if (!(mask & (1u << j)) || block_pos0 + j < vec) continue;
+            const int i = __popc(mask & ((1u << j) - 1u));
+            const PassConst q = pc[j];
+            const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
+            double g = 0.0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double p0, p1;
+                if (i < 5) {
+                    p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                    p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                } else {
+                    p0 = v1[w];
+                    p1 = v0[w];
+                }
+                g = fma(h0[w], flip(p0, s0), g);
+                g = fma(h1[w], flip(p1, s1), g);
+            }
+            accS[j] += g;
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxWarpLayers; ++j) {
+            if (!(mask & (1u << j))) continue;
+            const int i = __popc(mask & ((1u << j) - 1u));
+            const PassConst q = pc[j];
+            const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double p0, p1;
+                if (i < 5) {
+                    p0 = __shfl_xor_sync(0xffffffffu, v0[w], 1 << i);
+                    p1 = __shfl_xor_sync(0xffffffffu, v1[w], 1 << i);
+                } else {
+                    p0 = v1[w];
+                    p1 = v0[w];
+                }
+                v0[w] = rot_scaled(q, v0[w], p0, s0);
+                v1[w] = rot_scaled(q, v1[w], p1, s1);
+            }
+        }
+        const double sigma = sig[mask];
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            if (ok0) t[(size_t)z0 * W + w] = sigma * v0[w];
+            if (ok1) t[(size_t)z1 * W + w] = sigma * v1[w];
+        }
+    }
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < kMaxWarpLayers; ++j) {
+        double v = accS[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[j][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kMaxSlots) {
+        double sum = 0.0;
+        if (threadIdx.x < kMaxWarpLayers)
+            for (int w = 0; w < kWarpThreads / 32; ++w) sum += red[threadIdx.x][w];
+        partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + threadIdx.x] = sum;
     }
 }
 
@@ -1655,12 +1674,8 @@ int set_smem_limits(int dev)
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     auto need = [](int nv, int W) { return (size_t)kTileElems * (nv * W * 8 + 4); };
     int bad = 0;
-    bad += set_smem(k_block_rot<1>, need(1, 1), optin);
-    bad += set_smem(k_block_rot<2>, need(1, 2), optin);
     bad += set_smem(k_block_tangent<1>, need(1, 1), optin);
     bad += set_smem(k_block_tangent<2>, need(1, 2), optin);
-    bad += set_smem(k_block_hess<1>, need(3, 1), optin);
-    bad += set_smem(k_block_hess<2>, need(3, 2), optin);
     // the on-the-fly kernel's need depends on N (<= 150 KB at 14 orbitals): allow the most
     for (int W = 1; W <= 2; ++W) {
         cudaFuncAttributes fa{};
@@ -2775,6 +2790,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
     if (!proj && !e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the Hessian needs a batch size of 1");
+    if (e->excs.size() > 65535) return e->fail(AEGPU_ERR_UNSUPPORTED, "the Hessian supports at most 65535 operators");
     const int nops = (int)e->excs.size();
     const int W = e->W;
     const int64_t D = (int64_t)e->B.D;
@@ -2801,7 +2817,8 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         for (auto &pa : hs.allocs) e->release(pa.first, pa.second);
         hs = aegpu_engine::HessScratch{};
         int64_t maxpart = 0;
-        for (auto &b : e->dblocks) maxpart = std::max<int64_t>(maxpart, (int64_t)b.ntiles * nops * kMaxSlots);
+        for (auto &b : e->dblocks)
+            maxpart = std::max<int64_t>(maxpart, (int64_t)std::max(b.ntiles, b.wgrid) * nops * kMaxSlots);
         auto get = [&](auto *&ptr, size_t count) {
             using T = std::remove_reference_t<decltype(*ptr)>;
             ptr = e->alloc<T>(count);
@@ -2842,13 +2859,17 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             e->launches += 3;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args((int)bi, 1.0);
-            // earlier tangents carried through the block: one CTA per (tile, vector)
-            const dim3 gv(b.ntiles, std::min(p0, 4096));
+            // earlier tangents carried through the pass by the warp-register pass kernel:
+            // the p0 tangents are its "instances" (same angles: strides 0, no mask)
+            BlockArgs av = a;
+            av.pc_stride = av.sig_stride = 0;
+            av.active = nullptr;
+            const dim3 gv(b.wgrid, std::min(p0, 65535));
             if (W == 1) {
-                if (p0 > 0) k_block_rot<1><<<gv, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                if (p0 > 0 && b.nwtasks) k_warp_rot<1><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
                 k_block_tangent<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             } else {
-                if (p0 > 0) k_block_rot<2><<<gv, kRotThreads, e->rot_smem(1), s>>>(a, T, n, p0);
+                if (p0 > 0 && b.nwtasks) k_warp_rot<2><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
                 k_block_tangent<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             }
             e->launches += 2;
@@ -2891,23 +2912,23 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
                                                                             b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
             k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), e->d_h, 0, 1, nullptr, 0, 0);
             e->launches += 4;
-        } else if (b.ntiles) {
+        } else if (b.nwtasks) {
+            // warp-register pass kernels, adjoint direction, one vector per grid.y row
             BlockArgs a = e->block_args(bi, -1.0);
-            // vectors per CTA: enough CTAs to fill the GPU (about 4 per SM), at most 8
-            const int vchunk =
-                std::max(1, std::min(8, (int)(((int64_t)b.ntiles * nvec) / ((int64_t)e->sm_count * 4))));
-            dim3 g(b.ntiles, (nvec + vchunk - 1) / vchunk);
-            if (W == 1) {
-                k_block_hess<1><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);
-            } else {
-                k_block_hess<2><<<g, kRotThreads, e->rot_smem(3), s>>>(a, e->d_h, T, n, nvec, vchunk, p0, hpart);
-            }
-            k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, b.ntiles, nvec, b.nslots, e->d_pos_op,
-                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
+            a.pc_stride = a.sig_stride = 0;
+            a.active = nullptr;
+            const dim3 g(b.wgrid, std::min(nvec, 65535));
             if (W == 1)
-                k_block_rot<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_h, 0, 1);
+                k_warp_hess<1><<<g, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
             else
-                k_block_rot<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_h, 0, 1);
+                k_warp_hess<2><<<g, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
+            k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, b.wgrid, nvec, b.nslots, e->d_pos_op,
+                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
+            // the bra back through the pass
+            if (W == 1)
+                k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, 0, nullptr, 0);
+            else
+                k_warp_rot<2><<<b.wgrid, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, 0, nullptr, 0);
             e->launches += 3;
         }
     }
