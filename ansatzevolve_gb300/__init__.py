@@ -135,6 +135,13 @@ def lib(build_if_missing=True):
         "setIntegrals": (ctypes.c_int, [ctypes.c_int, _DP, _DP, ctypes.c_int, _P]),
         "setNuclearEnergy": (ctypes.c_int, [ctypes.c_double, _P]),
         "optimise": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+        "setRunFiles": (ctypes.c_int, [ctypes.c_char_p, _P]),
+        # run-file readers (include/aegpu_runfiles.h)
+        "aegpu_run_files_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
+        "aegpu_run_files_error": (ctypes.c_char_p, []),
+        "aegpu_run_files_sizes": (ctypes.c_int, [_P] + [_IP] * 6),
+        "aegpu_run_files_get": (ctypes.c_int, [_P, _IP, _DP, _IP, _IP, _DP, _DP, _DP, _DP]),
+        "aegpu_run_files_free": (None, [_P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -568,6 +575,20 @@ class stateAnsatzManager:
 
     def storeRunPath(self, path):
         return self.L.setRunPath(path.encode(), self.ctx) == 0
+
+    def storeRunFiles(self, prefix):
+        """The whole setup the reference's driver reads from `prefix` (initial state,
+        operators, order, nuclear energy, Hamiltonian files); returns the loaded
+        ``runfiles.RunFiles`` (its parameter_sets are the file's angle sets)."""
+        from .runfiles import load_run_files
+        rf = load_run_files(prefix)
+        if self.L.setRunFiles(prefix.encode(), self.ctx) != 0:
+            raise AegpuError("setRunFiles refused " + prefix)
+        self._nq = rf.nq
+        self._ops = [list(map(int, o)) for o in rf.operators]
+        self._order = [(int(p), float(c)) for p, c in zip(rf.order, rf.scale)]
+        self._P = rf.n_params
+        return rf
 
     def storeIntegrals(self, h1, g2, mode=HAM_AUTO):
         h1 = _f64(h1)

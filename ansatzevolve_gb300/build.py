@@ -13,7 +13,7 @@ OUT = os.path.join(HERE, "libansatzevolve_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["engine.cu", "mlp.cu"]
-CPP = ["setup.cpp", "otf_tables.cpp", "manager.cpp", "newton.cpp", "interface.cpp", "optimise.cpp"]
+CPP = ["setup.cpp", "otf_tables.cpp", "manager.cpp", "newton.cpp", "interface.cpp", "optimise.cpp", "runfiles.cpp"]
 
 
 def _nvcc():
@@ -32,7 +32,7 @@ def _run(cmd):
 
 def sources():
     return [os.path.join(CSRC, f) for f in CU + CPP] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")] + \
-        [os.path.join(HERE, "..", "include", h) for h in ("aegpu.h", "AnsatzSynthInterface.h")]
+        [os.path.join(HERE, "..", "include", h) for h in ("aegpu.h", "AnsatzSynthInterface.h", "aegpu_runfiles.h")]
 
 
 def up_to_date():

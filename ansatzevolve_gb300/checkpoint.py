@@ -7,15 +7,16 @@ import numpy as np
 
 def write_parameters(path, angle_sets, energies=None):
     """One block per angle set: the count, an 'Energy of minimum k= E' line (the
-    reference reads the number after '='), then one angle per line."""
+    reference reads the number after '='), then one angle per line, each number with
+    17 significant digits so that it reads back exactly."""
     sets = [np.asarray(a, dtype=np.float64).ravel() for a in np.atleast_2d(angle_sets)]
     with open(path, "w") as f:
         for k, a in enumerate(sets):
             E = 0.0 if energies is None else float(np.atleast_1d(energies)[k])
             f.write("%d\n" % a.size)
-            f.write("Energy of minimum %6d=  %.15f written by ansatzevolve_gb300\n" % (k + 1, E))
+            f.write("Energy of minimum %6d=  %.17g written by ansatzevolve_gb300\n" % (k + 1, E))
             for v in a:
-                f.write("%.15f\n" % v)
+                f.write("%.17g\n" % v)
 
 
 def read_parameters(path):

@@ -2,6 +2,7 @@
 // stateAnsatzManager: same argument checks, index conventions and return codes.
 #include "../../include/AnsatzSynthInterface.h"
 #include "manager.h"
+#include "runfiles.h"
 
 #include <cstdio>
 #include <cstring>
@@ -10,6 +11,9 @@
 
 using ae::log_line;
 using ae::stateAnsatzManager;
+using ae::RunFiles;
+using ae::loadRunFiles;
+using ae::storeRunFiles;
 
 static bool traceInterfaceCalls = false;
 
@@ -281,6 +285,21 @@ int optimise(int NAngles, double *angles, double *energy, void *ctx)
     if (NAngles == m->numberOfParameters())
         memcpy(angles, x.data(), x.size() * sizeof(double));
     if (energy && !m->getExpectationValue(*energy)) return 3;
+    return 0;
+}
+
+int setRunFiles(const char *prefix, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (!prefix || !*prefix) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    RunFiles rf;
+    std::string err;
+    if (!loadRunFiles(prefix, false, rf, err) || !storeRunFiles(*m, rf, prefix, err)) {
+        log_line("setRunFiles: " + err);
+        return 3;
+    }
     return 0;
 }
 

@@ -53,11 +53,16 @@ void setTraceInterfaceCalls(int val);
  * setNuclearEnergy -- constant added to every energy
  * optimise         -- Newton-Raphson from the current angles; writes the optimised
  *                     compressed angles and energy
+ * setRunFiles      -- the whole setup the reference's command-line driver reads from a
+ *                     path prefix (src/main.cpp:235-386): <prefix>_Initial.dat,
+ *                     _Operators.dat, _Order.dat, _Nuclear_Energy.dat (if present) and
+ *                     the Hamiltonian files of setRunPath (formats: aegpu_runfiles.h)
  * All return 0 on success, 1 for a null handle, 2 for bad arguments, 3 on failure. */
 int setRunPath(const char *path, void *ctx);
 int setIntegrals(int norb, const double *h1, const double *g2, int mode, void *ctx);
 int setNuclearEnergy(double e, void *ctx);
 int optimise(int nangles, double *angles, double *energy, void *ctx);
+int setRunFiles(const char *prefix, void *ctx);
 
 #ifdef __cplusplus
 }

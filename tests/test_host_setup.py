@@ -83,7 +83,7 @@ def test_orbit_tables_reproduce_sequential_rotations(N, na, nb):
 
 def _declared_symbols():
     names = set()
-    for h in ("aegpu.h", "AnsatzSynthInterface.h"):
+    for h in sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")):
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]+?\b(\w+)\s*\(", src, flags=re.M):
