@@ -21,6 +21,16 @@ _LIB = None
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
 TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR = 1, 2, 3, 4
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
+PROP_HESSIAN, PROP_OVERLAP = 1, 2
+# rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)
+PROPERTY_NAMES = ("Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
+                  "NumberOfNegativeHessianEValues", "NumberOfNearZeroHessianEValues",
+                  "NumberOfPositiveHessianEValues", "NumberOfNegativeHessianDiagValues",
+                  "NumberOfNearZeroHessianDiagValues", "NumberOfPositiveHessianDiagValues",
+                  "NumberOfPositiveMetricEValues", "NumberOfZeroMetricEValues", "NumberOfZeroMetricDiagonalValues",
+                  "NormOfGradVector", "OverlapWithState_0 (re)", "OverlapWithState_0 (im)",
+                  "MagOfOverlapWithState_0")
+PROPERTY_ROWS = len(PROPERTY_NAMES)
 
 _P = ctypes.c_void_p
 _DP = ctypes.POINTER(ctypes.c_double)
@@ -99,6 +109,17 @@ def lib(build_if_missing=True):
         "aegpu_apply_h": (ctypes.c_int, [_P, _DP, _DP]),
         "aegpu_gradient_proj": (ctypes.c_int, [_P, _DP, _DP, _DP, _DP]),
         "aegpu_hessian_proj": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, _DP, _DP, _DP, _DP]),
+        "aegpu_hessian_metric": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, _DP, _DP, _DP, _DP]),
+        "aegpu_lowest_eigenpair": (ctypes.c_int, [_P, ctypes.c_double, ctypes.c_int, ctypes.c_int, _DP, _DP, _IP]),
+        "aegpu_ground_state": (ctypes.c_int, [_P, _DP]),
+        "aegpu_ground_overlap": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_real_energy": (ctypes.c_int, [_P, _DP, _DP]),
+        "aegpu_subspace_matrices": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, _DP, _DP, _DP]),
+        "aegpu_subspace_eigenvalues": (ctypes.c_int, [_P, ctypes.c_int, _DP, _DP, _IP]),
+        "aegpu_host_tridiag_lowest": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP, _DP]),
+        "aegpu_host_subspace_eigenvalues": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _DP, _DP, _DP, _IP]),
+        "aegpu_path_properties": (ctypes.c_int, [_P, _DP, _IP, _DP, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                 _DP, _DP, _DP]),
         "aegpu_gradient_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
         "aegpu_energy_dev": (ctypes.c_int, [_P, _P, _P, _P]),
         "aegpu_state_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
@@ -136,6 +157,9 @@ def lib(build_if_missing=True):
         "setNuclearEnergy": (ctypes.c_int, [ctypes.c_double, _P]),
         "optimise": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
         "setRunFiles": (ctypes.c_int, [ctypes.c_char_p, _P]),
+        "getProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
+        "getLowestEigenvalue": (ctypes.c_int, [_DP, _DP, _P]),
+        "getSubspaceEigenvalues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _IP, _P]),
         # run-file readers (include/aegpu_runfiles.h)
         "aegpu_run_files_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
         "aegpu_run_files_error": (ctypes.c_char_p, []),
@@ -322,6 +346,78 @@ class Engine:
         self._check(self.L.aegpu_hessian_proj(self.h, dptr(a), iptr(p), dptr(s), P, dptr(pr), dptr(ov), dptr(g),
                                               dptr(H)))
         return ov[0], g, H
+
+    def hessian_metric(self, angles_ops, param0, scale):
+        """(E, gradient, Hessian, metric Re(T_C^dagger T_C)) in the compressed parameters."""
+        a = _f64(angles_ops)
+        p = _i32(param0)
+        s = _f64(scale)
+        P = int(p.max()) + 1
+        E = np.zeros(1)
+        g = np.zeros(P)
+        H = np.zeros((P, P))
+        M = np.zeros((P, P))
+        self._check(self.L.aegpu_hessian_metric(self.h, dptr(a), iptr(p), dptr(s), P, dptr(E), dptr(g), dptr(H),
+                                                dptr(M)))
+        return E[0], g, H, M
+
+    def lowest_eigenpair(self, tol=1e-8, basis=100, max_products=5000):
+        """(eigenvalue, residual ||H v - lambda v||, H products) of the lowest eigenpair of
+        H in the sector, by Lanczos from the initial state; the eigenvector stays on the
+        device (ground_state, ground_overlap)."""
+        lam, res = np.zeros(1), np.zeros(1)
+        nprod = ctypes.c_int()
+        self._check(self.L.aegpu_lowest_eigenpair(self.h, float(tol), int(basis), int(max_products), dptr(lam),
+                                                  dptr(res), ctypes.byref(nprod)))
+        return lam[0], res[0], nprod.value
+
+    def ground_state(self):
+        v = np.zeros(self.D * self.W)
+        self._check(self.L.aegpu_ground_state(self.h, dptr(v)))
+        return v if self.W == 1 else v[0::2] + 1j * v[1::2]
+
+    def ground_overlap(self, angles_ops):
+        """<psi(angles)|v> with the lowest eigenvector (complex)."""
+        ov = np.zeros(2)
+        self._check(self.L.aegpu_ground_overlap(self.h, dptr(self._angles(angles_ops)), dptr(ov)))
+        return complex(ov[0], ov[1])
+
+    def real_energy(self, angles_ops):
+        out = np.zeros(1)
+        self._check(self.L.aegpu_real_energy(self.h, dptr(self._angles(angles_ops)), dptr(out)))
+        return out[0]
+
+    def subspace_matrices(self, angle_sets_ops):
+        """(H, S): <psi_i|H|psi_j> and <psi_i|psi_j> of the states of the angle sets
+        (complex arrays)."""
+        a = _f64(np.atleast_2d(angle_sets_ops))
+        n = a.shape[0]
+        hr, hi, sr, si = (np.zeros((n, n)) for _ in range(4))
+        self._check(self.L.aegpu_subspace_matrices(self.h, n, dptr(a), dptr(hr), dptr(hi), dptr(sr), dptr(si)))
+        return hr + 1j * hi, sr + 1j * si
+
+    def subspace_eigenvalues(self, angle_sets_ops):
+        """(eigenvalues of S^-1/2 H S^-1/2, dimension of S's null space)."""
+        a = _f64(np.atleast_2d(angle_sets_ops))
+        w = np.zeros(a.shape[0])
+        nr = ctypes.c_int()
+        self._check(self.L.aegpu_subspace_eigenvalues(self.h, a.shape[0], dptr(a), dptr(w), ctypes.byref(nr)))
+        return w, nr.value
+
+    def path_properties(self, angles_ops, param0, scale, nuclear_energy=0.0, hessian=True, overlap=False):
+        """One path's row of the properties table (PROPERTY_NAMES order, NaN where not
+        computed), plus the Hessian and metric when `hessian`."""
+        a = self._angles(angles_ops)
+        p = _i32(param0)
+        s = _f64(scale)
+        P = int(p.max()) + 1
+        row = np.zeros(PROPERTY_ROWS)
+        H = np.zeros((P, P))
+        M = np.zeros((P, P))
+        flags = (PROP_HESSIAN if hessian else 0) | (PROP_OVERLAP if overlap else 0)
+        self._check(self.L.aegpu_path_properties(self.h, dptr(a), iptr(p), dptr(s), P, float(nuclear_energy), flags,
+                                                 dptr(row), dptr(H), dptr(M)))
+        return row, (H if hessian else None), (M if hessian else None)
 
     def apply_h(self, x):
         x = _f64(x)
@@ -633,6 +729,34 @@ class stateAnsatzManager:
 
     def getExpectationValues(self, angles):
         return np.array([self.getExpectationValue(row) for row in np.atleast_2d(angles)])
+
+    def getProperties(self, paths, hessian=True, overlap=True):
+        """writeProperties' table: {row name: values per path} (PROPERTY_NAMES rows, NaN
+        where not computed)."""
+        a = _f64(np.atleast_2d(paths))
+        t = np.zeros((a.shape[0], PROPERTY_ROWS))
+        flags = (PROP_HESSIAN if hessian else 0) | (PROP_OVERLAP if overlap else 0)
+        rc = self.L.getProperties(a.shape[0], a.shape[1], dptr(a), flags, dptr(t), self.ctx)
+        if rc:
+            raise AegpuError("getProperties returned %d" % rc)
+        return {name: t[:, k] for k, name in enumerate(PROPERTY_NAMES)}
+
+    def getLowestEigenvalue(self):
+        """(lowest eigenvalue of H in the sector, without the nuclear energy; residual)."""
+        E, r = np.zeros(1), np.zeros(1)
+        rc = self.L.getLowestEigenvalue(dptr(E), dptr(r), self.ctx)
+        if rc:
+            raise AegpuError("getLowestEigenvalue returned %d" % rc)
+        return E[0], r[0]
+
+    def getSubspaceEigenvalues(self, paths):
+        a = _f64(np.atleast_2d(paths))
+        w = np.zeros(a.shape[0])
+        nr = ctypes.c_int()
+        rc = self.L.getSubspaceEigenvalues(a.shape[0], a.shape[1], dptr(a), dptr(w), ctypes.byref(nr), self.ctx)
+        if rc:
+            raise AegpuError("getSubspaceEigenvalues returned %d" % rc)
+        return w, nr.value
 
     def optimise(self, angles):
         a = _f64(angles).copy()

@@ -41,6 +41,7 @@
 // from run to run.
 #include "../../include/aegpu.h"
 #include "exc_rule.h"
+#include "newton.h"
 #include "otf_tables.h"
 #include "setup.h"
 
@@ -54,6 +55,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -1464,10 +1466,16 @@ struct aegpu_engine {
     struct HessScratch {
         int V = 0;
         double *T = nullptr, *TC = nullptr, *HTC = nullptr, *THT = nullptr, *Hops = nullptr, *hpart = nullptr;
+        double *MET = nullptr;  // metric of the compressed tangents
         int *pptr = nullptr, *ppos = nullptr;
         double *pscale = nullptr;
         std::vector<std::pair<void *, size_t>> allocs;
     } hess;
+
+    // lowest eigenpair of H (aegpu_lowest_eigenpair), valid until H is replaced
+    double *d_ground = nullptr;
+    double ground_value = 0.0;
+    bool ground_valid = false;
 
     // state caching: psi / hpsi valid for these angles
     std::vector<double> cached_angles;
@@ -1582,6 +1590,7 @@ struct aegpu_engine {
         d_h1 = d_g2 = nullptr;
         drop_graph();
         h_valid = false;
+        ground_valid = false;
     }
     void drop_graph()
     {
@@ -2783,8 +2792,17 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
 // or projected Hessian of <proj|psi(theta)> (FusedEvolve::evolveHessianProj,
 // fusedevolve.cpp:2882-3183: no T^T H T term, second-derivative sweeps against the
 // fixed bra, factor 1); energy receives <psi|H psi> or <proj|psi>.
+static int ensure_cublas(aegpu_engine *e)
+{
+    if (!e->cublas && cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS)
+        return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
+    cublasSetStream(e->cublas, e->stream);
+    return AEGPU_OK;
+}
+
 static int hessian_impl(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
-                        const double *proj, double *energy, double *grad_comp, double *hess_comp)
+                        const double *proj, double *energy, double *grad_comp, double *hess_comp,
+                        double *metric = nullptr)
 {
     NvtxRange r(proj ? "aegpu projected Hessian" : "aegpu Hessian");
     if (!e || !angles || !param || !scale || nparams < 1 || !hess_comp) return AEGPU_ERR_ARG;
@@ -2826,6 +2844,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             return ptr != nullptr;
         };
         bool ok = get(hs.T, n * nops) && get(hs.TC, n * V) && get(hs.HTC, n * V) && get(hs.THT, (size_t)V * V) &&
+                  get(hs.MET, (size_t)V * V) &&
                   get(hs.Hops, (size_t)nops * nops) && get(hs.hpart, maxpart) && get(hs.pptr, (size_t)nparams + 1) &&
                   get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops);
         if (!ok) {
@@ -2879,11 +2898,15 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     //    of them as one batched product, Gram matrix 2 T_C^T H T_C
     k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
     e->launches += 1;
-    if (!e->cublas) {
-        if (cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS) return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
-    }
-    cublasSetStream(e->cublas, s);
+    if ((rc = ensure_cublas(e))) return rc;
     const int DW = (int)(D * W);
+    if (metric) {
+        // g = Re(T_C^dagger T_C) over the P tangent columns (tupsquantities.cpp:386-389):
+        // with re / im interleaved the real dot product over D*W entries is Re(a^dagger b)
+        const double one = 1.0, zero = 0.0;
+        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nparams, nparams, DW, &one, TC, DW, TC, DW, &zero, hs.MET,
+                    nparams);
+    }
     if (proj) {
         // projected: <proj|T_C v> for every column (the last is <proj|psi>), bra for the sweeps
         cudaMemcpyAsync(e->d_h, proj, n * sizeof(double), cudaMemcpyHostToDevice, s);
@@ -2934,6 +2957,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     }
     std::vector<double> hops((size_t)nops * nops), tht((size_t)V * V);
     cudaMemcpyAsync(hops.data(), Hops, hops.size() * 8, cudaMemcpyDeviceToHost, s);
+    if (metric) cudaMemcpyAsync(metric, hs.MET, (size_t)nparams * nparams * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(tht.data(), THT, (proj ? (size_t)V : tht.size()) * 8, cudaMemcpyDeviceToHost, s);
     rc = stream_sync(e, "hessian");
     e->psi_valid = e->h_valid = false;
@@ -2974,6 +2998,266 @@ int aegpu_hessian_proj(aegpu_engine *e, const double *angles, const int *param, 
 {
     if (!proj) return AEGPU_ERR_ARG;
     return hessian_impl(e, angles, param, scale, nparams, proj, overlap, grad_comp, hess_comp);
+}
+
+int aegpu_hessian_metric(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                         double *energy, double *grad_comp, double *hess_comp, double *metric)
+{
+    if (!metric) return AEGPU_ERR_ARG;
+    return hessian_impl(e, angles, param, scale, nparams, nullptr, energy, grad_comp, hess_comp, metric);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ properties --
+// The quantities TUPSQuantities::writeProperties and doSubspaceDiagonalisation report
+// (tupsquantities.cpp:185-568, 1600-1769): the lowest eigenpair of H, overlaps of
+// evolved states with it, and the Hamiltonian / overlap matrices of a set of states.
+
+extern "C" {
+
+int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
+                           double *residual, int *products)
+{
+    NvtxRange r("aegpu lowest eigenpair");
+    if (!e || !eigenvalue || !(tol > 0) || basis < 2 || max_products < 2) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the ground state needs a batch size of 1");
+    const size_t n = e->vec_elems();
+    if (n > (size_t)std::numeric_limits<int>::max()) return e->fail(AEGPU_ERR_UNSUPPORTED, "vector too long");
+    const int m = (int)std::min<size_t>((size_t)basis, n);
+    int rc = ensure_cublas(e);
+    if (rc) return rc;
+    e->ground_valid = false;
+    if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
+    double *Vb = e->alloc<double>((size_t)(m + 1) * n);
+    double *d_c = e->alloc<double>((size_t)m + 1);
+    auto release = [&] {
+        e->release(Vb, (size_t)(m + 1) * n * sizeof(double));
+        e->release(d_c, (size_t)(m + 1) * sizeof(double));
+    };
+    if (!Vb || !d_c) {
+        release();
+        return e->fail(AEGPU_ERR_NOMEM, "Lanczos basis allocation failed");
+    }
+    cublasHandle_t h = e->cublas;
+    cudaStream_t s = e->stream;
+    const int ni = (int)n;
+    const double one = 1.0, zero = 0.0, mone = -1.0;
+    // Lanczos with full reorthogonalisation from the initial state, restarted from the
+    // Ritz vector when the basis is full
+    cudaMemcpyAsync(e->d_ground, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    int prod = 0;
+    bool done = false;
+    std::vector<double> al, be, sv;
+    while (!done) {
+        double nx = 0.0;
+        cublasDnrm2(h, ni, e->d_ground, 1, &nx);
+        if (!(nx > 0.0)) {
+            release();
+            return e->fail(AEGPU_ERR_STATE, "the start vector is zero");
+        }
+        cudaMemcpyAsync(Vb, e->d_ground, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        const double inx = 1.0 / nx;
+        cublasDscal(h, ni, &inx, Vb, 1);
+        al.clear();
+        be.clear();
+        int k = 0;
+        for (int j = 0; j < m; ++j) {
+            double *v = Vb + (size_t)j * n, *w = Vb + (size_t)(j + 1) * n;
+            if ((rc = run_apply(e, v, w, nullptr, 1, nullptr, false))) {
+                release();
+                return rc;
+            }
+            ++prod;
+            double a = 0.0, b = 0.0;
+            cublasDdot(h, ni, v, 1, w, 1, &a);
+            const double ma = -a;
+            cublasDaxpy(h, ni, &ma, v, 1, w, 1);
+            if (j > 0) {
+                const double mb = -be[j - 1];
+                cublasDaxpy(h, ni, &mb, Vb + (size_t)(j - 1) * n, 1, w, 1);
+            }
+            for (int pass = 0; pass < 2; ++pass) {
+                cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, &one, Vb, ni, w, 1, &zero, d_c, 1);
+                cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, &mone, Vb, ni, d_c, 1, &one, w, 1);
+            }
+            cublasDnrm2(h, ni, w, 1, &b);
+            al.push_back(a);
+            be.push_back(b);
+            k = j + 1;
+            const double theta = ae::tridiag_lowest(al, be, k, sv);
+            const double est = std::abs(b * sv[k - 1]);
+            if (est <= 0.5 * tol || prod >= max_products || k == ni || !(b > 1e-300)) {
+                done = true;
+                break;
+            }
+            (void)theta;
+            const double ib = 1.0 / b;
+            cublasDscal(h, ni, &ib, w, 1);
+        }
+        // Ritz vector: x = V s (restart vector, or the result)
+        cudaMemcpyAsync(d_c, sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
+        cublasDgemv(h, CUBLAS_OP_N, ni, k, &one, Vb, ni, d_c, 1, &zero, e->d_ground, 1);
+        if ((rc = stream_sync(e, "Lanczos"))) {
+            release();
+            return rc;
+        }
+    }
+    // unit norm, <start|x> >= 0, and the Rayleigh quotient and true residual
+    double nx = 0.0, ov = 0.0, lam = 0.0, res = 0.0;
+    cublasDnrm2(h, ni, e->d_ground, 1, &nx);
+    cublasDdot(h, ni, e->d_start, 1, e->d_ground, 1, &ov);
+    const double f = (ov < 0 ? -1.0 : 1.0) / nx;
+    cublasDscal(h, ni, &f, e->d_ground, 1);
+    double *w = Vb;
+    if ((rc = run_apply(e, e->d_ground, w, nullptr, 1, nullptr, false))) {
+        release();
+        return rc;
+    }
+    ++prod;
+    cublasDdot(h, ni, e->d_ground, 1, w, 1, &lam);
+    const double ml = -lam;
+    cublasDaxpy(h, ni, &ml, e->d_ground, 1, w, 1);
+    cublasDnrm2(h, ni, w, 1, &res);
+    rc = stream_sync(e, "Lanczos");
+    release();
+    if (rc) return rc;
+    e->ground_value = lam;
+    e->ground_valid = true;
+    *eigenvalue = lam;
+    if (residual) *residual = res;
+    if (products) *products = prod;
+    return AEGPU_OK;
+}
+
+int aegpu_ground_state(aegpu_engine *e, double *state)
+{
+    if (!e || !state) return AEGPU_ERR_ARG;
+    if (!e->ground_valid) return e->fail(AEGPU_ERR_STATE, "no ground state: call aegpu_lowest_eigenpair first");
+    cudaMemcpyAsync(state, e->d_ground, e->vec_elems() * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+    return stream_sync(e, "ground state");
+}
+
+int aegpu_ground_overlap(aegpu_engine *e, const double *angles, double *overlap)
+{
+    NvtxRange r("aegpu ground overlap");
+    if (!e || !angles || !overlap) return AEGPU_ERR_ARG;
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "overlaps need a batch size of 1");
+    if (!e->ground_valid) return e->fail(AEGPU_ERR_STATE, "no ground state: call aegpu_lowest_eigenpair first");
+    int rc = ensure_state(e, angles);
+    if (!rc) rc = ensure_cublas(e);
+    if (rc) return rc;
+    const int64_t D = (int64_t)e->B.D;
+    if (e->W == 1) {
+        cublasDdot(e->cublas, (int)D, e->d_psi, 1, e->d_ground, 1, &overlap[0]);
+        overlap[1] = 0.0;
+    } else {
+        cuDoubleComplex z;
+        cublasZdotc(e->cublas, (int)D, (const cuDoubleComplex *)e->d_psi, 1, (const cuDoubleComplex *)e->d_ground, 1, &z);
+        overlap[0] = cuCreal(z);
+        overlap[1] = cuCimag(z);
+    }
+    return stream_sync(e, "ground overlap");
+}
+
+int aegpu_real_energy(aegpu_engine *e, const double *angles, double *real_energy)
+{
+    if (!e || !angles || !real_energy) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the real-part energy needs a batch size of 1");
+    int rc = ensure_state(e, angles);
+    if (!rc && !e->h_valid) {
+        rc = run_energy(e, e->d_scalar, 1);
+        if (!rc) e->h_valid = true;
+    }
+    if (!rc) rc = ensure_cublas(e);
+    if (rc) return rc;
+    const int n = (int)e->B.D, inc = e->W;
+    // H is real, so Re(H psi) = H Re(psi): <r|H r> / <r|r> from the even (real) entries
+    double rhr = 0.0, rr = 0.0;
+    cublasDdot(e->cublas, n, e->d_psi, inc, e->d_h, inc, &rhr);
+    cublasDdot(e->cublas, n, e->d_psi, inc, e->d_psi, inc, &rr);
+    if ((rc = stream_sync(e, "real-part energy"))) return rc;
+    *real_energy = rhr / rr;
+    return AEGPU_OK;
+}
+
+int aegpu_subspace_matrices(aegpu_engine *e, int nsets, const double *angles, double *h_re, double *h_im, double *s_re,
+                            double *s_im)
+{
+    NvtxRange r("aegpu subspace matrices");
+    if (!e || nsets < 1 || nsets > 65535 || !angles || !h_re || !s_re) return AEGPU_ERR_ARG;
+    if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "subspace matrices need a batch size of 1");
+    const size_t n = e->vec_elems(), nops = e->excs.size();
+    if (n * (size_t)e->W > (size_t)std::numeric_limits<int>::max()) return e->fail(AEGPU_ERR_UNSUPPORTED, "vector too long");
+    int rc = ensure_cublas(e);
+    if (rc) return rc;
+    double *Psi = e->alloc<double>(n * nsets), *HPsi = e->alloc<double>(n * nsets), *M = e->alloc<double>((size_t)4 * nsets * nsets);
+    auto release = [&] {
+        e->release(Psi, n * nsets * sizeof(double));
+        e->release(HPsi, n * nsets * sizeof(double));
+        e->release(M, (size_t)4 * nsets * nsets * sizeof(double));
+    };
+    if (!Psi || !HPsi || !M) {
+        release();
+        return e->fail(AEGPU_ERR_NOMEM, "subspace buffers allocation failed");
+    }
+    cudaStream_t s = e->stream;
+    // the evolved states as columns, then H on all of them as one batched product
+    for (int k = 0; k < nsets; ++k) {
+        if ((rc = upload_angles(e, angles + (size_t)k * nops, true, 1, false)) || (rc = run_evolve(e, 1))) {
+            release();
+            return rc;
+        }
+        cudaMemcpyAsync(Psi + (size_t)k * n, e->d_psi, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    }
+    e->psi_valid = e->h_valid = false;
+    e->cached_angles.clear();
+    if ((rc = run_apply(e, Psi, HPsi, nullptr, nsets, nullptr, false))) {
+        release();
+        return rc;
+    }
+    const size_t nn = (size_t)nsets * nsets;
+    if (e->W == 1) {
+        const double one = 1.0, zero = 0.0;
+        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nsets, nsets, (int)n, &one, Psi, (int)n, HPsi, (int)n, &zero, M,
+                    nsets);
+        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nsets, nsets, (int)n, &one, Psi, (int)n, Psi, (int)n, &zero,
+                    M + nn, nsets);
+    } else {
+        // <psi_i|H psi_j> and <psi_i|psi_j> as complex products (conjugate transpose)
+        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+        const int D = (int)e->B.D;
+        cuDoubleComplex *Mz = (cuDoubleComplex *)M;
+        cublasZgemm(e->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nsets, nsets, D, &one, (const cuDoubleComplex *)Psi, D,
+                    (const cuDoubleComplex *)HPsi, D, &zero, Mz, nsets);
+        cublasZgemm(e->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nsets, nsets, D, &one, (const cuDoubleComplex *)Psi, D,
+                    (const cuDoubleComplex *)Psi, D, &zero, Mz + nn, nsets);
+    }
+    std::vector<double> hm((size_t)4 * nn);
+    cudaMemcpyAsync(hm.data(), M, hm.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+    rc = stream_sync(e, "subspace matrices");
+    release();
+    if (rc) return rc;
+    // column-major (i, j) -> row-major out[i * nsets + j]
+    for (int i = 0; i < nsets; ++i)
+        for (int j = 0; j < nsets; ++j) {
+            const size_t cm = (size_t)j * nsets + i, rm = (size_t)i * nsets + j;
+            if (e->W == 1) {
+                h_re[rm] = hm[cm];
+                s_re[rm] = hm[nn + cm];
+                if (h_im) h_im[rm] = 0.0;
+                if (s_im) s_im[rm] = 0.0;
+            } else {
+                h_re[rm] = hm[2 * cm];
+                s_re[rm] = hm[2 * (nn + cm)];
+                if (h_im) h_im[rm] = hm[2 * cm + 1];
+                if (s_im) s_im[rm] = hm[2 * (nn + cm) + 1];
+            }
+        }
+    return AEGPU_OK;
 }
 
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream)

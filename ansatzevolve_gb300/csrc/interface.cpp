@@ -288,6 +288,54 @@ int optimise(int NAngles, double *angles, double *energy, void *ctx)
     return 0;
 }
 
+static bool angle_rows(int npaths, int nangles, const double *angles, std::vector<std::vector<double>> &rows)
+{
+    if (npaths < 1 || nangles < 1 || !angles) return false;
+    rows.clear();
+    for (int k = 0; k < npaths; ++k) rows.emplace_back(angles + (size_t)k * nangles, angles + (size_t)(k + 1) * nangles);
+    return true;
+}
+
+int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    std::vector<std::vector<double>> rows;
+    if (!table || !angle_rows(npaths, nangles, angles, rows)) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> t;
+    if (!m->getProperties(rows, flags, t)) return 3;
+    std::copy(t.begin(), t.end(), table);
+    return 0;
+}
+
+int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (!eigenvalue) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    double res = 0;
+    if (!m->getLowestEigenvalue(*eigenvalue, res)) return 3;
+    if (residual) *residual = res;
+    return 0;
+}
+
+int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    std::vector<std::vector<double>> rows;
+    if (!eigenvalues || !angle_rows(npaths, nangles, angles, rows)) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> w;
+    int nr = 0;
+    if (!m->getSubspaceEigenvalues(rows, w, nr)) return 3;
+    std::copy(w.begin(), w.end(), eigenvalues);
+    if (nullRank) *nullRank = nr;
+    return 0;
+}
+
 int setRunFiles(const char *prefix, void *ctx)
 {
     if (ctx == nullptr) return 1;

@@ -564,6 +564,67 @@ bool stateAnsatzManager::getExpectationValues(const std::vector<double> &angles,
     return evolveIfNeeded();
 }
 
+bool stateAnsatzManager::getLowestEigenvalue(double &eigenvalue, double &residual, double tol)
+{
+    if (!validateToRun()) return false;
+    // the Hamiltonian is fixed once constructed: one Lanczos run per tolerance
+    if (!m_haveGround || tol < m_groundTol) {
+        int products = 0;
+        int rc = aegpu_lowest_eigenpair(m_engine, tol, 100, 100000, &m_groundE, &m_groundRes, &products);
+        if (rc) { log_line(std::string("lowest eigenpair failed: ") + aegpu_last_error(m_engine)); return false; }
+        if (m_groundRes > tol) log_line("lowest eigenpair: residual " + std::to_string(m_groundRes) + " above the tolerance");
+        m_haveGround = true;
+        m_groundTol = tol;
+    }
+    eigenvalue = m_groundE;
+    residual = m_groundRes;
+    return true;
+}
+
+bool stateAnsatzManager::getProperties(const std::vector<std::vector<double>> &paths, int flags, std::vector<double> &table,
+                                       std::vector<std::vector<double>> *hessians,
+                                       std::vector<std::vector<double>> *metrics)
+{
+    if (!validateToRun()) return false;
+    if (flags & AEGPU_PROP_OVERLAP) {
+        double lam = 0, res = 0;
+        if (!getLowestEigenvalue(lam, res)) return false;
+    }
+    const size_t P = (size_t)m_numberOfUniqueParameters;
+    table.assign(paths.size() * AEGPU_PROPERTY_ROWS, 0.0);
+    if (hessians) hessians->assign(paths.size(), std::vector<double>(P * P));
+    if (metrics) metrics->assign(paths.size(), std::vector<double>(P * P));
+    for (size_t k = 0; k < paths.size(); ++k) {
+        std::vector<double> a;
+        if (!decompress(paths[k], a)) return false;
+        int rc = aegpu_path_properties(m_engine, a.data(), m_param.data(), m_scale.data(), (int)P, m_nuclearEnergy, flags,
+                                       &table[k * AEGPU_PROPERTY_ROWS], hessians ? (*hessians)[k].data() : nullptr,
+                                       metrics ? (*metrics)[k].data() : nullptr);
+        if (rc) { log_line(std::string("properties failed: ") + aegpu_last_error(m_engine)); return false; }
+    }
+    m_haveEvolved = false;
+    return evolveIfNeeded();
+}
+
+bool stateAnsatzManager::getSubspaceEigenvalues(const std::vector<std::vector<double>> &paths, std::vector<double> &eigs,
+                                                int &nullRank)
+{
+    if (!validateToRun()) return false;
+    if (paths.empty()) { log_line("no paths given"); return false; }
+    const size_t nops = m_excitations.size();
+    std::vector<double> all(paths.size() * nops);
+    for (size_t k = 0; k < paths.size(); ++k) {
+        std::vector<double> a;
+        if (!decompress(paths[k], a)) return false;
+        std::copy(a.begin(), a.end(), all.begin() + k * nops);
+    }
+    eigs.assign(paths.size(), 0.0);
+    int rc = aegpu_subspace_eigenvalues(m_engine, (int)paths.size(), all.data(), eigs.data(), &nullRank);
+    if (rc) { log_line(std::string("subspace diagonalisation failed: ") + aegpu_last_error(m_engine)); return false; }
+    m_haveEvolved = false;
+    return evolveIfNeeded();
+}
+
 }  // namespace ae
 
 #include "newton.h"

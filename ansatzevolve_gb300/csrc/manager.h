@@ -60,6 +60,19 @@ public:
     // Newton-Raphson with cubic backtracking (TUPSQuantities::OptimiseTups).
     bool optimise();
 
+    // TUPSQuantities::writeProperties (tupsquantities.cpp:185-568): one row of
+    // AEGPU_PROPERTY_ROWS values per path (compressed or per-operator angles), flags
+    // AEGPU_PROP_HESSIAN / AEGPU_PROP_OVERLAP; the overlap rows use the lowest eigenvector,
+    // computed first when needed.  Hessians / metrics (optional) per path, row-major.
+    bool getProperties(const std::vector<std::vector<double>> &paths, int flags, std::vector<double> &table,
+                       std::vector<std::vector<double>> *hessians = nullptr,
+                       std::vector<std::vector<double>> *metrics = nullptr);
+    // Lowest eigenvalue of H in the sector (electronic, without the nuclear energy).
+    bool getLowestEigenvalue(double &eigenvalue, double &residual, double tol = 1e-10);
+    // TUPSQuantities::doSubspaceDiagonalisation (tupsquantities.cpp:1600-1700).
+    bool getSubspaceEigenvalues(const std::vector<std::vector<double>> &paths, std::vector<double> &eigenvalues,
+                                int &nullRank);
+
     // introspection (not in the reference API)
     int numberOfQubits() const { return m_numberOfQubits; }
     int numberOfParameters() const { return m_numberOfUniqueParameters; }
@@ -103,6 +116,8 @@ private:
     aegpu_engine *m_engine = nullptr;
     std::vector<double> m_angles;          // per operator
     bool m_haveEvolved = false;
+    bool m_haveGround = false;             // lowest eigenpair computed (kept on the device)
+    double m_groundE = 0, m_groundRes = 0, m_groundTol = 0;
 };
 
 void log_line(const std::string &s);

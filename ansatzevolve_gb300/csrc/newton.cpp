@@ -66,6 +66,57 @@ void sym_eig(int n, const std::vector<double> &A_in, std::vector<double> &w, std
     V.swap(V2);
 }
 
+// Lowest eigenpair of the symmetric tridiagonal matrix with diagonal a[0..k-1] and
+// off-diagonal b[0..k-2]: the eigenvalue by Sturm-sequence bisection, the unit
+// eigenvector by inverse iteration with the LDL^T factors of the shifted matrix, which
+// the shift just below the eigenvalue keeps positive definite.
+double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int k, std::vector<double> &v)
+{
+    double lo = a[0], hi = a[0], scale = 0.0;
+    for (int i = 0; i < k; ++i) {
+        const double r = (i > 0 ? std::abs(b[i - 1]) : 0.0) + (i + 1 < k ? std::abs(b[i]) : 0.0);
+        lo = std::min(lo, a[i] - r);
+        hi = std::max(hi, a[i] + r);
+        scale = std::max(scale, std::abs(a[i]) + r);
+    }
+    const double tiny = std::max(scale, 1e-300) * 1e-300;
+    auto below = [&](double x) {  // number of eigenvalues below x
+        int c = 0;
+        double q = a[0] - x;
+        for (int i = 0;; ++i) {
+            if (q < 0) ++c;
+            if (i + 1 == k) break;
+            if (std::abs(q) < tiny) q = -tiny;
+            q = a[i + 1] - x - b[i] * b[i] / q;
+        }
+        return c;
+    };
+    for (int it = 0; it < 2100 && hi - lo > 4e-16 * std::max(std::abs(lo), std::abs(hi)); ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (below(mid) >= 1) hi = mid; else lo = mid;
+    }
+    const double theta = 0.5 * (lo + hi);
+    const double sigma = theta - std::max(scale, 1e-300) * 1e-13;
+    std::vector<double> d(k), l(k, 0.0);
+    d[0] = a[0] - sigma;
+    for (int i = 1; i < k; ++i) {
+        l[i] = b[i - 1] / d[i - 1];
+        d[i] = a[i] - sigma - l[i] * b[i - 1];
+    }
+    v.assign(k, 1.0 / std::sqrt((double)k));
+    for (int it = 0; it < 3; ++it) {
+        for (int i = 1; i < k; ++i) v[i] -= l[i] * v[i - 1];
+        for (int i = 0; i < k; ++i) v[i] /= d[i];
+        for (int i = k - 2; i >= 0; --i) v[i] -= l[i + 1] * v[i + 1];
+        double nv = 0.0;
+        for (double x : v) nv += x * x;
+        nv = std::sqrt(nv);
+        for (double &x : v) x /= nv;
+    }
+    return theta;
+}
+
 static double norm2(const std::vector<double> &v)
 {
     double s = 0;

@@ -22,6 +22,9 @@ struct NewtonStats {
 };
 
 void sym_eig(int n, const std::vector<double> &A, std::vector<double> &w, std::vector<double> &V);
+// Lowest eigenvalue (returned) and unit eigenvector v of the symmetric tridiagonal
+// matrix with diagonal a[0..k-1] and off-diagonal b[0..k-2].
+double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int k, std::vector<double> &v);
 bool optimise_newton(NewtonProblem &p, std::vector<double> &theta, NewtonStats &st, bool verbose);
 
 // The projected iteration (TUPSQuantities::iterativeTups, tupsquantities.cpp:2044-2145,

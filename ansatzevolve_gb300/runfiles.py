@@ -21,7 +21,7 @@ from typing import Optional
 
 import numpy as np
 
-from . import AegpuError, _DP, _IP, _P, lib, stateAnsatzManager
+from . import PROPERTY_NAMES, AegpuError, _DP, _IP, _P, lib, stateAnsatzManager
 from .checkpoint import write_parameters
 
 
@@ -160,3 +160,45 @@ def optimise_run(prefix, extracted_min=False, out=None):
     if out is not None:
         write_parameters(out, [x], [E])
     return E, x, rf
+
+
+def format_properties(table, have_hf=True):
+    """The table in the reference's text layout (printOutputHeaders / printOutputLine,
+    tupsquantities.cpp:2158-2205): a 40-character name column, then one 26-character
+    column per path ("HF" first when the zero path is included)."""
+    npath = len(next(iter(table.values())))
+    out = ["", "%-40s %40s " % ("Results:", "Path Number")]
+    head = "%-40s" % ""
+    labels = (["HF"] if have_hf else []) + [str(i) for i in range(1, npath + (0 if have_hf else 1))]
+    out.append(head + "".join("%-26s" % c for c in labels))
+    for name in PROPERTY_NAMES:
+        vals = np.asarray(table[name])
+        if np.all(np.isnan(vals)):
+            continue
+        out.append("%-40s" % name + "".join("%-26.16g" % v for v in vals))
+    return "\n".join(out) + "\n"
+
+
+def properties_run(prefix, extracted_min=False, no_hf_path=False, no_hess=False, lowest_eigenvalue=True,
+                   optimise=False):
+    """The reference driver's ``writeproperties`` verb (src/main.cpp:520-529; with
+    ``optimise`` first, as ``optimise writeproperties`` runs them, :489-500): the
+    properties table over the zero path (unless no_hf_path) and the run files' angle
+    sets (plus the optimised set).  Returns (table dict, subspace eigenvalues, null
+    rank, lowest eigenvalue or None, text)."""
+    m = stateAnsatzManager()
+    try:
+        rf = m.storeRunFiles(prefix)
+        if extracted_min:
+            rf = load_run_files(prefix, extracted_min=True)
+        sets = [np.asarray(x) for x in rf.parameter_sets]
+        if optimise:
+            x0 = sets[0] if sets else np.zeros(rf.n_params)
+            sets.append(m.optimise(x0)[1])
+        paths = ([] if no_hf_path else [np.zeros(rf.n_params)]) + sets
+        table = m.getProperties(paths, hessian=not no_hess, overlap=lowest_eigenvalue)
+        lam = m.getLowestEigenvalue()[0] if lowest_eigenvalue else None
+        w, nr = m.getSubspaceEigenvalues(sets) if sets else (np.zeros(0), 0)
+    finally:
+        m.close()
+    return table, w, nr, lam, format_properties(table, have_hf=not no_hf_path)

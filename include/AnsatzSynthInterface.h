@@ -63,6 +63,17 @@ int setIntegrals(int norb, const double *h1, const double *g2, int mode, void *c
 int setNuclearEnergy(double e, void *ctx);
 int optimise(int nangles, double *angles, double *energy, void *ctx);
 int setRunFiles(const char *prefix, void *ctx);
+/* Properties (the reference's writeProperties / subspace diagonalisation, which its
+ * C ABI does not expose): npaths angle rows of nangles (compressed or per operator).
+ * getProperties writes npaths rows of AEGPU_PROPERTY_ROWS values (include/aegpu.h:
+ * energies, Hessian / metric counts with AEGPU_PROP_HESSIAN, gradient norm, overlaps
+ * with the lowest eigenvector with AEGPU_PROP_OVERLAP; NaN where not computed).
+ * getLowestEigenvalue: the lowest eigenvalue of H in the sector (electronic).
+ * getSubspaceEigenvalues: the npaths eigenvalues of S^-1/2 H S^-1/2 and S's null rank. */
+int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);
+int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx);
+int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank,
+                           void *ctx);
 
 #ifdef __cplusplus
 }

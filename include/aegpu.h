@@ -118,6 +118,73 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y);
  * d<proj|psi>/dx and overlap <proj|psi>; proj[D*(1+complex)], batch of 1. */
 int aegpu_hessian_proj(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
                        const double *proj, double *overlap, double *grad_comp, double *hess_comp);
+/* aegpu_hessian plus the metric g = Re(T_C^dagger T_C) of the compressed tangents
+ * T_C mu = d psi / d x_mu (nparams x nparams; tupsquantities.cpp:386-389). */
+int aegpu_hessian_metric(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                         double *energy, double *grad_comp, double *hess_comp, double *metric);
+
+/* Properties (TUPSQuantities::writeProperties, tupsquantities.cpp:185-568;
+ * doSubspaceDiagonalisation, :1600-1769).  Batch of 1.
+ *
+ * aegpu_lowest_eigenpair: the lowest eigenvalue of H in the determinant sector and its
+ * eigenvector, kept on the device until H is replaced.  Lanczos from the initial state
+ * with full reorthogonalisation, restarted from the Ritz vector after `basis` products,
+ * until the residual estimate is below tol / 2 or max_products H products are spent;
+ * eigenvalue is the Rayleigh quotient of the unit eigenvector, residual its true
+ * ||H v - lambda v||, products the H products used.  Its sign makes <start|v> >= 0.
+ * (The reference iterates v <- H v / |H v| from the same start, which converges to the
+ * eigenvector of largest |lambda|: the same vector whenever the lowest eigenvalue is
+ * also the largest in magnitude.)  Not converging within max_products is not an error:
+ * compare the residual with tol. */
+int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
+                           double *residual, int *products);
+/* The eigenvector, D*(1+complex) doubles in sector order. */
+int aegpu_ground_state(aegpu_engine *e, double *state);
+/* <psi(angles)|v>: overlap[0] real part, overlap[1] imaginary part. */
+int aegpu_ground_overlap(aegpu_engine *e, const double *angles, double *overlap);
+/* <r|H|r> / <r|r> for the real part r of psi(angles) (tupsquantities.cpp:418-423; the
+ * energy itself for real states). */
+int aegpu_real_energy(aegpu_engine *e, const double *angles, double *real_energy);
+/* For nsets angle vectors (angles[nsets][nops]): H_ij = <psi_i|H|psi_j> and
+ * S_ij = <psi_i|psi_j>, row-major nsets x nsets; the imaginary parts (h_im, s_im, may
+ * be NULL) are 0 for real states. */
+int aegpu_subspace_matrices(aegpu_engine *e, int nsets, const double *angles, double *h_re, double *h_im, double *s_re,
+                            double *s_im);
+
+/* One path's row of the reference's properties table (printOutputLine calls,
+ * tupsquantities.cpp:538-566), at per-operator angles with the compressed parameters
+ * (param, scale): row[AEGPU_PROPERTY_ROWS], NaN where not computed.  flags:
+ * AEGPU_PROP_HESSIAN adds the Hessian / metric counts (eigenvalues and diagonal entries
+ * below -1e-10, within 1e-10, above 1e-10; :466-533) and fills hessian / metric
+ * (nparams^2 each, nullable); AEGPU_PROP_OVERLAP adds <psi|v> with the eigenvector of
+ * aegpu_lowest_eigenpair.  Energies exclude nuclear_energy except the third row. */
+#define AEGPU_PROP_HESSIAN 1
+#define AEGPU_PROP_OVERLAP 2
+#define AEGPU_PROP_ELEC_ENERGY 0
+#define AEGPU_PROP_REAL_ELEC_ENERGY 1
+#define AEGPU_PROP_ELEC_NUC_ENERGY 2
+#define AEGPU_PROP_NEG_HESSIAN_EVALUES 3
+#define AEGPU_PROP_NEAR_ZERO_HESSIAN_EVALUES 4
+#define AEGPU_PROP_POS_HESSIAN_EVALUES 5
+#define AEGPU_PROP_NEG_HESSIAN_DIAG 6
+#define AEGPU_PROP_NEAR_ZERO_HESSIAN_DIAG 7
+#define AEGPU_PROP_POS_HESSIAN_DIAG 8
+#define AEGPU_PROP_POS_METRIC_EVALUES 9
+#define AEGPU_PROP_ZERO_METRIC_EVALUES 10
+#define AEGPU_PROP_ZERO_METRIC_DIAG 11
+#define AEGPU_PROP_NORM_OF_GRAD 12
+#define AEGPU_PROP_OVERLAP_RE 13
+#define AEGPU_PROP_OVERLAP_IM 14
+#define AEGPU_PROP_OVERLAP_MAG 15
+#define AEGPU_PROPERTY_ROWS 16
+int aegpu_path_properties(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
+                          double nuclear_energy, int flags, double *row, double *hessian, double *metric);
+/* Subspace diagonalisation of nsets states (doSubspaceDiagonalisation,
+ * tupsquantities.cpp:1600-1700): the eigenvalues (ascending, nsets) of S^-1/2 H S^-1/2,
+ * with S's eigenvalues below 1e-14 treated as its null space (whose directions give
+ * eigenvalue 0, as in the reference), and that null space's dimension. */
+int aegpu_subspace_eigenvalues(aegpu_engine *e, int nsets, const double *angles, double *eigenvalues, int *null_rank);
+
 /* Projected sweep (FusedEvolve::evolveDerivativeProj, fusedevolve.cpp:2814-2880):
  * overlap[b] = <proj_b|psi_b(theta_b)> and grad[b][op] = d overlap / d theta_op for a
  * fixed bra proj[nb][D*(1+complex)] (no factor 2, unlike the energy gradient). */
@@ -210,6 +277,13 @@ int aegpu_problem_info(const aegpu_engine *e, int64_t *info);
 /* Device pointers of the current state and of H*state (D or 2D doubles). */
 int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi);
 
+/* Host-only (no GPU): the lowest eigenpair of a symmetric tridiagonal matrix
+ * (diagonal a[k], off-diagonal b[k-1]) as aegpu_lowest_eigenpair's Lanczos step solves it. */
+int aegpu_host_tridiag_lowest(int k, const double *a, const double *b, double *v, double *theta);
+/* Host-only: the eigen-analysis of aegpu_subspace_eigenvalues on given matrices
+ * (row-major nsets x nsets real / imaginary parts; the imaginary parts may be NULL). */
+int aegpu_host_subspace_eigenvalues(int nsets, const double *h_re, const double *h_im, const double *s_re,
+                                    const double *s_im, double *eigenvalues, int *null_rank);
 /* Host-only inspection of the setup (no GPU needed): the operator application order
  * and block sizes (negative = diagonal block) that aegpu_set_problem would use, and
  * the orbit tables of one block of excitations.  For tests of the setup logic.

@@ -18,6 +18,11 @@
 //   pairs 0|1                            (dump the per-excitation partner/sign rule)
 //   optimise 0|1
 //   time k                               (k timed evolve+evolveDerivative units)
+//   properties <prefix>                  (TUPSQuantities::writeProperties over the zero
+//                                         path + the angle sets; its table goes to
+//                                         <prefix>_table.txt, its matrices to <prefix>_Path_*)
+//   subspace n                           (with properties: doSubspaceDiagonalisation of
+//                                         the first n angle sets; printed on stderr)
 //   end
 // Output: for every angle set, E, gradient, Hessian (column-major), final state;
 // then the pair table, then the optimised energy + angles, then timings.
@@ -61,6 +66,8 @@ int main(int argc, char **argv)
     double nuclear = 0;
     std::vector<std::vector<double>> angleSets;
     int wantE = 1, wantG = 1, wantH = 0, wantS = 0, wantPairs = 0, wantOpt = 0, timeK = 0;
+    std::string propsPrefix;
+    int subspaceN = 0;
 
     std::string tok;
     while (in >> tok) {
@@ -96,6 +103,8 @@ int main(int argc, char **argv)
         else if (tok == "pairs") in >> wantPairs;
         else if (tok == "optimise") in >> wantOpt;
         else if (tok == "time") in >> timeK;
+        else if (tok == "properties") in >> propsPrefix;
+        else if (tok == "subspace") in >> subspaceN;
         else if (tok == "end") break;
         else { fprintf(stderr, "bad token %s\n", tok.c_str()); return 2; }
     }
@@ -196,6 +205,35 @@ int main(int argc, char **argv)
         put1(out, (double)times.size());
         put(out, times.data(), times.size());
         put1(out, E);
+    }
+    if (!propsPrefix.empty() && !intsPrefix.empty()) {
+        // the reference's own properties pass (tupsquantities.cpp:185-568) on the
+        // integral Hamiltonian, as the CLI's writeproperties verb runs it (main.cpp:520-529)
+        uint32_t ones = -1;
+        int spinUp = bitwiseDot(initIdx[0] >> (nq / 2), ones, 32), spinDown = bitwiseDot(initIdx[0], ones, nq / 2);
+        std::shared_ptr<compressor> comp = std::make_shared<SZAndnumberOperatorCompressor>(1u << nq, spinUp, spinDown);
+        vector<numType> full;
+        full.resize(1u << nq, false, nullptr);
+        for (size_t k = 0; k < initIdx.size(); ++k) full[initIdx[k]] = initCoeff[k];
+        vector<numType> start;
+        compressor::compressVector<numType>(full, start, comp);
+        auto Ham = std::make_shared<HamiltonianMatrix<realNumType, numType>>(intsPrefix, nq, comp);
+        int P = 0;
+        for (auto &o : order) P = std::max(P, o.first + 1);
+        FILE *table = fopen((propsPrefix + "_table.txt").c_str(), "w");
+        TUPSQuantities q(Ham, order, P, nuclear, propsPrefix, table);
+        auto FE = std::make_shared<FusedEvolve>(start, Ham, q.m_compressMatrix, q.m_deCompressMatrix);
+        FE->updateExc(excs);
+        std::vector<std::vector<ansatz::rotationElement>> paths(1, std::vector<ansatz::rotationElement>(excs.size(), {0, 0.0}));
+        for (auto &a0 : angleSets) {
+            paths.emplace_back(excs.size(), ansatz::rotationElement{0, 0.0});
+            for (size_t i = 0; i < excs.size(); ++i)
+                paths.back()[i].second = a0.size() == excs.size() ? a0[i] : a0[order[i].first] * order[i].second;
+        }
+        TUPSQuantitiesOptions opts;
+        q.writeProperties(nullptr, FE, paths, opts);
+        fclose(table);
+        if (subspaceN > 0) q.doSubspaceDiagonalisation(nullptr, FE, (size_t)subspaceN, paths);
     }
     fclose(out);
     return 0;

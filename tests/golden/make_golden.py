@@ -16,8 +16,14 @@ Sources of the inputs:
               sampled final-state amplitudes
   ref12    -- the benchmark's 12-orbital inputs (seed 0, 3 layers): E, gradient,
               sampled final-state amplitudes (the reference's Hessian takes minutes here)
-Only the ref10 / ref12 cases can be regenerated alone:
-    python tests/golden/make_golden.py ref10 ref12
+  props_h4, props_h4c, props_syn6
+           -- the reference's own TUPSQuantities::writeProperties table (energies,
+              Hessian / metric eigenvalue and diagonal counts, gradient norms, overlaps
+              with the lowest eigenvector), its Hessian and metric matrices per path, and
+              doSubspaceDiagonalisation's eigenvalues, over the zero path and the angle
+              sets of the h4 / h4c / syn6 inputs plus a repeat of the first set
+Only the ref10 / ref12 / props_* cases can be regenerated alone:
+    python tests/golden/make_golden.py ref10 ref12 props_h4 props_h4c props_syn6
 """
 import os
 import re
@@ -213,6 +219,71 @@ def synthetic_case(tag, N, na, nb, layers, seed, pairs=False, hess=True):
     print(tag, res["E"])
 
 
+PROPERTY_ROWS = ("Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
+                 "NumberOfNegativeHessianEValues", "NumberOfNearZeroHessianEValues",
+                 "NumberOfPositiveHessianEValues", "NumberOfNegativeHessianDiagValues",
+                 "NumberOfNearZeroHessianDiagValues", "NumberOfPositiveHessianDiagValues",
+                 "NumberOfPositiveMetricEValues", "NumberOfZeroMetricEValues", "NumberOfZeroMetricDiagonalValues",
+                 "NormOfGradVector", "OverlapWithState_0", "MagOfOverlapWithState_0")
+
+
+def properties_case(tag, base, cplx=False):
+    """writeProperties + doSubspaceDiagonalisation of the reference over the zero path,
+    the angle sets of fixture `base` and a repeat of its first set (a rank-deficient
+    overlap matrix for the subspace step)."""
+    fx = dict(np.load(os.path.join(OUT, base + ".npz")))
+    if base.startswith("syn"):
+        N = int(fx["N"])
+        h1, g2 = synthetic_integrals(N, int(fx["seed"]))
+        nq, init, nuclear = 2 * N, [(int(fx["hf"]), 1.0, 0.0)], 0.0
+    else:
+        h1, g2 = fx["h1"], fx["g2"]
+        nq, nuclear = int(fx["nq"]), float(fx["nuclear"])
+        init = [(int(i), float(r), float(m)) for i, r, m in
+                zip(fx["init_idx"], fx["init_re"], fx.get("init_im", np.zeros(len(fx["init_idx"]))))]
+    sets = [np.asarray(a) for a in fx["angles"]] + [np.asarray(fx["angles"][0])]
+    P = int(np.asarray(fx["order_1b"]).max())
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, "p")
+        write_integrals(prefix, h1, g2)
+        sp = spec(nq, init, np.asarray(fx["ops_1b"]) - 1, np.asarray(fx["order_1b"]) - 1, fx["scale"],
+                  [f"ham ints {prefix}"], sets, want=(1, 0, 0, 0), nuclear=nuclear)
+        sp += [f"properties {prefix}", f"subspace {len(sets)}"]
+        sf, of = os.path.join(td, "spec"), os.path.join(td, "out")
+        open(sf, "w").write("\n".join(sp) + "\nend\n")
+        r = subprocess.run([DRV + ("_cplx" if cplx else ""), sf, of], check=True, capture_output=True, text=True,
+                           env=dict(os.environ, OMP_NUM_THREADS="4"))
+        npath = len(sets) + 1
+        rows = np.full((len(PROPERTY_ROWS), npath), np.nan)
+        ov = np.zeros(npath, dtype=complex)
+        for ln in open(prefix + "_table.txt").read().splitlines():
+            name = ln[:40].strip()
+            if name not in PROPERTY_ROWS:
+                continue
+            vals = [float(t) for t in ln[40:].replace(",", " ").split()]
+            if name == "OverlapWithState_0":
+                ov = np.array(vals[0::2]) + 1j * np.array(vals[1::2]) if cplx else np.array(vals, dtype=complex)
+                rows[PROPERTY_ROWS.index(name)] = ov.real
+            else:
+                rows[PROPERTY_ROWS.index(name)] = vals
+        hess = np.stack([np.fromfile(f"{prefix}_Path_{k}_Hessian.Matbin").reshape(P, P) for k in range(npath)])
+        met = []
+        for k in range(npath):
+            if cplx:
+                m = np.fromfile(f"{prefix}_Path_{k}_Metric.CMatbin").reshape(P, P, 2)
+                met.append(m[..., 0])
+            else:
+                met.append(np.fromfile(f"{prefix}_Path_{k}_Metric.Matbin").reshape(P, P))
+        lines = r.stderr.splitlines()
+        k = next(i for i, ln in enumerate(lines) if "Rank of Null space of overlap matrix" in ln)
+        null_rank = int(lines[k].split(":")[-1])
+        sub = np.array([float(t) for t in lines[k + 1].split()])
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), base=base, sets=np.array(sets), rows=rows,
+                        row_names=np.array(PROPERTY_ROWS), overlap=ov, hess=hess, metric=np.stack(met),
+                        subspace_eigs=sub, subspace_null_rank=null_rank)
+    print(tag, rows[0], ov, sub, null_rank)
+
+
 def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
     """The benchmark's own inputs at 10 / 12 orbitals (integrals of `seed`, angles
     default_rng(seed + 1).uniform(-0.1, 0.1)): energy, gradient, (Hessian), and a seeded
@@ -246,7 +317,10 @@ def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
 if __name__ == "__main__":
     if len(sys.argv) > 1:
         for t in sys.argv[1:]:
-            large_case(t, int(t[3:]), int(t[3:]) // 2, int(t[3:]) // 2, 3, 0, hess=t == "ref10")
+            if t.startswith("props_"):
+                properties_case(t, t[6:], cplx=t.endswith("c"))
+            else:
+                large_case(t, int(t[3:]), int(t[3:]) // 2, int(t[3:]) // 2, 3, 0, hess=t == "ref10")
         sys.exit(0)
     fortran_case()
     hams_case("TestFermionic", None, tag="ferm")
@@ -256,3 +330,6 @@ if __name__ == "__main__":
     synthetic_case("syn8", 8, 4, 4, 2, 0)
     large_case("ref10", 10, 5, 5, 3, 0, hess=True)
     large_case("ref12", 12, 6, 6, 3, 0, hess=False)
+    properties_case("props_h4", "h4")
+    properties_case("props_h4c", "h4c", cplx=True)
+    properties_case("props_syn6", "syn6")

@@ -138,3 +138,48 @@ def test_oracle_matches_reference_at_benchmark_sizes(golden, name):
     psi = o.evolve_ops(np.asarray(fx["scale"]) * np.asarray(fx["x"])[p0])
     np.testing.assert_allclose(psi[fx["sample_rank"]], fx["sample_amp"], atol=1e-12, rtol=0)
     assert abs(np.dot(psi, psi) - float(fx["norm"])) < 1e-12
+
+
+def props_inputs(golden, tag):
+    """(oracle, compressed paths incl. the zero path, param0, scale, nuclear, fixture)."""
+    px = golden(tag)
+    base = str(px["base"])
+    fx = golden(base)
+    if base.startswith("syn"):
+        pb = synthetic_problem(int(fx["N"]), int(fx["na"]), int(fx["nb"]), int(fx["layers"]), int(fx["seed"]))
+        o, nuclear = oracle_synthetic(pb), 0.0
+    else:
+        o, nuclear = oracle_from_golden(fx, cplx=base == "h4c"), float(fx["nuclear"])
+    p0 = np.asarray(fx["order_1b"]) - 1
+    paths = [np.zeros(int(p0.max()) + 1)] + list(px["sets"])
+    return o, paths, p0, np.asarray(fx["scale"]), nuclear, px
+
+
+@pytest.mark.parametrize("tag", ["props_h4", "props_h4c", "props_syn6"])
+def test_properties_restatement_matches_reference(golden, tag):
+    """The numpy restatement of writeProperties / doSubspaceDiagonalisation
+    (oracle/properties_ref.py) reproduces the reference's own table, Hessians, metrics
+    (here by finite differences) and subspace eigenvalues."""
+    from oracle.properties_ref import decompress, lowest_eigenpair, path_row, subspace_eigenvalues
+    o, paths, p0, scale, nuclear, px = props_inputs(golden, tag)
+    lam, v0 = lowest_eigenpair(o)
+    v0 = v0.astype(complex)
+    ours = []
+    for k, x in enumerate(paths):
+        row, H, M = path_row(o, x, p0, scale, nuclear, v0)
+        ref = px["rows"][:, k]
+        np.testing.assert_allclose(row[:3], ref[:3], atol=1e-10, rtol=0)
+        assert np.array_equal(row[3:12], ref[3:12]), (k, row[3:12], ref[3:12])
+        assert abs(row[12] - ref[12]) < 1e-9
+        assert abs(row[15] - ref[14]) < 1e-9
+        np.testing.assert_allclose(H, px["hess"][k], atol=1e-9, rtol=0)
+        np.testing.assert_allclose(M, px["metric"][k], atol=1e-7, rtol=0)
+        ours.append(row[13] + 1j * row[14])
+    # the eigenvector's phase is arbitrary: one phase for all paths
+    ours, ref = np.array(ours), px["overlap"]
+    ph = ours[0] / ref[0]
+    ph /= abs(ph)
+    np.testing.assert_allclose(ours, ph * ref, atol=1e-9, rtol=0)
+    eigs, null = subspace_eigenvalues(o, [decompress(x, p0, scale) for x in px["sets"]])
+    np.testing.assert_allclose(eigs, px["subspace_eigs"], atol=1e-12, rtol=0)
+    assert null == int(px["subspace_null_rank"])

@@ -1,0 +1,91 @@
+"""Host parts of the properties entry points, on the CPU: the tridiagonal eigen-solve
+inside the Lanczos iteration (aegpu_host_tridiag_lowest) against numpy, including
+clustered, degenerate and badly scaled spectra."""
+import numpy as np
+import pytest
+
+from ansatzevolve_gb300 import dptr, lib
+
+
+def _solve(a, b):
+    k = len(a)
+    v = np.zeros(k)
+    th = np.zeros(1)
+    assert lib().aegpu_host_tridiag_lowest(k, dptr(np.ascontiguousarray(a, dtype=float)),
+                                           dptr(np.ascontiguousarray(b if k > 1 else [0.0], dtype=float)),
+                                           dptr(v), dptr(th)) == 0
+    return th[0], v
+
+
+@pytest.mark.parametrize("k,seed,scale", [(1, 0, 1.0), (2, 1, 1.0), (7, 2, 1.0), (60, 3, 1.0), (150, 4, 1e3),
+                                          (40, 5, 1e-6)])
+def test_tridiagonal_lowest_eigenpair(k, seed, scale):
+    rng = np.random.default_rng(seed)
+    a = rng.normal(size=k) * scale
+    b = rng.normal(size=k - 1) * scale
+    T = np.diag(a) + np.diag(b, 1) + np.diag(b, -1)
+    w, V = np.linalg.eigh(T)
+    th, v = _solve(a, b)
+    assert abs(th - w[0]) <= 1e-13 * np.abs(w).max()
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-13
+    assert np.linalg.norm(T @ v - th * v) <= 1e-10 * np.abs(w).max()
+
+
+def test_tridiagonal_with_tiny_couplings_and_clusters():
+    # a Lanczos matrix near convergence: tiny off-diagonals and a near-degenerate bottom
+    a = np.array([-3.0, -3.0 + 1e-9, -1.0, 0.5, 2.0])
+    b = np.array([1e-12, 1e-6, 0.3, 0.0])
+    T = np.diag(a) + np.diag(b, 1) + np.diag(b, -1)
+    w = np.linalg.eigvalsh(T)
+    th, v = _solve(a, b)
+    assert abs(th - w[0]) < 1e-14
+    assert np.linalg.norm(T @ v - th * v) < 1e-10
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_subspace_eigen_analysis_matches_numpy(cplx):
+    """S^-1/2 H S^-1/2 with a rank-deficient overlap matrix (two states repeated): the
+    null space gives eigenvalue 0 (doSubspaceDiagonalisation keeps it) and its rank is
+    reported."""
+    import ctypes
+    rng = np.random.default_rng(7)
+    D, n = 30, 6
+    X = rng.normal(size=(D, n - 2)) + (1j * rng.normal(size=(D, n - 2)) if cplx else 0)
+    X = np.column_stack([X, X[:, 0], X[:, 1]])
+    X /= np.linalg.norm(X, axis=0)  # unit states, as evolved states are
+    A = rng.normal(size=(D, D)) + (1j * rng.normal(size=(D, D)) if cplx else 0)
+    Hd = 0.5 * (A + A.conj().T)
+    S = X.conj().T @ X
+    H = X.conj().T @ Hd @ X
+    ws, Vs = np.linalg.eigh(S)
+    f = np.where(ws < 1e-14, 0.0, 1 / np.sqrt(np.abs(ws)))
+    Y = (Vs * f) @ Vs.conj().T @ H @ (Vs * f) @ Vs.conj().T
+    want = np.linalg.eigvalsh(0.5 * (Y + Y.conj().T))
+    w = np.zeros(n)
+    nr = ctypes.c_int()
+    c = lambda M: dptr(np.ascontiguousarray(M, dtype=float))  # noqa: E731
+    hr, hi, sr, si = H.real.copy(), H.imag.copy(), S.real.copy(), S.imag.copy()
+    assert lib().aegpu_host_subspace_eigenvalues(n, c(hr), c(hi), c(sr), c(si), dptr(w), ctypes.byref(nr)) == 0
+    assert nr.value == int((ws < 1e-14).sum()) == 2
+    np.testing.assert_allclose(w, want, atol=1e-9 * np.abs(want).max(), rtol=0)
+
+
+def test_properties_c_abi_status_codes():
+    import ctypes
+    L = lib()
+    a = np.zeros(4)
+    t = np.zeros(64)
+    nr = ctypes.c_int()
+    assert L.getProperties(1, 4, dptr(a), 3, dptr(t), None) == 1
+    assert L.getLowestEigenvalue(dptr(a), dptr(a), None) == 1
+    assert L.getSubspaceEigenvalues(1, 4, dptr(a), dptr(a), ctypes.byref(nr), None) == 1
+    ctx = ctypes.c_void_p(L.init())
+    try:
+        assert L.getProperties(0, 4, dptr(a), 3, dptr(t), ctx) == 2
+        assert L.getProperties(1, 4, dptr(a), 3, None, ctx) == 2
+        assert L.getLowestEigenvalue(None, None, ctx) == 2
+        assert L.getSubspaceEigenvalues(1, 0, dptr(a), dptr(a), ctypes.byref(nr), ctx) == 2
+        # nothing set up: the first evaluation fails cleanly (no GPU work happens)
+        assert L.getProperties(1, 4, dptr(a), 3, dptr(t), ctx) == 3
+    finally:
+        L.cleanup(ctypes.byref(ctx))
