@@ -96,6 +96,10 @@ def lib(build_if_missing=True):
         "aegpu_amplitude_width": (ctypes.c_int, [_P]),
         "aegpu_optimise_projected": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double, ctypes.c_int,
                                                     _DP, _DP, ctypes.POINTER(i64), ctypes.POINTER(i64), _IP]),
+        "aegpu_optimise_projected_diis": (ctypes.c_int, [_P, ctypes.c_int, _IP, _DP, _DP, ctypes.c_double,
+                                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP,
+                                                         ctypes.POINTER(i64), ctypes.POINTER(i64), _IP]),
+        "aegpu_host_diis_coefficients": (ctypes.c_int, [ctypes.c_int, _DP, ctypes.c_int, _DP]),
         "aegpu_group_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.c_int]),
         "aegpu_group_launch": (ctypes.c_int, [_P, _P]),
         "aegpu_group_launch_count": (i64, [_P]),
@@ -466,16 +470,19 @@ class Engine:
                                                  ctypes.byref(nh), ctypes.byref(ne)))
         return x, E[0], gn[0], nh.value, ne.value
 
-    def optimise_projected(self, x0, param0, scale, gtol=1e-5, max_outer=3000):
-        """The reference's projected iteration (iterativeTups): (x, E, |g_proj|, Hessians, evaluations, renewals)."""
+    def optimise_projected(self, x0, param0, scale, gtol=1e-5, max_outer=3000, diis=0, ediis=True):
+        """The reference's projected iteration (iterativeTups): (x, E, |g_proj|, Hessians,
+        evaluations, renewals).  diis > 0 extrapolates the angles over that many renewals
+        (EDIIS, or Pulay DIIS with ediis=False); the reference ships it off (0)."""
         x = _f64(x0).copy()
         p, s = _i32(param0), _f64(scale)
         E, gn = np.zeros(1), np.zeros(1)
         nh, ne = ctypes.c_int64(), ctypes.c_int64()
         it = ctypes.c_int()
-        self._check(self.L.aegpu_optimise_projected(self.h, len(x), iptr(p), dptr(s), dptr(x), gtol, int(max_outer),
-                                                    dptr(E), dptr(gn), ctypes.byref(nh), ctypes.byref(ne),
-                                                    ctypes.byref(it)))
+        self._check(self.L.aegpu_optimise_projected_diis(self.h, len(x), iptr(p), dptr(s), dptr(x), gtol,
+                                                         int(max_outer), int(diis), int(bool(ediis)), dptr(E),
+                                                         dptr(gn), ctypes.byref(nh), ctypes.byref(ne),
+                                                         ctypes.byref(it)))
         return x, E[0], gn[0], nh.value, ne.value, it.value
 
     def optimise_batch(self, x0, param0, scale, gtol=1e-6, max_rounds=2000, max_step=1.0, hinv=None):

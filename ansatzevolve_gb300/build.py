@@ -13,7 +13,7 @@ OUT = os.path.join(HERE, "libansatzevolve_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["engine.cu", "mlp.cu"]
-CPP = ["setup.cpp", "otf_tables.cpp", "manager.cpp", "newton.cpp", "interface.cpp", "optimise.cpp", "runfiles.cpp", "properties.cpp"]
+CPP = ["setup.cpp", "otf_tables.cpp", "manager.cpp", "newton.cpp", "interface.cpp", "optimise.cpp", "runfiles.cpp", "properties.cpp", "diis.cpp"]
 
 
 def _nvcc():

@@ -7,6 +7,8 @@
 // model line search on t in (0, 1.5].
 #include "newton.h"
 
+#include "diis.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -358,17 +360,36 @@ static bool run_newton_projected(ProjectedProblem &p, std::vector<double> &th, c
 
 bool optimise_projected(ProjectedProblem &p, std::vector<double> &th, NewtonStats &st, int &outer_iters)
 {
-    std::vector<double> psiH, g;
-    if (!p.bra(th, psiH)) return false;
+    std::vector<double> psiH, g, psi, prevPsi;
+    if (!p.bra(th, psiH, prevPsi)) return false;
     outer_iters = 0;
     double E = 0, gnorm = 0;
+    Diis diis((size_t)std::max(p.diis_size, 1), p.ediis);
+    const size_t nops = th.size();
     while (outer_iters++ < p.max_outer) {
         if (!run_newton_projected(p, th, psiH, st)) return false;
-        if (!p.bra(th, psiH)) return false;
+        if (!p.bra(th, psiH, psi)) return false;
         if (!p.proj_grad(th, psiH, E, g)) return false;
         st.energy_evals++;
         gnorm = norm2(g);
         if (gnorm < p.gtol) break;
+        if (p.diis_size > 0 && outer_iters < p.max_outer) {  // the returned angles keep their energy
+            // compressed angles (first operator of each parameter) and the change of
+            // the state as the error vector; the extrapolated angles start the next
+            // Newton run, with the bra of the unextrapolated state (:2101-2122)
+            std::vector<double> x(p.nparams, 0.0), err(psi.size());
+            std::vector<bool> seen(p.nparams, false);
+            for (size_t o = 0; o < nops; ++o)
+                if (!seen[p.param[o]] && p.scale[o] != 0) {
+                    x[p.param[o]] = th[o] / p.scale[o];
+                    seen[p.param[o]] = true;
+                }
+            for (size_t i = 0; i < psi.size(); ++i) err[i] = psi[i] - prevPsi[i];
+            diis.addNew(x, err);
+            diis.getNext(x);
+            for (size_t o = 0; o < nops; ++o) th[o] = p.scale[o] * x[p.param[o]];
+        }
+        prevPsi.swap(psi);
     }
     st.energy = E;
     st.gnorm = gnorm;

@@ -37,8 +37,12 @@ struct ProjectedProblem {
     std::vector<double> scale;
     double gtol = 1e-5;             // tupsquantities.cpp:2096
     int max_outer = 3000;           // :2076
-    // psiH = H psi(theta) (device-size vector on the host)
-    std::function<bool(const std::vector<double> &theta, std::vector<double> &psiH)> bra;
+    // DIIS over the outer iterations (:2101-2122, off in the reference: doDIIS = false):
+    // history length (0 = off; the reference's is 15) and EDIIS (true) or Pulay DIIS
+    int diis_size = 0;
+    bool ediis = true;
+    // psi = psi(theta) and psiH = H psi (device-size vectors on the host)
+    std::function<bool(const std::vector<double> &theta, std::vector<double> &psiH, std::vector<double> &psi)> bra;
     // overlap <psiH|psi(theta)> and its compressed gradient
     std::function<bool(const std::vector<double> &theta, const std::vector<double> &psiH, double &ov,
                        std::vector<double> &g)> proj_grad;

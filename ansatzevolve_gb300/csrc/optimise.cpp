@@ -13,6 +13,7 @@
 //   are masked out of it (aegpu_set_active).  No counterpart in the reference, which
 //   optimises one angle vector at a time.
 #include "../../include/aegpu.h"
+#include "diis.h"
 #include "newton.h"
 
 #include <algorithm>
@@ -259,7 +260,16 @@ int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, con
                              double gtol, int max_outer, double *energy, double *gnorm, int64_t *hessian_evals,
                              int64_t *energy_evals, int *outer_iters)
 {
-    if (!e || nparams < 1 || !param || !scale || !x || !(gtol > 0) || max_outer < 1) return AEGPU_ERR_ARG;
+    return aegpu_optimise_projected_diis(e, nparams, param, scale, x, gtol, max_outer, 0, 1, energy, gnorm,
+                                         hessian_evals, energy_evals, outer_iters);
+}
+
+int aegpu_optimise_projected_diis(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x,
+                                  double gtol, int max_outer, int diis_size, int ediis, double *energy, double *gnorm,
+                                  int64_t *hessian_evals, int64_t *energy_evals, int *outer_iters)
+{
+    if (!e || nparams < 1 || !param || !scale || !x || !(gtol > 0) || max_outer < 1 || diis_size < 0)
+        return AEGPU_ERR_ARG;
     if (aegpu_batch_size(e) != 1) return AEGPU_ERR_UNSUPPORTED;
     int64_t info[8];
     int rc = aegpu_problem_info(e, info);
@@ -274,10 +284,12 @@ int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, con
     p.scale.assign(scale, scale + nops);
     p.gtol = gtol;
     p.max_outer = max_outer;
+    p.diis_size = diis_size;
+    p.ediis = ediis != 0;
     int err = AEGPU_OK;
-    std::vector<double> psi(n);
-    p.bra = [&](const std::vector<double> &th, std::vector<double> &psiH) {
+    p.bra = [&](const std::vector<double> &th, std::vector<double> &psiH, std::vector<double> &psi) {
         psiH.assign(n, 0.0);
+        psi.assign(n, 0.0);
         return (err = aegpu_evolve(e, th.data(), psi.data())) == AEGPU_OK &&
                (err = aegpu_apply_h(e, psi.data(), psiH.data())) == AEGPU_OK;
     };
@@ -312,6 +324,15 @@ int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, con
     if (hessian_evals) *hessian_evals = st.hessian_evals;
     if (energy_evals) *energy_evals = st.energy_evals;
     if (outer_iters) *outer_iters = outer;
+    return AEGPU_OK;
+}
+
+int aegpu_host_diis_coefficients(int n, const double *B, int ediis, double *c)
+{
+    if (n < 1 || !B || !c) return AEGPU_ERR_ARG;
+    std::vector<double> b(B, B + (size_t)n * n), cv;
+    ae::diis_coefficients(n, b, ediis != 0, cv);
+    std::copy(cv.begin(), cv.end(), c);
     return AEGPU_OK;
 }
 

@@ -243,6 +243,16 @@ int aegpu_optimise_batch(aegpu_engine *e, int nparams, const int *param, const d
 int aegpu_optimise_projected(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x,
                              double gtol, int max_outer, double *energy, double *gnorm, int64_t *hessian_evals,
                              int64_t *energy_evals, int *outer_iters);
+/* The same with DIIS over the renewals (the reference's iterativeTups with doDIIS,
+ * tupsquantities.cpp:2101-2122; diis.h:16-209): the compressed angles are extrapolated
+ * from the last diis_size iterations with the state changes as error vectors; ediis
+ * selects EDIIS (non-negative coefficients, the reference's choice, size 15) over
+ * Pulay DIIS.  diis_size 0 is aegpu_optimise_projected. */
+int aegpu_optimise_projected_diis(aegpu_engine *e, int nparams, const int *param, const double *scale, double *x,
+                                  double gtol, int max_outer, int diis_size, int ediis, double *energy, double *gnorm,
+                                  int64_t *hessian_evals, int64_t *energy_evals, int *outer_iters);
+/* Host-only: the DIIS coefficients for an n x n matrix of error inner products. */
+int aegpu_host_diis_coefficients(int n, const double *B, int ediis, double *c);
 /* Learned warm start (no counterpart in the reference): an MLP
  * n_in -> n_hidden -> n_hidden -> n_out with GELU activations, BF16 weights in every
  * product, FP32 accumulation, FP32 master weights trained by Adam on the mean squared

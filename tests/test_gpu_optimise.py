@@ -85,3 +85,40 @@ def test_projected_iteration_reaches_a_stationary_point(golden):
     xn, En, gn, _, _ = e.optimise_newton(x, p0, scale, gtol=1e-10)
     assert abs(En - E) < 1e-8
     e.close()
+
+
+def _h4_engine(golden):
+    from tests.fixtures import sector_of
+    fx = golden("h4")
+    nq = int(fx["nq"])
+    ops0 = np.asarray(fx["ops_1b"]) - 1
+    kind, ne, na, nbe = sector_of(nq, fx["init_idx"], ops0)
+    p0 = np.asarray(fx["order_1b"]) - 1
+    e = ae.Engine(nq, kind, ne, na, nbe, ops0)
+    init = np.zeros(e.D)
+    init[np.searchsorted(e.states(), np.asarray(fx["init_idx"]))] = fx["init_re"]
+    e.set_initial(init)
+    e.set_ham_integrals(fx["h1"], fx["g2"], ae.HAM_STORED)
+    return e, fx, p0, np.asarray(fx["scale"])
+
+
+def test_projected_iteration_with_diis(golden):
+    """DIIS over the renewals (iterativeTups with doDIIS): a history of one vector
+    extrapolates to the last angles, so the run is identical to the plain iteration;
+    EDIIS (15, the reference's setting) and Pulay DIIS runs return angles whose energy
+    is the one reported."""
+    e, fx, p0, scale = _h4_engine(golden)
+    P = int(p0.max()) + 1
+    x0 = np.asarray(fx["angles"][1])[:P]
+    plain = e.optimise_projected(x0, p0, scale, gtol=1e-5)
+    for ediis in (True, False):
+        one = e.optimise_projected(x0, p0, scale, gtol=1e-5, diis=1, ediis=ediis)
+        assert np.array_equal(one[0], plain[0]) and one[1:] == plain[1:]
+    for size, ediis in ((15, True), (6, False)):
+        x, E, gp, nh, nev, outer = e.optimise_projected(x0, p0, scale, gtol=1e-5, max_outer=500, diis=size,
+                                                         ediis=ediis)
+        assert outer >= 1 and np.isfinite(gp)
+        assert abs(e.energy(scale * x[p0]) - E) < 1e-12
+        print("DIIS %d %s: E %.12f |g_proj| %.2e after %d renewals (plain: %d)" %
+              (size, "EDIIS" if ediis else "Pulay", E, gp, outer, plain[5]))
+    e.close()

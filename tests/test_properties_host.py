@@ -89,3 +89,33 @@ def test_properties_c_abi_status_codes():
         assert L.getProperties(1, 4, dptr(a), 3, dptr(t), ctx) == 3
     finally:
         L.cleanup(ctypes.byref(ctx))
+
+
+@pytest.mark.parametrize("ediis", [False, True])
+@pytest.mark.parametrize("n,seed", [(1, 0), (3, 1), (8, 2), (15, 3)])
+def test_diis_coefficients_match_restatement(ediis, n, seed):
+    """The DIIS step of the projected iteration (aegpu_host_diis_coefficients) against
+    the numpy restatement of diis.h / diis.cpp, on Gram matrices of error vectors."""
+    from oracle.diis_ref import ediis as ediis_ref, pulay
+    rng = np.random.default_rng(seed)
+    E = rng.normal(size=(n, 40)) * np.geomspace(1, 1e-3, n)[:, None]  # shrinking errors
+    B = E @ E.T
+    c = np.zeros(n)
+    assert lib().aegpu_host_diis_coefficients(n, dptr(np.ascontiguousarray(B)), int(ediis), dptr(c)) == 0
+    want = ediis_ref(B) if ediis else pulay(B)
+    np.testing.assert_allclose(c, want, atol=1e-9, rtol=0)
+    if not ediis:
+        assert abs(c.sum() - 1) < 1e-12
+    else:
+        assert (c >= 0).all()
+
+
+def test_pulay_with_rank_deficient_errors():
+    from oracle.diis_ref import pulay
+    rng = np.random.default_rng(9)
+    e = rng.normal(size=(3, 20))
+    E = np.vstack([e, e[0] + e[1]])  # four errors spanning three directions
+    B = E @ E.T
+    c = np.zeros(4)
+    assert lib().aegpu_host_diis_coefficients(4, dptr(np.ascontiguousarray(B)), 0, dptr(c)) == 0
+    np.testing.assert_allclose(c, pulay(B), atol=1e-9, rtol=0)
