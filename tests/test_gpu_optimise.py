@@ -116,7 +116,7 @@ def test_projected_iteration_with_diis(golden):
         np.testing.assert_allclose(one[0], plain[0], atol=1e-9, rtol=0)
         assert abs(one[1] - plain[1]) < 1e-12 and one[2] < 1e-5
     for size, ediis in ((15, True), (6, False)):
-        x, E, gp, nh, nev, outer = e.optimise_projected(x0, p0, scale, gtol=1e-5, max_outer=500, diis=size,
+        x, E, gp, nh, nev, outer = e.optimise_projected(x0, p0, scale, gtol=1e-5, max_outer=200, diis=size,
                                                          ediis=ediis)
         assert outer >= 1 and np.isfinite(gp)
         assert abs(e.energy(scale * x[p0]) - E) < 1e-12
