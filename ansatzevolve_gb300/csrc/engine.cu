@@ -2904,8 +2904,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         // g = Re(T_C^dagger T_C) over the P tangent columns (tupsquantities.cpp:386-389):
         // with re / im interleaved the real dot product over D*W entries is Re(a^dagger b)
         const double one = 1.0, zero = 0.0;
-        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nparams, nparams, DW, &one, TC, DW, TC, DW, &zero, hs.MET,
-                    nparams);
+        cublasDsyrk(e->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, nparams, DW, &one, TC, DW, &zero, hs.MET, nparams);
     }
     if (proj) {
         // projected: <proj|T_C v> for every column (the last is <proj|psi>), bra for the sweeps
@@ -2916,8 +2915,9 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         // the V columns as V instances of the H product (the matrix or tables are shared)
         rc = run_apply(e, TC, HTC, nullptr, V, nullptr, false);
         if (rc) return rc;
+        // T_C^T (H T_C) is symmetric (H is): only its upper triangle is computed
         const double two = 2.0, zero = 0.0;
-        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, V, V, DW, &two, TC, DW, HTC, DW, &zero, THT, V);
+        cublasDsyrkx(e->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, V, DW, &two, TC, DW, HTC, DW, &zero, THT, V);
         // H psi for the backward sweeps: the last column
         cudaMemcpyAsync(e->d_h, HTC + (size_t)nparams * DW, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     }
@@ -2962,6 +2962,9 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     rc = stream_sync(e, "hessian");
     e->psi_valid = e->h_valid = false;
     if (rc) return rc;
+    if (metric)  // upper triangle (column-major) to the full symmetric matrix
+        for (int j = 0; j < nparams; ++j)
+            for (int i = j + 1; i < nparams; ++i) metric[(size_t)j * nparams + i] = metric[(size_t)i * nparams + j];
     if (proj) {
         // Hessian = C Hops C^T (fusedevolve.cpp:3171); gradient and overlap from <proj|T_C>
         for (size_t k = 0; k < (size_t)nparams * nparams; ++k) hess_comp[k] = 0.0;
@@ -2973,9 +2976,11 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         if (energy) *energy = tht[nparams];
         return AEGPU_OK;
     }
-    // Hessian = C Hops C^T + THT (fusedevolve.cpp:2762-2763); THT column-major V x V
+    // Hessian = C Hops C^T + THT (fusedevolve.cpp:2762-2763); THT column-major V x V,
+    // upper triangle (i <= j at tht[j * V + i])
     for (int i = 0; i < nparams; ++i)
-        for (int j = 0; j < nparams; ++j) hess_comp[(size_t)i * nparams + j] = tht[(size_t)j * V + i];
+        for (int j = 0; j < nparams; ++j)
+            hess_comp[(size_t)i * nparams + j] = i <= j ? tht[(size_t)j * V + i] : tht[(size_t)i * V + j];
     for (int a = 0; a < nops; ++a)
         for (int b = 0; b < nops; ++b)
             hess_comp[(size_t)param[a] * nparams + param[b]] += scale[a] * scale[b] * hops[(size_t)a * nops + b];
