@@ -30,7 +30,7 @@ CANDIDATES = {
     TUNE_OTF_THREADS: (128, 256, 512),
     TUNE_SPMV_TPR: (1, 2, 4, 8),
 }
-DEFAULT = {TUNE_PASS_OPS: 6, TUNE_CTAS_PER_SM: 8, TUNE_OTF_THREADS: 512, TUNE_SPMV_TPR: 0}
+DEFAULT = {TUNE_PASS_OPS: 6, TUNE_CTAS_PER_SM: 4, TUNE_OTF_THREADS: 512, TUNE_SPMV_TPR: 0}
 
 
 def cache_path():

@@ -1421,7 +1421,7 @@ struct aegpu_engine {
     // launch-shape knobs (aegpu_set_tuning): excitations per pass (<= kMaxWarpLayers),
     // CTAs per SM of the pass kernels, threads per CTA of the on-the-fly H kernel
     int tune_pass_ops = kMaxWarpLayers;
-    int tune_ctas_per_sm = 8;
+    int tune_ctas_per_sm = 4;  // best single-instance shape at 10-12 orbitals on GB300
     int tune_otf_threads = 512;
     int tune_spmv_tpr = 0;  // threads per stored-H row: 0 = by size (>= 4 CTAs per SM)
     int spmv_tpr() const
