@@ -37,6 +37,9 @@
 //                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
 //   k_otf_strings    y = H x with no stored matrix: CTA per alpha string, thread per
 //                    determinant, one FP64 FMA per matrix element (otf_tables.cpp)
+//   k_lanczos_update, k_scale_inverse
+//                    the device side of the Lanczos recurrence for the lowest eigenpair
+//                    (alpha and beta stay in device memory between the H products)
 // All reductions are two-stage and in a fixed order, so results are bit-identical
 // from run to run.
 #include "../../include/aegpu.h"
@@ -3019,6 +3022,26 @@ int aegpu_hessian_metric(aegpu_engine *e, const double *angles, const int *param
 // (tupsquantities.cpp:185-568, 1600-1769): the lowest eigenpair of H, overlaps of
 // evolved states with it, and the Hamiltonian / overlap matrices of a set of states.
 
+// Lanczos three-term step on the device: w -= alpha v + beta v_prev (beta, v_prev
+// absent on the first step), with alpha and beta read from device memory.
+__global__ void k_lanczos_update(double *__restrict__ w, const double *__restrict__ v, const double *__restrict__ vp,
+                                 const double *alpha, const double *beta, int64_t n)
+{
+    const double a = *alpha, b = vp ? *beta : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] = vp ? w[i] - a * v[i] - b * vp[i] : w[i] - a * v[i];
+}
+
+// w /= beta, or w = 0 when beta vanishes (the Krylov space is exhausted; the host
+// stops at that step).
+__global__ void k_scale_inverse(double *__restrict__ w, const double *beta, int64_t n)
+{
+    const double b = *beta;
+    const double f = b > 1e-300 ? 1.0 / b : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        w[i] *= f;
+}
+
 extern "C" {
 
 int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
@@ -3035,28 +3058,40 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
     if (rc) return rc;
     e->ground_valid = false;
     if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
+    // basis vectors, reorthogonalisation coefficients, alpha / beta of the recurrence,
+    // and the constants 1, 0, -1 for device-pointer cuBLAS calls
+    const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 3;
     double *Vb = e->alloc<double>((size_t)(m + 1) * n);
-    double *d_c = e->alloc<double>((size_t)m + 1);
+    double *scal = e->alloc<double>(nscal);
     auto release = [&] {
+        cublasSetPointerMode(e->cublas, CUBLAS_POINTER_MODE_HOST);
         e->release(Vb, (size_t)(m + 1) * n * sizeof(double));
-        e->release(d_c, (size_t)(m + 1) * sizeof(double));
+        e->release(scal, nscal * sizeof(double));
     };
-    if (!Vb || !d_c) {
+    if (!Vb || !scal) {
         release();
         return e->fail(AEGPU_ERR_NOMEM, "Lanczos basis allocation failed");
     }
+    double *d_c = scal, *d_alpha = scal + (m + 1), *d_beta = d_alpha + m, *d_k = d_beta + m;
+    const double consts[3] = {1.0, 0.0, -1.0};
     cublasHandle_t h = e->cublas;
     cudaStream_t s = e->stream;
+    cudaMemcpyAsync(d_k, consts, sizeof(consts), cudaMemcpyHostToDevice, s);
     const int ni = (int)n;
-    const double one = 1.0, zero = 0.0, mone = -1.0;
+    const double one = 1.0, zero = 0.0;
+    const int vgrid = (int)std::min<int64_t>(((int64_t)n + 255) / 256, (int64_t)e->sm_count * 8);
     // Lanczos with full reorthogonalisation from the initial state, restarted from the
-    // Ritz vector when the basis is full
+    // Ritz vector when the basis is full.  The recurrence runs on the device (alpha and
+    // beta stay in device memory, cuBLAS in device-pointer mode); the host reads them and
+    // checks the Ritz pair every kCheck products.
+    constexpr int kCheck = 8;
     cudaMemcpyAsync(e->d_ground, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     int prod = 0;
     bool done = false;
     std::vector<double> al, be, sv;
     while (!done) {
         double nx = 0.0;
+        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST);
         cublasDnrm2(h, ni, e->d_ground, 1, &nx);
         if (!(nx > 0.0)) {
             release();
@@ -3065,43 +3100,51 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
         cudaMemcpyAsync(Vb, e->d_ground, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
         const double inx = 1.0 / nx;
         cublasDscal(h, ni, &inx, Vb, 1);
-        al.clear();
-        be.clear();
-        int k = 0;
-        for (int j = 0; j < m; ++j) {
+        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_DEVICE);
+        int k = 0, checked = 0;
+        for (int j = 0; j < m && !done; ++j) {
             double *v = Vb + (size_t)j * n, *w = Vb + (size_t)(j + 1) * n;
             if ((rc = run_apply(e, v, w, nullptr, 1, nullptr, false))) {
                 release();
                 return rc;
             }
             ++prod;
-            double a = 0.0, b = 0.0;
-            cublasDdot(h, ni, v, 1, w, 1, &a);
-            const double ma = -a;
-            cublasDaxpy(h, ni, &ma, v, 1, w, 1);
-            if (j > 0) {
-                const double mb = -be[j - 1];
-                cublasDaxpy(h, ni, &mb, Vb + (size_t)(j - 1) * n, 1, w, 1);
-            }
+            cublasDdot(h, ni, v, 1, w, 1, d_alpha + j);
+            k_lanczos_update<<<vgrid, 256, 0, s>>>(w, v, j ? Vb + (size_t)(j - 1) * n : nullptr, d_alpha + j,
+                                                   j ? d_beta + (j - 1) : nullptr, (int64_t)n);
             for (int pass = 0; pass < 2; ++pass) {
-                cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, &one, Vb, ni, w, 1, &zero, d_c, 1);
-                cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, &mone, Vb, ni, d_c, 1, &one, w, 1);
+                cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, d_k, Vb, ni, w, 1, d_k + 1, d_c, 1);
+                cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, d_k + 2, Vb, ni, d_c, 1, d_k, w, 1);
             }
-            cublasDnrm2(h, ni, w, 1, &b);
-            al.push_back(a);
-            be.push_back(b);
-            k = j + 1;
-            const double theta = ae::tridiag_lowest(al, be, k, sv);
-            const double est = std::abs(b * sv[k - 1]);
-            if (est <= 0.5 * tol || prod >= max_products || k == ni || !(b > 1e-300)) {
-                done = true;
-                break;
+            cublasDnrm2(h, ni, w, 1, d_beta + j);
+            k_scale_inverse<<<vgrid, 256, 0, s>>>(w, d_beta + j, (int64_t)n);
+            e->launches += 2;
+            const int jn = j + 1;
+            if (jn - checked < kCheck && jn < m && prod < max_products && jn < ni) continue;
+            // read alpha / beta so far; the first k at which the Ritz pair converged, or the
+            // basis is exhausted (beta ~ 0), ends the run
+            al.resize(jn);
+            be.resize(jn);
+            cudaMemcpyAsync(al.data(), d_alpha, jn * sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(be.data(), d_beta, jn * sizeof(double), cudaMemcpyDeviceToHost, s);
+            if ((rc = stream_sync(e, "Lanczos"))) {
+                release();
+                return rc;
             }
-            (void)theta;
-            const double ib = 1.0 / b;
-            cublasDscal(h, ni, &ib, w, 1);
+            for (int kk = checked + 1; kk <= jn; ++kk) {
+                std::vector<double> a(al.begin(), al.begin() + kk), b(be.begin(), be.begin() + kk);
+                ae::tridiag_lowest(a, b, kk, sv);
+                k = kk;
+                if (std::abs(be[kk - 1] * sv[kk - 1]) <= 0.5 * tol || !(be[kk - 1] > 1e-300)) {
+                    done = true;
+                    break;
+                }
+            }
+            checked = jn;
+            if (prod >= max_products || jn == ni) done = true;
         }
-        // Ritz vector: x = V s (restart vector, or the result)
+        // Ritz vector: x = V s over the first k basis vectors (restart vector, or the result)
+        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST);
         cudaMemcpyAsync(d_c, sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
         cublasDgemv(h, CUBLAS_OP_N, ni, k, &one, Vb, ni, d_c, 1, &zero, e->d_ground, 1);
         if ((rc = stream_sync(e, "Lanczos"))) {
