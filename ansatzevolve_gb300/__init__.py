@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
 _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
-TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR = 1, 2, 3, 4
+TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL = 1, 2, 3, 4, 5
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 PROP_HESSIAN, PROP_OVERLAP = 1, 2
 # rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)
@@ -209,7 +209,7 @@ class Engine:
         for knob in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM):
             if tuning and knob in tuning:
                 self._check(self.L.aegpu_set_tuning(h, knob, int(tuning[knob])))
-        for knob in (TUNE_OTF_THREADS, TUNE_SPMV_TPR):
+        for knob in (TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL):
             if tuning and knob in tuning:
                 self._check(self.L.aegpu_set_tuning(h, knob, int(tuning[knob])))
         ops = _i32(ops0).reshape(-1, 4)
@@ -504,7 +504,7 @@ class Engine:
 
     def tuning(self):
         return {k: int(self.L.aegpu_get_tuning(self.h, k))
-                for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR)}
+                for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL)}
 
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))

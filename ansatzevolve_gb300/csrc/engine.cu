@@ -421,11 +421,32 @@ __global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *
 
 // Instance b = blockIdx.y.  ckpt (nullable): the pass's amplitudes after rotation,
 // stored in the pass's orbit order (same index as the rank list), for the adjoint.
+// Programmatic dependent launch: a pass kernel launched with the programmatic-
+// serialisation attribute may start while the previous kernel drains.  Before the
+// wait it touches only set-up data (task lists and orbit rank / bitstring tables,
+// written before any evaluation); after it, everything the previous kernels wrote is
+// visible.  It then lets its own successor start, which in turn can only pass its
+// wait once this grid has completed.  Without the attribute both are no-ops.
+__device__ __forceinline__ void pdl_prologue(const BlockArgs &a, const WarpTask *__restrict__ tasks, int ntasks)
+{
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (t < ntasks) {
+        const WarpTask task = tasks[t];
+        if (2 * lane < (int)task.n) {  // inside this task's entries
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.idx + task.elem_off + 2 * lane));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(a.obits + task.elem_off + 2 * lane));
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <int W>
 __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const WarpTask *__restrict__ tasks, int ntasks,
                                                            double *vecs, int64_t inst_stride, double *__restrict__ ckpt,
                                                            int64_t ckpt_stride)
 {
+    pdl_prologue(a, tasks, ntasks);
     const int lane = threadIdx.x & 31, b = blockIdx.y;
     if (skip_instance(a.active, b)) return;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
@@ -493,6 +514,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
                                                            int64_t part_stride)
 {
     __shared__ double red[kMaxWarpLayers][kWarpThreads / 32];
+    pdl_prologue(a, tasks, ntasks);
     const int lane = threadIdx.x & 31, b = blockIdx.y;
     if (skip_instance(a.active, b)) return;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
@@ -1427,6 +1449,12 @@ struct aegpu_engine {
     int tune_ctas_per_sm = 4;  // best single-instance shape at 10-12 orbitals on GB300
     int tune_otf_threads = 512;
     int tune_spmv_tpr = 0;  // threads per stored-H row: 0 = by size (>= 4 CTAs per SM)
+    // programmatic dependent launch of the pass kernels: -1 = by size (on up to 2^20
+    // amplitudes per launch, where launch latency is a visible share of a pass; off
+    // above, where early-resident dependents slow the FP64-bound passes: GB300,
+    // 8 / 10 orbitals -6 %, 12 orbitals +1.5 %)
+    int tune_pdl = -1;
+    bool pdl_on() const { return tune_pdl >= 0 ? tune_pdl != 0 : (int64_t)B.D * W * nb <= (int64_t)1 << 20; }
     int spmv_tpr() const
     {
         if (tune_spmv_tpr) return tune_spmv_tpr;
@@ -1701,6 +1729,24 @@ int set_smem_limits(int dev)
 
 // Forward evolution of the first ninst instances from the start vector (pass
 // constants already prepared from d_ang).
+// Launch of a pass kernel, with the programmatic-serialisation attribute when the PDL
+// knob is on (captured graphs keep it as a programmatic edge).
+template <typename... KArgs, typename... Args>
+void launch_pass(const aegpu_engine *e, void (*kernel)(KArgs...), dim3 grid, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kWarpThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = e->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = e->pdl_on() ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 int run_evolve(aegpu_engine *e, int ninst)
 {
     NvtxRange r("aegpu evolve");
@@ -1720,9 +1766,9 @@ int run_evolve(aegpu_engine *e, int ninst)
             BlockArgs a = e->block_args(bi, 1.0);
             const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
-                k_warp_rot<1><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
+                launch_pass(e, k_warp_rot<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             else
-                k_warp_rot<2><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
+                launch_pass(e, k_warp_rot<2>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             e->launches += 1;
         }
     }
@@ -1830,11 +1876,11 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
             BlockArgs a = e->block_args(bi, -1.0);
             const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
-                k_warp_adj<1><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n, part,
-                                                                 e->n_partials);
+                launch_pass(e, k_warp_adj<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n,
+                            part, e->n_partials);
             else
-                k_warp_adj<2><<<g, kWarpThreads, 0, e->stream>>>(a, b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n, part,
-                                                                 e->n_partials);
+                launch_pass(e, k_warp_adj<2>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n,
+                            part, e->n_partials);
             e->launches += 1;
         } else {
             cudaMemset2DAsync(part, e->n_partials * sizeof(double), 0, (size_t)b.wgrid * kMaxSlots * sizeof(double),
@@ -2432,6 +2478,11 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         if (e->ham_kind) return e->fail(AEGPU_ERR_STATE, "set the thread count before the Hamiltonian");
         e->tune_otf_threads = value;
         return AEGPU_OK;
+    case AEGPU_TUNE_PDL:
+        if (value < -1 || value > 1) return e->fail(AEGPU_ERR_ARG, "programmatic dependent launch must be -1, 0 or 1");
+        e->tune_pdl = value;
+        e->drop_graph();
+        return AEGPU_OK;
     case AEGPU_TUNE_SPMV_TPR:
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return e->fail(AEGPU_ERR_ARG, "threads per row must be 0 (by size), 1, 2, 4 or 8");
@@ -2451,6 +2502,7 @@ int aegpu_get_tuning(const aegpu_engine *e, int knob)
     case AEGPU_TUNE_CTAS_PER_SM: return e->tune_ctas_per_sm;
     case AEGPU_TUNE_OTF_THREADS: return e->tune_otf_threads;
     case AEGPU_TUNE_SPMV_TPR: return e->spmv_tpr();
+    case AEGPU_TUNE_PDL: return e->pdl_on() ? 1 : 0;
     default: return -1;
     }
 }

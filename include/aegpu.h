@@ -89,9 +89,13 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * excitations fused per pass (1..6; before aegpu_set_problem), CTAs per SM of the
  * pass kernels (1..64; before aegpu_set_problem), threads per CTA of the on-the-fly
  * H kernel (64..512, multiple of 32; before the Hamiltonian), threads per row of the
- * stored-H product (1, 2, 4, 8; 0 = chosen by size; before the first evaluation).
- * No counterpart in the reference. */
-enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4 };
+ * stored-H product (1, 2, 4, 8; 0 = chosen by size; before the first evaluation),
+ * programmatic dependent launch of the pass kernels (0 off, 1 on, -1 by size, the
+ * default: on up to 2^20 amplitudes per launch; each pass's CTAs are scheduled while
+ * the previous pass drains and wait on the device for its results; any time, it
+ * rebuilds the captured graphs).  No counterpart in the reference. */
+enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
+       AEGPU_TUNE_PDL = 5 };
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
 int aegpu_batch_size(const aegpu_engine *e);

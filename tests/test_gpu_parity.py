@@ -204,6 +204,38 @@ def test_device_resident_graph_path_matches_host_path():
     eng.close()
 
 
+@pytest.mark.parametrize("N,layers,batch", [(10, 3, 1), (12, 3, 1), (8, 2, 16)])
+def test_programmatic_dependent_launch_is_bit_identical(N, layers, batch):
+    """With the pass kernels launched as programmatic dependents (AEGPU_TUNE_PDL) the
+    host path, the captured-graph path and a batch give bit-identical energies and
+    gradients to the plain launches."""
+    torch = pytest.importorskip("torch")
+    pb = synthetic_problem(N, N // 2, N // 2, layers, 0)
+    ops0 = np.asarray(pb["ops_1b"]) - 1
+    rng = np.random.default_rng(N)
+    angs = rng.uniform(-0.3, 0.3, (batch, len(ops0)))
+    out = []
+    for pdl in (0, 1):
+        eng = ae.Engine(2 * N, ae.BASIS_SZ, N, N // 2, N // 2, ops0, tuning={ae.TUNE_PDL: pdl})
+        eng.set_batch(batch)
+        init = np.zeros(eng.D)
+        init[np.searchsorted(eng.states(), pb["hf"])] = 1.0
+        eng.set_initial(init)
+        eng.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+        E, g = eng.gradient(angs.ravel())
+        a = torch.tensor(angs.ravel(), dtype=torch.float64, device="cuda")
+        Ed = torch.zeros(batch, dtype=torch.float64, device="cuda")
+        gd = torch.zeros(batch * len(ops0), dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            eng.gradient_dev(a.data_ptr(), Ed.data_ptr(), gd.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        out.append((np.atleast_1d(E), np.ravel(g), Ed.cpu().numpy(), gd.cpu().numpy()))
+        eng.close()
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(out[1][0], out[1][2]) and np.array_equal(out[1][1], out[1][3])
+
+
 def test_14_orbital_on_the_fly_rows_and_gradient():
     """14 orbitals, 7a+7b (11,778,624 determinants), H applied on the fly.  The oracle
     checks H x on sampled rows (a full apply would take minutes on the host); the
