@@ -174,3 +174,24 @@ def test_writeproperties_verb_on_run_files(golden, tmp_path):
     assert nr == int(px["subspace_null_rank"])
     assert "Elec. Energy" in text and "MagOfOverlapWithState_0" in text
     assert lam < rows[0].min()
+
+
+def test_writeproperties_verb_complex_and_extracted_min(golden, tmp_path):
+    """The writeproperties verb on the complex H4 inputs (diagonal phase operators),
+    with the angle sets read from an extractedmin file instead of the Parameters file:
+    rows equal the reference's for the same sets."""
+    from ansatzevolve_gb300.runfiles import properties_run, write_extracted_min
+    from tests.test_gpu_runfiles import write_fixture
+    px = golden("props_h4c")
+    fx = golden("h4c")
+    prefix = str(tmp_path / "H4c")
+    P = int(np.asarray(fx["order_1b"]).max())
+    write_fixture(prefix, fx, [np.zeros(P)])  # Parameters: one set, P angles (sizes extractedmin)
+    write_extracted_min(prefix + "_extractedmin", px["sets"])
+    table, w, nr, lam, text = properties_run(prefix, extracted_min=True)
+    rows = np.array([table[n] for n in ae.PROPERTY_NAMES])
+    np.testing.assert_allclose(rows[:3], px["rows"][:3], atol=1e-10, rtol=0)
+    assert np.array_equal(rows[3:12], px["rows"][3:12])
+    np.testing.assert_allclose(rows[15], px["rows"][14], atol=1e-9, rtol=0)
+    np.testing.assert_allclose(w, px["subspace_eigs"], atol=1e-10, rtol=0)
+    assert nr == int(px["subspace_null_rank"])
