@@ -161,6 +161,7 @@ def lib(build_if_missing=True):
         "setNuclearEnergy": (ctypes.c_int, [ctypes.c_double, _P]),
         "optimise": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
         "setRunFiles": (ctypes.c_int, [ctypes.c_char_p, _P]),
+        "getExpectationValues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _P]),
         "getProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
         "getLowestEigenvalue": (ctypes.c_int, [_DP, _DP, _P]),
         "getSubspaceEigenvalues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _IP, _P]),
@@ -735,7 +736,14 @@ class stateAnsatzManager:
         return H.reshape(len(a), len(a), order="F")
 
     def getExpectationValues(self, angles):
-        return np.array([self.getExpectationValue(row) for row in np.atleast_2d(angles)])
+        """Energies of the angle rows (compressed or per operator), one batched GPU
+        evaluation (evolveMultiple + getEnergies in the reference)."""
+        a = _f64(np.atleast_2d(angles))
+        E = np.zeros(a.shape[0])
+        rc = self.L.getExpectationValues(a.shape[0], a.shape[1], dptr(a), dptr(E), self.ctx)
+        if rc:
+            raise AegpuError("getExpectationValues returned %d" % rc)
+        return E
 
     def getProperties(self, paths, hessian=True, overlap=True):
         """writeProperties' table: {row name: values per path} (PROPERTY_NAMES rows, NaN

@@ -309,6 +309,19 @@ int getProperties(int npaths, int nangles, const double *angles, int flags, doub
     return 0;
 }
 
+int getExpectationValues(int nrows, int nangles, const double *angles, double *energies, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (nrows < 1 || nangles < 1 || !angles || !energies) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> E;
+    if (!m->getExpectationValues(std::vector<double>(angles, angles + (size_t)nrows * nangles), nrows, nangles, E))
+        return 3;
+    std::copy(E.begin(), E.end(), energies);
+    return 0;
+}
+
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx)
 {
     if (ctx == nullptr) return 1;

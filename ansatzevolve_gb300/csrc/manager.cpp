@@ -547,21 +547,51 @@ bool stateAnsatzManager::getHessianComp(const std::vector<double> &a, std::vecto
     return setAngles(a) && getHessianComp(H);
 }
 
+// AnsatzManager.cpp:709-754 (evolveMultiple + getEnergies): the rows are evaluated as
+// instances of a batched engine (shared Hamiltonian), in chunks whose per-instance
+// buffers (state, H*state, pass checkpoints) stay within a few GB; the engine returns to
+// a batch of one afterwards.
 bool stateAnsatzManager::getExpectationValues(const std::vector<double> &angles, int nrows, int ncols, std::vector<double> &E)
 {
     if (!validateToRun()) return false;
     if (nrows < 0 || ncols < 0 || angles.size() != (size_t)nrows * ncols) { log_line("Incorrect angle matrix"); return false; }
-    E.assign(nrows, 0.0);
+    const size_t nops = m_excitations.size();
+    std::vector<double> all((size_t)nrows * nops);
     for (int r = 0; r < nrows; ++r) {
         std::vector<double> row(angles.begin() + (size_t)r * ncols, angles.begin() + (size_t)(r + 1) * ncols), a;
         if (!decompress(row, a)) return false;
-        int rc = aegpu_energy(m_engine, a.data(), &E[r]);
-        if (rc) { log_line(std::string("energy failed: ") + aegpu_last_error(m_engine)); return false; }
-        E[r] += m_nuclearEnergy;
+        std::copy(a.begin(), a.end(), all.begin() + (size_t)r * nops);
+    }
+    E.assign(nrows, 0.0);
+    int64_t info[8] = {0};
+    aegpu_problem_info(m_engine, info);
+    const double perInstance = (double)(info[2] + 4) * (double)info[0] * (m_complex ? 16.0 : 8.0);
+    const int chunk = (int)std::max(1.0, std::min({256.0, (double)nrows, 8e9 / std::max(perInstance, 1.0)}));
+    bool ok = true;
+    for (int r0 = 0; r0 < nrows && ok; r0 += chunk) {
+        const int n = std::min(chunk, nrows - r0);
+        // a short last chunk repeats its last row up to the batch size (no reallocation)
+        std::vector<double> a((size_t)chunk * nops), e(chunk);
+        for (int k = 0; k < chunk; ++k) {
+            const int src = r0 + std::min(k, n - 1);
+            std::copy(all.begin() + (size_t)src * nops, all.begin() + (size_t)(src + 1) * nops, a.begin() + (size_t)k * nops);
+        }
+        int rc = aegpu_set_batch(m_engine, chunk);
+        if (!rc) rc = aegpu_energy(m_engine, a.data(), e.data());
+        if (rc) {
+            log_line(std::string("energy failed: ") + aegpu_last_error(m_engine));
+            ok = false;
+            break;
+        }
+        for (int k = 0; k < n; ++k) E[r0 + k] = e[k] + m_nuclearEnergy;
+    }
+    if (aegpu_set_batch(m_engine, 1)) {
+        log_line(std::string("restoring a batch of one failed: ") + aegpu_last_error(m_engine));
+        return false;
     }
     // leave the manager's current state where it was
     m_haveEvolved = false;
-    return evolveIfNeeded();
+    return ok && evolveIfNeeded();
 }
 
 bool stateAnsatzManager::getLowestEigenvalue(double &eigenvalue, double &residual, double tol)

@@ -70,6 +70,10 @@ int setRunFiles(const char *prefix, void *ctx);
  * with the lowest eigenvector with AEGPU_PROP_OVERLAP; NaN where not computed).
  * getLowestEigenvalue: the lowest eigenvalue of H in the sector (electronic).
  * getSubspaceEigenvalues: the npaths eigenvalues of S^-1/2 H S^-1/2 and S's null rank. */
+/* getExpectationValues: energies (with the nuclear energy) of nrows angle rows of
+ * nangles (compressed or per operator), evaluated as one batch on the GPU
+ * (stateAnsatzManager::getExpectationValues, src/AnsatzManager.cpp:709-754). */
+int getExpectationValues(int nrows, int nangles, const double *angles, double *energies, void *ctx);
 int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx);
 int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank,

@@ -318,3 +318,33 @@ def test_hessian_12_orbitals_directional_derivative():
     fd = (grad(x + h * d) - grad(x - h * d)) / (2 * h)
     np.testing.assert_allclose(H @ d, fd, atol=5e-6, rtol=0)
     eng.close()
+
+
+@pytest.mark.parametrize("name", ["h4", "h4c", "syn8"])
+def test_get_expectation_values_batched(golden, name):
+    """getExpectationValues evaluates its rows as one batch (evolveMultiple +
+    getEnergies): bit-identical to the row-by-row energies, compressed or per-operator
+    rows, and the manager keeps working with a batch of one afterwards (Hessian)."""
+    fx = golden(name)
+    if name.startswith("syn"):
+        N = int(fx["N"])
+        pb = synthetic_problem(N, int(fx["na"]), int(fx["nb"]), int(fx["layers"]), int(fx["seed"]))
+        m = ae.stateAnsatzManager()
+        assert m.storeInitial(2 * N, [int(fx["hf"])], [1.0])
+        assert m.storeOperators(np.asarray(fx["ops_1b"]).tolist())
+        assert m.storeParameterDependencies(list(zip(np.asarray(fx["order_1b"]) - 1, fx["scale"])))
+        assert m.storeIntegrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    else:
+        m = manager_from_fixture(fx)
+    P = int(np.asarray(fx["order_1b"]).max())
+    rows = np.random.default_rng(2).uniform(-0.5, 0.5, (7, P))
+    single = np.array([m.getExpectationValue(r) for r in rows])
+    batch = m.getExpectationValues(rows)
+    assert np.array_equal(batch, single)
+    p0, sc = np.asarray(fx["order_1b"]) - 1, np.asarray(fx["scale"])
+    ops_rows = sc * rows[:, p0]
+    assert np.array_equal(m.getExpectationValues(ops_rows), single)
+    H = m.getHessianComp(np.asarray(fx["angles"][0])[:P])
+    if "H" in fx:
+        np.testing.assert_allclose(H, fx["H"][0], atol=TOL_G, rtol=0)
+    assert abs(m.getExpectationValue(np.asarray(fx["angles"][0])[:P]) - fx["E"][0]) < TOL_E
