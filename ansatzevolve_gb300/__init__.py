@@ -171,6 +171,11 @@ def lib(build_if_missing=True):
         "aegpu_run_files_sizes": (ctypes.c_int, [_P] + [_IP] * 6),
         "aegpu_run_files_get": (ctypes.c_int, [_P, _IP, _DP, _IP, _IP, _DP, _DP, _DP, _DP]),
         "aegpu_run_files_free": (None, [_P]),
+        "aegpu_run_file_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
+        "aegpu_run_files_parameters": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
+                                                      ctypes.POINTER(_P)]),
+        "getGradient": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
+        "getHessian": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -629,6 +634,7 @@ class stateAnsatzManager:
         self._order = None
         self._nq = None
         self._P = None
+        self._angles = None
 
     def close(self):
         if getattr(self, "ctx", None) is not None and self.ctx.value:
@@ -698,16 +704,50 @@ class stateAnsatzManager:
         h1 = _f64(h1)
         return self.L.setIntegrals(h1.shape[0], dptr(h1), dptr(_f64(g2)), mode, self.ctx) == 0
 
-    def getExpectationValue(self, angles):
-        a = _f64(angles)
+    # current angles (setAngles / getAngles, AnsatzManager.cpp:467-506): the getters
+    # without angles evaluate at them, the getters with angles set them first
+    def setAngles(self, angles):
+        a = _f64(angles).copy()
+        n_ops = len(self._ops) if self._ops is not None else None
+        if self._P is not None and n_ops is not None and a.size not in (self._P, n_ops):
+            return False
+        self._angles = a
+        return True
+
+    def getAngles(self):
+        """The current angles, compressed (the first operator of each parameter divided
+        by its scale when per-operator angles were set)."""
+        a = self._current(None)
+        if self._order is None or a.size == self._P:
+            return a.copy()
+        x = np.zeros(self._P)
+        seen = np.zeros(self._P, dtype=bool)
+        for o, (p, c) in enumerate(self._order):
+            if not seen[p] and c != 0:
+                x[p], seen[p] = a[o] / c, True
+        return x
+
+    def _current(self, angles):
+        if angles is not None:
+            if not self.setAngles(angles):
+                raise AegpuError("Incorrect number of angles given %d" % np.size(angles))
+        if getattr(self, "_angles", None) is None:
+            raise AegpuError("no angles set")
+        return self._angles
+
+    def _per_op(self, a):
+        return self._ops is not None and self._P is not None and a.size == len(self._ops) and a.size != self._P
+
+    def getExpectationValue(self, angles=None):
+        a = self._current(angles)
         E = np.zeros(1)
         rc = self.L.getEnergy(len(a), dptr(a), dptr(E), self.ctx)
         if rc:
             raise AegpuError("getEnergy returned %d" % rc)
         return E[0]
 
-    def getFinalState(self, angles, complex_state=False):
-        a = _f64(angles)
+    def getFinalState(self, angles=None, complex_state=False):
+        a = self._current(angles)
         n = 1 << self._nq
         if complex_state:
             out = np.zeros(n, dtype=np.complex128)
@@ -719,16 +759,46 @@ class stateAnsatzManager:
             raise AegpuError("getFinalState returned %d" % rc)
         return out
 
-    def getGradientComp(self, angles):
-        a = _f64(angles)
+    def getGradient(self, angles=None):
+        """Derivatives with respect to every operator's angle (the reference's fused build
+        traps here; every operator is its own parameter)."""
+        a = self._current(angles)
+        g = np.zeros(len(self._ops))
+        rc = self.L.getGradient(len(a), dptr(a), dptr(g), self.ctx)
+        if rc:
+            raise AegpuError("getGradient returned %d" % rc)
+        return g
+
+    def getHessian(self, angles=None):
+        a = self._current(angles)
+        n = len(self._ops)
+        H = np.zeros(n * n)
+        rc = self.L.getHessian(len(a), dptr(a), dptr(H), self.ctx)
+        if rc:
+            raise AegpuError("getHessian returned %d" % rc)
+        return H.reshape(n, n)
+
+    def _compress_rows(self):
+        C = np.zeros((self._P, len(self._order)))
+        for o, (p, c) in enumerate(self._order):
+            C[p, o] = c
+        return C
+
+    def getGradientComp(self, angles=None):
+        a = self._current(angles)
+        if self._per_op(a):  # the C entry point takes compressed angles only
+            return self._compress_rows() @ self.getGradient()
         g = np.zeros(len(a))
         rc = self.L.getGradient_COMP(len(a), dptr(a), dptr(g), self.ctx)
         if rc:
             raise AegpuError("getGradient_COMP returned %d" % rc)
         return g
 
-    def getHessianComp(self, angles):
-        a = _f64(angles)
+    def getHessianComp(self, angles=None):
+        a = self._current(angles)
+        if self._per_op(a):
+            C = self._compress_rows()
+            return C @ self.getHessian() @ C.T
         H = np.zeros(len(a) * len(a))
         rc = self.L.getHessian_COMP(len(a), dptr(a), dptr(H), self.ctx)
         if rc:
@@ -773,10 +843,18 @@ class stateAnsatzManager:
             raise AegpuError("getSubspaceEigenvalues returned %d" % rc)
         return w, nr.value
 
-    def optimise(self, angles):
-        a = _f64(angles).copy()
+    def optimise(self, angles=None):
+        """Newton-Raphson from the given (or current) angles; returns (energy, optimised
+        compressed angles) and makes them the current angles (the reference binding's
+        optimise() returns only its success flag)."""
+        a = _f64(self._current(angles)).copy()
         E = np.zeros(1)
         rc = self.L.optimise(len(a), dptr(a), dptr(E), self.ctx)
         if rc:
             raise AegpuError("optimise returned %d" % rc)
+        self._angles = a.copy()
         return E[0], a
+
+
+# the reference binding's module functions (file readers), at package level as there
+from .runfiles import loadNuclearEnergy, loadOperators, loadParameters, loadPath, readCsvState  # noqa: E402,F401

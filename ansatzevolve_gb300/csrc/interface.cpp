@@ -309,6 +309,30 @@ int getProperties(int npaths, int nangles, const double *angles, int flags, doub
     return 0;
 }
 
+int getGradient(int NAngles, const double *angles, double *gradient, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (NAngles < 1 || !angles || !gradient) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> g;
+    if (!m->getGradient(std::vector<double>(angles, angles + NAngles), g)) return 3;
+    std::copy(g.begin(), g.end(), gradient);
+    return 0;
+}
+
+int getHessian(int NAngles, const double *angles, double *hessian, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (NAngles < 1 || !angles || !hessian) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> H;
+    if (!m->getHessian(std::vector<double>(angles, angles + NAngles), H)) return 3;
+    std::copy(H.begin(), H.end(), hessian);  // symmetric: row- and column-major agree
+    return 0;
+}
+
 int getExpectationValues(int nrows, int nangles, const double *angles, double *energies, void *ctx)
 {
     if (ctx == nullptr) return 1;

@@ -526,6 +526,42 @@ bool stateAnsatzManager::getHessianComp(std::vector<double> &H)
     return true;
 }
 
+// Per-operator derivatives (AnsatzManager.cpp:562-579, 608-624).  The reference's fused
+// build cannot provide them and traps; here they are the gradient and Hessian with
+// every operator its own parameter (identity compression).
+bool stateAnsatzManager::getGradient(std::vector<double> &g)
+{
+    if (!validateToRun()) return false;
+    g.assign(m_excitations.size(), 0.0);
+    double E;
+    int rc = aegpu_gradient(m_engine, m_angles.data(), &E, g.data());
+    if (rc) { log_line(std::string("gradient failed: ") + aegpu_last_error(m_engine)); return false; }
+    return true;
+}
+
+bool stateAnsatzManager::getHessian(std::vector<double> &H)
+{
+    if (!validateToRun()) return false;
+    const int n = (int)m_excitations.size();
+    std::vector<int> id(n);
+    for (int i = 0; i < n; ++i) id[i] = i;
+    std::vector<double> one(n, 1.0), g(n);
+    H.assign((size_t)n * n, 0.0);
+    double E;
+    int rc = aegpu_hessian(m_engine, m_angles.data(), id.data(), one.data(), n, &E, g.data(), H.data());
+    if (rc) { log_line(std::string("hessian failed: ") + aegpu_last_error(m_engine)); return false; }
+    return true;
+}
+
+bool stateAnsatzManager::getGradient(const std::vector<double> &a, std::vector<double> &g)
+{
+    return setAngles(a) && getGradient(g);
+}
+bool stateAnsatzManager::getHessian(const std::vector<double> &a, std::vector<double> &H)
+{
+    return setAngles(a) && getHessian(H);
+}
+
 bool stateAnsatzManager::getExpectationValue(const std::vector<double> &a, double &E)
 {
     return setAngles(a) && getExpectationValue(E);

@@ -48,12 +48,17 @@ public:
     bool getFinalState(std::vector<std::complex<double>> &finalState);   // 2^nq entries
     bool getGradientComp(std::vector<double> &gradient);
     bool getHessianComp(std::vector<double> &hessian);                   // P x P, row-major (symmetric)
+    // per operator (nOps and nOps x nOps): the reference's fused build traps here
+    bool getGradient(std::vector<double> &gradient);
+    bool getHessian(std::vector<double> &hessian);
 
     bool getExpectationValue(const std::vector<double> &angles, double &exptValue);
     bool getFinalState(const std::vector<double> &angles, std::vector<double> &finalState);
     bool getFinalState(const std::vector<double> &angles, std::vector<std::complex<double>> &finalState);
     bool getGradientComp(const std::vector<double> &angles, std::vector<double> &gradient);
     bool getHessianComp(const std::vector<double> &angles, std::vector<double> &hessian);
+    bool getGradient(const std::vector<double> &angles, std::vector<double> &gradient);
+    bool getHessian(const std::vector<double> &angles, std::vector<double> &hessian);
     // rows of `angles` (row-major, nrows x ncols) are angle sets; ncols = P or nOps
     bool getExpectationValues(const std::vector<double> &angles, int nrows, int ncols, std::vector<double> &exptValues);
 

@@ -240,15 +240,13 @@ bool LoadNuclearEnergy(double &nuclearEnergy, const std::string &prefix)
     return true;
 }
 
-bool loadRunFiles(const std::string &prefix, bool extractedMin, RunFiles &rf, std::string &err)
+bool loadParameters(const std::string &orderPath, const std::string &parameterPath, size_t nOps,
+                    const std::string &extractedMinPath, RunFiles &rf, std::string &err)
 {
-    rf = RunFiles();
-    if (!readCsvState(prefix + "_Initial.dat", rf.numberOfQubits, rf.initialIndex, rf.initialCoeff, err)) return false;
-    if (!loadOperators(prefix + "_Operators.dat", rf.operators, err)) return false;
-    if (!loadOrder(prefix + "_Order.dat", rf.orders, err)) return false;
-    if (rf.orders.size() != rf.operators.size()) {
-        err = prefix + "_Order.dat: " + std::to_string(rf.orders.size()) + " relations for " +
-              std::to_string(rf.operators.size()) + " operators (More operators in path than relations given)";
+    if (!loadOrder(orderPath, rf.orders, err)) return false;
+    if (rf.orders.size() != nOps) {
+        err = orderPath + ": " + std::to_string(rf.orders.size()) + " relations for " + std::to_string(nOps) +
+              " operators (More operators in path than relations given)";
         return false;
     }
     int maxOrder = -1;
@@ -258,25 +256,37 @@ bool loadRunFiles(const std::string &prefix, bool extractedMin, RunFiles &rf, st
     std::vector<std::vector<double>> raw;
     std::string perr;
     int lastCount = 0;
-    if (loadParameterFile(prefix + "_Parameters.dat", raw, rf.parameterEnergies, perr)) {
+    rf.parameterEnergies.clear();
+    if (loadParameterFile(parameterPath, raw, rf.parameterEnergies, perr)) {
         if (!raw.empty()) lastCount = (int)raw.back().size();
     } else if (perr.rfind("cannot open", 0) != 0) {
         err = perr;  // present but malformed
         return false;
     }
     rf.numberOfUniqueParameters = std::max(rf.numberOfParameters, lastCount);
-    if (extractedMin) {
-        rf.parameterEnergies.clear();
-        if (!loadExtractedMin(prefix + "_extractedmin", rf.numberOfUniqueParameters, raw, err)) return false;
+    if (!extractedMinPath.empty()) {
+        if (!loadExtractedMin(extractedMinPath, rf.numberOfUniqueParameters, raw, err)) return false;
         lastCount = rf.numberOfUniqueParameters;
         rf.parameterEnergies.assign(raw.size(), std::nan(""));
     }
+    rf.parameterSets.clear();
     for (const auto &set : raw) {
         std::vector<double> x((size_t)rf.numberOfParameters, 0.0);
         for (int p = 0; p < rf.numberOfParameters; ++p)
             if (p < lastCount && (size_t)p < set.size()) x[(size_t)p] = set[(size_t)p];
         rf.parameterSets.push_back(std::move(x));
     }
+    return true;
+}
+
+bool loadRunFiles(const std::string &prefix, bool extractedMin, RunFiles &rf, std::string &err)
+{
+    rf = RunFiles();
+    if (!readCsvState(prefix + "_Initial.dat", rf.numberOfQubits, rf.initialIndex, rf.initialCoeff, err)) return false;
+    if (!loadOperators(prefix + "_Operators.dat", rf.operators, err)) return false;
+    if (!loadParameters(prefix + "_Order.dat", prefix + "_Parameters.dat", rf.operators.size(),
+                        extractedMin ? prefix + "_extractedmin" : std::string(), rf, err))
+        return false;
     rf.haveNuclearEnergy = LoadNuclearEnergy(rf.nuclearEnergy, prefix);
     return true;
 }
@@ -322,6 +332,47 @@ int aegpu_run_files_load(const char *prefix, int extracted_min, aegpu_run_files 
     return 0;
 }
 
+int aegpu_run_file_read(const char *path, int kind, aegpu_run_files **out)
+{
+    if (!path || !*path || !out || kind < AEGPU_RUN_FILE_INITIAL || kind > AEGPU_RUN_FILE_NUCLEAR) {
+        g_run_files_error = "null, empty or unknown argument";
+        return 2;
+    }
+    *out = nullptr;
+    auto *f = new aegpu_run_files();
+    bool ok = true;
+    if (kind == AEGPU_RUN_FILE_INITIAL)
+        ok = ae::readCsvState(path, f->rf.numberOfQubits, f->rf.initialIndex, f->rf.initialCoeff, g_run_files_error);
+    else if (kind == AEGPU_RUN_FILE_OPERATORS)
+        ok = ae::loadOperators(path, f->rf.operators, g_run_files_error);
+    else
+        f->rf.haveNuclearEnergy = ae::LoadNuclearEnergy(f->rf.nuclearEnergy, path);
+    if (!ok) {
+        delete f;
+        return 3;
+    }
+    g_run_files_error.clear();
+    *out = f;
+    return 0;
+}
+
+int aegpu_run_files_parameters(const char *order_path, const char *parameter_path, int n_ops, aegpu_run_files **out)
+{
+    if (!order_path || !*order_path || !parameter_path || n_ops < 0 || !out) {
+        g_run_files_error = "null or empty argument";
+        return 2;
+    }
+    *out = nullptr;
+    auto *f = new aegpu_run_files();
+    if (!ae::loadParameters(order_path, parameter_path, (size_t)n_ops, std::string(), f->rf, g_run_files_error)) {
+        delete f;
+        return 3;
+    }
+    g_run_files_error.clear();
+    *out = f;
+    return 0;
+}
+
 const char *aegpu_run_files_error(void) { return g_run_files_error.c_str(); }
 
 int aegpu_run_files_sizes(const aegpu_run_files *f, int *nq, int *n_initial, int *n_ops, int *n_params,
@@ -330,7 +381,7 @@ int aegpu_run_files_sizes(const aegpu_run_files *f, int *nq, int *n_initial, int
     if (!f) return 2;
     if (nq) *nq = f->rf.numberOfQubits;
     if (n_initial) *n_initial = (int)f->rf.initialIndex.size();
-    if (n_ops) *n_ops = (int)f->rf.operators.size();
+    if (n_ops) *n_ops = (int)std::max(f->rf.operators.size(), f->rf.orders.size());
     if (n_params) *n_params = f->rf.numberOfParameters;
     if (n_unique) *n_unique = f->rf.numberOfUniqueParameters;
     if (n_sets) *n_sets = (int)f->rf.parameterSets.size();
@@ -349,6 +400,7 @@ int aegpu_run_files_get(const aegpu_run_files *f, int *initial_index, double *in
             initial_coeff[2 * i + 1] = rf.initialCoeff[i].imag();
         }
     }
+    // a handle holds operators, orders or both (a single file read fills one of them)
     for (size_t i = 0; i < rf.operators.size(); ++i) {
         const ae::Exc4 &e = rf.operators[i];
         if (operators_1b) {
@@ -357,6 +409,8 @@ int aegpu_run_files_get(const aegpu_run_files *f, int *initial_index, double *in
             operators_1b[4 * i + 2] = e.third + 1;
             operators_1b[4 * i + 3] = e.fourth + 1;
         }
+    }
+    for (size_t i = 0; i < rf.orders.size(); ++i) {
         if (order_1b) order_1b[i] = rf.orders[i].first + 1;
         if (scale) scale[i] = rf.orders[i].second;
     }

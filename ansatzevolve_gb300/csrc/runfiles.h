@@ -55,6 +55,12 @@ bool loadExtractedMin(const std::string &path, int n, std::vector<std::vector<do
 // TUPSLoadingUtils.cpp:156-173: false (energy 0) when the file is missing or empty.
 bool LoadNuclearEnergy(double &nuclearEnergy, const std::string &prefix);
 
+// TUPSLoadingUtils.cpp:176-296 (loadParameters): the order file (one relation per
+// operator, nOps of them) and the Parameters file (optional) into rf's orders, parameter
+// counts, angle sets and energies; with extractedMinPath, the sets of that file instead.
+bool loadParameters(const std::string &orderPath, const std::string &parameterPath, size_t nOps,
+                    const std::string &extractedMinPath, RunFiles &rf, std::string &err);
+
 // All of the above for one prefix, as the driver loads them (main.cpp:235-386).  A
 // missing Parameters file leaves no angle sets (the driver carries on with only the
 // zero-angle path); extractedMin replaces the Parameters file's sets with those of

@@ -43,14 +43,14 @@ class RunFiles:
         return int(self.order.max()) + 1 if len(self.order) else 0
 
 
-def load_run_files(prefix, extracted_min=False):
-    """All run files of `prefix`; raises AegpuError naming the file that is missing or
-    malformed.  The Parameters and Nuclear_Energy files are optional."""
+def _read(opener, what):
+    """Open a run-files handle through `opener(ctypes.byref(handle))` and copy out every
+    field (the ones the opener did not fill come back empty)."""
     L = lib()
     h = _P()
-    rc = L.aegpu_run_files_load(str(prefix).encode(), int(bool(extracted_min)), ctypes.byref(h))
+    rc = opener(ctypes.byref(h))
     if rc:
-        raise AegpuError("run files %s: %s" % (prefix, L.aegpu_run_files_error().decode()))
+        raise AegpuError("run files %s: %s" % (what, L.aegpu_run_files_error().decode()))
     try:
         n = [ctypes.c_int() for _ in range(6)]
         L.aegpu_run_files_sizes(h, *[ctypes.byref(v) for v in n])
@@ -72,6 +72,13 @@ def load_run_files(prefix, extracted_min=False):
                     operators=ops.reshape(nops, 4), order=order - 1, scale=scale, n_unique=nuniq,
                     parameter_sets=sets[:nsets * P].reshape(nsets, P), energies=energies[:nsets],
                     nuclear_energy=None if np.isnan(nuc[0]) else float(nuc[0]))
+
+
+def load_run_files(prefix, extracted_min=False):
+    """All run files of `prefix`; raises AegpuError naming the file that is missing or
+    malformed.  The Parameters and Nuclear_Energy files are optional."""
+    L = lib()
+    return _read(lambda h: L.aegpu_run_files_load(str(prefix).encode(), int(bool(extracted_min)), h), prefix)
 
 
 def write_initial(path, nq, index, coeff):
@@ -202,3 +209,55 @@ def properties_run(prefix, extracted_min=False, no_hf_path=False, no_hess=False,
     finally:
         m.close()
     return table, w, nr, lam, format_properties(table, have_hf=not no_hf_path)
+
+
+# ------------------------------------------------------------------------------
+# The reference binding's module functions (PyAnsatzEvolve.cpp:101-147), same names and
+# return shapes, over the C++ readers.  A rotation path is a list of (operator index,
+# angle) pairs; the reference's module fills the index with 0 (loadPath without an
+# operator pool).
+
+
+def loadOperators(filepath):
+    """Operators of an Operators file, 1-based [a, b, c, d] lists (0 = absent)."""
+    L = lib()
+    rf = _read(lambda h: L.aegpu_run_file_read(str(filepath).encode(), 2, h), filepath)
+    return [list(map(int, o)) for o in rf.operators]
+
+
+def loadPath(filepath):
+    """One (0, 0.0) rotation element per operator of an Operators file."""
+    return [(0, 0.0) for _ in loadOperators(filepath)]
+
+
+def loadNuclearEnergy(filepath):
+    """The number in <filepath>_Nuclear_Energy.dat, 0.0 when the file is missing."""
+    L = lib()
+    rf = _read(lambda h: L.aegpu_run_file_read(str(filepath).encode(), 3, h), filepath)
+    return 0.0 if rf.nuclear_energy is None else rf.nuclear_energy
+
+
+def readCsvState(filepath):
+    """The Initial file as a dense real vector of 2^(longest bitstring) entries (the
+    reference's real readCsvState drops imaginary parts)."""
+    L = lib()
+    rf = _read(lambda h: L.aegpu_run_file_read(str(filepath).encode(), 1, h), filepath)
+    out = np.zeros(1 << rf.nq)
+    out[rf.initial_index] = rf.initial_coeff.real
+    return out.tolist()
+
+
+def loadParameters(orderFilePath, parameterFilepath, templatePath):
+    """(rotationPaths, order, numberOfUniqueParameters) as the reference binding returns
+    them: the template path first (its own angles), then one path per angle set of the
+    Parameters file with angle = set[order] * scale (0 where the file's last set has no
+    such parameter); order is [(parameter, scale)], 0-based."""
+    L = lib()
+    template = [(int(i), float(a)) for i, a in templatePath]
+    rf = _read(lambda h: L.aegpu_run_files_parameters(str(orderFilePath).encode(), str(parameterFilepath).encode(),
+                                                      len(template), h), orderFilePath)
+    order = [(int(p), float(c)) for p, c in zip(rf.order, rf.scale)]
+    paths = [list(template)]
+    for x in rf.parameter_sets:
+        paths.append([(template[k][0], float(x[p] * c)) for k, (p, c) in enumerate(order)])
+    return paths, order, rf.n_unique

@@ -74,6 +74,12 @@ int setRunFiles(const char *prefix, void *ctx);
  * nangles (compressed or per operator), evaluated as one batch on the GPU
  * (stateAnsatzManager::getExpectationValues, src/AnsatzManager.cpp:709-754). */
 int getExpectationValues(int nrows, int nangles, const double *angles, double *energies, void *ctx);
+/* getGradient / getHessian: derivatives with respect to every operator's angle (nOps and
+ * nOps x nOps values) at compressed or per-operator angles.  The reference's fused build
+ * traps on these (src/AnsatzManager.cpp:570-574, 616-620); here every operator is its
+ * own parameter. */
+int getGradient(int nangles, const double *angles, double *gradient, void *ctx);
+int getHessian(int nangles, const double *angles, double *hessian, void *ctx);
 int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx);
 int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank,

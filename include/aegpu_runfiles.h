@@ -35,8 +35,18 @@ extern "C" {
 typedef struct aegpu_run_files aegpu_run_files;
 
 int aegpu_run_files_load(const char *prefix, int extracted_min, aegpu_run_files **out);
+/* One file alone: AEGPU_RUN_FILE_INITIAL (an Initial file), AEGPU_RUN_FILE_OPERATORS (an
+ * Operators file) or AEGPU_RUN_FILE_NUCLEAR (path is the prefix of a _Nuclear_Energy.dat
+ * file; a missing file is not an error, nuclear then reads NaN); the other fields stay
+ * empty. */
+enum { AEGPU_RUN_FILE_INITIAL = 1, AEGPU_RUN_FILE_OPERATORS = 2, AEGPU_RUN_FILE_NUCLEAR = 3 };
+int aegpu_run_file_read(const char *path, int kind, aegpu_run_files **out);
+/* An order file for n_ops operators and a Parameters file (optional): orders, parameter
+ * counts, angle sets and energies (loadParameters, src/TUPSLoadingUtils.cpp:176-296). */
+int aegpu_run_files_parameters(const char *order_path, const char *parameter_path, int n_ops, aegpu_run_files **out);
 const char *aegpu_run_files_error(void);
-/* Any output pointer may be null. */
+/* Any output pointer may be null.  n_ops counts the operators or, for a handle from
+ * aegpu_run_files_parameters, the order relations. */
 int aegpu_run_files_sizes(const aegpu_run_files *f, int *nq, int *n_initial, int *n_ops, int *n_params,
                           int *n_unique, int *n_sets);
 /* initial_index[n_initial] (0-based, full 2^nq space); initial_coeff[2*n_initial]

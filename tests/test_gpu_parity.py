@@ -348,3 +348,41 @@ def test_get_expectation_values_batched(golden, name):
     if "H" in fx:
         np.testing.assert_allclose(H, fx["H"][0], atol=TOL_G, rtol=0)
     assert abs(m.getExpectationValue(np.asarray(fx["angles"][0])[:P]) - fx["E"][0]) < TOL_E
+
+
+@pytest.mark.parametrize("name", ["h4", "h4c"])
+def test_python_binding_current_angles_and_per_operator_derivatives(golden, name):
+    """The reference binding's surface (PyAnsatzEvolve.cpp:17-96): setAngles / getAngles,
+    getters without angles evaluate at the current angles, getGradient / getHessian per
+    operator (compressing them gives the reference's compressed values), compressed
+    getters accept per-operator angles, optimise() starts from the current angles."""
+    fx = golden(name)
+    m = manager_from_fixture(fx)
+    P = int(np.asarray(fx["order_1b"]).max())
+    p0, sc = np.asarray(fx["order_1b"]) - 1, np.asarray(fx["scale"])
+    x = np.asarray(fx["angles"][1])[:P]
+    assert m.setAngles(x)
+    assert np.array_equal(m.getAngles(), x)
+    E = m.getExpectationValue()
+    assert abs(E - fx["E"][1]) < TOL_E and E == m.getExpectationValue(x)
+    np.testing.assert_allclose(m.getGradientComp(), fx["G"][1], atol=TOL_G, rtol=0)
+    np.testing.assert_allclose(m.getHessianComp(), fx["H"][1], atol=TOL_G, rtol=0)
+    C = np.zeros((P, len(p0)))
+    C[p0, np.arange(len(p0))] = sc
+    g_ops, H_ops = m.getGradient(), m.getHessian()
+    np.testing.assert_allclose(C @ g_ops, fx["G"][1], atol=TOL_G, rtol=0)
+    np.testing.assert_allclose(C @ H_ops @ C.T, fx["H"][1], atol=TOL_G, rtol=0)
+    np.testing.assert_allclose(H_ops, H_ops.T, atol=1e-12, rtol=0)
+    # per-operator angles (the decompressed x) through the compressed getters
+    th = sc * x[p0]
+    np.testing.assert_allclose(m.getGradientComp(th), fx["G"][1], atol=TOL_G, rtol=0)
+    np.testing.assert_allclose(m.getHessianComp(th), fx["H"][1], atol=TOL_G, rtol=0)
+    np.testing.assert_allclose(m.getAngles(), x, atol=1e-15, rtol=0)
+    s = m.getFinalState(complex_state=name == "h4c")
+    want = fx["S"][1] if name != "h4c" else fx["S"][1][0::2] + 1j * fx["S"][1][1::2]
+    np.testing.assert_allclose(s, want, atol=TOL_S, rtol=0)
+    if name == "h4":
+        m.setAngles(np.asarray(fx["angles"][2])[:P])
+        Eopt, xopt = m.optimise()
+        assert abs(Eopt - float(fx["nuclear"]) - (-2.838345804245581)) < 1e-8
+        assert np.array_equal(m.getAngles(), xopt)

@@ -200,3 +200,44 @@ def test_round_trip_random_files(tmp_path):
         else:
             assert rf.parameter_sets.shape[0] == 0
         assert rf.nuclear_energy == nuc
+
+
+def test_reference_named_loaders(tmp_path):
+    """The reference binding's module functions (PyAnsatzEvolve.cpp:101-147): loadOperators
+    (1-based lists), loadPath ((0, 0.0) per operator), loadNuclearEnergy (0 when missing),
+    readCsvState (dense real vector), loadParameters (template path first, then one path
+    per angle set with angle = set[order] * scale)."""
+    import ansatzevolve_gb300 as ae
+    prefix, a = _case(tmp_path)
+    assert ae.loadOperators(prefix + "_Operators.dat") == a["operators_1b"].tolist()
+    assert ae.loadPath(prefix + "_Operators.dat") == [(0, 0.0)] * len(a["operators_1b"])
+    assert ae.loadNuclearEnergy(prefix) == 0.7
+    assert ae.loadNuclearEnergy(str(tmp_path / "none")) == 0.0
+    dense = ae.readCsvState(prefix + "_Initial.dat")
+    want = np.zeros(256)
+    want[a["initial_index"]] = a["initial_coeff"]
+    assert np.array_equal(dense, want)
+    template = [(3, 0.25)] * 5
+    paths, order, nuniq = ae.loadParameters(prefix + "_Order.dat", prefix + "_Parameters.dat", template)
+    assert order == [(int(p), float(c)) for p, c in zip(a["order0"], a["scale"])] and nuniq == 3
+    assert paths[0] == template and len(paths) == 1 + len(a["parameter_sets"])
+    for x, path in zip(a["parameter_sets"], paths[1:]):
+        assert path == [(3, float(x[p] * c)) for p, c in order]
+    with pytest.raises(AegpuError, match="relations"):
+        ae.loadParameters(prefix + "_Order.dat", prefix + "_Parameters.dat", template[:3])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "Hams")), reason="reference checkout not present")
+def test_reference_named_loaders_on_fixtures(golden):
+    import ansatzevolve_gb300 as ae
+    fx = golden("h4")
+    base = os.path.join(REF, "Hams", "H4", "L1", "H4")
+    assert ae.loadOperators(base + "_Operators.dat") == np.asarray(fx["ops_1b"]).tolist()
+    assert ae.loadNuclearEnergy(base) == float(fx["nuclear"])
+    st = ae.readCsvState(base + "_Initial.dat")
+    assert len(st) == 256 and [i for i, v in enumerate(st) if v] == list(fx["init_idx"])
+    paths, order, nuniq = ae.loadParameters(base + "_Order.dat", base + "_Parameters.dat",
+                                            ae.loadPath(base + "_Operators.dat"))
+    assert nuniq == 9 and len(paths) == 3
+    p0, sc = np.asarray(fx["order_1b"]) - 1, np.asarray(fx["scale"])
+    assert np.array_equal([a for _, a in paths[2]], sc * np.asarray(fx["angles"][0])[p0])
