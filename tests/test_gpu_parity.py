@@ -377,7 +377,11 @@ def test_python_binding_current_angles_and_per_operator_derivatives(golden, name
     th = sc * x[p0]
     np.testing.assert_allclose(m.getGradientComp(th), fx["G"][1], atol=TOL_G, rtol=0)
     np.testing.assert_allclose(m.getHessianComp(th), fx["H"][1], atol=TOL_G, rtol=0)
-    np.testing.assert_allclose(m.getAngles(), x, atol=1e-15, rtol=0)
+    # a parameter whose operators all have scale 0 cannot be recovered (its angle reads 0,
+    # like the reference's normalised compression)
+    recoverable = np.zeros(P, dtype=bool)
+    recoverable[p0[sc != 0]] = True
+    np.testing.assert_allclose(m.getAngles(), np.where(recoverable, x, 0.0), atol=1e-15, rtol=0)
     s = m.getFinalState(complex_state=name == "h4c")
     want = fx["S"][1] if name != "h4c" else fx["S"][1][0::2] + 1j * fx["S"][1][1::2]
     np.testing.assert_allclose(s, want, atol=TOL_S, rtol=0)
