@@ -174,6 +174,7 @@ def lib(build_if_missing=True):
         "aegpu_run_file_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
         "aegpu_run_files_parameters": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
                                                       ctypes.POINTER(_P)]),
+        "generatePathsForSubspace": (ctypes.c_int, [ctypes.c_int, _DP, _IP, _DP, _P]),
         "getGradient": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
         "getHessian": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
     }
@@ -825,6 +826,17 @@ class stateAnsatzManager:
         if rc:
             raise AegpuError("getProperties returned %d" % rc)
         return {name: t[:, k] for k, name in enumerate(PROPERTY_NAMES)}
+
+    def generatePathsForSubspace(self, numberOfPaths):
+        """Distinct minima from seeded random starts and the subspace diagonalisation over
+        them: (eigenvalues, overlap null rank, minima energies with the nuclear energy)."""
+        n = int(numberOfPaths)
+        w, E = np.zeros(n), np.zeros(n)
+        nr = ctypes.c_int()
+        rc = self.L.generatePathsForSubspace(n, dptr(w), ctypes.byref(nr), dptr(E), self.ctx)
+        if rc:
+            raise AegpuError("generatePathsForSubspace returned %d" % rc)
+        return w, nr.value, E
 
     def getLowestEigenvalue(self):
         """(lowest eigenvalue of H in the sector, without the nuclear energy; residual)."""

@@ -309,6 +309,21 @@ int getProperties(int npaths, int nangles, const double *angles, int flags, doub
     return 0;
 }
 
+int generatePathsForSubspace(int numberOfPaths, double *eigenvalues, int *nullRank, double *energies, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (numberOfPaths < 1) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    std::vector<double> w, E;
+    int nr = 0;
+    if (!m->generatePathsForSubspace((size_t)numberOfPaths, &w, &nr, nullptr, &E)) return 3;
+    if (eigenvalues) std::copy(w.begin(), w.end(), eigenvalues);
+    if (energies) std::copy(E.begin(), E.end(), energies);
+    if (nullRank) *nullRank = nr;
+    return 0;
+}
+
 int getGradient(int NAngles, const double *angles, double *gradient, void *ctx)
 {
     if (ctx == nullptr) return 1;

@@ -3,6 +3,7 @@
 #include "manager.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -698,6 +699,53 @@ bool stateAnsatzManager::getSubspaceEigenvalues(const std::vector<std::vector<do
 namespace ae {
 
 // AnsatzManager.cpp:756-773 -> TUPSQuantities::OptimiseTups
+// AnsatzManager.cpp:775-829: minima from random starts (std::srand(100), angles
+// 2 pi rand() / RAND_MAX per parameter), each optimised by Newton-Raphson and kept when
+// its energy differs from the ones found by more than 1e-10, then the subspace
+// diagonalisation over them.  The reference's fused build refuses this (standard ansatz
+// only) and otherwise loops until it finds enough minima; here at most 50 starts per
+// requested path are tried.
+bool stateAnsatzManager::generatePathsForSubspace(size_t numberOfPaths, std::vector<double> *eigenvalues, int *nullRank,
+                                                  std::vector<std::vector<double>> *minima,
+                                                  std::vector<double> *energies)
+{
+    if (!validateToRun()) return false;
+    if (numberOfPaths == 0) { log_line("numberOfPaths must be positive"); return false; }
+    std::srand(100);
+    const int P = m_numberOfUniqueParameters;
+    std::vector<double> Es;
+    std::vector<std::vector<double>> paths;
+    const size_t maxTries = 50 * numberOfPaths;
+    for (size_t tries = 0; paths.size() < numberOfPaths && tries < maxTries; ++tries) {
+        std::vector<double> x((size_t)P);
+        for (int i = 0; i < P; ++i) x[(size_t)i] = (2 * M_PI * std::rand()) / RAND_MAX;
+        double E = 0;
+        if (!setAngles(x) || !optimise() || !getExpectationValue(E)) return false;
+        if (std::none_of(Es.begin(), Es.end(), [&](double e) { return std::abs(e - E) < 1e-10; })) {
+            Es.push_back(E);
+            paths.push_back(m_angles);
+        }
+    }
+    if (paths.size() < numberOfPaths) {
+        log_line("generatePathsForSubspace: found " + std::to_string(paths.size()) + " distinct minima of " +
+                 std::to_string(numberOfPaths));
+        return false;
+    }
+    log_line("Found following Energies " + [&] {
+        std::string t;
+        for (double e : Es) t += std::to_string(e) + " ";
+        return t;
+    }());
+    std::vector<double> w;
+    int nr = 0;
+    if (!getSubspaceEigenvalues(paths, w, nr)) return false;
+    if (eigenvalues) *eigenvalues = w;
+    if (nullRank) *nullRank = nr;
+    if (minima) *minima = paths;
+    if (energies) *energies = Es;
+    return true;
+}
+
 bool stateAnsatzManager::optimise()
 {
     if (!validateToRun()) return false;

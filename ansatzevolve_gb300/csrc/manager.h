@@ -64,6 +64,11 @@ public:
 
     // Newton-Raphson with cubic backtracking (TUPSQuantities::OptimiseTups).
     bool optimise();
+    // Distinct minima from seeded random starts, then the subspace diagonalisation over
+    // them (AnsatzManager.cpp:775-829); the outputs are optional (minima per operator).
+    bool generatePathsForSubspace(size_t numberOfPaths, std::vector<double> *eigenvalues = nullptr,
+                                  int *nullRank = nullptr, std::vector<std::vector<double>> *minima = nullptr,
+                                  std::vector<double> *energies = nullptr);
 
     // TUPSQuantities::writeProperties (tupsquantities.cpp:185-568): one row of
     // AEGPU_PROPERTY_ROWS values per path (compressed or per-operator angles), flags

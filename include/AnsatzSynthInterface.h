@@ -78,6 +78,11 @@ int getExpectationValues(int nrows, int nangles, const double *angles, double *e
  * nOps x nOps values) at compressed or per-operator angles.  The reference's fused build
  * traps on these (src/AnsatzManager.cpp:570-574, 616-620); here every operator is its
  * own parameter. */
+/* generatePathsForSubspace (src/AnsatzManager.cpp:775-829): numberOfPaths distinct
+ * minima (energies, with the nuclear energy; NULL to skip) from seeded random starts,
+ * then the eigenvalues of the subspace Hamiltonian over them and its overlap matrix's
+ * null rank.  3 when fewer distinct minima turn up in 50 starts per path. */
+int generatePathsForSubspace(int numberOfPaths, double *eigenvalues, int *nullRank, double *energies, void *ctx);
 int getGradient(int nangles, const double *angles, double *gradient, void *ctx);
 int getHessian(int nangles, const double *angles, double *hessian, void *ctx);
 int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);

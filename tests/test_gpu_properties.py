@@ -195,3 +195,37 @@ def test_writeproperties_verb_complex_and_extracted_min(golden, tmp_path):
     np.testing.assert_allclose(rows[15], px["rows"][14], atol=1e-9, rtol=0)
     np.testing.assert_allclose(w, px["subspace_eigs"], atol=1e-10, rtol=0)
     assert nr == int(px["subspace_null_rank"])
+
+
+def test_generate_paths_for_subspace(golden):
+    """generatePathsForSubspace: distinct Newton minima from the seeded random starts
+    and the subspace diagonalisation over them.  H4 L1 has one minimum reachable from
+    them (one path: the subspace eigenvalue is that energy; asking for more fails
+    cleanly after the bounded number of starts); on the 6-orbital synthetic inputs three
+    are found, and the lowest subspace eigenvalue lies between H's lowest eigenvalue and
+    the lowest minimum.  The call is repeatable (seeded)."""
+    from tests.test_gpu_parity import manager_from_fixture
+    fx = golden("h4")
+    m = manager_from_fixture(fx)
+    w, nr, E = m.generatePathsForSubspace(1)
+    assert abs(w[0] - (E[0] - float(fx["nuclear"]))) < 1e-10 and nr == 0
+    with pytest.raises(ae.AegpuError):
+        m.generatePathsForSubspace(2)
+    m.close()
+    fx = golden("syn6")
+    N = int(fx["N"])
+    pb = synthetic_problem(N, int(fx["na"]), int(fx["nb"]), int(fx["layers"]), int(fx["seed"]))
+    m = ae.stateAnsatzManager()
+    assert m.storeInitial(2 * N, [int(fx["hf"])], [1.0])
+    assert m.storeOperators(np.asarray(fx["ops_1b"]).tolist())
+    assert m.storeParameterDependencies(list(zip(np.asarray(fx["order_1b"]) - 1, fx["scale"])))
+    assert m.storeIntegrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    w, nr, E = m.generatePathsForSubspace(3)
+    assert len(set(np.round(E, 9))) == 3
+    lam, res = m.getLowestEigenvalue()
+    assert lam - 1e-9 <= w[0] <= E.min() + 1e-9
+    assert np.all(np.diff(w) >= -1e-12)
+    w2, nr2, E2 = m.generatePathsForSubspace(3)
+    np.testing.assert_allclose(w2, w, atol=1e-9, rtol=0)
+    np.testing.assert_allclose(E2, E, atol=1e-9, rtol=0)
+    m.close()
