@@ -175,6 +175,7 @@ def lib(build_if_missing=True):
         "aegpu_run_files_parameters": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int,
                                                       ctypes.POINTER(_P)]),
         "generatePathsForSubspace": (ctypes.c_int, [ctypes.c_int, _DP, _IP, _DP, _P]),
+        "iterativeOptimise": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
         "getGradient": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
         "getHessian": (ctypes.c_int, [ctypes.c_int, _DP, _DP, _P]),
     }
@@ -826,6 +827,17 @@ class stateAnsatzManager:
         if rc:
             raise AegpuError("getProperties returned %d" % rc)
         return {name: t[:, k] for k, name in enumerate(PROPERTY_NAMES)}
+
+    def iterativeOptimise(self, angles=None):
+        """The projected iteration (iterativeTups) then Newton-Raphson from the given (or
+        current) angles; returns (energy, compressed angles), which become current."""
+        a = _f64(self._current(angles)).copy()
+        E = np.zeros(1)
+        rc = self.L.iterativeOptimise(len(a), dptr(a), dptr(E), self.ctx)
+        if rc:
+            raise AegpuError("iterativeOptimise returned %d" % rc)
+        self._angles = a.copy()
+        return E[0], a
 
     def generatePathsForSubspace(self, numberOfPaths):
         """Distinct minima from seeded random starts and the subspace diagonalisation over

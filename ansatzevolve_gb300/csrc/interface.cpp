@@ -309,6 +309,20 @@ int getProperties(int npaths, int nangles, const double *angles, int flags, doub
     return 0;
 }
 
+int iterativeOptimise(int NAngles, double *angles, double *energy, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    if (!angles || NAngles < 1) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    if (!m->setAngles(std::vector<double>(angles, angles + NAngles))) return 3;
+    if (!m->iterativeOptimise()) return 3;
+    std::vector<double> x = m->getAngles();
+    if (NAngles == m->numberOfParameters()) memcpy(angles, x.data(), x.size() * sizeof(double));
+    if (energy && !m->getExpectationValue(*energy)) return 3;
+    return 0;
+}
+
 int generatePathsForSubspace(int numberOfPaths, double *eigenvalues, int *nullRank, double *energies, void *ctx)
 {
     if (ctx == nullptr) return 1;

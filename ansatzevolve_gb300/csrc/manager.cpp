@@ -746,6 +746,31 @@ bool stateAnsatzManager::generatePathsForSubspace(size_t numberOfPaths, std::vec
     return true;
 }
 
+// The driver's iterativeOptimise verb (main.cpp:502-515): TUPSQuantities::iterativeTups
+// (the projected iteration, tupsquantities.cpp:2044-2145) from the current angles, then
+// Newton-Raphson (OptimiseTups) from where it stopped.
+bool stateAnsatzManager::iterativeOptimise()
+{
+    if (!validateToRun()) return false;
+    const int P = m_numberOfUniqueParameters;
+    std::vector<double> x((size_t)P, 0.0);
+    std::vector<bool> seen((size_t)P, false);
+    for (size_t o = 0; o < m_angles.size(); ++o)
+        if (!seen[(size_t)m_param[o]] && m_scale[o] != 0) {
+            x[(size_t)m_param[o]] = m_angles[o] / m_scale[o];
+            seen[(size_t)m_param[o]] = true;
+        }
+    double E = 0, gn = 0;
+    int64_t nh = 0, ne = 0;
+    int outer = 0;
+    int rc = aegpu_optimise_projected(m_engine, P, m_param.data(), m_scale.data(), x.data(), 1e-5, 3000, &E, &gn, &nh,
+                                      &ne, &outer);
+    if (rc) { log_line(std::string("iterative optimisation failed: ") + aegpu_last_error(m_engine)); return false; }
+    log_line("iterativeTups: energy " + std::to_string(E) + " projected gradient " + std::to_string(gn) + " after " +
+             std::to_string(outer) + " renewals");
+    return setAngles(x) && optimise();
+}
+
 bool stateAnsatzManager::optimise()
 {
     if (!validateToRun()) return false;

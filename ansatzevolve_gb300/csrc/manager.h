@@ -64,6 +64,8 @@ public:
 
     // Newton-Raphson with cubic backtracking (TUPSQuantities::OptimiseTups).
     bool optimise();
+    // The projected iteration (TUPSQuantities::iterativeTups) then optimise().
+    bool iterativeOptimise();
     // Distinct minima from seeded random starts, then the subspace diagonalisation over
     // them (AnsatzManager.cpp:775-829); the outputs are optional (minima per operator).
     bool generatePathsForSubspace(size_t numberOfPaths, std::vector<double> *eigenvalues = nullptr,

@@ -150,7 +150,13 @@ def write_run_files(prefix, nq, initial_index, initial_coeff, operators_1b, orde
         write_sparse_hamiltonian(prefix, *ham_triplets)
 
 
-def optimise_run(prefix, extracted_min=False, out=None):
+def iterative_optimise_run(prefix, extracted_min=False, out=None):
+    """The driver's ``iterativeOptimise`` verb (src/main.cpp:502-515): the projected
+    iteration then Newton-Raphson from the first angle set; as `optimise_run`."""
+    return optimise_run(prefix, extracted_min, out, iterative=True)
+
+
+def optimise_run(prefix, extracted_min=False, out=None, iterative=False):
     """The reference driver's ``optimise`` verb (src/main.cpp:489-500): set up from the
     run files, Newton-Raphson (TUPSQuantities::OptimiseTups) from the first angle set
     (zero angles when the files hold none), on the GPU.  Returns (energy, compressed
@@ -161,7 +167,7 @@ def optimise_run(prefix, extracted_min=False, out=None):
         if extracted_min:
             rf = load_run_files(prefix, extracted_min=True)
         x0 = rf.parameter_sets[0] if len(rf.parameter_sets) else np.zeros(rf.n_params)
-        E, x = m.optimise(x0)
+        E, x = m.iterativeOptimise(x0) if iterative else m.optimise(x0)
     finally:
         m.close()
     if out is not None:

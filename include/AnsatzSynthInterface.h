@@ -83,6 +83,10 @@ int getExpectationValues(int nrows, int nangles, const double *angles, double *e
  * then the eigenvalues of the subspace Hamiltonian over them and its overlap matrix's
  * null rank.  3 when fewer distinct minima turn up in 50 starts per path. */
 int generatePathsForSubspace(int numberOfPaths, double *eigenvalues, int *nullRank, double *energies, void *ctx);
+/* iterativeOptimise: the driver's iterativeOptimise verb (src/main.cpp:502-515), the
+ * projected iteration (iterativeTups) then Newton-Raphson; angles and energy as in
+ * optimise. */
+int iterativeOptimise(int nangles, double *angles, double *energy, void *ctx);
 int getGradient(int nangles, const double *angles, double *gradient, void *ctx);
 int getHessian(int nangles, const double *angles, double *hessian, void *ctx);
 int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);

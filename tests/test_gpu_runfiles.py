@@ -65,3 +65,19 @@ def test_optimise_verb_reaches_the_h4_minimum(golden, tmp_path):
     assert np.linalg.norm(m.getGradientComp(rf2.parameter_sets[0])) < 1e-6
     m.close()
     assert load_run_files(prefix).n_params == len(x)
+
+
+def test_iterative_optimise_verb(golden, tmp_path):
+    """The driver's iterativeOptimise verb on the H4 L1 run files: the projected
+    iteration then Newton from the Parameters file's first set ends at a stationary
+    point whose energy is the engine's at the returned angles."""
+    from ansatzevolve_gb300.runfiles import iterative_optimise_run
+    fx = golden("h4")
+    prefix = str(tmp_path / "H4")
+    write_fixture(prefix, fx, [fx["angles"][2], fx["angles"][0]])
+    E, x, rf = iterative_optimise_run(prefix)
+    m = ae.stateAnsatzManager()
+    m.storeRunFiles(prefix)
+    assert abs(m.getExpectationValue(x) - E) < 1e-12
+    assert np.linalg.norm(m.getGradientComp(x)) < 1e-6
+    m.close()
