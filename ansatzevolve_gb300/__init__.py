@@ -21,7 +21,7 @@ _LIB = None
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
 TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL = 1, 2, 3, 4, 5
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
-PROP_HESSIAN, PROP_OVERLAP = 1, 2
+PROP_HESSIAN, PROP_OVERLAP, PROP_HF_PATH = 1, 2, 4
 # rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)
 PROPERTY_NAMES = ("Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
                   "NumberOfNegativeHessianEValues", "NumberOfNearZeroHessianEValues",
@@ -164,6 +164,7 @@ def lib(build_if_missing=True):
         "getExpectationValues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _P]),
         "getProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
         "getLowestEigenvalue": (ctypes.c_int, [_DP, _DP, _P]),
+        "writeProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, ctypes.c_char_p, _P]),
         "getSubspaceEigenvalues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _IP, _P]),
         # run-file readers (include/aegpu_runfiles.h)
         "aegpu_run_files_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
@@ -849,6 +850,16 @@ class stateAnsatzManager:
         if rc:
             raise AegpuError("generatePathsForSubspace returned %d" % rc)
         return w, nr.value, E
+
+    def writeProperties(self, paths, runPath=None, hessian=True, overlap=True, hf_path=True):
+        """The reference's writeProperties output: its table on stdout and, with a run
+        path, the per-path Hessian / metric files and the ground-state overlap vector."""
+        a = _f64(np.atleast_2d(paths))
+        flags = (PROP_HESSIAN if hessian else 0) | (PROP_OVERLAP if overlap else 0) | (PROP_HF_PATH if hf_path else 0)
+        rc = self.L.writeProperties(a.shape[0], a.shape[1], dptr(a), flags,
+                                    None if runPath is None else str(runPath).encode(), self.ctx)
+        if rc:
+            raise AegpuError("writeProperties returned %d" % rc)
 
     def getLowestEigenvalue(self):
         """(lowest eigenvalue of H in the sector, without the nuclear energy; residual)."""

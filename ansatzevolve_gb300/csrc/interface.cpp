@@ -375,6 +375,19 @@ int getExpectationValues(int nrows, int nangles, const double *angles, double *e
     return 0;
 }
 
+int writeProperties(int npaths, int nangles, const double *angles, int flags, const char *runPath, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    std::vector<std::vector<double>> rows;
+    if (!angle_rows(npaths, nangles, angles, rows)) return 2;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    return m->writeProperties(rows, !(flags & AEGPU_PROP_HESSIAN), (flags & AEGPU_PROP_OVERLAP) != 0,
+                              (flags & AEGPU_PROP_HF_PATH) != 0, runPath ? runPath : "")
+               ? 0
+               : 3;
+}
+
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx)
 {
     if (ctx == nullptr) return 1;

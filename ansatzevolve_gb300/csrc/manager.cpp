@@ -673,6 +673,108 @@ bool stateAnsatzManager::getProperties(const std::vector<std::vector<double>> &p
     return evolveIfNeeded();
 }
 
+namespace {
+
+// writeMatrix / writeVector / writeColumnVector of tupsquantities.cpp:25-164: row-major
+// binary and a %.10g CSV for matrices (complex: re, im pairs and "re+imj,"), a row
+// binary plus %.16g CSVs for vectors.
+void write_matrix(const std::string &name, const std::vector<double> &M, size_t n, bool complexFile)
+{
+    if (FILE *f = fopen((name + (complexFile ? ".CMatbin" : ".Matbin")).c_str(), "wb")) {
+        for (size_t i = 0; i < n * n; ++i) {
+            const double z[2] = {M[i], 0.0};
+            fwrite(z, sizeof(double), complexFile ? 2 : 1, f);
+        }
+        fclose(f);
+    }
+    if (FILE *f = fopen((name + (complexFile ? ".CMatcsv" : ".Matcsv")).c_str(), "w")) {
+        for (size_t i = 0; i < n; ++i) {
+            for (size_t j = 0; j < n; ++j) {
+                if (complexFile) fprintf(f, "%.10g+%.10gj,", M[i * n + j], 0.0);
+                else fprintf(f, "%.10g,", M[i * n + j]);
+            }
+            fprintf(f, "\n");
+        }
+        fclose(f);
+    }
+}
+
+void write_vector(const std::string &name, const std::vector<double> &v)
+{
+    if (FILE *f = fopen((name + ".Vecbin").c_str(), "wb")) {
+        fwrite(v.data(), sizeof(double), v.size(), f);
+        fclose(f);
+    }
+    if (FILE *f = fopen((name + ".Veccsv").c_str(), "w")) {
+        for (double x : v) fprintf(f, "%.16g,", x);
+        fprintf(f, "\n");
+        fclose(f);
+    }
+    if (FILE *f = fopen((name + ".ColVeccsv").c_str(), "w")) {
+        for (double x : v) fprintf(f, "%.16g\n", x);
+        fclose(f);
+    }
+}
+
+}  // namespace
+
+// TUPSQuantities::writeProperties (tupsquantities.cpp:185-568) with its printout
+// (printOutputHeaders / printOutputLine, :2146-2205) and files: per path the Hessian
+// and the metric (<runPath>_Path_<k>_Hessian / _Metric), and the overlap magnitudes
+// with the ground state (<runPath>_MagOfOverlapWithGroundState_0).  haveHF: the first
+// path is the zero-angle one (the "HF" column).
+bool stateAnsatzManager::writeProperties(const std::vector<std::vector<double>> &paths, bool noHess, bool lowestEigenvalue,
+                                         bool haveHF, const std::string &runPath, FILE *out)
+{
+    if (!validateToRun()) return false;
+    std::vector<double> table;
+    std::vector<std::vector<double>> H, M;
+    const int flags = (noHess ? 0 : AEGPU_PROP_HESSIAN) | (lowestEigenvalue ? AEGPU_PROP_OVERLAP : 0);
+    if (!getProperties(paths, flags, table, noHess ? nullptr : &H, noHess ? nullptr : &M)) return false;
+    const size_t np = paths.size(), P = (size_t)m_numberOfUniqueParameters;
+    if (!noHess && !runPath.empty())
+        for (size_t k = 0; k < np; ++k) {
+            write_matrix(runPath + "_Path_" + std::to_string(k) + "_Hessian", H[k], P, false);
+            write_matrix(runPath + "_Path_" + std::to_string(k) + "_Metric", M[k], P, m_complex);
+        }
+    const int col = m_complex ? 42 : 26;
+    if (!out) out = stdout;
+    fprintf(out, "\n%-40s %40s \n%-40s", "Results:", "Path Number", "");
+    if (haveHF) fprintf(out, "%-*s", col, "HF");
+    for (size_t i = 1; i <= (haveHF ? np - 1 : np); ++i) fprintf(out, "%-*zu", col, i);
+    fprintf(out, "\n");
+    static const char *names[] = {"Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
+                                  "NumberOfNegativeHessianEValues", "NumberOfNearZeroHessianEValues",
+                                  "NumberOfPositiveHessianEValues", "NumberOfNegativeHessianDiagValues",
+                                  "NumberOfNearZeroHessianDiagValues", "NumberOfPositiveHessianDiagValues",
+                                  "NumberOfPositiveMetricEValues", "NumberOfZeroMetricEValues",
+                                  "NumberOfZeroMetricDiagonalValues", "NormOfGradVector"};
+    for (int r = 0; r <= AEGPU_PROP_NORM_OF_GRAD; ++r) {
+        if (noHess && r >= AEGPU_PROP_NEG_HESSIAN_EVALUES && r <= AEGPU_PROP_ZERO_METRIC_DIAG) continue;
+        fprintf(out, "%-40s", names[r]);
+        for (size_t k = 0; k < np; ++k) fprintf(out, "%-*.16g", col, table[k * AEGPU_PROPERTY_ROWS + r]);
+        fprintf(out, "\n");
+    }
+    if (lowestEigenvalue) {
+        std::vector<double> mag(np);
+        fprintf(out, "%-40s", "OverlapWithState_0");
+        for (size_t k = 0; k < np; ++k) {
+            const double *row = &table[k * AEGPU_PROPERTY_ROWS];
+            if (m_complex)
+                fprintf(out, "%-20.16g, %-20.16g", row[AEGPU_PROP_OVERLAP_RE], row[AEGPU_PROP_OVERLAP_IM]);
+            else
+                fprintf(out, "%-*.16g", col, row[AEGPU_PROP_OVERLAP_RE]);
+            mag[k] = row[AEGPU_PROP_OVERLAP_MAG];
+        }
+        fprintf(out, "\n%-40s", "MagOfOverlapWithState_0");
+        for (double v : mag) fprintf(out, "%-*.16g", col, v);
+        fprintf(out, "\n");
+        if (!runPath.empty()) write_vector(runPath + "_MagOfOverlapWithGroundState_0", mag);
+    }
+    fflush(out);
+    return true;
+}
+
 bool stateAnsatzManager::getSubspaceEigenvalues(const std::vector<std::vector<double>> &paths, std::vector<double> &eigs,
                                                 int &nullRank)
 {

@@ -7,6 +7,7 @@
 #include "../../include/aegpu.h"
 
 #include <complex>
+#include <cstdio>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -79,6 +80,10 @@ public:
     bool getProperties(const std::vector<std::vector<double>> &paths, int flags, std::vector<double> &table,
                        std::vector<std::vector<double>> *hessians = nullptr,
                        std::vector<std::vector<double>> *metrics = nullptr);
+    // TUPSQuantities::writeProperties: the table printed to `out` (stdout when null) in
+    // the reference's layout and, with a run path, its Hessian / metric / overlap files.
+    bool writeProperties(const std::vector<std::vector<double>> &paths, bool noHess, bool lowestEigenvalue,
+                         bool haveHF, const std::string &runPath, FILE *out = nullptr);
     // Lowest eigenvalue of H in the sector (electronic, without the nuclear energy).
     bool getLowestEigenvalue(double &eigenvalue, double &residual, double tol = 1e-10);
     // TUPSQuantities::doSubspaceDiagonalisation (tupsquantities.cpp:1600-1700).

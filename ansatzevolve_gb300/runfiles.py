@@ -193,12 +193,13 @@ def format_properties(table, have_hf=True):
 
 
 def properties_run(prefix, extracted_min=False, no_hf_path=False, no_hess=False, lowest_eigenvalue=True,
-                   optimise=False):
+                   optimise=False, write_files=False):
     """The reference driver's ``writeproperties`` verb (src/main.cpp:520-529; with
     ``optimise`` first, as ``optimise writeproperties`` runs them, :489-500): the
     properties table over the zero path (unless no_hf_path) and the run files' angle
     sets (plus the optimised set).  Returns (table dict, subspace eigenvalues, null
-    rank, lowest eigenvalue or None, text)."""
+    rank, lowest eigenvalue or None, text); write_files also writes the reference's
+    per-path Hessian / metric files and overlap vector next to the run files."""
     m = stateAnsatzManager()
     try:
         rf = m.storeRunFiles(prefix)
@@ -210,6 +211,9 @@ def properties_run(prefix, extracted_min=False, no_hf_path=False, no_hess=False,
             sets.append(m.optimise(x0)[1])
         paths = ([] if no_hf_path else [np.zeros(rf.n_params)]) + sets
         table = m.getProperties(paths, hessian=not no_hess, overlap=lowest_eigenvalue)
+        if write_files:  # the reference's files beside the run files, and its printout
+            m.writeProperties(paths, runPath=prefix, hessian=not no_hess, overlap=lowest_eigenvalue,
+                              hf_path=not no_hf_path)
         lam = m.getLowestEigenvalue()[0] if lowest_eigenvalue else None
         w, nr = m.getSubspaceEigenvalues(sets) if sets else (np.zeros(0), 0)
     finally:

@@ -91,6 +91,11 @@ int getGradient(int nangles, const double *angles, double *gradient, void *ctx);
 int getHessian(int nangles, const double *angles, double *hessian, void *ctx);
 int getProperties(int npaths, int nangles, const double *angles, int flags, double *table, void *ctx);
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx);
+/* writeProperties: the reference's printed table on stdout and, when runPath is given,
+ * its files <runPath>_Path_<k>_Hessian / _Metric (.Matbin / .Matcsv, complex runs write
+ * the metric as .CMatbin / .CMatcsv) and <runPath>_MagOfOverlapWithGroundState_0
+ * (.Vecbin / .Veccsv / .ColVeccsv); flags as getProperties plus AEGPU_PROP_HF_PATH. */
+int writeProperties(int npaths, int nangles, const double *angles, int flags, const char *runPath, void *ctx);
 int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank,
                            void *ctx);
 

@@ -164,6 +164,7 @@ int aegpu_subspace_matrices(aegpu_engine *e, int nsets, const double *angles, do
  * aegpu_lowest_eigenpair.  Energies exclude nuclear_energy except the third row. */
 #define AEGPU_PROP_HESSIAN 1
 #define AEGPU_PROP_OVERLAP 2
+#define AEGPU_PROP_HF_PATH 4  /* writeProperties: the first path is the zero-angle ("HF") one */
 #define AEGPU_PROP_ELEC_ENERGY 0
 #define AEGPU_PROP_REAL_ELEC_ENERGY 1
 #define AEGPU_PROP_ELEC_NUC_ENERGY 2

@@ -229,3 +229,31 @@ def test_generate_paths_for_subspace(golden):
     np.testing.assert_allclose(w2, w, atol=1e-9, rtol=0)
     np.testing.assert_allclose(E2, E, atol=1e-9, rtol=0)
     m.close()
+
+
+@pytest.mark.parametrize("name", ["h4", "h4c"])
+def test_writeproperties_files(golden, tmp_path, capfd, name):
+    """writeProperties' files next to the run files, in the reference's formats: per
+    path the Hessian (.Matbin) and the metric (.Matbin, or .CMatbin for complex runs),
+    and the ground-state overlap magnitudes (.Vecbin), equal to the reference's own; its
+    table goes to stdout."""
+    from ansatzevolve_gb300.runfiles import properties_run
+    from tests.test_gpu_runfiles import write_fixture
+    px = golden("props_" + name)
+    fx = golden(name)
+    prefix = str(tmp_path / "H4")
+    write_fixture(prefix, fx, px["sets"])
+    properties_run(prefix, write_files=True)
+    assert "Results:" in capfd.readouterr().out
+    P = int(np.asarray(fx["order_1b"]).max())
+    for k in range(len(px["sets"]) + 1):
+        H = np.fromfile("%s_Path_%d_Hessian.Matbin" % (prefix, k)).reshape(P, P)
+        np.testing.assert_allclose(H, px["hess"][k], atol=1e-9, rtol=0)
+        if name == "h4c":
+            M = np.fromfile("%s_Path_%d_Metric.CMatbin" % (prefix, k)).reshape(P, P, 2)[..., 0]
+        else:
+            M = np.fromfile("%s_Path_%d_Metric.Matbin" % (prefix, k)).reshape(P, P)
+        np.testing.assert_allclose(M, px["metric"][k], atol=1e-9, rtol=0)
+    mag = np.fromfile(prefix + "_MagOfOverlapWithGroundState_0.Vecbin")
+    np.testing.assert_allclose(mag, px["rows"][14], atol=1e-9, rtol=0)
+    assert open(prefix + "_MagOfOverlapWithGroundState_0.ColVeccsv").read().count("\n") == len(mag)
