@@ -22,7 +22,7 @@ import time
 
 import numpy as np
 
-from . import HAM_ON_THE_FLY, HAM_STORED, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_PASS_OPS, TUNE_SPMV_TPR
+from . import HAM_ON_THE_FLY, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_PASS_OPS, TUNE_SPMV_TPR
 
 CANDIDATES = {
     TUNE_CTAS_PER_SM: (2, 4, 8, 16),
@@ -117,7 +117,6 @@ def tune(key, build, knobs=(TUNE_CTAS_PER_SM, TUNE_PASS_OPS, TUNE_OTF_THREADS), 
 def tups_builder(n_orb, n_alpha, layers, nb, integrals, ham_mode, angles, per_instance=True):
     """build(tuning) for a TUPS batch with the given integrals ([(h1, g2)] per
     instance, or one pair shared) and angles [nb, nops]."""
-    from .warmstart import family_engine
 
     def build(tuning):
         from . import BASIS_SZ, Engine

@@ -13,7 +13,7 @@ import pytest
 
 import ansatzevolve_gb300 as ae
 from ansatzevolve_gb300.synthetic import write_integrals
-from tests.fixtures import oracle_synthetic, sector_of, synthetic_problem
+from tests.fixtures import oracle_synthetic, synthetic_problem
 
 pytestmark = pytest.mark.gpu
 TOL_E, TOL_G, TOL_S = 1e-10, 1e-9, 1e-12

@@ -100,9 +100,6 @@ def test_synthetic_tups_matches_reference(golden):
 def test_projected_gradient_is_the_derivative_of_the_overlap():
     """The oracle's projected sweep (evolveDerivativeProj) against central differences
     of <proj|psi(theta)>, real and complex."""
-    import numpy as np
-    from oracle.oracle import Oracle
-    from tests.fixtures import oracle_synthetic, synthetic_problem
     pb = synthetic_problem(6, 3, 3, 2, 4)
     o = oracle_synthetic(pb)
     rng = np.random.default_rng(3)

@@ -8,8 +8,6 @@ engine allocated), on two calls in a row, and that an input over the fixed limit
 rejected.  Collected last so that a run stopping at the first failure has already run
 every other test; it also passes on its own in a fresh process.
 """
-import ctypes
-
 import numpy as np
 import pytest
 
