@@ -52,3 +52,31 @@ def test_argument_codes_and_cleanup():
     assert L.cleanup(ctypes.byref(ctx)) == 0
     assert ctx.value is None
     assert L.cleanup(ctypes.byref(ctx)) == 0
+
+
+def test_extension_status_codes():
+    """The C ABI extensions (per-operator derivatives, batched energies, the optimise /
+    properties verbs) follow the same codes: 1 for a null handle, 2 for bad arguments,
+    3 when the setup is missing (the first evaluation fails before any GPU work)."""
+    L = lib()
+    a = np.zeros(4)
+    nr = ctypes.c_int()
+    assert L.getGradient(4, dptr(a), dptr(a), None) == 1
+    assert L.getHessian(4, dptr(a), dptr(a), None) == 1
+    assert L.getExpectationValues(1, 4, dptr(a), dptr(a), None) == 1
+    assert L.iterativeOptimise(4, dptr(a), dptr(a), None) == 1
+    assert L.generatePathsForSubspace(2, dptr(a), ctypes.byref(nr), dptr(a), None) == 1
+    assert L.writeProperties(1, 4, dptr(a), 3, None, None) == 1
+    ctx = ctypes.c_void_p(L.init())
+    try:
+        assert L.getGradient(0, dptr(a), dptr(a), ctx) == 2
+        assert L.getHessian(4, None, dptr(a), ctx) == 2
+        assert L.getExpectationValues(0, 4, dptr(a), dptr(a), ctx) == 2
+        assert L.iterativeOptimise(4, None, dptr(a), ctx) == 2
+        assert L.generatePathsForSubspace(0, dptr(a), ctypes.byref(nr), dptr(a), ctx) == 2
+        assert L.writeProperties(0, 4, dptr(a), 3, None, ctx) == 2
+        assert L.getGradient(4, dptr(a), dptr(a), ctx) == 3
+        assert L.getExpectationValues(1, 4, dptr(a), dptr(a), ctx) == 3
+        assert L.generatePathsForSubspace(2, dptr(a), ctypes.byref(nr), dptr(a), ctx) == 3
+    finally:
+        L.cleanup(ctypes.byref(ctx))
