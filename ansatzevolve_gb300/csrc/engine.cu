@@ -349,6 +349,31 @@ __device__ __forceinline__ double flip(double x, int s)
     return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)(s < 0) << 63));
 }
 
+// The warp sums of six per-lane values at once, by recursive halving: at each step a
+// lane keeps half of its values and adds its partner's copies of them, so the six sums
+// take 9 double shuffles instead of 6 x 5.  Lane l with (l & 3) == 0 returns the sum of
+// value l >> 2 (l >> 2 = 6, 7: padding).  The order of the additions is fixed.
+static_assert(kMaxWarpLayers == 6, "warp_sum6 reduces six values");
+__device__ __forceinline__ double warp_sum6(const double (&x)[kMaxWarpLayers], int lane)
+{
+    double v8[8];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) v8[i] = x[i];
+    v8[6] = v8[7] = 0.0;
+    const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+    double v4[4], v2[2];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        v4[i] = (b4 ? v8[i + 4] : v8[i]) + __shfl_xor_sync(0xffffffffu, b4 ? v8[i] : v8[i + 4], 16);
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        v2[i] = (b3 ? v4[i + 2] : v4[i]) + __shfl_xor_sync(0xffffffffu, b3 ? v4[i] : v4[i + 2], 8);
+    double v = (b2 ? v2[1] : v2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? v2[0] : v2[1], 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    return v;
+}
+
 // One DFMA whatever the form: the operands are chosen with integer selects, so the
 // compiler cannot evaluate both forms on the FP64 pipe.
 __device__ __forceinline__ double rot_scaled(const PassConst &q, double v, double vp, int s)
@@ -590,15 +615,10 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
             if (ok1) h[(size_t)z1 * W + w] = sigma * h1[w];
         }
     }
-    // fixed-order CTA sum: a butterfly over each warp's lanes, then the warps in order
+    // fixed-order CTA sum: the warp's six sums by recursive halving, then the warps in order
     const int warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < kMaxWarpLayers; ++j) {
-        double v = accS[j];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[j][warp] = v;
-    }
+    const double wsum = warp_sum6(accS, lane);
+    if ((lane & 3) == 0 && (lane >> 2) < kMaxWarpLayers) red[lane >> 2][warp] = wsum;
     __syncthreads();
     if (threadIdx.x < kMaxSlots) {
         double sum = 0.0;
@@ -693,13 +713,8 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const W
         }
     }
     const int warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < kMaxWarpLayers; ++j) {
-        double v = accS[j];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[j][warp] = v;
-    }
+    const double wsum = warp_sum6(accS, lane);
+    if ((lane & 3) == 0 && (lane >> 2) < kMaxWarpLayers) red[lane >> 2][warp] = wsum;
     __syncthreads();
     if (threadIdx.x < kMaxSlots) {
         double sum = 0.0;
