@@ -818,7 +818,7 @@ __global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__re
         y[0] = c * hr - s * hi;
         y[1] = s * hr + c * hi;
     }
-    for (int i = 0; i < kMaxSlots; ++i) {
+    for (int i = 0; i < a.nslots; ++i) {  // the block's own slots only (uniform bound: block_sum syncs)
         const double g = block_sum(acc[i], red);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kMaxSlots + i] = g;
     }
@@ -867,7 +867,7 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
         x[0] = c * xr - s * xi;
         x[1] = s * xr + c * xi;
     }
-    for (int i = 0; i < kMaxSlots; ++i) {
+    for (int i = 0; i < a.nslots; ++i) {
         const double g = block_sum(acc[i], red);
         if (threadIdx.x == 0) partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + i] = g;
     }

@@ -364,7 +364,9 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--ham", default="stored", choices=["stored", "otf"])
+    ap.add_argument("--ham", default=None, choices=["stored", "otf"],
+                    help="stored (default up to 12 orbitals) or on the fly (default at 14: the stored "
+                         "operator of D = 11.8M does not fit in HBM)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--orbitals", type=int, default=12, choices=[8, 10, 12, 14],
@@ -398,6 +400,8 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import ansatzevolve_gb300 as ae
     pb = problem()
+    if args.ham is None:
+        args.ham = "otf" if args.orbitals >= 14 else "stored"
     mode = ae.HAM_STORED if args.ham == "stored" else ae.HAM_ON_THE_FLY
 
     e2e = None
