@@ -764,61 +764,125 @@ __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
     return m;
 }
 
-// ckpt (nullable, single vector): the amplitudes after the pass, for the adjoint sweep.
-__global__ void k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec, double *__restrict__ ckpt,
-                           int64_t inst_stride, int64_t ckpt_stride)
+// The streaming diagonal kernels take kDiagUnroll amplitudes z, z + S, ... (S = grid
+// threads) per iteration: their masks first, then all their loads, then the arithmetic,
+// so that each thread keeps several HBM loads in flight (one amplitude per iteration left
+// the kernels latency-bound).  A thread still visits its amplitudes in ascending order,
+// so every per-thread sum keeps its order.
+constexpr int kDiagUnroll = 4;
+
+// The slots' annihilation masks in shared memory (read once per CTA, not per amplitude).
+__device__ __forceinline__ void diag_load_masks(const DiagArgs &a, uint32_t *ann)
 {
+    if (threadIdx.x < a.nslots) ann[threadIdx.x] = a.codes[a.ops[threadIdx.x]].annihilate;
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t diag_mask_s(const uint32_t *ann, int nslots, uint32_t bits)
+{
+    uint32_t m = 0;
+    for (int i = 0; i < nslots; ++i)
+        if ((bits & ann[i]) == ann[i]) m |= 1u << i;
+    return m;
+}
+
+// ckpt (nullable, single vector): the amplitudes after the pass, for the adjoint sweep.
+__global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec,
+                                                     double *__restrict__ ckpt, int64_t inst_stride, int64_t ckpt_stride)
+{
+    __shared__ uint32_t ann[kMaxSlots];
     const uint64_t D = a.basis.D;
     if (skip_instance(a.active, blockIdx.y)) return;
+    diag_load_masks(a, ann);
     a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
     vecs += (size_t)blockIdx.y * inst_stride;
     if (ckpt) ckpt += (size_t)blockIdx.y * ckpt_stride;
-    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
-        if (!m) continue;
-        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+    const uint64_t S = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t z0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z0 < D; z0 += kDiagUnroll * S) {
+        uint32_t m[kDiagUnroll];
+#pragma unroll
+        for (int u = 0; u < kDiagUnroll; ++u) {
+            const uint64_t z = z0 + u * S;
+            m[u] = z < D ? diag_mask_s(ann, a.nslots, a.basis.bits((uint32_t)z)) : 0u;
+        }
         for (int vec = 0; vec < nvec; ++vec) {
-            double *p = vecs + vec * vstride + 2 * z;
-            const double re = p[0], im = p[1];
-            p[0] = c * re - s * im;
-            p[1] = s * re + c * im;
-            if (ckpt) {
-                ckpt[2 * z] = p[0];
-                ckpt[2 * z + 1] = p[1];
+            double *p = vecs + vec * vstride;
+            double2 v[kDiagUnroll];
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u)
+                if (m[u]) v[u] = *reinterpret_cast<const double2 *>(p + 2 * (z0 + u * S));
+#pragma unroll
+            for (int u = 0; u < kDiagUnroll; ++u) {
+                if (!m[u]) continue;
+                const uint64_t z = z0 + u * S;
+                const double c = a.table[2 * m[u]], s = a.table[2 * m[u] + 1];
+                const double2 r = make_double2(c * v[u].x - s * v[u].y, s * v[u].x + c * v[u].y);
+                *reinterpret_cast<double2 *>(p + 2 * z) = r;
+                if (ckpt) *reinterpret_cast<double2 *>(ckpt + 2 * z) = r;
             }
         }
     }
 }
 
 // Checkpointed adjoint of a diagonal pass: gradient <h|i n psi> at the pass output
-// (psi from the checkpoint), then h rotated back; psi untouched.
-__global__ void __launch_bounds__(256) k_diag_adj(DiagArgs a, const double *__restrict__ ckpt, int64_t ckpt_stride,
-                                                  double *h, int64_t inst_stride, double *partials, int64_t part_stride)
+// (psi from the checkpoint), then h rotated back; psi untouched.  ONE: a pass with a
+// single operator (most LUCJ phase passes), whose one gradient sum needs one register;
+// otherwise kMaxSlots sums in registers and half the loads in flight, so that four
+// 256-thread CTAs per SM (the fixed grid kDiagGrid) stay resident.
+template <bool ONE>
+__global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *__restrict__ ckpt, int64_t ckpt_stride,
+                                                     double *h, int64_t inst_stride, double *partials,
+                                                     int64_t part_stride)
 {
+    constexpr int NS = ONE ? 1 : kMaxSlots;
+    constexpr int U = ONE ? kDiagUnroll : kDiagUnroll / 2;
     __shared__ double red[8];
+    __shared__ uint32_t ann[kMaxSlots];
     if (skip_instance(a.active, blockIdx.y)) return;
+    diag_load_masks(a, ann);
     a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
     ckpt += (size_t)blockIdx.y * ckpt_stride;
     h += (size_t)blockIdx.y * inst_stride;
     partials += (size_t)blockIdx.y * part_stride;
-    double acc[kMaxSlots];
+    double acc[NS];
 #pragma unroll
-    for (int i = 0; i < kMaxSlots; ++i) acc[i] = 0;
+    for (int i = 0; i < NS; ++i) acc[i] = 0;
     const uint64_t D = a.basis.D;
-    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
-        if (!m) continue;
-        double *y = h + 2 * z;
-        const double xr = ckpt[2 * z], xi = ckpt[2 * z + 1], hr = y[0], hi = y[1];
-        const double q = hi * xr - hr * xi;
+    const uint64_t S = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t z0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z0 < D; z0 += U * S) {
+        uint32_t m[U];
+        double2 x[U], y[U];
 #pragma unroll
-        for (int i = 0; i < kMaxSlots; ++i)
-            if (m & (1u << i)) acc[i] += q;
-        const double c = a.table[2 * m], s = a.table[2 * m + 1];
-        y[0] = c * hr - s * hi;
-        y[1] = s * hr + c * hi;
+        for (int u = 0; u < U; ++u) {
+            const uint64_t z = z0 + u * S;
+            m[u] = z < D ? diag_mask_s(ann, a.nslots, a.basis.bits((uint32_t)z)) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (m[u]) {
+                const uint64_t z = z0 + u * S;
+                x[u] = __ldg(reinterpret_cast<const double2 *>(ckpt + 2 * z));
+                y[u] = *reinterpret_cast<const double2 *>(h + 2 * z);
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (!m[u]) continue;
+            const double q = y[u].y * x[u].x - y[u].x * x[u].y;
+            // FP64 adds past the pass's own slots would still take FP64 issue slots when
+            // predicated off: leave the unrolled loop at the (uniform) slot count
+#pragma unroll
+            for (int i = 0; i < NS; ++i) {
+                if (i == a.nslots) break;
+                if (ONE || (m[u] & (1u << i))) acc[i] += q;
+            }
+            const double c = a.table[2 * m[u]], s = a.table[2 * m[u] + 1];
+            *reinterpret_cast<double2 *>(h + 2 * (z0 + u * S)) =
+                make_double2(c * y[u].x - s * y[u].y, s * y[u].x + c * y[u].y);
+        }
     }
-    for (int i = 0; i < a.nslots; ++i) {  // the block's own slots only (uniform bound: block_sum syncs)
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {  // the block's own slots only (uniform bound: block_sum syncs)
+        if (i == a.nslots) break;
         const double g = block_sum(acc[i], red);
         if (threadIdx.x == 0) partials[(size_t)blockIdx.x * kMaxSlots + i] = g;
     }
@@ -861,13 +925,17 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
         const double xr = x[0], xi = x[1], hr = h[2 * z], hi = h[2 * z + 1];
         const double q = hi * xr - hr * xi;
 #pragma unroll
-        for (int i = 0; i < kMaxSlots; ++i)
+        for (int i = 0; i < kMaxSlots; ++i) {
+            if (i == a.nslots) break;  // uniform bound, as in k_diag_adj
             if ((m & (1u << i)) && block_pos0 + i >= vec) acc[i] += q;
+        }
         const double c = a.table[2 * m], s = a.table[2 * m + 1];
         x[0] = c * xr - s * xi;
         x[1] = s * xr + c * xi;
     }
-    for (int i = 0; i < a.nslots; ++i) {
+#pragma unroll
+    for (int i = 0; i < kMaxSlots; ++i) {  // compile-time indices keep acc in registers
+        if (i == a.nslots) break;
         const double g = block_sum(acc[i], red);
         if (threadIdx.x == 0) partials[((size_t)blockIdx.x * nvec + vec) * kMaxSlots + i] = g;
     }
@@ -1884,8 +1952,12 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         if (b.diagonal) {
             k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
                 e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table, nops, e->d_active);
-            k_diag_adj<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h, n, part,
-                                                                     e->n_partials);
+            if (b.nslots == 1)
+                k_diag_adj<true><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h,
+                                                                               n, part, e->n_partials);
+            else
+                k_diag_adj<false><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h,
+                                                                                n, part, e->n_partials);
             e->launches += 2;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, -1.0);
