@@ -27,7 +27,7 @@ from . import HAM_ON_THE_FLY, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_PASS_OPS,
 CANDIDATES = {
     TUNE_CTAS_PER_SM: (2, 4, 8, 16),
     TUNE_PASS_OPS: (4, 5, 6),
-    TUNE_OTF_THREADS: (128, 256, 512),
+    TUNE_OTF_THREADS: (128, 256, 512, 1024),
     TUNE_SPMV_TPR: (1, 2, 4, 8),
 }
 DEFAULT = {TUNE_PASS_OPS: 6, TUNE_CTAS_PER_SM: 4, TUNE_OTF_THREADS: 512, TUNE_SPMV_TPR: 0}

@@ -1314,11 +1314,11 @@ __device__ __forceinline__ double flipc(double v, int32_t code)
 }
 
 template <int W>
-__global__ void __launch_bounds__(512) k_otf_strings(OtfArgs a, const double *__restrict__ x, double *__restrict__ y,
-                                                     double *__restrict__ epart)
+__global__ void __launch_bounds__(1024) k_otf_strings(OtfArgs a, const double *__restrict__ x, double *__restrict__ y,
+                                                      double *__restrict__ epart)
 {
     extern __shared__ double sm[];
-    __shared__ double red[16];
+    __shared__ double red[32];
     const int N = a.N, NN = a.N * a.N, nsa = a.nsa, nda = a.nda;
     const int ra = blockIdx.x;
     if (skip_instance(a.active, blockIdx.z)) return;
@@ -1531,6 +1531,7 @@ struct aegpu_engine {
     int tune_pass_ops = kMaxWarpLayers;
     int tune_ctas_per_sm = 4;  // best single-instance shape at 10-12 orbitals on GB300
     int tune_otf_threads = 512;
+    bool otf_threads_set = false;  // set through the knob: no automatic CTA size
     int tune_spmv_tpr = 0;  // threads per stored-H row: 0 = by size (>= 4 CTAs per SM)
     // programmatic dependent launch of the pass kernels: -1 = by size (on up to 2^20
     // amplitudes per launch, where launch latency is a visible share of a pass; off
@@ -2488,6 +2489,14 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
         if (smem + 1024 > (size_t)optin) return e->fail(AEGPU_ERR_UNSUPPORTED, "too many orbitals for the on-the-fly kernel");
         e->otf = o;
         e->otf_threads = (int)std::min<int64_t>(e->tune_otf_threads, ((int64_t)o.nB + 31) / 32 * 32);
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (!e->otf_threads_set && smem_sm > 0 && (size_t)smem_sm < 2 * (smem + 1024)) {
+            // the string tables leave room for one CTA per SM (14 orbitals: ~150 KB): make
+            // it as large as the registers allow (1024 threads), in equal beta chunks
+            const int chunks = (o.nB + 1023) / 1024;
+            e->otf_threads = ((o.nB + chunks - 1) / chunks + 31) / 32 * 32;
+        }
         e->otf_chunks = (o.nB + e->otf_threads - 1) / e->otf_threads;
         const int64_t nparts = (int64_t)o.nA * e->otf_chunks;
         if (nparts > e->n_epart) {
@@ -2561,9 +2570,10 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         e->tune_ctas_per_sm = value;
         return AEGPU_OK;
     case AEGPU_TUNE_OTF_THREADS:
-        if (value < 64 || value > 512 || value % 32) return e->fail(AEGPU_ERR_ARG, "threads must be 64..512, x32");
+        if (value < 64 || value > 1024 || value % 32) return e->fail(AEGPU_ERR_ARG, "threads must be 64..1024, x32");
         if (e->ham_kind) return e->fail(AEGPU_ERR_STATE, "set the thread count before the Hamiltonian");
         e->tune_otf_threads = value;
+        e->otf_threads_set = true;
         return AEGPU_OK;
     case AEGPU_TUNE_PDL:
         if (value < -1 || value > 1) return e->fail(AEGPU_ERR_ARG, "programmatic dependent launch must be -1, 0 or 1");

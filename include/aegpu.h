@@ -88,7 +88,9 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
 /* Launch-shape knobs (picked by the autotuner, ansatzevolve_gb300/autotune.py):
  * excitations fused per pass (1..6; before aegpu_set_problem), CTAs per SM of the
  * pass kernels (1..64; before aegpu_set_problem), threads per CTA of the on-the-fly
- * H kernel (64..512, multiple of 32; before the Hamiltonian), threads per row of the
+ * H kernel (64..1024, multiple of 32; before the Hamiltonian; unset, 512, or as many as
+ * fit in equal beta chunks of up to 1024 when the string tables leave room for only one
+ * CTA per SM), threads per row of the
  * stored-H product (1, 2, 4, 8; 0 = chosen by size; before the first evaluation),
  * programmatic dependent launch of the pass kernels (0 off, 1 on, -1 by size, the
  * default: on up to 2^20 amplitudes per launch; each pass's CTAs are scheduled while

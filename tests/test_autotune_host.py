@@ -29,6 +29,7 @@ def test_greedy_search_finds_the_fastest_and_caches(tmp_path):
     assert key == "tups_N10_a5_b5_L3_nb192_otf_own"
     best, t, trials = at.tune(key, lambda tuning: FakeEngine(cost(tuning)), reps=2, path=path)
     assert best == {TUNE_CTAS_PER_SM: 4, TUNE_PASS_OPS: 5, TUNE_OTF_THREADS: 256, at.TUNE_SPMV_TPR: 0}
-    assert len(trials) == 1 + 3 + 2 + 2
+    # the default, then the other candidates of each knob: CTAs 3, pass size 2, threads 3
+    assert len(trials) == 1 + 3 + 2 + 3
     assert at.lookup(key, path) == best
     assert at.lookup("other", path) == {}
