@@ -1533,12 +1533,12 @@ struct aegpu_engine {
     int tune_otf_threads = 512;
     bool otf_threads_set = false;  // set through the knob: no automatic CTA size
     int tune_spmv_tpr = 0;  // threads per stored-H row: 0 = by size (>= 4 CTAs per SM)
-    // programmatic dependent launch of the pass kernels: -1 = by size (on up to 2^20
+    // programmatic dependent launch of the pass kernels: -1 = by size (on up to 2^19
     // amplitudes per launch, where launch latency is a visible share of a pass; off
     // above, where early-resident dependents slow the FP64-bound passes: GB300,
-    // 8 / 10 orbitals -6 %, 12 orbitals +1.5 %)
+    // 8 / 10 orbitals -6 %, 12 orbitals (853,776 amplitudes) +1.7 %)
     int tune_pdl = -1;
-    bool pdl_on() const { return tune_pdl >= 0 ? tune_pdl != 0 : (int64_t)B.D * W * nb <= (int64_t)1 << 20; }
+    bool pdl_on() const { return tune_pdl >= 0 ? tune_pdl != 0 : (int64_t)B.D * W * nb <= (int64_t)1 << 19; }
     int spmv_tpr() const
     {
         if (tune_spmv_tpr) return tune_spmv_tpr;

@@ -93,7 +93,7 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * CTA per SM), threads per row of the
  * stored-H product (1, 2, 4, 8; 0 = chosen by size; before the first evaluation),
  * programmatic dependent launch of the pass kernels (0 off, 1 on, -1 by size, the
- * default: on up to 2^20 amplitudes per launch; each pass's CTAs are scheduled while
+ * default: on up to 2^19 amplitudes per launch; each pass's CTAs are scheduled while
  * the previous pass drains and wait on the device for its results; any time, it
  * rebuilds the captured graphs).  No counterpart in the reference. */
 enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
