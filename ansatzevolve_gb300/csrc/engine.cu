@@ -3261,10 +3261,13 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             cublasDdot(h, ni, v, 1, w, 1, d_alpha + j);
             k_lanczos_update<<<vgrid, 256, 0, s>>>(w, v, j ? Vb + (size_t)(j - 1) * n : nullptr, d_alpha + j,
                                                    j ? d_beta + (j - 1) : nullptr, (int64_t)n);
-            for (int pass = 0; pass < 2; ++pass) {
-                cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, d_k, Vb, ni, w, 1, d_k + 1, d_c, 1);
-                cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, d_k + 2, Vb, ni, d_c, 1, d_k, w, 1);
-            }
+            // one classical Gram-Schmidt pass against the whole basis: the three-term update
+            // above already removed the v_j and v_{j-1} components (where the cancellation
+            // happens), so this pass is the second orthogonalisation for them and leaves the
+            // older components at rounding level ("twice is enough", Giraud, Langou and
+            // Rozloznik 2005); a second full pass would read the basis twice more
+            cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, d_k, Vb, ni, w, 1, d_k + 1, d_c, 1);
+            cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, d_k + 2, Vb, ni, d_c, 1, d_k, w, 1);
             cublasDnrm2(h, ni, w, 1, d_beta + j);
             k_scale_inverse<<<vgrid, 256, 0, s>>>(w, d_beta + j, (int64_t)n);
             e->launches += 2;
