@@ -37,7 +37,7 @@
 //                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
 //   k_otf_strings    y = H x with no stored matrix: CTA per alpha string, thread per
 //                    determinant, one FP64 FMA per matrix element (otf_tables.cpp)
-//   k_lanczos_update, k_scale_inverse
+//   k_lanczos_update, k_scale_inverse, k_dot_partial, k_dot_finish
 //                    the device side of the Lanczos recurrence for the lowest eigenpair
 //                    (alpha and beta stay in device memory between the H products)
 // All reductions are two-stage and in a fixed order, so results are bit-identical
@@ -3191,6 +3191,32 @@ __global__ void k_scale_inverse(double *__restrict__ w, const double *beta, int6
         w[i] *= f;
 }
 
+// First stage of <a|b> over the whole grid: each CTA writes the sum of its grid-stride
+// share to partial[blockIdx.x].  The grid covers every SM several times, so the pass
+// streams at the copy bandwidth (the library's dot and nrm2 reductions measured about
+// 50 us on a 6.8 MB vector, a fraction of it); the grid and the summation order are
+// fixed, so repeated calls give identical sums.
+__global__ void k_dot_partial(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
+                              double *__restrict__ partial)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s = fma(a[i], b[i], s);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Second stage: *out = the sum of m partials, or its square root (a 2-norm), one CTA.
+__global__ void k_dot_finish(const double *__restrict__ partial, int m, double *out, int take_sqrt)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) s += partial[i];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) *out = take_sqrt ? sqrt(fmax(s, 0.0)) : s;
+}
+
 extern "C" {
 
 int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
@@ -3208,8 +3234,10 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
     e->ground_valid = false;
     if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
     // basis vectors, reorthogonalisation coefficients, alpha / beta of the recurrence,
-    // and the constants 1, 0, -1 for device-pointer cuBLAS calls
-    const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 3;
+    // the constants 1, 0, -1 for device-pointer cuBLAS calls, and one partial sum per CTA
+    // of the dot-product and norm reductions
+    const int vgrid = (int)std::min<int64_t>(((int64_t)n + 255) / 256, (int64_t)e->sm_count * 8);
+    const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 3 + (size_t)vgrid;
     double *Vb = e->alloc<double>((size_t)(m + 1) * n);
     double *scal = e->alloc<double>(nscal);
     auto release = [&] {
@@ -3221,14 +3249,13 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
         release();
         return e->fail(AEGPU_ERR_NOMEM, "Lanczos basis allocation failed");
     }
-    double *d_c = scal, *d_alpha = scal + (m + 1), *d_beta = d_alpha + m, *d_k = d_beta + m;
+    double *d_c = scal, *d_alpha = scal + (m + 1), *d_beta = d_alpha + m, *d_k = d_beta + m, *d_part = d_k + 3;
     const double consts[3] = {1.0, 0.0, -1.0};
     cublasHandle_t h = e->cublas;
     cudaStream_t s = e->stream;
     cudaMemcpyAsync(d_k, consts, sizeof(consts), cudaMemcpyHostToDevice, s);
     const int ni = (int)n;
     const double one = 1.0, zero = 0.0;
-    const int vgrid = (int)std::min<int64_t>(((int64_t)n + 255) / 256, (int64_t)e->sm_count * 8);
     // Lanczos with full reorthogonalisation from the initial state, restarted from the
     // Ritz vector when the basis is full.  The recurrence runs on the device (alpha and
     // beta stay in device memory, cuBLAS in device-pointer mode); the host reads them and
@@ -3258,7 +3285,8 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
                 return rc;
             }
             ++prod;
-            cublasDdot(h, ni, v, 1, w, 1, d_alpha + j);
+            k_dot_partial<<<vgrid, 256, 0, s>>>(v, w, (int64_t)n, d_part);
+            k_dot_finish<<<1, 256, 0, s>>>(d_part, vgrid, d_alpha + j, 0);
             k_lanczos_update<<<vgrid, 256, 0, s>>>(w, v, j ? Vb + (size_t)(j - 1) * n : nullptr, d_alpha + j,
                                                    j ? d_beta + (j - 1) : nullptr, (int64_t)n);
             // one classical Gram-Schmidt pass against the whole basis: the three-term update
@@ -3268,9 +3296,10 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             // Rozloznik 2005); a second full pass would read the basis twice more
             cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, d_k, Vb, ni, w, 1, d_k + 1, d_c, 1);
             cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, d_k + 2, Vb, ni, d_c, 1, d_k, w, 1);
-            cublasDnrm2(h, ni, w, 1, d_beta + j);
+            k_dot_partial<<<vgrid, 256, 0, s>>>(w, w, (int64_t)n, d_part);
+            k_dot_finish<<<1, 256, 0, s>>>(d_part, vgrid, d_beta + j, 1);
             k_scale_inverse<<<vgrid, 256, 0, s>>>(w, d_beta + j, (int64_t)n);
-            e->launches += 2;
+            e->launches += 6;
             const int jn = j + 1;
             if (jn - checked < kCheck && jn < m && prod < max_products && jn < ni) continue;
             // read alpha / beta so far; the first k at which the Ritz pair converged, or the
