@@ -134,6 +134,11 @@ def lib(build_if_missing=True):
         "aegpu_apply_dev": (ctypes.c_int, [_P, _P, _P, _P, _P]),
         "aegpu_use_graphs": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_csr_energy_noalloc": (ctypes.c_int, [i64, _P, _P, _P, _P, _P, _P, _P]),
+        "aegpu_gram_upper_dev": (ctypes.c_int, [_P, i64, _P, i64, i64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                _P, _P, ctypes.c_int, _P]),
+        "aegpu_exc_rule_dev": (ctypes.c_int, [ctypes.c_int, _IP, _P, i64, _P, _P, _P]),
+        "aegpu_host_exc_rule": (ctypes.c_int, [ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_uint32), i64,
+                                               ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int8)]),
         "aegpu_phase_timing": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_phase_times": (ctypes.c_int, [_P, _DP, ctypes.POINTER(i64)]),
         "aegpu_problem_info": (ctypes.c_int, [_P, ctypes.POINTER(i64)]),

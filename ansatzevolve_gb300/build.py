@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libansatzevolve_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["engine.cu", "mlp.cu"]
+CU = ["engine.cu", "mlp.cu", "dense.cu"]
 CPP = ["setup.cpp", "otf_tables.cpp", "manager.cpp", "newton.cpp", "interface.cpp", "optimise.cpp", "runfiles.cpp", "properties.cpp", "diis.cpp"]
 
 
@@ -63,7 +63,7 @@ def build(force=False, verbose=False):
                 print(r.stderr, file=sys.stderr)
     objs = [os.path.join(BUILD, f + ".o") for f in CU + CPP]
     tmp = OUT + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcublas", "-lpthread"])
+    _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"])
     os.replace(tmp, OUT)
     return OUT
 

@@ -47,8 +47,8 @@
 #include "newton.h"
 #include "otf_tables.h"
 #include "setup.h"
+#include "dense.h"
 
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
@@ -1450,7 +1450,6 @@ struct aegpu_engine {
     bool alloc_failed = false;  // a set-up allocation failed (checked at the end of set-up)
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
-    cublasHandle_t cublas = nullptr;
     int sm_count = 152;
 
     Basis B;
@@ -1582,6 +1581,7 @@ struct aegpu_engine {
         int V = 0;
         double *T = nullptr, *TC = nullptr, *HTC = nullptr, *THT = nullptr, *Hops = nullptr, *hpart = nullptr;
         double *MET = nullptr;  // metric of the compressed tangents
+        double *gram = nullptr; // partial sums of the Gram / projection contractions
         int *pptr = nullptr, *ppos = nullptr;
         double *pscale = nullptr;
         std::vector<std::pair<void *, size_t>> allocs;
@@ -1589,6 +1589,9 @@ struct aegpu_engine {
 
     // lowest eigenpair of H (aegpu_lowest_eigenpair), valid until H is replaced
     double *d_ground = nullptr;
+    // scalar results and dot-product partial sums of the properties pass
+    double *d_small = nullptr;
+    size_t small_len() const { return 8 + 16 * (size_t)sm_count; }
     double ground_value = 0.0;
     bool ground_valid = false;
 
@@ -1603,7 +1606,6 @@ struct aegpu_engine {
             for (auto ev : m) cudaEventDestroy(ev);
         for (auto ev : ev_pool) cudaEventDestroy(ev);
         drop_graph();
-        if (cublas) cublasDestroy(cublas);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -2104,8 +2106,65 @@ __global__ void k_fp64_probe(double *out, int iters, double a, double b)
     if (s == 12345.678) out[0] = s;  // keeps the chains live; practically never taken
 }
 
+// Excitation rule over a list of determinants, on the device: what the pass kernels and
+// the orbit-table builder apply (exc_rule.h), in the reference's output convention
+// (applyExcToBasisState_, fusedevolve.cpp:27-145): a paired determinant gives its
+// partner and sign, an inactive one itself and -1, an active phase operator itself and
+// +1.  The sign of a paired determinant is also recomputed with exc_sign (the pass
+// kernels' form); a disagreement is reported as sign 0.
+__global__ void k_exc_rule(ExcCode code, const uint32_t *__restrict__ states, int64_t n, uint32_t *__restrict__ partner,
+                           int8_t *__restrict__ sign)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t p;
+        int sg;
+        const int st = apply_exc(code, states[i], p, sg);
+        if (st == 1 && exc_sign(code, states[i]) != sg) sg = 0;
+        partner[i] = p;
+        sign[i] = (int8_t)(st == 0 ? -1 : sg);
+    }
+}
+
 // ==================================================================== C ABI ==
 extern "C" {
+
+int aegpu_exc_rule_dev(int nops, const int *ops, const uint32_t *states_dev, int64_t n, uint32_t *partner_dev,
+                       int8_t *sign_dev, void *stream)
+{
+    if (nops < 0 || (nops && !ops) || n < 0 || (n && (!states_dev || !partner_dev || !sign_dev))) return AEGPU_ERR_ARG;
+    for (int o = 0; o < nops; ++o)
+        for (int k = 0; k < 4; ++k)
+            if (ops[4 * o + k] < -1 || ops[4 * o + k] > 31) return AEGPU_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+    for (int o = 0; o < nops && n > 0; ++o) {
+        const int *q = ops + 4 * o;
+        k_exc_rule<<<grid, 256, 0, s>>>(make_exc_code(q[0], q[1], q[2], q[3]), states_dev, n, partner_dev + (size_t)o * n,
+                                        sign_dev + (size_t)o * n);
+    }
+    const cudaError_t rc = cudaGetLastError();
+    return rc == cudaSuccess ? AEGPU_OK : AEGPU_ERR_CUDA;
+}
+
+int aegpu_host_exc_rule(int nops, const int *ops, const uint32_t *states, int64_t n, uint32_t *partner, int8_t *sign)
+{
+    if (nops < 0 || (nops && !ops) || n < 0 || (n && (!states || !partner || !sign))) return AEGPU_ERR_ARG;
+    for (int o = 0; o < nops; ++o) {
+        const int *q = ops + 4 * o;
+        for (int k = 0; k < 4; ++k)
+            if (q[k] < -1 || q[k] > 31) return AEGPU_ERR_ARG;
+        const ExcCode code = make_exc_code(q[0], q[1], q[2], q[3]);
+        for (int64_t i = 0; i < n; ++i) {
+            uint32_t p;
+            int sg;
+            const int st = apply_exc(code, states[i], p, sg);
+            if (st == 1 && exc_sign(code, states[i]) != sg) sg = 0;
+            partner[(size_t)o * n + i] = p;
+            sign[(size_t)o * n + i] = (int8_t)(st == 0 ? -1 : sg);
+        }
+    }
+    return AEGPU_OK;
+}
 
 int aegpu_create(aegpu_engine **out)
 {
@@ -2944,13 +3003,6 @@ int aegpu_apply_h(aegpu_engine *e, const double *x, double *y)
 // or projected Hessian of <proj|psi(theta)> (FusedEvolve::evolveHessianProj,
 // fusedevolve.cpp:2882-3183: no T^T H T term, second-derivative sweeps against the
 // fixed bra, factor 1); energy receives <psi|H psi> or <proj|psi>.
-static int ensure_cublas(aegpu_engine *e)
-{
-    if (!e->cublas && cublasCreate(&e->cublas) != CUBLAS_STATUS_SUCCESS)
-        return e->fail(AEGPU_ERR_CUDA, "cublasCreate failed");
-    cublasSetStream(e->cublas, e->stream);
-    return AEGPU_OK;
-}
 
 static int hessian_impl(aegpu_engine *e, const double *angles, const int *param, const double *scale, int nparams,
                         const double *proj, double *energy, double *grad_comp, double *hess_comp,
@@ -2995,8 +3047,10 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             hs.allocs.push_back({(void *)ptr, std::max<size_t>(count, 1) * sizeof(T)});
             return ptr != nullptr;
         };
+        const int64_t ngram = std::max(gram_scratch_doubles(V, 1, (int64_t)n, e->sm_count),
+                                       gemv_scratch_doubles(V, e->sm_count));
         bool ok = get(hs.T, n * nops) && get(hs.TC, n * V) && get(hs.HTC, n * V) && get(hs.THT, (size_t)V * V) &&
-                  get(hs.MET, (size_t)V * V) &&
+                  get(hs.MET, (size_t)V * V) && get(hs.gram, (size_t)ngram) &&
                   get(hs.Hops, (size_t)nops * nops) && get(hs.hpart, maxpart) && get(hs.pptr, (size_t)nparams + 1) &&
                   get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops);
         if (!ok) {
@@ -3050,28 +3104,29 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     //    of them as one batched product, Gram matrix 2 T_C^T H T_C
     k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
     e->launches += 1;
-    if ((rc = ensure_cublas(e))) return rc;
-    const int DW = (int)(D * W);
+    // With re / im interleaved, the real dot product over the D*W doubles of two columns
+    // is Re(a^dagger b), so every contraction below runs on real columns of n doubles.
     if (metric) {
-        // g = Re(T_C^dagger T_C) over the P tangent columns (tupsquantities.cpp:386-389):
-        // with re / im interleaved the real dot product over D*W entries is Re(a^dagger b)
-        const double one = 1.0, zero = 0.0;
-        cublasDsyrk(e->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, nparams, DW, &one, TC, DW, &zero, hs.MET, nparams);
+        // g = Re(T_C^dagger T_C) over the P tangent columns (tupsquantities.cpp:386-389),
+        // upper triangle
+        e->launches += gram_upper(TC, (int64_t)n, TC, (int64_t)n, (int64_t)n, 1, nparams, 1.0, hs.MET, nullptr, nparams,
+                                  hs.gram, e->sm_count, s);
     }
     if (proj) {
-        // projected: <proj|T_C v> for every column (the last is <proj|psi>), bra for the sweeps
+        // projected: Re <proj|T_C v> for every column (the last is <proj|psi>;
+        // fusedevolve.cpp:3053-3062), bra for the sweeps
         cudaMemcpyAsync(e->d_h, proj, n * sizeof(double), cudaMemcpyHostToDevice, s);
-        const double one = 1.0, zero = 0.0;
-        cublasDgemv(e->cublas, CUBLAS_OP_T, DW, V, &one, TC, DW, e->d_h, 1, &zero, THT, 1);
+        e->launches += gemv_t(TC, (int64_t)n, (int64_t)n, V, e->d_h, 1.0, THT, hs.gram, e->sm_count, s);
     } else {
         // the V columns as V instances of the H product (the matrix or tables are shared)
         rc = run_apply(e, TC, HTC, nullptr, V, nullptr, false);
         if (rc) return rc;
-        // T_C^T (H T_C) is symmetric (H is): only its upper triangle is computed
-        const double two = 2.0, zero = 0.0;
-        cublasDsyrkx(e->cublas, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, V, DW, &two, TC, DW, HTC, DW, &zero, THT, V);
+        // 2 Re(T_C^dagger H T_C) (fusedevolve.cpp:2633-2650) is symmetric (H is): only its
+        // upper triangle is computed; column P holds the gradient and twice the energy
+        e->launches += gram_upper(TC, (int64_t)n, HTC, (int64_t)n, (int64_t)n, 1, V, 2.0, THT, nullptr, V, hs.gram,
+                                  e->sm_count, s);
         // H psi for the backward sweeps: the last column
-        cudaMemcpyAsync(e->d_h, HTC + (size_t)nparams * DW, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(e->d_h, HTC + (size_t)nparams * n, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
     }
     // 3. second-derivative sweeps
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
@@ -3181,40 +3236,12 @@ __global__ void k_lanczos_update(double *__restrict__ w, const double *__restric
         w[i] = vp ? w[i] - a * v[i] - b * vp[i] : w[i] - a * v[i];
 }
 
-// w /= beta, or w = 0 when beta vanishes (the Krylov space is exhausted; the host
-// stops at that step).
-__global__ void k_scale_inverse(double *__restrict__ w, const double *beta, int64_t n)
+// Small device scratch of the properties pass: scalar results and the partial sums of
+// the dot products (dense.cu), allocated once per engine.
+static double *small_scratch(aegpu_engine *e)
 {
-    const double b = *beta;
-    const double f = b > 1e-300 ? 1.0 / b : 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        w[i] *= f;
-}
-
-// First stage of <a|b> over the whole grid: each CTA writes the sum of its grid-stride
-// share to partial[blockIdx.x].  The grid covers every SM several times, so the pass
-// streams at the copy bandwidth (the library's dot and nrm2 reductions measured about
-// 50 us on a 6.8 MB vector, a fraction of it); the grid and the summation order are
-// fixed, so repeated calls give identical sums.
-__global__ void k_dot_partial(const double *__restrict__ a, const double *__restrict__ b, int64_t n,
-                              double *__restrict__ partial)
-{
-    __shared__ double red[32];
-    double s = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        s = fma(a[i], b[i], s);
-    s = block_sum(s, red);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
-}
-
-// Second stage: *out = the sum of m partials, or its square root (a 2-norm), one CTA.
-__global__ void k_dot_finish(const double *__restrict__ partial, int m, double *out, int take_sqrt)
-{
-    __shared__ double red[32];
-    double s = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) s += partial[i];
-    s = block_sum(s, red);
-    if (threadIdx.x == 0) *out = take_sqrt ? sqrt(fmax(s, 0.0)) : s;
+    if (!e->d_small) e->d_small = e->alloc<double>(e->small_len());
+    return e->d_small;
 }
 
 extern "C" {
@@ -3227,21 +3254,18 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the ground state needs a batch size of 1");
     const size_t n = e->vec_elems();
-    if (n > (size_t)std::numeric_limits<int>::max()) return e->fail(AEGPU_ERR_UNSUPPORTED, "vector too long");
     const int m = (int)std::min<size_t>((size_t)basis, n);
-    int rc = ensure_cublas(e);
-    if (rc) return rc;
+    if (m + 1 > 4096) return e->fail(AEGPU_ERR_UNSUPPORTED, "Lanczos basis larger than 4095 vectors");
     e->ground_valid = false;
     if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
-    // basis vectors, reorthogonalisation coefficients, alpha / beta of the recurrence,
-    // the constants 1, 0, -1 for device-pointer cuBLAS calls, and one partial sum per CTA
-    // of the dot-product and norm reductions
-    const int vgrid = (int)std::min<int64_t>(((int64_t)n + 255) / 256, (int64_t)e->sm_count * 8);
-    const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 3 + (size_t)vgrid;
+    double *sm = small_scratch(e);
+    if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
+    // basis vectors; reorthogonalisation coefficients, alpha / beta of the recurrence, the
+    // norm before the Gram-Schmidt pass, a repeat flag and the partial sums of gemv_t
+    const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 2 + (size_t)gemv_scratch_doubles(m + 1, e->sm_count);
     double *Vb = e->alloc<double>((size_t)(m + 1) * n);
     double *scal = e->alloc<double>(nscal);
     auto release = [&] {
-        cublasSetPointerMode(e->cublas, CUBLAS_POINTER_MODE_HOST);
         e->release(Vb, (size_t)(m + 1) * n * sizeof(double));
         e->release(scal, nscal * sizeof(double));
     };
@@ -3249,34 +3273,37 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
         release();
         return e->fail(AEGPU_ERR_NOMEM, "Lanczos basis allocation failed");
     }
-    double *d_c = scal, *d_alpha = scal + (m + 1), *d_beta = d_alpha + m, *d_k = d_beta + m, *d_part = d_k + 3;
-    const double consts[3] = {1.0, 0.0, -1.0};
-    cublasHandle_t h = e->cublas;
+    double *d_c = scal, *d_alpha = scal + (m + 1), *d_beta = d_alpha + m, *d_wn = d_beta + m, *d_part = d_wn + 2;
+    int *d_again = (int *)(d_wn + 1);
+    double *d_res = sm, *d_dpart = sm + 4;
     cudaStream_t s = e->stream;
-    cudaMemcpyAsync(d_k, consts, sizeof(consts), cudaMemcpyHostToDevice, s);
-    const int ni = (int)n;
-    const double one = 1.0, zero = 0.0;
+    const int64_t ni = (int64_t)n;
+    const int vgrid = (int)std::min<int64_t>((ni + 255) / 256, (int64_t)e->sm_count * 8);
+    auto host_scalars = [&](int k, double *out) {
+        cudaMemcpyAsync(out, d_res, k * sizeof(double), cudaMemcpyDeviceToHost, s);
+        return stream_sync(e, "Lanczos");
+    };
     // Lanczos with full reorthogonalisation from the initial state, restarted from the
     // Ritz vector when the basis is full.  The recurrence runs on the device (alpha and
-    // beta stay in device memory, cuBLAS in device-pointer mode); the host reads them and
-    // checks the Ritz pair every kCheck products.
+    // beta stay in device memory); the host reads them and checks the Ritz pair every
+    // kCheck products.
     constexpr int kCheck = 8;
     cudaMemcpyAsync(e->d_ground, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    int prod = 0;
+    int prod = 0, rc = 0;
     bool done = false;
     std::vector<double> al, be, sv;
     while (!done) {
         double nx = 0.0;
-        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST);
-        cublasDnrm2(h, ni, e->d_ground, 1, &nx);
+        e->launches += ae::dot(e->d_ground, e->d_ground, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
+        if ((rc = host_scalars(1, &nx))) {
+            release();
+            return rc;
+        }
         if (!(nx > 0.0)) {
             release();
             return e->fail(AEGPU_ERR_STATE, "the start vector is zero");
         }
-        cudaMemcpyAsync(Vb, e->d_ground, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
-        const double inx = 1.0 / nx;
-        cublasDscal(h, ni, &inx, Vb, 1);
-        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_DEVICE);
+        e->launches += ae::axpby(Vb, e->d_ground, ni, 0.0, 1.0 / nx, nullptr, s);
         int k = 0, checked = 0;
         for (int j = 0; j < m && !done; ++j) {
             double *v = Vb + (size_t)j * n, *w = Vb + (size_t)(j + 1) * n;
@@ -3285,21 +3312,26 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
                 return rc;
             }
             ++prod;
-            k_dot_partial<<<vgrid, 256, 0, s>>>(v, w, (int64_t)n, d_part);
-            k_dot_finish<<<1, 256, 0, s>>>(d_part, vgrid, d_alpha + j, 0);
+            e->launches += ae::dot(v, w, ni, 1, d_alpha + j, 0, d_dpart, e->sm_count, s);
             k_lanczos_update<<<vgrid, 256, 0, s>>>(w, v, j ? Vb + (size_t)(j - 1) * n : nullptr, d_alpha + j,
-                                                   j ? d_beta + (j - 1) : nullptr, (int64_t)n);
-            // one classical Gram-Schmidt pass against the whole basis: the three-term update
-            // above already removed the v_j and v_{j-1} components (where the cancellation
-            // happens), so this pass is the second orthogonalisation for them and leaves the
-            // older components at rounding level ("twice is enough", Giraud, Langou and
-            // Rozloznik 2005); a second full pass would read the basis twice more
-            cublasDgemv(h, CUBLAS_OP_T, ni, j + 1, d_k, Vb, ni, w, 1, d_k + 1, d_c, 1);
-            cublasDgemv(h, CUBLAS_OP_N, ni, j + 1, d_k + 2, Vb, ni, d_c, 1, d_k, w, 1);
-            k_dot_partial<<<vgrid, 256, 0, s>>>(w, w, (int64_t)n, d_part);
-            k_dot_finish<<<1, 256, 0, s>>>(d_part, vgrid, d_beta + j, 1);
-            k_scale_inverse<<<vgrid, 256, 0, s>>>(w, d_beta + j, (int64_t)n);
-            e->launches += 6;
+                                                   j ? d_beta + (j - 1) : nullptr, ni);
+            ++e->launches;
+            // classical Gram-Schmidt against the whole basis.  The three-term update above
+            // already removed the v_j and v_{j-1} components (where the cancellation
+            // happens), so one pass is normally the second orthogonalisation for them
+            // ("twice is enough", Giraud, Langou and Rozloznik 2005).  A second pass runs
+            // only when the first removed a large part of w: ||w|| after it below 0.7 of
+            // ||w|| before it (the Daniel-Gragg-Kaufman-Stewart criterion); the decision
+            // is taken on the device, and the second pass's kernels return at once when
+            // it is not needed.
+            e->launches += ae::dot(w, w, ni, 1, d_wn, 1, d_dpart, e->sm_count, s);
+            e->launches += gemv_t(Vb, ni, ni, j + 1, w, 1.0, d_c, d_part, e->sm_count, s);
+            e->launches += gemv_n(Vb, ni, ni, j + 1, d_c, -1.0, 1.0, w, s);
+            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, d_wn, 0.7, d_again);
+            e->launches += gemv_t(Vb, ni, ni, j + 1, w, 1.0, d_c, d_part, e->sm_count, s, d_again);
+            e->launches += gemv_n(Vb, ni, ni, j + 1, d_c, -1.0, 1.0, w, s, d_again);
+            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, nullptr, 0.0, nullptr, d_again);
+            e->launches += ae::axpby(w, w, ni, 1.0, 0.0, d_beta + j, s);
             const int jn = j + 1;
             if (jn - checked < kCheck && jn < m && prod < max_products && jn < ni) continue;
             // read alpha / beta so far; the first k at which the Ritz pair converged, or the
@@ -3325,31 +3357,33 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             if (prod >= max_products || jn == ni) done = true;
         }
         // Ritz vector: x = V s over the first k basis vectors (restart vector, or the result)
-        cublasSetPointerMode(h, CUBLAS_POINTER_MODE_HOST);
         cudaMemcpyAsync(d_c, sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
-        cublasDgemv(h, CUBLAS_OP_N, ni, k, &one, Vb, ni, d_c, 1, &zero, e->d_ground, 1);
-        if ((rc = stream_sync(e, "Lanczos"))) {
-            release();
-            return rc;
-        }
+        e->launches += gemv_n(Vb, ni, ni, k, d_c, 1.0, 0.0, e->d_ground, s);
     }
     // unit norm, <start|x> >= 0, and the Rayleigh quotient and true residual
-    double nx = 0.0, ov = 0.0, lam = 0.0, res = 0.0;
-    cublasDnrm2(h, ni, e->d_ground, 1, &nx);
-    cublasDdot(h, ni, e->d_start, 1, e->d_ground, 1, &ov);
-    const double f = (ov < 0 ? -1.0 : 1.0) / nx;
-    cublasDscal(h, ni, &f, e->d_ground, 1);
+    double sc[2] = {0.0, 0.0};
+    e->launches += ae::dot(e->d_ground, e->d_ground, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
+    e->launches += ae::dot(e->d_start, e->d_ground, ni, 1, d_res + 1, 0, d_dpart, e->sm_count, s);
+    if ((rc = host_scalars(2, sc))) {
+        release();
+        return rc;
+    }
+    e->launches += ae::axpby(e->d_ground, e->d_ground, ni, (sc[1] < 0 ? -1.0 : 1.0) / sc[0], 0.0, nullptr, s);
     double *w = Vb;
     if ((rc = run_apply(e, e->d_ground, w, nullptr, 1, nullptr, false))) {
         release();
         return rc;
     }
     ++prod;
-    cublasDdot(h, ni, e->d_ground, 1, w, 1, &lam);
-    const double ml = -lam;
-    cublasDaxpy(h, ni, &ml, e->d_ground, 1, w, 1);
-    cublasDnrm2(h, ni, w, 1, &res);
-    rc = stream_sync(e, "Lanczos");
+    double lam = 0.0, res = 0.0;
+    e->launches += ae::dot(e->d_ground, w, ni, 1, d_res, 0, d_dpart, e->sm_count, s);
+    if ((rc = host_scalars(1, &lam))) {
+        release();
+        return rc;
+    }
+    e->launches += ae::axpby(w, e->d_ground, ni, 1.0, -lam, nullptr, s);
+    e->launches += ae::dot(w, w, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
+    rc = host_scalars(1, &res);
     release();
     if (rc) return rc;
     e->ground_value = lam;
@@ -3375,18 +3409,18 @@ int aegpu_ground_overlap(aegpu_engine *e, const double *angles, double *overlap)
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "overlaps need a batch size of 1");
     if (!e->ground_valid) return e->fail(AEGPU_ERR_STATE, "no ground state: call aegpu_lowest_eigenpair first");
     int rc = ensure_state(e, angles);
-    if (!rc) rc = ensure_cublas(e);
     if (rc) return rc;
+    double *sm = small_scratch(e);
+    if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
     const int64_t D = (int64_t)e->B.D;
     if (e->W == 1) {
-        cublasDdot(e->cublas, (int)D, e->d_psi, 1, e->d_ground, 1, &overlap[0]);
-        overlap[1] = 0.0;
+        e->launches += ae::dot(e->d_psi, e->d_ground, D, 1, sm, 0, sm + 4, e->sm_count, e->stream);
+        cudaMemsetAsync(sm + 1, 0, sizeof(double), e->stream);
     } else {
-        cuDoubleComplex z;
-        cublasZdotc(e->cublas, (int)D, (const cuDoubleComplex *)e->d_psi, 1, (const cuDoubleComplex *)e->d_ground, 1, &z);
-        overlap[0] = cuCreal(z);
-        overlap[1] = cuCimag(z);
+        // <psi|v> = sum conj(psi) v
+        e->launches += ae::dotc(e->d_psi, e->d_ground, D, sm, sm + 4, e->sm_count, e->stream);
     }
+    cudaMemcpyAsync(overlap, sm, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     return stream_sync(e, "ground overlap");
 }
 
@@ -3400,15 +3434,17 @@ int aegpu_real_energy(aegpu_engine *e, const double *angles, double *real_energy
         rc = run_energy(e, e->d_scalar, 1);
         if (!rc) e->h_valid = true;
     }
-    if (!rc) rc = ensure_cublas(e);
     if (rc) return rc;
-    const int n = (int)e->B.D, inc = e->W;
+    double *sm = small_scratch(e);
+    if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
+    const int64_t n = (int64_t)e->B.D, inc = e->W;
     // H is real, so Re(H psi) = H Re(psi): <r|H r> / <r|r> from the even (real) entries
-    double rhr = 0.0, rr = 0.0;
-    cublasDdot(e->cublas, n, e->d_psi, inc, e->d_h, inc, &rhr);
-    cublasDdot(e->cublas, n, e->d_psi, inc, e->d_psi, inc, &rr);
+    double v[2] = {0.0, 0.0};
+    e->launches += ae::dot(e->d_psi, e->d_h, n, inc, sm, 0, sm + 4, e->sm_count, e->stream);
+    e->launches += ae::dot(e->d_psi, e->d_psi, n, inc, sm + 1, 0, sm + 4, e->sm_count, e->stream);
+    cudaMemcpyAsync(v, sm, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     if ((rc = stream_sync(e, "real-part energy"))) return rc;
-    *real_energy = rhr / rr;
+    *real_energy = v[0] / v[1];
     return AEGPU_OK;
 }
 
@@ -3420,20 +3456,24 @@ int aegpu_subspace_matrices(aegpu_engine *e, int nsets, const double *angles, do
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "subspace matrices need a batch size of 1");
     const size_t n = e->vec_elems(), nops = e->excs.size();
-    if (n * (size_t)e->W > (size_t)std::numeric_limits<int>::max()) return e->fail(AEGPU_ERR_UNSUPPORTED, "vector too long");
-    int rc = ensure_cublas(e);
-    if (rc) return rc;
-    double *Psi = e->alloc<double>(n * nsets), *HPsi = e->alloc<double>(n * nsets), *M = e->alloc<double>((size_t)4 * nsets * nsets);
+    const int W = e->W;
+    const int64_t D = (int64_t)e->B.D;
+    const size_t nn = (size_t)nsets * nsets;
+    const int64_t ngram = gram_scratch_doubles(nsets, W, D, e->sm_count);
+    double *Psi = e->alloc<double>(n * nsets), *HPsi = e->alloc<double>(n * nsets), *M = e->alloc<double>(4 * nn),
+           *G = e->alloc<double>((size_t)ngram);
     auto release = [&] {
         e->release(Psi, n * nsets * sizeof(double));
         e->release(HPsi, n * nsets * sizeof(double));
-        e->release(M, (size_t)4 * nsets * nsets * sizeof(double));
+        e->release(M, 4 * nn * sizeof(double));
+        e->release(G, (size_t)ngram * sizeof(double));
     };
-    if (!Psi || !HPsi || !M) {
+    if (!Psi || !HPsi || !M || !G) {
         release();
         return e->fail(AEGPU_ERR_NOMEM, "subspace buffers allocation failed");
     }
     cudaStream_t s = e->stream;
+    int rc = 0;
     // the evolved states as columns, then H on all of them as one batched product
     for (int k = 0; k < nsets; ++k) {
         if ((rc = upload_angles(e, angles + (size_t)k * nops, true, 1, false)) || (rc = run_evolve(e, 1))) {
@@ -3448,43 +3488,27 @@ int aegpu_subspace_matrices(aegpu_engine *e, int nsets, const double *angles, do
         release();
         return rc;
     }
-    const size_t nn = (size_t)nsets * nsets;
-    if (e->W == 1) {
-        const double one = 1.0, zero = 0.0;
-        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nsets, nsets, (int)n, &one, Psi, (int)n, HPsi, (int)n, &zero, M,
-                    nsets);
-        cublasDgemm(e->cublas, CUBLAS_OP_T, CUBLAS_OP_N, nsets, nsets, (int)n, &one, Psi, (int)n, Psi, (int)n, &zero,
-                    M + nn, nsets);
-    } else {
-        // <psi_i|H psi_j> and <psi_i|psi_j> as complex products (conjugate transpose)
-        const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-        const int D = (int)e->B.D;
-        cuDoubleComplex *Mz = (cuDoubleComplex *)M;
-        cublasZgemm(e->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nsets, nsets, D, &one, (const cuDoubleComplex *)Psi, D,
-                    (const cuDoubleComplex *)HPsi, D, &zero, Mz, nsets);
-        cublasZgemm(e->cublas, CUBLAS_OP_C, CUBLAS_OP_N, nsets, nsets, D, &one, (const cuDoubleComplex *)Psi, D,
-                    (const cuDoubleComplex *)Psi, D, &zero, Mz + nn, nsets);
-    }
-    std::vector<double> hm((size_t)4 * nn);
-    cudaMemcpyAsync(hm.data(), M, hm.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+    // upper triangles of <psi_i|H psi_j> and <psi_i|psi_j> (complex: conjugate-linear in
+    // the first argument; real and imaginary parts), column-major nsets x nsets
+    e->launches += gram_upper(Psi, (int64_t)n, HPsi, (int64_t)n, D, W, nsets, 1.0, M, W == 2 ? M + nn : nullptr, nsets, G,
+                              e->sm_count, s);
+    e->launches += gram_upper(Psi, (int64_t)n, Psi, (int64_t)n, D, W, nsets, 1.0, M + 2 * nn, W == 2 ? M + 3 * nn : nullptr,
+                              nsets, G, e->sm_count, s);
+    std::vector<double> hm(4 * nn, 0.0);
+    cudaMemcpyAsync(hm.data(), M, (W == 2 ? 4 : 3) * nn * sizeof(double), cudaMemcpyDeviceToHost, s);
     rc = stream_sync(e, "subspace matrices");
     release();
     if (rc) return rc;
-    // column-major (i, j) -> row-major out[i * nsets + j]
+    // both matrices are Hermitian: (i, j) for i <= j from the upper triangle (column-major
+    // at j * nsets + i), the rest by conjugate symmetry; out[i * nsets + j] row-major
     for (int i = 0; i < nsets; ++i)
         for (int j = 0; j < nsets; ++j) {
-            const size_t cm = (size_t)j * nsets + i, rm = (size_t)i * nsets + j;
-            if (e->W == 1) {
-                h_re[rm] = hm[cm];
-                s_re[rm] = hm[nn + cm];
-                if (h_im) h_im[rm] = 0.0;
-                if (s_im) s_im[rm] = 0.0;
-            } else {
-                h_re[rm] = hm[2 * cm];
-                s_re[rm] = hm[2 * (nn + cm)];
-                if (h_im) h_im[rm] = hm[2 * cm + 1];
-                if (s_im) s_im[rm] = hm[2 * (nn + cm) + 1];
-            }
+            const size_t cm = i <= j ? (size_t)j * nsets + i : (size_t)i * nsets + j, rm = (size_t)i * nsets + j;
+            const double sg = i <= j ? 1.0 : -1.0;
+            h_re[rm] = hm[cm];
+            s_re[rm] = hm[2 * nn + cm];
+            if (h_im) h_im[rm] = W == 2 ? sg * hm[nn + cm] : 0.0;
+            if (s_im) s_im[rm] = W == 2 ? sg * hm[3 * nn + cm] : 0.0;
         }
     return AEGPU_OK;
 }
@@ -3618,6 +3642,11 @@ int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t
                              const double *x_dev, double *y_dev, double *energy_dev, void *stream)
 {
     if (D < 1 || !rowptr_dev || !col_dev || !val_dev || !x_dev || !y_dev || !energy_dev) return AEGPU_ERR_ARG;
+    // y is written while other rows still read x, and the energy while y is read: the
+    // three must be distinct (an in-place call would race and return wrong results)
+    if ((const void *)x_dev == (const void *)y_dev || (const void *)energy_dev == (const void *)x_dev ||
+        energy_dev == y_dev)
+        return AEGPU_ERR_ARG;
     if (D > kNoAllocMaxRows) {
         fprintf(stderr, "aegpu_csr_energy_noalloc: %lld rows exceed the fixed scratch limit of %lld rows\n",
                 (long long)D, (long long)kNoAllocMaxRows);

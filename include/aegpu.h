@@ -310,6 +310,29 @@ int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *bl
 int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int nops, const int *ops,
                       uint32_t *idx, int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles);
 
+/* The excitation rule itself, for bit-exact checks against the reference's
+ * applyExcToBasisState_ (fusedevolve.cpp:27-145): for every operator o (ops[4 o ..],
+ * 0-based spin orbitals, -1 absent) and determinant bitstring states[i],
+ * partner[o * n + i] and sign[o * n + i] in the reference's convention -- a paired
+ * determinant gives its partner and +1 / -1, an inactive one itself and -1, an active
+ * phase operator itself and +1 (0 would mean the pass kernels' sign form disagrees).
+ * aegpu_exc_rule_dev runs the device code the pass kernels use (device pointers,
+ * enqueued on `stream`); aegpu_host_exc_rule the host code the orbit tables are
+ * built with. */
+int aegpu_exc_rule_dev(int nops, const int *ops, const uint32_t *states_dev, int64_t n, uint32_t *partner_dev,
+                       int8_t *sign_dev, void *stream);
+int aegpu_host_exc_rule(int nops, const int *ops, const uint32_t *states, int64_t n, uint32_t *partner, int8_t *sign);
+
+/* The Hessian's Gram contraction on caller-held device columns (a test and timing
+ * hook; the engine calls the same kernels): the upper triangle (i <= j < V) of
+ * C = alpha * A^H B, column-major with leading dimension ldc, for V columns of nrows
+ * rows of W doubles (W = 2: complex, re / im interleaved; Cim receives the imaginary
+ * part).  Column c of A starts at A + c * lda (lda >= nrows * W).  Entries below the
+ * diagonal are left untouched.  Enqueued on `stream`; its scratch comes from the
+ * stream-ordered allocator. */
+int aegpu_gram_upper_dev(const double *A, int64_t lda, const double *B, int64_t ldb, int64_t nrows, int W, int V,
+                         double alpha, double *Cre, double *Cim, int ldc, void *stream);
+
 /* Allocation-free H * x (no counterpart in the reference).
  * For callers that cannot allocate device memory at all -- code running inside a
  * CUDA memory-pool or allocator callback, a library whose device memory is owned and
@@ -325,8 +348,13 @@ int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_bet
  * array: calls that overlap on the GPU (different streams, or host threads, without
  * ordering between them) race and give wrong sums; calls ordered on one stream are
  * safe.  Nothing needs clearing between calls -- each call writes every partial sum
- * it reads.  x, y, energy are device pointers; stream is a cudaStream_t (NULL = the
- * default stream).  The work is enqueued, not synchronised. */
+ * it reads.  x, y, energy are device pointers that must not overlap (the product is
+ * not in place: x == y, or energy on x or y, returns AEGPU_ERR_ARG); stream is a
+ * cudaStream_t (NULL = the default stream).  The work is enqueued, not synchronised.
+ * The array's device address is looked up once per device and kept until the process
+ * exits: it belongs to the device context current at that first call, so after a
+ * cudaDeviceReset (or another library resetting the primary context) this entry point
+ * must not be called again in that process. */
 int aegpu_csr_energy_noalloc(int64_t D, const int64_t *rowptr_dev, const int32_t *col_dev, const double *val_dev,
                              const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 

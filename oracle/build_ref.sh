@@ -4,10 +4,11 @@
 # Test infrastructure only: oracle/_ref/ validates the C restatement in
 # oracle/oracle.c and produces the golden fixtures under tests/golden/.
 # The reference's CMake project needs gfortran, so the translation units are
-# compiled directly.  Needs the reference checkout (default /root/reference).
+# compiled directly.  Needs the reference checkout: AE_REFERENCE, else a `reference`
+# directory beside this repository.
 set -euo pipefail
-REF=${AE_REFERENCE:-/root/reference}/src
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${AE_REFERENCE:-$HERE/../../reference}/src
 OUT=$HERE/_ref
 [ -d "$REF" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
 mkdir -p "$OUT/obj_real" "$OUT/obj_cplx"

@@ -16,6 +16,10 @@
 //   anglesets m len {values}             (compressed or per-operator angles)
 //   want e g h s                         (0/1 flags per output)
 //   pairs 0|1                            (dump the per-excitation partner/sign rule)
+//   pairsfile <path>                     (the same rule over the sector of the initial
+//                                         state only, ascending bitstrings: for every
+//                                         excitation uint32 partners then int8 signs,
+//                                         written raw to <path>)
 //   optimise 0|1
 //   time k                               (k timed evolve+evolveDerivative units)
 //   properties <prefix>                  (TUPSQuantities::writeProperties over the zero
@@ -66,7 +70,7 @@ int main(int argc, char **argv)
     double nuclear = 0;
     std::vector<std::vector<double>> angleSets;
     int wantE = 1, wantG = 1, wantH = 0, wantS = 0, wantPairs = 0, wantOpt = 0, timeK = 0;
-    std::string propsPrefix;
+    std::string propsPrefix, pairsPath;
     int subspaceN = 0;
 
     std::string tok;
@@ -101,6 +105,7 @@ int main(int argc, char **argv)
             for (int k = 0; k < m; ++k) { std::vector<double> a(len); for (auto &x : a) in >> x; angleSets.push_back(a); }
         } else if (tok == "want") in >> wantE >> wantG >> wantH >> wantS;
         else if (tok == "pairs") in >> wantPairs;
+        else if (tok == "pairsfile") in >> pairsPath;
         else if (tok == "optimise") in >> wantOpt;
         else if (tok == "time") in >> timeK;
         else if (tok == "properties") in >> propsPrefix;
@@ -151,6 +156,30 @@ int main(int argc, char **argv)
                 double rec[2] = {(double)partner, r.second ? 1.0 : -1.0};
                 put(out, rec, 2);
             }
+    }
+    if (!pairsPath.empty()) {
+        // applyExcToBasisState_ (fusedevolve.cpp:27-145) over the ascending sector list
+        uint32_t ones = -1;
+        int spinUp = bitwiseDot(initIdx[0] >> (nq / 2), ones, 32), spinDown = bitwiseDot(initIdx[0], ones, nq / 2);
+        std::vector<uint32_t> sector;
+        for (uint32_t s = 0; s < (1u << nq); ++s)
+            if (bitwiseDot(s >> (nq / 2), ones, 32) == spinUp && bitwiseDot(s, ones, nq / 2) == spinDown)
+                sector.push_back(s);
+        FILE *pf = fopen(pairsPath.c_str(), "wb");
+        if (!pf) { fprintf(stderr, "cannot open %s\n", pairsPath.c_str()); return 2; }
+        std::vector<uint32_t> partner(sector.size());
+        std::vector<int8_t> sign(sector.size());
+        for (size_t e = 0; e < excs.size(); ++e) {
+            for (size_t k = 0; k < sector.size(); ++k) {
+                uint32_t in_s = isComplex ? (sector[k] << 1) : sector[k];
+                auto r = applyExcToBasisState_(in_s, excs[e]);
+                partner[k] = isComplex ? (r.first >> 1) : r.first;
+                sign[k] = r.second ? 1 : -1;
+            }
+            fwrite(partner.data(), sizeof(uint32_t), partner.size(), pf);
+            fwrite(sign.data(), 1, sign.size(), pf);
+        }
+        fclose(pf);
     }
     if (wantOpt) {
         auto t0 = std::chrono::steady_clock::now();

@@ -14,16 +14,26 @@ Sources of the inputs:
   syn6     -- synthetic 6-orbital TUPS, seed 3, plus the excitation rule table
   ref10    -- the benchmark's 10-orbital inputs (seed 0, 3 layers): E, gradient, Hessian,
               sampled final-state amplitudes
-  ref12    -- the benchmark's 12-orbital inputs (seed 0, 3 layers): E, gradient,
-              sampled final-state amplitudes (the reference's Hessian takes minutes here)
+  ref12    -- the benchmark's 12-orbital inputs (seed 0, 3 layers): E, gradient, Hessian,
+              sampled final-state amplitudes
+  ref14    -- the benchmark's 14-orbital inputs (7a+7b, seed 0, 4 layers; the reference
+              picks its on-the-fly H here): E, gradient, sampled final-state amplitudes
+  lucj14   -- the complex LUCJ circuit exp(-K) exp(iJ) exp(K) at 14 orbitals (K, J of
+              ansatzevolve_gb300.lucj.random_lucj(14, 3), integrals of seed 7), every
+              operator its own parameter: E, gradient, sampled final-state amplitudes
+  pairs12  -- the excitation rule of every operator of the 12-orbital, 3-layer TUPS circuit
+              over every determinant of the 6a+6b sector: SHA-256 digests of the partner
+              bitstrings and signs, active counts and a seeded sample of raw entries
   props_h4, props_h4c, props_syn6
            -- the reference's own TUPSQuantities::writeProperties table (energies,
               Hessian / metric eigenvalue and diagonal counts, gradient norms, overlaps
               with the lowest eigenvector), its Hessian and metric matrices per path, and
               doSubspaceDiagonalisation's eigenvalues, over the zero path and the angle
               sets of the h4 / h4c / syn6 inputs plus a repeat of the first set
-Only the ref10 / ref12 / props_* cases can be regenerated alone:
-    python tests/golden/make_golden.py ref10 ref12 props_h4 props_h4c props_syn6
+Only the ref10 / ref12 / ref14 / lucj14 / pairs12 / props_* cases can be regenerated alone:
+    python tests/golden/make_golden.py ref10 ref12 ref14 lucj14 pairs12 props_h4 props_h4c props_syn6
+The reference checkout is AE_REFERENCE (default: a `reference` directory beside this
+repository).
 """
 import os
 import re
@@ -38,13 +48,13 @@ sys.path.insert(0, ROOT)
 from ansatzevolve_gb300.synthetic import (hartree_fock_index, synthetic_integrals,  # noqa: E402
                                           tups_operators, write_integrals)
 
-REF = os.environ.get("AE_REFERENCE", "/root/reference")
+REF = os.environ.get("AE_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 DRV = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
 def run(spec_lines, cplx=False, threads=4):
-    with tempfile.TemporaryDirectory() as td:
+    with tempfile.TemporaryDirectory(dir=os.environ.get("AE_GOLDEN_TMP")) as td:
         sp, op = os.path.join(td, "spec"), os.path.join(td, "out")
         open(sp, "w").write("\n".join(spec_lines) + "\nend\n")
         drv = DRV + ("_cplx" if cplx else "")
@@ -284,15 +294,23 @@ def properties_case(tag, base, cplx=False):
     print(tag, rows[0], ov, sub, null_rank)
 
 
+def sector_list(N, na, nb):
+    """Ascending bitstrings of the (na alpha, nb beta) sector (alpha = high N bits)."""
+    pc = np.array([bin(v).count("1") for v in range(1 << N)], dtype=np.int64)
+    a = np.flatnonzero(pc == na).astype(np.uint32)
+    b = np.flatnonzero(pc == nb).astype(np.uint32)
+    return ((a[:, None] << np.uint32(N)) | b[None, :]).ravel()
+
+
 def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
-    """The benchmark's own inputs at 10 / 12 orbitals (integrals of `seed`, angles
+    """The benchmark's own inputs at 10 / 12 / 14 orbitals (integrals of `seed`, angles
     default_rng(seed + 1).uniform(-0.1, 0.1)): energy, gradient, (Hessian), and a seeded
     sample of the final state's sector amplitudes with the state's norm."""
     h, g = synthetic_integrals(N, seed)
     ops, param, scale = tups_operators(N, layers)
     P = int(param.max())
     x = np.random.default_rng(seed + 1).uniform(-0.1, 0.1, P)
-    with tempfile.TemporaryDirectory() as td:
+    with tempfile.TemporaryDirectory(dir=os.environ.get("AE_GOLDEN_TMP")) as td:
         prefix = os.path.join(td, "syn")
         write_integrals(prefix, h, g)
         hf = hartree_fock_index(N, na, nb)
@@ -301,9 +319,8 @@ def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
                 threads=8)
     res, _ = split_outputs(d, 1, P, 1 << (2 * N), want)
     state = res["S"][0]
-    allst = np.arange(1 << (2 * N), dtype=np.uint32)
-    pc = np.array([bin(v).count("1") for v in range(1 << N)], dtype=np.int64)
-    sect = np.flatnonzero((pc[allst >> N] == na) & (pc[allst & ((1 << N) - 1)] == nb)).astype(np.uint32)
+    del d
+    sect = sector_list(N, na, nb)
     pick = np.sort(np.random.default_rng(seed + 7).choice(len(sect), nsample, replace=False))
     fx = dict(N=N, na=na, nb=nb, layers=layers, seed=seed, hf=hf, ops_1b=ops, order_1b=param, scale=scale,
               x=x, E=res["E"][0], G=res["G"][0], sample_rank=pick.astype(np.int64), sample_bits=sect[pick],
@@ -314,13 +331,87 @@ def large_case(tag, N, na, nb, layers, seed, hess, nsample=256):
     print(tag, fx["E"])
 
 
+def lucj_case(tag, N, na, lucj_seed, ham_seed, nsample=256):
+    """The complex LUCJ circuit of ansatzevolve_gb300.lucj (every operator its own
+    parameter, scale 1) on the Hartree-Fock determinant, with the synthetic integrals
+    of `ham_seed`: energy, gradient per operator, sampled final-state amplitudes."""
+    from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+    K, J = random_lucj(N, lucj_seed)
+    ops, ang = lucj_operators(K, J)
+    h, g = synthetic_integrals(N, ham_seed)
+    P = len(ops)
+    with tempfile.TemporaryDirectory(dir=os.environ.get("AE_GOLDEN_TMP")) as td:
+        prefix = os.path.join(td, "lucj")
+        write_integrals(prefix, h, g)
+        hf = hartree_fock_index(N, na, na)
+        want = (1, 1, 0, 1)
+        d = run(spec(2 * N, [(hf, 1.0, 0.0)], ops, np.arange(P), np.ones(P), [f"ham ints {prefix}"], [ang],
+                     want=want), cplx=True, threads=8)
+    res, _ = split_outputs(d, 1, P, 1 << (2 * N), want, cplx=True)
+    state = res["S"][0]
+    del d
+    sect = sector_list(N, na, na)
+    pick = np.sort(np.random.default_rng(lucj_seed + 7).choice(len(sect), nsample, replace=False))
+    amp = state[2 * sect[pick].astype(np.int64)] + 1j * state[2 * sect[pick].astype(np.int64) + 1]
+    fx = dict(N=N, na=na, nb=na, lucj_seed=lucj_seed, ham_seed=ham_seed, hf=hf, ops=ops, x=ang, E=res["E"][0],
+              G=res["G"][0], sample_rank=pick.astype(np.int64), sample_bits=sect[pick], sample_amp=amp,
+              norm=float(np.dot(state, state)))
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), **fx)
+    print(tag, fx["E"])
+
+
+def pairs_case(tag, N, na, nb, layers, nsample=4096):
+    """The reference's excitation rule (applyExcToBasisState_, fusedevolve.cpp:27-145)
+    for every operator of the N-orbital TUPS circuit over every sector determinant in
+    ascending order: per operator the SHA-256 of the partner bitstrings (uint32 LE) and
+    of the signs (int8, +1 / -1; an inactive determinant is its own partner with sign
+    -1, as the reference returns it), the number of active determinants, and a seeded
+    sample of raw entries; plus the SHA-256 of the sector list itself."""
+    import hashlib
+    ops, param, scale = tups_operators(N, layers)
+    hf = hartree_fock_index(N, na, nb)
+    sect = sector_list(N, na, nb)
+    n = len(sect)
+    with tempfile.TemporaryDirectory(dir=os.environ.get("AE_GOLDEN_TMP")) as td:
+        pf = os.path.join(td, "pairs")
+        s = spec(2 * N, [(hf, 1.0, 0.0)], ops - 1, param - 1, scale, ["ham triplets 1", f"{hf} {hf} 1.0"],
+                 [np.zeros(int(param.max()))], want=(0, 0, 0, 0))
+        s.append(f"pairsfile {pf}")
+        run(s)
+        raw = np.fromfile(pf, dtype=np.uint8)
+    assert raw.size == len(ops) * n * 5
+    pick = np.sort(np.random.default_rng(17).choice(n, nsample, replace=False))
+    dig_p, dig_s, active, sp, ss = [], [], [], [], []
+    for k in range(len(ops)):
+        blk = raw[k * n * 5:(k + 1) * n * 5]
+        partner = blk[:4 * n].view("<u4")
+        sign = blk[4 * n:].view(np.int8)
+        dig_p.append(hashlib.sha256(partner.tobytes()).hexdigest())
+        dig_s.append(hashlib.sha256(sign.tobytes()).hexdigest())
+        active.append(int(np.count_nonzero(partner != sect)))
+        sp.append(partner[pick])
+        ss.append(sign[pick])
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), N=N, na=na, nb=nb, layers=layers, ops_1b=ops,
+                        sector_sha256=hashlib.sha256(sect.astype("<u4").tobytes()).hexdigest(),
+                        partner_sha256=np.array(dig_p), sign_sha256=np.array(dig_s), active=np.array(active),
+                        sample_rank=pick.astype(np.int64), sample_partner=np.array(sp), sample_sign=np.array(ss))
+    print(tag, len(ops), "operators over", n, "determinants; active", min(active), "..", max(active))
+
+
 if __name__ == "__main__":
+    single = {
+        "ref10": lambda: large_case("ref10", 10, 5, 5, 3, 0, hess=True),
+        "ref12": lambda: large_case("ref12", 12, 6, 6, 3, 0, hess=True),
+        "ref14": lambda: large_case("ref14", 14, 7, 7, 4, 0, hess=False),
+        "lucj14": lambda: lucj_case("lucj14", 14, 7, 3, 7),
+        "pairs12": lambda: pairs_case("pairs12", 12, 6, 6, 3),
+    }
     if len(sys.argv) > 1:
         for t in sys.argv[1:]:
             if t.startswith("props_"):
                 properties_case(t, t[6:], cplx=t.endswith("c"))
             else:
-                large_case(t, int(t[3:]), int(t[3:]) // 2, int(t[3:]) // 2, 3, 0, hess=t == "ref10")
+                single[t]()
         sys.exit(0)
     fortran_case()
     hams_case("TestFermionic", None, tag="ferm")
@@ -328,8 +419,8 @@ if __name__ == "__main__":
     hams_case("H4_Complex", "L1", cplx=True, tag="h4c")
     synthetic_case("syn6", 6, 3, 3, 2, 3, pairs=True)
     synthetic_case("syn8", 8, 4, 4, 2, 0)
-    large_case("ref10", 10, 5, 5, 3, 0, hess=True)
-    large_case("ref12", 12, 6, 6, 3, 0, hess=False)
+    for t in ("ref10", "ref12", "ref14", "lucj14", "pairs12"):
+        single[t]()
     properties_case("props_h4", "h4")
     properties_case("props_h4c", "h4c", cplx=True)
     properties_case("props_syn6", "syn6")
