@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
 _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
-TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL = 1, 2, 3, 4, 5
+TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL, TUNE_REUSE_HPSI = 1, 2, 3, 4, 5, 6
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 PROP_HESSIAN, PROP_OVERLAP, PROP_HF_PATH = 1, 2, 4
 # rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)

@@ -57,6 +57,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -1537,6 +1538,9 @@ struct aegpu_engine {
     // above, where early-resident dependents slow the FP64-bound passes: GB300,
     // 8 / 10 orbitals -6 %, 12 orbitals (853,776 amplitudes) +1.7 %)
     int tune_pdl = -1;
+    // keep H psi between an energy and a gradient at the same angles (AEGPU_REUSE_HPSI=0
+    // in the environment, or the knob, makes the gradient recompute it)
+    bool reuse_hpsi = true;
     bool pdl_on() const { return tune_pdl >= 0 ? tune_pdl != 0 : (int64_t)B.D * W * nb <= (int64_t)1 << 19; }
     int spmv_tpr() const
     {
@@ -2177,6 +2181,7 @@ int aegpu_create(aegpu_engine **out)
     }
     auto *e = new aegpu_engine();
     cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    if (const char *v = std::getenv("AEGPU_REUSE_HPSI")) e->reuse_hpsi = std::strcmp(v, "0") != 0;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete e;
@@ -2639,6 +2644,10 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         e->tune_pdl = value;
         e->drop_graph();
         return AEGPU_OK;
+    case AEGPU_TUNE_REUSE_HPSI:
+        if (value != 0 && value != 1) return e->fail(AEGPU_ERR_ARG, "H psi reuse must be 0 or 1");
+        e->reuse_hpsi = value != 0;
+        return AEGPU_OK;
     case AEGPU_TUNE_SPMV_TPR:
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return e->fail(AEGPU_ERR_ARG, "threads per row must be 0 (by size), 1, 2, 4 or 8");
@@ -2659,6 +2668,7 @@ int aegpu_get_tuning(const aegpu_engine *e, int knob)
     case AEGPU_TUNE_OTF_THREADS: return e->tune_otf_threads;
     case AEGPU_TUNE_SPMV_TPR: return e->spmv_tpr();
     case AEGPU_TUNE_PDL: return e->pdl_on() ? 1 : 0;
+    case AEGPU_TUNE_REUSE_HPSI: return e->reuse_hpsi ? 1 : 0;
     default: return -1;
     }
 }
@@ -2712,6 +2722,7 @@ int aegpu_gradient(aegpu_engine *e, const double *angles, double *energy, double
     if (!e || !angles || !grad_ops) return AEGPU_ERR_ARG;
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     const size_t nang = e->excs.size() * (size_t)e->nb;
+    if (!e->reuse_hpsi) e->h_valid = false;  // recompute H psi, as the reference does (fusedevolve.cpp:2292)
     if (e->use_graph && !e->timing && !(same_angles(e, angles) && e->h_valid)) {
         // the whole evaluation as one graph replay (H psi is not cached for these angles)
         if (!e->grad_graph) {

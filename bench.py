@@ -14,8 +14,9 @@ stream); `e2e` is the same metric through the reference-compatible C ABI
 (getEnergy + getGradient_COMP with host buffers, copies inside the timed region).
 Under torchrun every rank runs an independent replica (the path does not shard),
 timing is the max over ranks and `value` sums all ranks' evaluations.
-`--impl reference` times the reference algorithm's CPU implementation (the C
-restatement in oracle/, all host threads) on the same workload.
+`--impl reference` times the reference's own CPU implementation (built natively on
+this host from its sources by oracle/build_ref.sh --timing, all host threads) on the
+same workload; without that build, the oracle's C restatement of it.
 
 Two more objects on the same line: `batched` (512 instances of 8, 10 and 12 orbitals
 with their own integrals, one graph launch per step) and `time_to_converge` (a
@@ -24,6 +25,7 @@ time against the batched, network-warm-started path).
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -48,7 +50,8 @@ def set_orbitals(n):
 def workload_desc(D, P, nops, ham):
     if LUCJ:
         return {"workload": "LUCJ exp(-K) exp(iJ) exp(K), complex128, %d orbitals, %da+%db electrons (D=%d), %d "
-                            "operators, synthetic random integrals seed 0, H %s" % (N_ORB, N_A, N_B, D, nops, ham),
+                            "operators (K, J seed %d), synthetic random integrals seed %d, H %s"
+                            % (N_ORB, N_A, N_B, D, nops, LUCJ_SEED, LUCJ_HAM_SEED, ham),
                 "global_batch": 1, "parallelism": "replicas", "l2": "state vectors larger than L2"}
     return {"workload": "tUPS %d orbitals, %da+%db electrons (D=%d), %d layers (%d parameters, %d excitations), "
                         "synthetic random integrals seed 0, H %s" % (N_ORB, N_A, N_B, D, LAYERS, P, nops, ham),
@@ -61,14 +64,19 @@ LUCJ = False
 SELL_TRAFFIC_RATIO = (669.273856 + 3.678720) / 668.570112
 
 
+# the LUCJ circuit's seeds (K, J and the integrals), those of the reference-pinned
+# fixture tests/golden/lucj14.npz
+LUCJ_SEED, LUCJ_HAM_SEED = 3, 7
+
+
 def problem():
     from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
-    h1, g2 = synthetic_integrals(N_ORB, SEED)
+    h1, g2 = synthetic_integrals(N_ORB, LUCJ_HAM_SEED if LUCJ else SEED)
     hf = hartree_fock_index(N_ORB, N_A, N_B)
     if LUCJ:
         # exp(-K) exp(iJ) exp(K), K anti-Hermitian N(0, 0.1), nearest-neighbour J ~ N(0, 0.1)
         from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
-        K, J = random_lucj(N_ORB, SEED)
+        K, J = random_lucj(N_ORB, LUCJ_SEED)
         ops0, ang = lucj_operators(K, J)
         n = len(ops0)
         return dict(h1=h1, g2=g2, ops0=ops0, ops1=None, p0=np.arange(n), scale=np.ones(n), P=n, x=ang, hf=hf,
@@ -141,8 +149,19 @@ def measured_peak():
 
 
 def cpu_baseline(pb, max_seconds=30.0):
-    """The oracle (C restatement of the reference algorithm, OpenMP) on a bounded sample."""
+    """The reference itself on the host cores (oracle/_ref/ref_driver_native) on a bounded
+    sample, with the oracle's energy and gradient for the parity check; without the
+    reference build, the oracle (C restatement of the reference algorithm, OpenMP)."""
     from oracle.oracle import Oracle, lib as olib
+    if reference_available() is None and not LUCJ:
+        r = reference_timing(pb, 3, 0, max_seconds)
+        t = float(np.median(r["times"][1:])) if len(r["times"]) > 1 else float(r["times"][0])
+        return {"value": 1.0 / t, "unit": "evals/s", "cores": r["cores"], "kind": "reference",
+                "cpu_model": r["cpu_model"],
+                "sample": "%d FusedEvolve::evolve + evolveDerivative(&E) units of the same %d-orbital workload "
+                          "(median of all but the first), the reference built natively on this host "
+                          "(oracle/_ref/ref_driver_native); set-up %.1f s not timed"
+                          % (len(r["times"]), N_ORB, r["setup_s"])}, r["E"], r["g"]
     o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B, cplx=pb["cplx"])
     o.set_initial([pb["hf"]], [1.0])
     o.set_ops(pb["ops0"], pb["p0"], pb["scale"])
@@ -164,16 +183,100 @@ def cpu_baseline(pb, max_seconds=30.0):
                                                                   if len(times) > 1 else "single evaluation")}, E, g
 
 
+# the reference itself, built natively on this host from its own sources by
+# oracle/build_ref.sh --timing (build() does it when the sources are there)
+REF_DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver_native")
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return None
+
+
+def reference_timing(pb, steps, warmup, budget):
+    """The reference's own FusedEvolve::evolve + evolveDerivative(&E) -- the unit of the
+    metric, as its CLI benchmark times it (main.cpp:415-425) -- on all host threads:
+    oracle/_ref/ref_driver_native builds the reference's HamiltonianMatrix from the
+    integral files (at 12 orbitals the reference picks its on-the-fly operator list by
+    itself), then times `steps` units after `warmup` untimed ones, within `budget` s."""
+    import tempfile
+    from ansatzevolve_gb300.synthetic import write_integrals
+    threads = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, "ints")
+        write_integrals(prefix, pb["h1"], pb["g2"])
+        spec = ["nqubits %d" % (2 * N_ORB), "initial 1", "%d 1.0 0.0" % pb["hf"], "ops %d" % len(pb["ops0"])]
+        spec += [" ".join(str(int(v)) for v in o) for o in pb["ops0"]]
+        spec += ["order %d" % len(pb["p0"])] + ["%d %r" % (int(p), float(c)) for p, c in zip(pb["p0"], pb["scale"])]
+        spec += ["ham ints %s" % prefix, "nuclear 0.0", "anglesets 1 %d" % pb["P"], " ".join(repr(float(v)) for v in pb["x"]),
+                 "want 0 0 0 0", "time %d" % max(1, steps), "timewarmup %d" % max(0, warmup), "timebudget %r" % budget,
+                 "end"]
+        sp, op = os.path.join(td, "spec"), os.path.join(td, "out")
+        with open(sp, "w") as f:
+            f.write("\n".join(spec) + "\n")
+        t0 = time.perf_counter()
+        subprocess.run([REF_DRIVER, sp, op], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL,
+                       env=dict(os.environ, OMP_NUM_THREADS=str(threads)))
+        wall = time.perf_counter() - t0
+        d = np.fromfile(op, dtype="<f8")
+    n = int(d[2])
+    times = d[3:3 + n]
+    E = float(d[3 + n])
+    P = int(d[4 + n])
+    g = d[5 + n:5 + n + P]
+    return {"setup_s": float(d[0]), "cores": int(d[1]), "times": times, "E": E, "g": g, "wall_s": wall,
+            "cpu_model": cpu_model()}
+
+
+def reference_available():
+    if not os.path.exists(REF_DRIVER):
+        return "oracle/_ref/ref_driver_native not built (no reference sources on this host)"
+    return None
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     pb = problem()
+    budget = float(os.environ.get("AE_REFERENCE_BUDGET_S", "150"))
+    why = reference_available()
+    D = math.comb(N_ORB, N_A) * math.comb(N_ORB, N_B)
+    if why is None and not LUCJ:
+        r = reference_timing(pb, args.steps, args.warmup, budget)
+        done, dt = len(r["times"]), float(np.sum(r["times"]))
+        v = done / dt
+        cb = {"value": v, "unit": "evals/s", "cores": r["cores"], "kind": "reference", "cpu_model": r["cpu_model"],
+              "binary": "oracle/_ref/ref_driver_native (the reference's sources, g++ -O3 native, OpenMP)",
+              "sample": "%d of %d requested FusedEvolve::evolve + evolveDerivative(&E) units (main.cpp:415-425) "
+                        "within the %.0f s budget, after %d untimed; reference set-up %.1f s not timed"
+                        % (done, args.steps, budget, args.warmup, r["setup_s"])}
+        line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": done,
+                "warmup": args.warmup, "ms_per_step": 1e3 * dt / done, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random integrals)", "impl": "reference",
+                "config": workload_desc(D, pb["P"], len(pb["ops0"]),
+                                        "applied from the reference's operator list on the fly (its own choice at "
+                                        "this size)"),
+                "cpu_baseline": cb,
+                "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        ref = os.path.join(ROOT, "tests", "golden", "ref%d.npz" % N_ORB)
+        if os.path.exists(ref):
+            fx = np.load(ref)
+            line["parity_reference"] = {"dE": abs(r["E"] - float(fx["E"])), "max_dg": float(np.max(np.abs(r["g"] - fx["G"]))),
+                                        "source": "tests/golden/ref%d.npz" % N_ORB}
+        print(json.dumps(line), flush=True)
+        return
+    # fallback: the oracle's C restatement of the reference algorithm
     from oracle.oracle import Oracle, lib as olib
-    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B)
+    o = Oracle(2 * N_ORB, 2, N_A + N_B, N_A, N_B, cplx=pb["cplx"])
     o.set_initial([pb["hf"]], [1.0])
     o.set_ops(pb["ops0"], pb["p0"], pb["scale"])
     o.set_ham_integrals(pb["h1"], pb["g2"], csr=False)
-    budget = float(os.environ.get("AE_REFERENCE_BUDGET_S", "150"))
     for w in range(min(args.warmup, 1)):
         o.gradient_comp(pb["x"])
     t0 = time.perf_counter()
@@ -190,14 +293,19 @@ def run_reference(args, rank, world):
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": workload_desc(int(o.D), pb["P"], len(pb["ops0"]), "applied from the operator list on the fly"),
             "cpu_baseline": {"value": v, "unit": "evals/s", "cores": int(olib().or_num_threads()), "kind": "port",
+                             "cpu_model": cpu_model(), "why_port": why or "LUCJ circuit: complex build not timed",
                              "sample": "%d of %d requested steps within the %.0f s budget" % (done, args.steps, budget)},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def e2e_c_abi(pb, steps, warmup):
-    """getEnergy + getGradient_COMP through the reference-compatible C ABI, host buffers."""
+def e2e_c_abi(pb, steps, warmup, reuse_hpsi=True):
+    """getEnergy + getGradient_COMP through the reference-compatible C ABI, host buffers.
+    reuse_hpsi=False: getGradient_COMP recomputes H psi, as the reference's
+    evolveDerivative does (fusedevolve.cpp:2292), i.e. two H products per pair."""
     import ansatzevolve_gb300 as ae
+    saved = os.environ.get("AEGPU_REUSE_HPSI")
+    os.environ["AEGPU_REUSE_HPSI"] = "1" if reuse_hpsi else "0"
     m = ae.stateAnsatzManager()
     assert m.storeInitial(2 * N_ORB, [pb["hf"]], [1.0])
     assert m.storeOperators(pb["ops1"].tolist())
@@ -214,8 +322,14 @@ def e2e_c_abi(pb, steps, warmup):
     dt = time.perf_counter() - t0
     P = pb["P"]
     m.close()
+    if saved is None:
+        os.environ.pop("AEGPU_REUSE_HPSI", None)
+    else:
+        os.environ["AEGPU_REUSE_HPSI"] = saved
     return {"value": steps / dt, "unit": "evals/s", "h2d_bytes_per_step": 2 * 8 * P, "d2h_bytes_per_step": 8 + 8 * P,
-            "ms_per_step": 1e3 * dt / steps, "api": "getEnergy + getGradient_COMP (H*psi cached between the pair)"}
+            "ms_per_step": 1e3 * dt / steps,
+            "api": "getEnergy + getGradient_COMP (%s)" % ("H*psi cached between the pair" if reuse_hpsi else
+                                                          "H*psi recomputed by getGradient_COMP, as the reference does")}
 
 
 def max_over_ranks(ms, dist):
@@ -305,6 +419,96 @@ def batched_bench(stream, steps=10, warmup=3):
     return out
 
 
+def aux_case_bench(n_orb, lucj, stream, steps=5, warmup=2):
+    """Configuration 3: 14 orbitals, 7a+7b (11,778,624 determinants), 4 tUPS layers or the
+    complex128 LUCJ circuit, H regenerated on the fly from the integrals.  Energy +
+    gradient evaluations by graph replay (CUDA events), per-phase times on the stream
+    path, the FP64-pipe fraction of the H product, the HBM fraction of the forward and
+    adjoint sweeps (algorithmic bytes: 16 B per amplitude per pass forward, 32 B adjoint;
+    complex amplitudes count twice), and parity against the reference's own output
+    (tests/golden/ref14.npz, lucj14.npz)."""
+    global LUCJ
+    import torch
+    import ansatzevolve_gb300 as ae
+    from ansatzevolve_gb300 import autotune
+    saved = (N_ORB, LUCJ)
+    set_orbitals(n_orb)
+    LUCJ = lucj
+    try:
+        pb = problem()
+        mode = ae.HAM_ON_THE_FLY
+        tuning = tuned(autotune.problem_key(N_ORB, N_A, N_B, LAYERS, 1, mode, lucj))
+        t0 = time.perf_counter()
+        eng = ae.Engine(2 * N_ORB, ae.BASIS_SZ, N_A + N_B, N_A, N_B, pb["ops0"], complex_mode=pb["cplx"],
+                        tuning=tuning or None)
+        W = 2 if pb["cplx"] else 1
+        init = np.zeros(eng.D * W)
+        init[W * np.searchsorted(eng.states(), pb["hf"])] = 1.0
+        eng.set_initial(init)
+        eng.set_ham_integrals(pb["h1"], pb["g2"], mode)
+        setup_s = time.perf_counter() - t0
+        info = eng.info()
+        D = info["D"]
+        ang = torch.tensor(pb["scale"] * pb["x"][pb["p0"]], dtype=torch.float64, device="cuda")
+        E_d = torch.zeros(1, dtype=torch.float64, device="cuda")
+        g_d = torch.zeros(len(pb["ops0"]), dtype=torch.float64, device="cuda")
+        sp = stream.cuda_stream
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        eng.phase_timing(True)
+        eng.phase_times()
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
+        torch.cuda.synchronize()
+        phase_ms, nph = eng.phase_times()
+        eng.phase_timing(False)
+        ph = [phase_ms[k] / max(nph, 1) for k in range(3)]
+        fw = eng.fp64_work()
+        peak_t = ae.fp64_peak() / 2.0
+        peak, peak_kind = measured_peak()
+        passes = info["blocks"]
+        touched = info["active"]  # amplitudes touched per sweep (a diagonal pass touches all D)
+        fwd_bytes, adj_bytes = 16 * touched * W, 32 * touched * W
+        out = {"value": 1e3 / ms, "unit": "evals/s", "ms_per_step": ms, "steps": steps, "warmup": warmup,
+               "config": workload_desc(D, pb["P"], len(pb["ops0"]), "regenerated on the fly"),
+               "setup_s": setup_s, "passes": passes, "phase_ms": {"evolve": ph[0], "hpsi_energy": ph[1], "adjoint": ph[2]},
+               "hpsi_fp64": {"instructions": int(fw[0]), "achieved_T_per_s": fw[0] / (ph[1] / 1e3) / 1e12,
+                             "peak_T_per_s": peak_t, "frac": fw[0] / (ph[1] / 1e3) / 1e12 / peak_t,
+                             "peak_source": "measured (aegpu_fp64_peak)"},
+               "sweeps_hbm": {"algorithmic_bytes": {"evolve": fwd_bytes, "adjoint": adj_bytes},
+                              "achieved_gbs": {"evolve": fwd_bytes / (ph[0] / 1e3) / 1e9,
+                                               "adjoint": adj_bytes / (ph[2] / 1e3) / 1e9},
+                              "frac": {"evolve": fwd_bytes / (ph[0] / 1e3) / 1e9 / peak,
+                                       "adjoint": adj_bytes / (ph[2] / 1e3) / 1e9 / peak},
+                              "peak_gbs": peak, "peak_source": peak_kind},
+               "tuning": {"settings": {str(k): v for k, v in eng.tuning().items()}, "tuned": bool(tuning)}}
+        ref = os.path.join(ROOT, "tests", "golden", ("lucj%d.npz" if lucj else "ref%d.npz") % N_ORB)
+        if os.path.exists(ref):
+            fx = np.load(ref)
+            g_ops = g_d.cpu().numpy()
+            g = np.zeros(pb["P"])
+            np.add.at(g, pb["p0"], pb["scale"] * g_ops)
+            if np.allclose(fx["x"], pb["x"]):
+                out["parity_reference"] = {"dE": abs(float(E_d.item()) - float(fx["E"])),
+                                           "max_dg": float(np.max(np.abs(g - fx["G"]))),
+                                           "source": os.path.relpath(ref, ROOT)}
+        eng.close()
+        return out
+    finally:
+        set_orbitals(saved[0])
+        LUCJ = saved[1]
+
+
 def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     """Time to converge over a 10-orbital Hamiltonian family scan (5a+5b, 3 layers,
     81 parameters): h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1.  Both paths start the scan
@@ -376,6 +580,7 @@ def main():
     ap.add_argument("--no-hessian", action="store_true")
     ap.add_argument("--no-ground", action="store_true", help="skip the lowest-eigenpair (Lanczos) timing")
     ap.add_argument("--no-ttc", action="store_true")
+    ap.add_argument("--no-config3", action="store_true", help="skip the 14-orbital tUPS and LUCJ objects")
     ap.add_argument("--ttc-train", type=int, default=2000)
     ap.add_argument("--ttc-heldout", type=int, default=200)
     ap.add_argument("--ttc-plain", type=int, default=48)
@@ -404,9 +609,10 @@ def main():
         args.ham = "otf" if args.orbitals >= 14 else "stored"
     mode = ae.HAM_STORED if args.ham == "stored" else ae.HAM_ON_THE_FLY
 
-    e2e = None
+    e2e = e2e_uncached = None
     if not args.no_e2e:
         e2e = e2e_c_abi(pb, max(10, args.steps // 10), 2)
+        e2e_uncached = e2e_c_abi(pb, max(10, args.steps // 10), 2, reuse_hpsi=False)
 
     from ansatzevolve_gb300 import autotune
     tuning = tuned(autotune.problem_key(N_ORB, N_A, N_B, LAYERS, 1, mode, False))
@@ -531,6 +737,7 @@ def main():
     }
     if e2e:
         line["e2e"] = e2e
+        line["e2e_uncached"] = e2e_uncached
     if hess_ms is not None:
         line["hessian"] = {"ms": hess_ms, "parameters": pb["P"], "api": "aegpu_hessian (host buffers), median of 3"}
     if ground is not None:
@@ -538,6 +745,9 @@ def main():
     eng.close()
     if not args.no_batched:
         line["batched"] = batched_bench(stream)
+    if not args.no_config3 and N_ORB == 12 and not LUCJ:
+        line["config3"] = aux_case_bench(14, False, stream)
+        line["lucj14"] = aux_case_bench(14, True, stream, steps=3)
     if not args.no_ttc:
         line["time_to_converge"] = ttc_bench(args.ttc_train, args.ttc_heldout, args.ttc_plain)
     # parity of this very run against the reference's own output for the same inputs

@@ -95,9 +95,13 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * programmatic dependent launch of the pass kernels (0 off, 1 on, -1 by size, the
  * default: on up to 2^19 amplitudes per launch; each pass's CTAs are scheduled while
  * the previous pass drains and wait on the device for its results; any time, it
- * rebuilds the captured graphs).  No counterpart in the reference. */
+ * rebuilds the captured graphs), reuse of H psi between an energy and a gradient at the
+ * same angles (1, the default, or 0: the gradient recomputes H psi as the reference's
+ * evolveDerivative does, fusedevolve.cpp:2292; the environment variable
+ * AEGPU_REUSE_HPSI=0 sets 0 for engines created afterwards, e.g. the one behind the
+ * reference-compatible C ABI).  No counterpart in the reference. */
 enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
-       AEGPU_TUNE_PDL = 5 };
+       AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6 };
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
 int aegpu_batch_size(const aegpu_engine *e);

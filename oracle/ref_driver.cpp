@@ -22,6 +22,8 @@
 //                                         written raw to <path>)
 //   optimise 0|1
 //   time k                               (k timed evolve+evolveDerivative units)
+//   timewarmup w                         (untimed units before them, default 1)
+//   timebudget s                         (stop timing after s seconds, default none)
 //   properties <prefix>                  (TUPSQuantities::writeProperties over the zero
 //                                         path + the angle sets; its table goes to
 //                                         <prefix>_table.txt, its matrices to <prefix>_Path_*)
@@ -29,7 +31,8 @@
 //                                         the first n angle sets; printed on stderr)
 //   end
 // Output: for every angle set, E, gradient, Hessian (column-major), final state;
-// then the pair table, then the optimised energy + angles, then timings.
+// then the pair table, then the optimised energy + angles, then timings (set-up
+// seconds, thread count, n, n unit times, E, P, the compressed gradient).
 #include "AnsatzManager.h"
 #include "fusedevolve.h"
 #include "hamiltonianmatrix.h"
@@ -69,7 +72,8 @@ int main(int argc, char **argv)
     std::string intsPrefix;
     double nuclear = 0;
     std::vector<std::vector<double>> angleSets;
-    int wantE = 1, wantG = 1, wantH = 0, wantS = 0, wantPairs = 0, wantOpt = 0, timeK = 0;
+    int wantE = 1, wantG = 1, wantH = 0, wantS = 0, wantPairs = 0, wantOpt = 0, timeK = 0, timeWarm = 1;
+    double timeBudget = 0.0;
     std::string propsPrefix, pairsPath;
     int subspaceN = 0;
 
@@ -108,6 +112,8 @@ int main(int argc, char **argv)
         else if (tok == "pairsfile") in >> pairsPath;
         else if (tok == "optimise") in >> wantOpt;
         else if (tok == "time") in >> timeK;
+        else if (tok == "timewarmup") in >> timeWarm;
+        else if (tok == "timebudget") in >> timeBudget;
         else if (tok == "properties") in >> propsPrefix;
         else if (tok == "subspace") in >> subspaceN;
         else if (tok == "end") break;
@@ -220,20 +226,24 @@ int main(int argc, char **argv)
         FE.evolve(dest, ang);
         FE.evolveDerivative(dest, deriv, ang, &E);
         auto t1 = std::chrono::steady_clock::now();
-        for (int w = 0; w < 1; ++w) { FE.evolve(dest, ang); FE.evolveDerivative(dest, deriv, ang, &E); }
+        for (int w = 0; w < timeWarm; ++w) { FE.evolve(dest, ang); FE.evolveDerivative(dest, deriv, ang, &E); }
         std::vector<double> times;
+        const auto tstart = std::chrono::steady_clock::now();
         for (int k = 0; k < timeK; ++k) {
             auto a = std::chrono::steady_clock::now();
             FE.evolve(dest, ang);
             FE.evolveDerivative(dest, deriv, ang, &E);
             auto b = std::chrono::steady_clock::now();
             times.push_back(std::chrono::duration<double>(b - a).count());
+            if (timeBudget > 0 && std::chrono::duration<double>(b - tstart).count() > timeBudget) break;
         }
         put1(out, std::chrono::duration<double>(t1 - t0).count());
         put1(out, (double)NUM_CORES);
         put1(out, (double)times.size());
         put(out, times.data(), times.size());
         put1(out, E);
+        put1(out, (double)deriv.size());
+        put(out, &deriv[0], deriv.size());
     }
     if (!propsPrefix.empty() && !intsPrefix.empty()) {
         // the reference's own properties pass (tupsquantities.cpp:185-568) on the
