@@ -174,8 +174,11 @@ GramShape gram_shape(int V, int W, int64_t nrows, int sm_count)
     return g;
 }
 
-// Partial sums of y = A^T x: CTA b covers rows [b * rows_per, (b + 1) * rows_per) and
-// writes partial[b * k + j] for every column j, eight columns at a time.
+// Partial sums of y = A^T x: CTA (b, g) covers rows [b * rows_per, (b + 1) * rows_per)
+// of the eight columns of group g = blockIdx.y and writes partial[b * k + j] for them.
+// Each thread walks its rows with a stride of the CTA size, so a CTA streams a long
+// contiguous stretch of every column (the loads of several rows are in flight per
+// thread), and the eight sums meet in one block reduction at the end.
 __global__ void __launch_bounds__(kGemvThreads) k_gemv_t(const double *__restrict__ A, int64_t lda, int64_t n, int k,
                                                          const double *__restrict__ x, int64_t rows_per,
                                                          double *__restrict__ partial, const int *flag)
@@ -184,42 +187,44 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemv_t(const double *__restric
     __shared__ double red[kGemvGroup][kGemvThreads / 32];
     const int64_t r0 = (int64_t)blockIdx.x * rows_per, r1 = r0 + rows_per < n ? r0 + rows_per : n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int j0 = 0; j0 < k; j0 += kGemvGroup) {
-        const int nj = k - j0 < kGemvGroup ? k - j0 : kGemvGroup;
-        double acc[kGemvGroup];
+    const int j0 = blockIdx.y * kGemvGroup;
+    const int nj = k - j0 < kGemvGroup ? k - j0 : kGemvGroup;
+    double acc[kGemvGroup];
 #pragma unroll
-        for (int q = 0; q < kGemvGroup; ++q) acc[q] = 0.0;
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += kGemvThreads) {
-            const double xr = x[r];
+    for (int q = 0; q < kGemvGroup; ++q) acc[q] = 0.0;
+    const double *Aj = A + (int64_t)j0 * lda;
+#pragma unroll 2
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += kGemvThreads) {
+        const double xr = x[r];
 #pragma unroll
-            for (int q = 0; q < kGemvGroup; ++q)
-                if (q < nj) acc[q] = fma(A[r + (int64_t)(j0 + q) * lda], xr, acc[q]);
-        }
+        for (int q = 0; q < kGemvGroup; ++q)
+            if (q < nj) acc[q] = fma(Aj[r + (int64_t)q * lda], xr, acc[q]);
+    }
 #pragma unroll
-        for (int q = 0; q < kGemvGroup; ++q) {
-            const double v = warp_sum(acc[q]);
-            if (lane == 0) red[q][warp] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < nj) {
-            double s = 0.0;
-            for (int w = 0; w < kGemvThreads / 32; ++w) s += red[threadIdx.x][w];
-            partial[(int64_t)blockIdx.x * k + j0 + threadIdx.x] = s;
-        }
-        __syncthreads();
+    for (int q = 0; q < kGemvGroup; ++q) {
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) red[q][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nj) {
+        double s = 0.0;
+        for (int w = 0; w < kGemvThreads / 32; ++w) s += red[threadIdx.x][w];
+        partial[(int64_t)blockIdx.x * k + j0 + threadIdx.x] = s;
     }
 }
 
-// y[j] = alpha * sum over the m CTAs' partials (fixed order).
+// y[j] = alpha * sum of the m chunks' partials: one warp per column, lane l adding the
+// partials l, l + 32, ... and the lanes combined by a fixed butterfly.
 __global__ void k_gemv_t_finish(const double *__restrict__ partial, int m, int k, double alpha, double *__restrict__ y,
                                 const int *flag)
 {
     if (flag && !*flag) return;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (j >= k) return;
     double s = 0.0;
-    for (int b = 0; b < m; ++b) s += partial[(int64_t)b * k + j];
-    y[j] = alpha * s;
+    for (int b = lane; b < m; b += 32) s += partial[(int64_t)b * k + j];
+    s = warp_sum(s);
+    if (lane == 0) y[j] = alpha * s;
 }
 
 // y[r] = beta y[r] + alpha sum_j A[r + j lda] c[j]; the coefficients are staged in
@@ -271,19 +276,26 @@ __global__ void k_dot_part(const double *__restrict__ a, const double *__restric
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// *out = sum of m partials (or its square root); optionally *flag = *out < f * *cmp.
-__global__ void k_dot_fin(const double *__restrict__ part, int m, double *out, int take_sqrt, const double *cmp,
-                          double f, int *flag, const int *flag_in)
+// *out = sum of m partials (or its square root).  With `coef` (k values), also
+// *flag = (*out < f * sqrt(*out^2 + sum coef^2)): after w -= V c with orthonormal V,
+// the norm before the subtraction is sqrt(|w|^2 + |c|^2).
+__global__ void k_dot_fin(const double *__restrict__ part, int m, double *out, int take_sqrt, const double *coef,
+                          int k, double f, int *flag, const int *flag_in)
 {
     __shared__ double red[32];
     if (flag_in && !*flag_in) return;
     double s = 0.0;
     for (int i = threadIdx.x; i < m; i += blockDim.x) s += part[i];
     s = block_sum(s, red);
+    double c2 = 0.0;
+    if (flag) {
+        for (int i = threadIdx.x; i < k; i += blockDim.x) c2 = fma(coef[i], coef[i], c2);
+        c2 = block_sum(c2, red);
+    }
     if (threadIdx.x == 0) {
         const double v = take_sqrt ? sqrt(fmax(s, 0.0)) : s;
         *out = v;
-        if (flag) *flag = cmp ? (v < f * *cmp) : 0;
+        if (flag) *flag = v < f * sqrt(v * v + c2);
     }
 }
 
@@ -370,10 +382,13 @@ int gemv_t(const double *A, int64_t lda, int64_t n, int k, const double *x, doub
            int sm_count, cudaStream_t s, const int *flag)
 {
     if (k < 1) return 0;
-    const int m = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count * 4, (n + kGemvThreads - 1) / kGemvThreads));
+    // about 8 CTAs per SM over all column groups, each chunk at least 8 rows per thread
+    const int groups = (k + kGemvGroup - 1) / kGemvGroup;
+    const int m = (int)std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(1, (int64_t)sm_count * 8 / groups),
+                                                              (n + 8 * kGemvThreads - 1) / (8 * kGemvThreads)));
     const int64_t rows_per = (n + m - 1) / m;
-    k_gemv_t<<<m, kGemvThreads, 0, s>>>(A, lda, n, k, x, rows_per, scratch, flag);
-    k_gemv_t_finish<<<(k + 127) / 128, 128, 0, s>>>(scratch, m, k, alpha, y, flag);
+    k_gemv_t<<<dim3(m, groups), kGemvThreads, 0, s>>>(A, lda, n, k, x, rows_per, scratch, flag);
+    k_gemv_t_finish<<<(k + 7) / 8, 256, 0, s>>>(scratch, m, k, alpha, y, flag);
     return 2;
 }
 
@@ -386,11 +401,11 @@ int gemv_n(const double *A, int64_t lda, int64_t n, int k, const double *c, doub
 }
 
 int dot(const double *a, const double *b, int64_t n, int64_t inc, double *out, int take_sqrt, double *scratch,
-        int sm_count, cudaStream_t s, const double *cmp, double cmp_factor, int *flag, const int *flag_in)
+        int sm_count, cudaStream_t s, const double *coef, int ncoef, double cmp_factor, int *flag, const int *flag_in)
 {
     const int m = vec_grid(n, sm_count);
     k_dot_part<<<m, 256, 0, s>>>(a, b, n, inc, scratch, flag_in);
-    k_dot_fin<<<1, 256, 0, s>>>(scratch, m, out, take_sqrt, cmp, cmp_factor, flag, flag_in);
+    k_dot_fin<<<1, 256, 0, s>>>(scratch, m, out, take_sqrt, coef, ncoef, cmp_factor, flag, flag_in);
     return 2;
 }
 

@@ -33,11 +33,11 @@ int gemv_t(const double *A, int64_t lda, int64_t n, int k, const double *x, doub
 int gemv_n(const double *A, int64_t lda, int64_t n, int k, const double *c, double alpha, double beta, double *y,
            cudaStream_t s, const int *flag = nullptr);
 // *out = sum_r a[r * inc] b[r * inc] over n terms (or its square root when take_sqrt).
-// With `cmp` (nullable), also *flag = (result < cmp_factor * *cmp).  With `flag_in`
-// (nullable), nothing happens unless *flag_in != 0.
+// With `flag` (nullable), also *flag = (result < cmp_factor * sqrt(result^2 + sum of the
+// ncoef squares of coef)).  With `flag_in` (nullable), nothing happens unless *flag_in != 0.
 int dot(const double *a, const double *b, int64_t n, int64_t inc, double *out, int take_sqrt, double *scratch,
-        int sm_count, cudaStream_t s, const double *cmp = nullptr, double cmp_factor = 0.0, int *flag = nullptr,
-        const int *flag_in = nullptr);
+        int sm_count, cudaStream_t s, const double *coef = nullptr, int ncoef = 0, double cmp_factor = 0.0,
+        int *flag = nullptr, const int *flag_in = nullptr);
 // out[0] + i out[1] = sum_r conj(a_r) b_r over n complex entries (re, im interleaved).
 int dotc(const double *a, const double *b, int64_t n, double *out, double *scratch, int sm_count, cudaStream_t s);
 // y[r] = alpha * y[r] + beta * x[r] (alpha = 0: y = beta * x, whatever y held); with

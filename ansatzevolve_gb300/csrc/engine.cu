@@ -1577,7 +1577,8 @@ struct aegpu_engine {
     cudaGraphExec_t energy_graph = nullptr, back_graph = nullptr;
     int64_t energy_graph_launches = 0, back_graph_launches = 0;
     int64_t graph_launches = 0;  // kernels inside the graph
-    int64_t generation = 0;      // bumped whenever device buffers or the Hamiltonian change
+    int64_t generation = 0;      // bumped whenever device buffers or the Hamiltonian's buffers change
+    int ints_ntab = 0, ints_mode_asked = -1;  // shape of the current integral Hamiltonian
     bool use_graph = true;
 
     // Hessian scratch, kept between calls with the same parameter count
@@ -1703,6 +1704,8 @@ struct aegpu_engine {
         ham_allocs.clear();
         ham_alloc_bytes.clear();
         ham_kind = 0;
+        ints_ntab = 0;
+        ints_mode_asked = -1;
         ham_per_instance = false;
         ell_stride_inst = 0;
         d_rowptr = nullptr;
@@ -2426,11 +2429,82 @@ namespace {
 
 // Hamiltonian from integrals for ntab table sets: ntab = 1 shares one Hamiltonian
 // between all instances, ntab = nb gives instance b the integrals h1s[b], g2s[b].
+// New integral values for an integral Hamiltonian of the same shape (same instances
+// and representation): the values are written into the existing buffers -- stored rows
+// rebuilt, on-the-fly integral tables and diagonal rebuilt; the string tables do not
+// depend on the integrals -- so every device pointer, and the captured evaluation
+// graphs that hold them, stay valid.  A family scan changes only the values.
+static int refresh_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int ntab)
+{
+    NvtxRange r("aegpu refresh Hamiltonian");
+    const int N = e->B.N;
+    const size_t NN = (size_t)N * N, N4 = NN * NN;
+    cudaStream_t s = e->stream;
+    if (stream_sync(e, "refresh integrals")) return AEGPU_ERR_CUDA;  // nothing in flight reads the old values
+    cudaMemcpy(e->d_h1, h1s, sizeof(double) * NN * ntab, cudaMemcpyHostToDevice);
+    cudaMemcpy(e->d_g2, g2s, sizeof(double) * N4 * ntab, cudaMemcpyHostToDevice);
+    const int64_t D = (int64_t)e->B.D;
+    IntArgs a = e->ints;
+    if (e->ham_kind == 2) {
+        const int64_t Dpad = (D + 31) & ~(int64_t)31;
+        const size_t per = (size_t)Dpad * a.stride;
+        const int64_t chunk = 1 << 16;
+        for (int t = 0; t < ntab; ++t) {
+            IntArgs ai = a;
+            ai.h1 = e->d_h1 + NN * t;
+            ai.g2 = e->d_g2 + N4 * t;
+            for (int64_t r0 = 0; r0 < Dpad; r0 += chunk) {
+                k_ell_build<<<e->sm_count * 8, 256, 0, s>>>(ai, e->d_col + per * t, e->d_val + per * t, r0,
+                                                            std::min(Dpad, r0 + chunk));
+                e->launches += 1;
+            }
+        }
+    } else {
+        std::vector<OtfTables> T(ntab);
+        const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        std::atomic<int> next{0};
+        for (int w = 0; w < std::min(hw, ntab); ++w)
+            pool.emplace_back([&]() {
+                for (int t; (t = next.fetch_add(1)) < ntab;) {
+                    std::vector<double> hv(h1s + NN * t, h1s + NN * (t + 1)), gv(g2s + N4 * t, g2s + N4 * (t + 1));
+                    build_otf_tables(e->B, hv, gv, T[t], false);
+                }
+            });
+        for (auto &th : pool) th.join();
+        auto put = [&](const double *dst, std::vector<double> OtfTables::*m) {
+            const size_t per = (T[0].*m).size();
+            std::vector<double> all;
+            all.reserve(per * ntab);
+            for (auto &x : T) all.insert(all.end(), (x.*m).begin(), (x.*m).end());
+            cudaMemcpy((void *)dst, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice);
+        };
+        put(e->otf.vss, &OtfTables::vss);
+        put(e->otf.vab, &OtfTables::vab);
+        put(e->otf.a_alpha, &OtfTables::a_alpha);
+        put(e->otf.b_alpha, &OtfTables::b_alpha);
+        put(e->otf.a_beta, &OtfTables::a_beta);
+        put(e->otf.b_beta, &OtfTables::b_beta);
+        for (int t = 0; t < ntab; ++t) {
+            IntArgs ai = a;
+            ai.h1 = e->d_h1 + NN * t;
+            ai.g2 = e->d_g2 + N4 * t;
+            k_diag_build<<<e->sm_count * 8, 256, 0, s>>>(ai, (double *)e->otf.diag + (size_t)D * t);
+            e->launches += 1;
+        }
+    }
+    e->h_valid = false;
+    e->ground_valid = false;
+    return stream_sync(e, "refresh integrals");
+}
+
 int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int ntab, int mode)
 {
     NvtxRange r("aegpu set Hamiltonian");
     if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
     if (e->B.kind != BASIS_SZ) return e->fail(AEGPU_ERR_UNSUPPORTED, "integral Hamiltonians need the Sz sector");
+    if ((e->ham_kind == 2 || e->ham_kind == 3) && e->d_h1 && e->ints_ntab == ntab && e->ints_mode_asked == mode)
+        return refresh_integrals(e, h1s, g2s, ntab);
     const int N = e->B.N;
     const size_t NN = (size_t)N * N, N4 = NN * NN;
     IntArgs a{};
@@ -2473,6 +2547,7 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
     const double ell_bytes = (double)Dpad * a.stride * 12.0 * ntab;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
+    const int mode_asked = mode;
     if (mode == AEGPU_HAM_AUTO) mode = ell_bytes < 0.6 * (double)free_b ? AEGPU_HAM_STORED : AEGPU_HAM_ON_THE_FLY;
     e->ham_per_instance = ntab > 1;
     if (mode == AEGPU_HAM_STORED) {
@@ -2572,6 +2647,8 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
         e->ham_entries = 0;
         e->ell_stride_inst = 0;
     }
+    e->ints_ntab = ntab;
+    e->ints_mode_asked = mode_asked;
     e->h_valid = false;
     return stream_sync(e, "set_ham_integrals");
 }
@@ -3271,8 +3348,8 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
     if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
     double *sm = small_scratch(e);
     if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
-    // basis vectors; reorthogonalisation coefficients, alpha / beta of the recurrence, the
-    // norm before the Gram-Schmidt pass, a repeat flag and the partial sums of gemv_t
+    // basis vectors; reorthogonalisation coefficients, alpha / beta of the recurrence, a
+    // spare slot, a repeat flag and the partial sums of gemv_t
     const size_t nscal = (size_t)(m + 1) + 2 * (size_t)m + 2 + (size_t)gemv_scratch_doubles(m + 1, e->sm_count);
     double *Vb = e->alloc<double>((size_t)(m + 1) * n);
     double *scal = e->alloc<double>(nscal);
@@ -3332,16 +3409,16 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             // happens), so one pass is normally the second orthogonalisation for them
             // ("twice is enough", Giraud, Langou and Rozloznik 2005).  A second pass runs
             // only when the first removed a large part of w: ||w|| after it below 0.7 of
-            // ||w|| before it (the Daniel-Gragg-Kaufman-Stewart criterion); the decision
+            // ||w|| before it (the Daniel-Gragg-Kaufman-Stewart criterion; with an
+            // orthonormal basis the norm before is sqrt(||w||^2 + ||c||^2)).  The decision
             // is taken on the device, and the second pass's kernels return at once when
             // it is not needed.
-            e->launches += ae::dot(w, w, ni, 1, d_wn, 1, d_dpart, e->sm_count, s);
             e->launches += gemv_t(Vb, ni, ni, j + 1, w, 1.0, d_c, d_part, e->sm_count, s);
             e->launches += gemv_n(Vb, ni, ni, j + 1, d_c, -1.0, 1.0, w, s);
-            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, d_wn, 0.7, d_again);
+            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, d_c, j + 1, 0.7, d_again);
             e->launches += gemv_t(Vb, ni, ni, j + 1, w, 1.0, d_c, d_part, e->sm_count, s, d_again);
             e->launches += gemv_n(Vb, ni, ni, j + 1, d_c, -1.0, 1.0, w, s, d_again);
-            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, nullptr, 0.0, nullptr, d_again);
+            e->launches += ae::dot(w, w, ni, 1, d_beta + j, 1, d_dpart, e->sm_count, s, nullptr, 0, 0.0, nullptr, d_again);
             e->launches += ae::axpby(w, w, ni, 1.0, 0.0, d_beta + j, s);
             const int jn = j + 1;
             if (jn - checked < kCheck && jn < m && prod < max_products && jn < ni) continue;

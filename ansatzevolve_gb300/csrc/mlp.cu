@@ -44,33 +44,52 @@ __device__ __forceinline__ float gelu_grad(float z)
     return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
 }
 
+__device__ __forceinline__ float epilogue(float v, int64_t o, int n, const float *__restrict__ bias,
+                                          float *__restrict__ Z, int epi)
+{
+    if (epi == kBias || epi == kBiasGelu) v += bias[n];
+    if (epi == kBiasGelu) {
+        Z[o] = v;
+        v = gelu(v);
+    } else if (epi == kGeluGrad) {
+        v *= gelu_grad(Z[o]);
+    }
+    return v;
+}
+
 // C[m][n] = sum_k A(m,k) B(k,n), A(m,k) = A[m*a_rs + k*a_cs], B(k,n) = B[k*b_rs + n*b_cs],
 // then the epilogue:
 //   kPlain:    C = acc
 //   kBias:     C = acc + bias[n]
 //   kBiasGelu: Z = acc + bias[n] (pre-activation, stored), C = gelu(Z)
 //   kGeluGrad: C = acc * gelu'(Z[m][n])  (Z read)
+// Split K (gridDim.z > 1, for products with few output tiles): CTA z sums k in
+// [z * kz, (z + 1) * kz) and writes its raw partial to C + z * M * N (a workspace);
+// k_gemm_reduce adds the partials in z order and applies the epilogue.  The tile loads
+// walk the operand's unit-stride dimension fastest, so they coalesce.
 template <typename TB>
 __global__ void __launch_bounds__(kGemmThreads) k_gemm(const float *__restrict__ A, int64_t a_rs, int64_t a_cs,
                                                        const TB *__restrict__ B, int64_t b_rs, int64_t b_cs,
-                                                       float *__restrict__ C, int M, int N, int K,
+                                                       float *__restrict__ C, int M, int N, int K, int kz,
                                                        const float *__restrict__ bias, float *__restrict__ Z, int epi)
 {
     __shared__ float As[kTK][kTM + 1];
     __shared__ float Bs[kTK][kTN + 1];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+    const int kb = blockIdx.z * kz, ke = kb + kz < K ? kb + kz : K;
+    const bool a_k_fast = a_cs == 1, b_k_fast = b_rs == 1;
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += kTK) {
+    for (int k0 = kb; k0 < ke; k0 += kTK) {
         for (int i = threadIdx.x; i < kTK * kTM; i += kGemmThreads) {
-            const int kk = i / kTM, mm = i % kTM;
+            const int kk = a_k_fast ? i % kTK : i / kTM, mm = a_k_fast ? i / kTK : i % kTM;
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < K) ? A[(int64_t)m * a_rs + (int64_t)k * a_cs] : 0.0f;
+            As[kk][mm] = (m < M && k < ke) ? A[(int64_t)m * a_rs + (int64_t)k * a_cs] : 0.0f;
         }
         for (int i = threadIdx.x; i < kTK * kTN; i += kGemmThreads) {
-            const int kk = i / kTN, nn = i % kTN;
+            const int kk = b_k_fast ? i % kTK : i / kTN, nn = b_k_fast ? i / kTK : i % kTN;
             const int n = n0 + nn, k = k0 + kk;
-            Bs[kk][nn] = (n < N && k < K) ? ldf(B + (int64_t)k * b_rs + (int64_t)n * b_cs) : 0.0f;
+            Bs[kk][nn] = (n < N && k < ke) ? ldf(B + (int64_t)k * b_rs + (int64_t)n * b_cs) : 0.0f;
         }
         __syncthreads();
 #pragma unroll
@@ -87,6 +106,8 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm(const float *__restrict__
         }
         __syncthreads();
     }
+    const bool split = gridDim.z > 1;
+    float *Cz = C + (split ? (int64_t)blockIdx.z * M * N : 0);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -94,16 +115,20 @@ __global__ void __launch_bounds__(kGemmThreads) k_gemm(const float *__restrict__
             const int m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
             if (m >= M || n >= N) continue;
             const int64_t o = (int64_t)m * N + n;
-            float v = acc[i][j];
-            if (epi == kBias || epi == kBiasGelu) v += bias[n];
-            if (epi == kBiasGelu) {
-                Z[o] = v;
-                v = gelu(v);
-            } else if (epi == kGeluGrad) {
-                v *= gelu_grad(Z[o]);
-            }
-            C[o] = v;
+            Cz[o] = split ? acc[i][j] : epilogue(acc[i][j], o, n, bias, Z, epi);
         }
+}
+
+// C = epilogue(sum over z of the split-K partials ws[z][M][N]), z in order.
+__global__ void k_gemm_reduce(const float *__restrict__ ws, int ksplit, int M, int N, float *__restrict__ C,
+                              const float *__restrict__ bias, float *__restrict__ Z, int epi)
+{
+    const int64_t MN = (int64_t)M * N;
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < MN; o += (int64_t)gridDim.x * blockDim.x) {
+        float v = 0.0f;
+        for (int z = 0; z < ksplit; ++z) v += ws[z * MN + o];
+        C[o] = epilogue(v, o, (int)(o % N), bias, Z, epi);
+    }
 }
 
 // column sums: out[n] = sum_m X[m][n] (bias gradients); one thread per column,
@@ -212,6 +237,7 @@ struct aegpu_mlp {
     int cap = 0;
     float *X0 = nullptr, *Z1 = nullptr, *A1 = nullptr, *Z2 = nullptr, *A2 = nullptr, *Y = nullptr;
     float *dY = nullptr, *dA = nullptr, *dZ = nullptr, *rowloss = nullptr;
+    float *ws = nullptr;  // split-K partial products
     int *idx = nullptr;
 
     ~aegpu_mlp()
@@ -279,12 +305,28 @@ struct aegpu_mlp {
 
 namespace {
 
+// Products with fewer than 64 output tiles split K over up to kMaxSplit CTAs per tile
+// (at least 64 k per CTA), so that more SMs share the latency-bound K loop.
+constexpr int kMaxSplit = 8;
+constexpr int64_t kSplitWorkspace = (int64_t)kMaxSplit * 64 * kTM * kTN;
+
 template <typename TB>
-void gemm(cudaStream_t s, const float *A, int64_t a_rs, int64_t a_cs, const TB *B, int64_t b_rs, int64_t b_cs, float *C,
-          int M, int N, int K, const float *bias, float *Z, int epi)
+void gemm(cudaStream_t s, float *ws, const float *A, int64_t a_rs, int64_t a_cs, const TB *B, int64_t b_rs,
+          int64_t b_cs, float *C, int M, int N, int K, const float *bias, float *Z, int epi)
 {
     dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM);
-    k_gemm<TB><<<grid, kGemmThreads, 0, s>>>(A, a_rs, a_cs, B, b_rs, b_cs, C, M, N, K, bias, Z, epi);
+    const int tiles = grid.x * grid.y;
+    int split = 1;
+    if (tiles < 64 && ws)
+        while (split < kMaxSplit && K / (split * 2) >= 64 && (int64_t)split * 2 * M * N <= kSplitWorkspace) split *= 2;
+    const int kz = (K + split - 1) / split;
+    grid.z = split;
+    k_gemm<TB><<<grid, kGemmThreads, 0, s>>>(A, a_rs, a_cs, B, b_rs, b_cs, split > 1 ? ws : C, M, N, K, kz, bias, Z,
+                                             epi);
+    if (split > 1) {
+        const int64_t MN = (int64_t)M * N;
+        k_gemm_reduce<<<(int)std::min<int64_t>((MN + 255) / 256, 1024), 256, 0, s>>>(ws, split, M, N, C, bias, Z, epi);
+    }
 }
 
 // forward of `rows` standardised input rows already in X0; output (standardised) in Y
@@ -294,9 +336,9 @@ void forward(aegpu_mlp *m, int rows)
     const __nv_bfloat16 *W1 = m->wq + m->off[0], *W2 = m->wq + m->off[2], *W3 = m->wq + m->off[4];
     const float *b1 = m->w + m->off[1], *b2 = m->w + m->off[3], *b3 = m->w + m->off[5];
     // Z = X W^T + b: B(k,n) = W[n][k]
-    gemm(m->stream, m->X0, ni, 1, W1, 1, ni, m->A1, rows, H, ni, b1, m->Z1, kBiasGelu);
-    gemm(m->stream, m->A1, H, 1, W2, 1, H, m->A2, rows, H, H, b2, m->Z2, kBiasGelu);
-    gemm(m->stream, m->A2, H, 1, W3, 1, H, m->Y, rows, no, H, b3, nullptr, kBias);
+    gemm(m->stream, m->ws, m->X0, ni, 1, W1, 1, ni, m->A1, rows, H, ni, b1, m->Z1, kBiasGelu);
+    gemm(m->stream, m->ws, m->A1, H, 1, W2, 1, H, m->A2, rows, H, H, b2, m->Z2, kBiasGelu);
+    gemm(m->stream, m->ws, m->A2, H, 1, W3, 1, H, m->Y, rows, no, H, b3, nullptr, kBias);
 }
 
 // gradients of the loss (dY already in m->dY) into m->g
@@ -307,15 +349,15 @@ void backward(aegpu_mlp *m, int rows)
     float *g = m->g;
     cudaStream_t s = m->stream;
     // layer 3: dW3[o][k] = sum_b dY[b][o] A2[b][k]; db3; dA2 = dY W3 (gelu' of Z2 fused)
-    gemm(s, m->dY, 1, no, m->A2, H, 1, g + m->off[4], no, H, rows, nullptr, nullptr, kPlain);
+    gemm(s, m->ws, m->dY, 1, no, m->A2, H, 1, g + m->off[4], no, H, rows, nullptr, nullptr, kPlain);
     k_colsum<<<(no + 127) / 128, 128, 0, s>>>(m->dY, rows, no, g + m->off[5]);
-    gemm(s, m->dY, no, 1, W3, H, 1, m->dZ, rows, H, no, nullptr, m->Z2, kGeluGrad);
+    gemm(s, m->ws, m->dY, no, 1, W3, H, 1, m->dZ, rows, H, no, nullptr, m->Z2, kGeluGrad);
     // layer 2
-    gemm(s, m->dZ, 1, H, m->A1, H, 1, g + m->off[2], H, H, rows, nullptr, nullptr, kPlain);
+    gemm(s, m->ws, m->dZ, 1, H, m->A1, H, 1, g + m->off[2], H, H, rows, nullptr, nullptr, kPlain);
     k_colsum<<<(H + 127) / 128, 128, 0, s>>>(m->dZ, rows, H, g + m->off[3]);
-    gemm(s, m->dZ, H, 1, W2, H, 1, m->dA, rows, H, H, nullptr, m->Z1, kGeluGrad);
+    gemm(s, m->ws, m->dZ, H, 1, W2, H, 1, m->dA, rows, H, H, nullptr, m->Z1, kGeluGrad);
     // layer 1 (no input gradient needed)
-    gemm(s, m->dA, 1, H, m->X0, ni, 1, g + m->off[0], H, ni, rows, nullptr, nullptr, kPlain);
+    gemm(s, m->ws, m->dA, 1, H, m->X0, ni, 1, g + m->off[0], H, ni, rows, nullptr, nullptr, kPlain);
     k_colsum<<<(H + 127) / 128, 128, 0, s>>>(m->dA, rows, H, g + m->off[1]);
 }
 
@@ -347,7 +389,8 @@ int aegpu_mlp_create(aegpu_mlp **out, int n_in, int n_hidden, int n_out, uint64_
     m->v = m->alloc<float>(n);
     m->wq = m->alloc<__nv_bfloat16>(n);
     m->scal = m->alloc<float>(2 * n_in + 3 * n_out);
-    if (!m->w || !m->g || !m->m || !m->v || !m->wq || !m->scal) {
+    m->ws = m->alloc<float>(kSplitWorkspace);
+    if (!m->w || !m->g || !m->m || !m->v || !m->wq || !m->scal || !m->ws) {
         delete m;
         return AEGPU_ERR_NOMEM;
     }
@@ -534,13 +577,11 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
             backward(m, rows);
             m->adam_t += 1;
             const float c1 = 1.0f - std::pow(b1, (float)m->adam_t), c2 = 1.0f - std::pow(b2, (float)m->adam_t);
-            // weights (with BF16 copies) and biases
-            for (int t = 0; t < 6; ++t) {
-                const int64_t o = m->off[t], cnt = m->off[t + 1] - o;
-                k_adam<<<std::min<int64_t>((cnt + 255) / 256, 1024), 256, 0, s>>>(
-                    m->w + o, (t % 2 == 0) ? m->wq + o : nullptr, m->g + o, m->m + o, m->v + o, cnt, lr, b1, b2, eps,
-                    c1, c2);
-            }
+            // every weight and bias in one launch (the parameters are contiguous); the BF16
+            // copies of the biases are written too but never read (biases stay FP32)
+            const int64_t cnt = m->nparams();
+            k_adam<<<std::min<int64_t>((cnt + 255) / 256, 1024), 256, 0, s>>>(m->w, m->wq, m->g, m->m, m->v, cnt, lr, b1,
+                                                                              b2, eps, c1, c2);
         }
     }
     int rc = AEGPU_OK;

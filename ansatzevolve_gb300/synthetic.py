@@ -30,24 +30,39 @@ def synthetic_integrals(n_orb, seed=0, n_factors=None):
     return np.ascontiguousarray(h), np.ascontiguousarray(g)
 
 
-def family_integrals(n_orb, s, seed=0, n_factors=None, pert=1.0):
-    """h(s) = h0 + s*h1 and L^k(s) = L^k0 + s*L^k1 for a Hamiltonian family scan; the
-    perturbation tensors h1, L^k1 are drawn at `pert` times the base tensors' scale."""
+def family_tensors(n_orb, seed=0, n_factors=None, pert=1.0):
+    """The seeded base and perturbation tensors of family_integrals: (damp, a0, a1,
+    [(l0, l1)] * n_factors), drawn in a fixed order."""
     rng = np.random.default_rng(seed)
     k = n_orb if n_factors is None else n_factors
     p = np.arange(n_orb)
     damp = np.exp(-np.abs(p[:, None] - p[None, :]) / 2.0)
     a0 = rng.normal(0.0, 1.0, (n_orb, n_orb))
     a1 = rng.normal(0.0, pert, (n_orb, n_orb))
-    h = 0.5 * ((a0 + s * a1) + (a0 + s * a1).T) * damp
-    g = np.zeros((n_orb,) * 4)
+    ls = []
     for _ in range(k):
         l0 = rng.normal(0.0, 0.3, (n_orb, n_orb))
         l1 = rng.normal(0.0, 0.3 * pert, (n_orb, n_orb))
+        ls.append((l0, l1))
+    return damp, a0, a1, ls
+
+
+def family_integrals_from(tensors, s):
+    """family_integrals at s from tensors drawn once by family_tensors."""
+    damp, a0, a1, ls = tensors
+    h = 0.5 * ((a0 + s * a1) + (a0 + s * a1).T) * damp
+    g = np.zeros((a0.shape[0],) * 4)
+    for l0, l1 in ls:
         l = l0 + s * l1
         l = 0.5 * (l + l.T)
-        g += np.einsum("pq,rs->pqrs", l, l)
+        g += np.multiply.outer(l, l)  # g_pqrs += l_pq l_rs
     return np.ascontiguousarray(h), np.ascontiguousarray(g)
+
+
+def family_integrals(n_orb, s, seed=0, n_factors=None, pert=1.0):
+    """h(s) = h0 + s*h1 and L^k(s) = L^k0 + s*L^k1 for a Hamiltonian family scan; the
+    perturbation tensors h1, L^k1 are drawn at `pert` times the base tensors' scale."""
+    return family_integrals_from(family_tensors(n_orb, seed, n_factors, pert), s)
 
 
 def tups_operators(n_orb, layers):

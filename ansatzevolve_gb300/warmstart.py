@@ -184,8 +184,10 @@ class FamilySpec:
         self.P = int(self.param0.max()) + 1
 
     def integrals(self, s):
-        from .synthetic import family_integrals
-        return family_integrals(self.n_orb, float(s), seed=self.seed, pert=self.pert)
+        from .synthetic import family_integrals_from, family_tensors
+        if getattr(self, "_tensors", None) is None:
+            self._tensors = family_tensors(self.n_orb, seed=self.seed, pert=self.pert)
+        return family_integrals_from(self._tensors, float(s))
 
     def features(self, svals):
         return np.stack([features(*self.integrals(s)) for s in svals])
@@ -259,6 +261,54 @@ def scan_bfgs_chain(spec, svals, x_start, gtol=1e-8, mode=None):
         its.append(int(it[0]))
     e.close()
     return np.array(xs), np.array(Es), np.array(gs), np.array(its)
+
+
+def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None):
+    """Training targets as a two-level continuation over the given (sorted) s values:
+    a sequential BFGS chain over n_seg segment heads (every L-th value, L = ceil(M /
+    n_seg)), then every segment walked at once -- step t optimises the t-th member of
+    all segments in one lockstep batch, each instance from its predecessor's converged
+    angles and final inverse Hessian (on-the-fly H per instance).  The same
+    continuation as scan_bfgs_chain, with n_seg + L sequential solves instead of M.
+    Returns (x [M, P], E [M], |g| [M], iterations [M])."""
+    from . import HAM_ON_THE_FLY, HAM_STORED
+    svals = np.asarray(svals, dtype=np.float64)
+    M = len(svals)
+    L = -(-M // n_seg)
+    heads = np.arange(0, M, L)
+    ends = np.append(heads[1:], M)  # one past each segment's last member
+    S = len(heads)
+    P = spec.P
+    xs, Es, gs, its = np.zeros((M, P)), np.zeros(M), np.zeros(M), np.zeros(M, dtype=np.int64)
+    # level 1: the heads, one after the other
+    e1 = spec.engine(1)
+    x = np.asarray(x_start, dtype=np.float64).reshape(1, -1).copy()
+    hinv = None
+    hinv_heads = np.zeros((S, P, P))
+    for k, h in enumerate(heads):
+        e1.set_ham_integrals(*spec.integrals(svals[h]), HAM_STORED if mode is None else mode)
+        if hinv is None:
+            hinv = np.ascontiguousarray(inverse_hessian(e1, x[0], spec)[None])
+        x, E, gn, it, _ = e1.optimise_batch(x, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=hinv)
+        xs[h], Es[h], gs[h], its[h] = x[0], np.atleast_1d(E)[0], np.atleast_1d(gn)[0], it[0]
+        hinv_heads[k] = hinv[0]
+    e1.close()
+    # level 2: all segments in lockstep; a finished segment repeats its last member,
+    # which is already converged and drops out of the launches at once
+    eb = spec.engine(S)
+    X = xs[heads].copy()
+    H = np.ascontiguousarray(hinv_heads)
+    for t in range(1, L):
+        idx = np.minimum(heads + t, ends - 1)
+        live = heads + t < ends
+        ints = [spec.integrals(svals[i]) for i in idx]
+        eb.set_ham_integrals_batch(np.stack([a for a, _ in ints]), np.stack([b for _, b in ints]),
+                                   HAM_ON_THE_FLY if mode is None else mode)
+        X, E, gn, it, _ = eb.optimise_batch(X, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=H)
+        E, gn = np.atleast_1d(E), np.atleast_1d(gn)
+        xs[idx[live]], Es[idx[live]], gs[idx[live]], its[idx[live]] = X[live], E[live], gn[live], it[live]
+    eb.close()
+    return xs, Es, gs, its
 
 
 def inverse_hessian(engine, x, spec, floor=1e-3):

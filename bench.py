@@ -78,6 +78,13 @@ def problem():
         from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
         K, J = random_lucj(N_ORB, LUCJ_SEED)
         ops0, ang = lucj_operators(K, J)
+        # at the size of the reference-pinned fixture, its own operators and angles (the
+        # decomposition of exp(K) may pick angles 2 pi apart on another machine's LAPACK)
+        fxp = os.path.join(ROOT, "tests", "golden", "lucj%d.npz" % N_ORB)
+        if os.path.exists(fxp):
+            fx = np.load(fxp)
+            if int(fx["lucj_seed"]) == LUCJ_SEED and int(fx["ham_seed"]) == LUCJ_HAM_SEED:
+                ops0, ang = np.asarray(fx["ops"]), np.asarray(fx["x"])
         n = len(ops0)
         return dict(h1=h1, g2=g2, ops0=ops0, ops1=None, p0=np.arange(n), scale=np.ones(n), P=n, x=ang, hf=hf,
                     cplx=True)
@@ -509,19 +516,95 @@ def aux_case_bench(n_orb, lucj, stream, steps=5, warmup=2):
         LUCJ = saved[1]
 
 
-def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
+def plain_mode(spec, s0, x0):
+    """The faster H representation for the plain path's single 10-orbital instances:
+    the reference's Newton method from x0 at s0, timed with each (after one untimed run)."""
+    import ansatzevolve_gb300 as ae
+    from ansatzevolve_gb300 import warmstart as ws
+    t = {}
+    for mode in (ae.HAM_STORED, ae.HAM_ON_THE_FLY):
+        ws.scan_newton(spec, [s0], x0, gtol=1e-6, mode=mode)
+        t[mode] = ws.scan_newton(spec, [s0], x0, gtol=1e-6, mode=mode)[2]
+    best = min(t, key=t.get)
+    return best, {"stored_s": t[ae.HAM_STORED], "on_the_fly_s": t[ae.HAM_ON_THE_FLY],
+                  "chosen": "stored" if best == ae.HAM_STORED else "on the fly"}
+
+
+def batched_columns_bench(stream, h=1e-4, n_line=8):
+    """Configuration 4's other use of a batch: for one instance of each size class
+    (8, 10, 12 orbitals; integral seed 0; angles U(-0.3, 0.3)), its line-search points
+    x + t d (d = -g, n_line values of t in (0, 1.5]) and all its Hessian columns by central
+    differences of the analytic gradient, (g(x + h e_i) - g(x - h e_i)) / 2h, evaluated
+    as ONE batched energy + gradient launch of 2P + n_line + 1 instances, checked against
+    the analytic Hessian of the same instance."""
+    import torch
+    import ansatzevolve_gb300 as ae
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
+    out = []
+    for N, na, L, mode in [(8, 4, 2, ae.HAM_STORED), (10, 5, 3, ae.HAM_ON_THE_FLY), (12, 6, 3, ae.HAM_ON_THE_FLY)]:
+        ops, param, scale = tups_operators(N, L)
+        p0, P = param - 1, int(param.max())
+        h1, g2 = synthetic_integrals(N, 0)
+        x = np.random.default_rng(N).uniform(-0.3, 0.3, P)
+        e1 = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1)
+        init = np.zeros(e1.D)
+        init[np.searchsorted(e1.states(), hartree_fock_index(N, na, na))] = 1.0
+        e1.set_initial(init)
+        e1.set_ham_integrals(h1, g2, ae.HAM_STORED)
+        t0 = time.perf_counter()
+        _, g0, Hx = e1.hessian(scale * x[p0], p0, scale)
+        t_hess = time.perf_counter() - t0
+        e1.close()
+        ts = np.linspace(1.5 / n_line, 1.5, n_line)
+        X = np.vstack([x + h * np.eye(P), x - h * np.eye(P), x[None, :] + ts[:, None] * (-g0)[None, :], x[None, :]])
+        nb = len(X)
+        e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1)
+        e.set_initial(init)
+        e.set_batch(nb)
+        e.set_ham_integrals(h1, g2, mode)
+        e.io_put_angles(scale[None, :] * X[:, p0])
+        e.io_get_results()
+        sp = stream.cuda_stream
+        for _ in range(2):
+            e.launch_io(sp)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(3):
+            e.launch_io(sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / 3
+        E, gops = e.io_get_results()
+        e.close()
+        G = np.zeros((nb, P))
+        for k in range(nb):
+            np.add.at(G[k], p0, scale * gops[k])
+        Hfd = (G[:P] - G[P:2 * P]) / (2 * h)
+        out.append({"orbitals": N, "parameters": P, "instances": nb, "ham": "stored" if mode == ae.HAM_STORED else
+                    "on the fly", "ms_per_batch": ms, "evals_per_s": nb / (ms / 1e3),
+                    "hessian_columns_max_dev": float(np.max(np.abs(Hfd - Hx))), "analytic_hessian_ms": 1e3 * t_hess,
+                    "line_search_E": [float(v) for v in E[2 * P:2 * P + n_line]], "E_at_x": float(E[-1])})
+    return {"classes": out, "fd_step": h,
+            "api": "aegpu_launch_io: one captured graph of the batched energy + gradient evaluation per class"}
+
+
+def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=250):
     """Time to converge over a 10-orbital Hamiltonian family scan (5a+5b, 3 layers,
     81 parameters): h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1.  Both paths start the scan
     from the s = 0 member's lowest minimum found by a 64-start batched search (shared,
     not timed).
     Plain: one instance at a time in increasing s, the reference's Newton method from
-    the previous converged angles (timed on the first n_plain held-out values, mean
-    per instance).  Batched + warm-started: all n_heldout instances in one batch,
-    network proposals screened by the engine against the s = 0 angles, then lockstep
-    BFGS from the inverse Hessians at 8 anchors (converged instances drop out of the
-    launches; any still unconverged after 2000 rounds would finish with the plain
-    method, timed).  The network is trained once per family on
-    n_train converged angle sets from a continuation chain (reported separately)."""
+    the previous converged angles, with the faster of the stored and on-the-fly H for a
+    single instance (measured first), timed on the first n_plain held-out values (all
+    of them by default; mean per instance).  Batched + warm-started: all n_heldout
+    instances in one batch, network proposals screened by the engine against the s = 0
+    angles, then lockstep BFGS from the inverse Hessians at 8 anchors (converged
+    instances drop out of the launches; any still unconverged after 2000 rounds would
+    finish with the plain method, timed).  The network is trained once per family on
+    n_train converged angle sets from a two-level continuation chain (n_seg heads in
+    sequence, then the segments in lockstep batches), its cost reported separately and
+    charged in speedup_including_training."""
     from ansatzevolve_gb300 import warmstart as ws
     spec = ws.FamilySpec(10, 5, 3, seed=0)
     t0 = time.perf_counter()
@@ -530,13 +613,14 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     s_tr = np.sort(np.random.default_rng(2024).uniform(0, 1, n_train))
     s_ho = np.sort(np.random.default_rng(77).uniform(0, 1, n_heldout))
     t0 = time.perf_counter()
-    xtr, Etr, gtr, its = ws.scan_bfgs_chain(spec, s_tr, x0, gtol=1e-8)
+    xtr, Etr, gtr, its = ws.scan_segmented_chain(spec, s_tr, x0, n_seg=n_seg, gtol=1e-8)
     t_chain = time.perf_counter() - t0
     t0 = time.perf_counter()
     model, hist = ws.train_warmstart(spec.features(s_tr), xtr, epochs=epochs, batch=128, lr=1e-3)
     t_train = time.perf_counter() - t0
     r = ws.scan_batched_warm(spec, s_ho, model, x0, gtol=1e-6, n_anchor=8)
-    xp, Ep, tp, nh, ne = ws.scan_newton(spec, s_ho[:n_plain], x0, gtol=1e-6)
+    mode, mode_info = plain_mode(spec, s_ho[0], x0)
+    xp, Ep, tp, nh, ne = ws.scan_newton(spec, s_ho[:n_plain], x0, gtol=1e-6, mode=mode)
     plain_per = tp / n_plain
     batched_per = r["seconds"] / n_heldout
     dE = r["E"][:n_plain] - Ep
@@ -545,7 +629,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
     return {"speedup": plain_per / batched_per, "unit": "x (plain seconds per instance / batched seconds per instance)",
             # the one-off training cost charged to this one scan of n_heldout instances
             "speedup_including_training": plain_per * n_heldout / (r["seconds"] + train_s),
-            "plain_s_per_instance": plain_per, "plain_instances_timed": n_plain,
+            "plain_s_per_instance": plain_per, "plain_instances_timed": n_plain, "plain_ham": mode_info,
             "plain_hessians": nh, "plain_energy_evals": ne,
             "batched_s_total": r["seconds"], "batched_instances": n_heldout, "batched_s_per_instance": batched_per,
             "batched_rounds": int(r["rounds"]), "batched_iters_median": float(np.median(r["iters"])),
@@ -555,11 +639,46 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=48, epochs=400):
             "energy_match_1e-8": int(np.sum(np.abs(dE) < 1e-8)), "energy_compared": n_plain,
             "max_abs_dE": float(np.abs(dE).max()),
             "training": {"instances": n_train, "chain_s": t_chain, "chain_iters_median": float(np.median(its)),
+                         "chain": "%d heads in sequence, then the %d segments walked in lockstep batches" % (n_seg, n_seg),
+                         "chain_max_gnorm": float(np.max(gtr)),
                          "mlp_train_s": t_train, "epochs": epochs, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1]), "origin_s": t_origin, "origin_energy": float(E0)},
             "workload": "10 orbitals 5a+5b, 3 layers (81 parameters), family h(s)=h0+s h1, L(s)=L0+s L1, seed 0, "
                         "h1 and L1 at %.2f of the base scale; %d training / %d held-out s ~ U(0,1)"
                         % (spec.pert, n_train, n_heldout)}
+
+
+def gram_kernel_bench(args, n=853776, V=100):
+    """The Hessian's Gram contraction 2 T_C^T (H T_C) on its own at the 12-orbital shape
+    (upper triangle, V = 100 columns of n doubles, random columns): CUDA-event time per
+    call and the DFMA rate of the 5,200 x n DFMAs it issues (325 micro-tiles of 4 x 4)."""
+    import torch
+    import ansatzevolve_gb300 as ae
+    L = ae.lib()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    TC = torch.randn(V, n, dtype=torch.float64, device="cuda", generator=g)
+    HTC = torch.randn(V, n, dtype=torch.float64, device="cuda", generator=g)
+    C = torch.zeros(V, V, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+
+    def call():
+        rc = L.aegpu_gram_upper_dev(TC.data_ptr(), n, HTC.data_ptr(), n, n, 1, V, 2.0, C.data_ptr(), 0, V, s.cuda_stream)
+        assert rc == 0
+
+    for _ in range(max(args.warmup, 3)):
+        call()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(s)
+    for _ in range(args.steps):
+        call()
+    b.record(s)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / args.steps
+    nb = (V + 3) // 4
+    dfma = nb * (nb + 1) // 2 * 16 * n
+    print(json.dumps({"kernel": "k_gram (aegpu_gram_upper_dev)", "n": n, "V": V, "ms": ms, "dfma": dfma,
+                      "T_dfma_per_s": dfma / (ms / 1e3) / 1e12, "peak_T_dfma_per_s": ae.fp64_peak() / 2.0}))
 
 
 def main():
@@ -581,9 +700,12 @@ def main():
     ap.add_argument("--no-ground", action="store_true", help="skip the lowest-eigenpair (Lanczos) timing")
     ap.add_argument("--no-ttc", action="store_true")
     ap.add_argument("--no-config3", action="store_true", help="skip the 14-orbital tUPS and LUCJ objects")
+    ap.add_argument("--kernel", default=None, choices=["gram"],
+                    help="time one kernel on its own instead (gram: the Hessian's Gram contraction at the "
+                         "12-orbital shape, 100 columns of 853,776 doubles)")
     ap.add_argument("--ttc-train", type=int, default=2000)
     ap.add_argument("--ttc-heldout", type=int, default=200)
-    ap.add_argument("--ttc-plain", type=int, default=48)
+    ap.add_argument("--ttc-plain", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gpu" else args.warmup
     set_orbitals(args.orbitals)
@@ -596,6 +718,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.kernel == "gram":
+        return gram_kernel_bench(args)
 
     import torch
     torch.cuda.set_device(local)
@@ -745,6 +869,8 @@ def main():
     eng.close()
     if not args.no_batched:
         line["batched"] = batched_bench(stream)
+    if not args.no_batched:
+        line["batched_columns"] = batched_columns_bench(stream)
     if not args.no_config3 and N_ORB == 12 and not LUCJ:
         line["config3"] = aux_case_bench(14, False, stream)
         line["lucj14"] = aux_case_bench(14, True, stream, steps=3)
