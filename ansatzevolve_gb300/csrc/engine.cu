@@ -1111,6 +1111,10 @@ struct IntArgs {
     int nOa, nVa, nOb, nVb;
     int64_t width;    // entries per row
     int64_t stride;   // stored entries per row (width rounded up to a multiple of 4; padding is col = row, val = 0)
+    // coded rows (see k_vell_build): explicit entries (diagonal + singles) and coded
+    // entries (doubles), each rounded up to a multiple of 4
+    int64_t width_e, stride_e, width_d, stride_d;
+    int NP;           // spatial orbital pairs N (N - 1) / 2
 };
 
 __device__ __forceinline__ double two_e(const IntArgs &a, int p, int q, int r, int s)
@@ -1274,6 +1278,247 @@ __global__ void k_ell_build(IntArgs a, int32_t *__restrict__ col, double *__rest
             col[p] = c;
             val[p] = v;
         }
+    }
+}
+
+// ------------------------------------------------------ coded stored rows --
+// 96 % of a row's entries are double excitations, whose value is a fermionic sign times
+// an integral combination that depends only on the four orbitals (two_e).  Coded rows
+// keep those as a 2-byte code -- sign << 15 | index into a value table of every distinct
+// two_e -- next to the 4-byte column, and keep the diagonal and the singles (whose values
+// depend on the determinant) explicit.  Table: [0] = 0 (padding), then the same-spin
+// values two_e(P, Q, R, S) for spatial pairs P < Q, R < S (alpha and beta share them),
+// then the alpha-beta values two_e(pb, pa, rb, ra) at ((pa N + ra) N + pb) N + rb.  The
+// product sign * table[index] is exactly the value row_entry builds.
+constexpr int kVtabMax = 1 << 15;
+constexpr int kVellThreads = 1024;
+constexpr int kVellNV1 = 4, kVellNV2 = 2;  // right-hand sides per thread (real, complex) of the multi-vector product
+
+__host__ __device__ __forceinline__ int64_t vtab_len(int N)
+{
+    const int64_t NP = (int64_t)N * (N - 1) / 2;
+    return 1 + NP * NP + (int64_t)N * N * N * N;
+}
+
+__device__ __forceinline__ int pair_index(int i, int j, int n)  // i < j, lexicographic (pair_of's order)
+{
+    return i * n - i * (i + 1) / 2 + (j - i - 1);
+}
+
+__global__ void k_vtab_build(IntArgs a, double *__restrict__ vtab)
+{
+    const int N = a.N, NP = a.NP;
+    const int64_t n = vtab_len(N), ss = (int64_t)NP * NP;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        if (k >= 1 && k <= ss) {
+            int P, Q, R, S;
+            pair_of((int)((k - 1) / NP), N, P, Q);
+            pair_of((int)((k - 1) % NP), N, R, S);
+            v = two_e(a, P + N, Q + N, R + N, S + N);
+        } else if (k > ss) {
+            const int64_t t = k - 1 - ss;
+            const int rb = (int)(t % N), pb = (int)((t / N) % N), ra = (int)((t / N / N) % N), pa = (int)(t / N / N / N);
+            v = two_e(a, pb, pa + N, rb, ra + N);
+        }
+        vtab[k] = v;
+    }
+}
+
+// Coded double d of row J (d counts the row's aa, bb, ab doubles in row_entry's order):
+// the input determinant and the code.
+__device__ void row_code(const IntArgs &a, uint32_t J, int64_t d, uint32_t &I, uint16_t &code)
+{
+    const int N = a.N;
+    const uint32_t full = below(N);
+    const uint32_t Ja = J >> N, Jb = J & full;
+    const uint32_t Va = ~Ja & full, Vb = ~Jb & full;
+    const int64_t Sb = (int64_t)a.nOb * a.nVb;
+    const int64_t Daa = (int64_t)(a.nOa * (a.nOa - 1) / 2) * (a.nVa * (a.nVa - 1) / 2);
+    const int64_t Dbb = (int64_t)(a.nOb * (a.nOb - 1) / 2) * (a.nVb * (a.nVb - 1) / 2);
+    int p, q, r, t;
+    int64_t idx;
+    if (d < Daa + Dbb) {
+        const bool alpha = d < Daa;
+        if (!alpha) d -= Daa;
+        const uint32_t O = alpha ? Ja : Jb, Vv = alpha ? Va : Vb;
+        const int nO = alpha ? a.nOa : a.nOb, nV = alpha ? a.nVa : a.nVb, off = alpha ? N : 0;
+        const int nvp = nV * (nV - 1) / 2;
+        int i0, i1, j0, j1;
+        pair_of((int)(d / nvp), nO, i0, i1);
+        pair_of((int)(d % nvp), nV, j0, j1);
+        const int P = nth_bit(O, i0), Q = nth_bit(O, i1), R = nth_bit(Vv, j0), S = nth_bit(Vv, j1);
+        p = P + off, q = Q + off, r = R + off, t = S + off;
+        idx = 1 + (int64_t)pair_index(P, Q, N) * a.NP + pair_index(R, S, N);
+    } else {
+        d -= Daa + Dbb;
+        const int64_t ea = d / Sb, eb = d % Sb;
+        const int pa = nth_bit(Ja, (int)(ea / a.nVa)), ra = nth_bit(Va, (int)(ea % a.nVa));
+        const int pb = nth_bit(Jb, (int)(eb / a.nVb)), rb = nth_bit(Vb, (int)(eb % a.nVb));
+        p = pb, q = pa + N, r = rb, t = ra + N;
+        idx = 1 + (int64_t)a.NP * a.NP + (((int64_t)pa * N + ra) * N + pb) * N + rb;
+    }
+    I = J ^ (1u << p) ^ (1u << q) ^ (1u << r) ^ (1u << t);
+    uint32_t m = below(p) ^ below(q) ^ below(r) ^ below(t);
+    m &= ~((1u << p) | (1u << q) | (1u << r) | (1u << t));
+    code = (uint16_t)((uint32_t)idx | ((__popc(J & m) & 1u) << 15));
+}
+
+// Coded rows of rows [r0, r1): both parts in the sliced layout of ell_pos (slabs of 32
+// rows, inside a slab the 4-entry groups of the 32 rows contiguous).
+__global__ void k_vell_build(IntArgs a, int32_t *__restrict__ colE, double *__restrict__ valE, int32_t *__restrict__ colD,
+                             uint16_t *__restrict__ codeD, int64_t r0, int64_t r1)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t qe = a.stride_e >> 2, qd = a.stride_d >> 2, D = (int64_t)a.basis.D;
+    for (int64_t r = r0 + (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < r1; r += warps) {
+        // padding: rows past D and entries past the row's width point at the row itself
+        // (row 0 past D) with value / code 0
+        const uint32_t J = r < D ? a.basis.bits((uint32_t)r) : 0u;
+        const int32_t self = r < D ? (int32_t)r : 0;
+        for (int64_t e = lane; e < a.stride_e; e += 32) {
+            uint32_t I = J;
+            double v = 0.0;
+            int32_t c = self;
+            if (r < D && e < a.width_e) {
+                row_entry(a, J, e, I, v);
+                c = (int32_t)a.basis.rank_of(I);
+            }
+            const size_t p = ell_pos(r, e, qe);
+            colE[p] = c;
+            valE[p] = v;
+        }
+        for (int64_t e = lane; e < a.stride_d; e += 32) {
+            uint32_t I = J;
+            uint16_t code = 0;
+            int32_t c = self;
+            if (r < D && e < a.width_d) {
+                row_code(a, J, e, I, code);
+                c = (int32_t)a.basis.rank_of(I);
+            }
+            const size_t p = ell_pos(r, e, qd);
+            colD[p] = c;
+            codeD[p] = code;
+        }
+    }
+}
+
+struct VellArgs {
+    const int32_t *colE, *colD;
+    const double *valE, *vtab;
+    const uint16_t *codeD;
+    int64_t qe, qd;               // groups of 4 per row
+    int64_t inst_e, inst_d;       // entries between instances' explicit / coded parts (0 = shared)
+    int64_t vtab_len, vtab_inst;  // table entries, entries between instances' tables (0 = shared)
+};
+
+__device__ __forceinline__ double signed_value(const double *tab, uint32_t code)
+{
+    const double t = tab[code & 0x7fffu];
+    return __longlong_as_double(__double_as_longlong(t) ^ ((long long)(code >> 15) << 63));
+}
+
+// y = H x with coded rows.  T threads per row as in k_spmv_sell.  Each CTA owns an
+// equal contiguous share of the rows (a multiple of 32), walked 1024 / T rows at a
+// time, so that every SM ends with the same work (the FP64 pipe is the limit, and a
+// grid of whole row blocks left some SMs one block behind the rest); the value table is
+// staged once per CTA, in shared memory.  NV > 1: one thread carries NV right-hand sides (instances
+// blockIdx.y * NV + v, shared matrix, no energy and no mask), so each matrix entry read
+// serves NV products.  Energy partial per CTA: sum over its rows of y_r x_r.
+template <int W, int T, int NV>
+__global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const double *__restrict__ x,
+                                                               double *__restrict__ y, int64_t D, int ninst,
+                                                               double *__restrict__ epart, const int *__restrict__ active)
+{
+    extern __shared__ double tab[];
+    __shared__ double red[kVellThreads / 32];
+    const int b0 = blockIdx.y * NV;
+    if (NV == 1 && skip_instance(active, b0)) return;
+    const double *vt = m.vtab + (size_t)b0 * m.vtab_inst;
+    for (int64_t i = threadIdx.x; i < m.vtab_len; i += blockDim.x) tab[i] = vt[i];
+    __syncthreads();
+    const int32_t *colE = m.colE + (size_t)b0 * m.inst_e, *colD = m.colD + (size_t)b0 * m.inst_d;
+    const double *valE = m.valE + (size_t)b0 * m.inst_e;
+    const uint16_t *codeD = m.codeD + (size_t)b0 * m.inst_d;
+    constexpr int RPW = 32 / T;
+    const int lane = threadIdx.x & 31, sub = lane / RPW;
+    const int64_t rows_per_iter = kVellThreads / T;
+    const int64_t share = ((D + gridDim.x - 1) / gridDim.x + 31) & ~(int64_t)31;
+    const int64_t r_lo = (int64_t)blockIdx.x * share, r_hi = r_lo + share < D ? r_lo + share : D;
+    double e = 0.0;
+    for (int64_t rb = r_lo; rb < r_hi; rb += rows_per_iter) {
+        const int64_t rr = rb + (threadIdx.x - lane) / T + lane % RPW;
+        const int64_t r = rr < r_hi ? rr : D;  // rows past the share: none
+        double acc[NV][W][2];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int w = 0; w < W; ++w) acc[v][w][0] = acc[v][w][1] = 0.0;
+        if (r < D) {
+            {
+                const size_t base = ell_pos(r, 0, m.qe);
+                const int4 *c4 = reinterpret_cast<const int4 *>(colE + base);
+                const double2 *v2 = reinterpret_cast<const double2 *>(valE + base);
+                for (int64_t g = sub; g < m.qe; g += T) {
+                    const int4 c = __ldg(c4 + 32 * g);
+                    const double2 h01 = __ldg(v2 + 64 * g), h23 = __ldg(v2 + 64 * g + 1);
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const double *xv = x + (size_t)(b0 + v < ninst ? b0 + v : b0) * D * W;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) {
+                            acc[v][w][0] = fma(h01.x, __ldg(xv + (size_t)c.x * W + w), acc[v][w][0]);
+                            acc[v][w][1] = fma(h01.y, __ldg(xv + (size_t)c.y * W + w), acc[v][w][1]);
+                            acc[v][w][0] = fma(h23.x, __ldg(xv + (size_t)c.z * W + w), acc[v][w][0]);
+                            acc[v][w][1] = fma(h23.y, __ldg(xv + (size_t)c.w * W + w), acc[v][w][1]);
+                        }
+                    }
+                }
+            }
+            {
+                const size_t base = ell_pos(r, 0, m.qd);
+                const int4 *c4 = reinterpret_cast<const int4 *>(colD + base);
+                const uint2 *k2 = reinterpret_cast<const uint2 *>(codeD + base);
+                for (int64_t g = sub; g < m.qd; g += T) {
+                    const int4 c = __ldg(c4 + 32 * g);
+                    const uint2 k = __ldg(k2 + 32 * g);
+                    const double h0 = signed_value(tab, k.x & 0xffffu), h1 = signed_value(tab, k.x >> 16);
+                    const double h2 = signed_value(tab, k.y & 0xffffu), h3 = signed_value(tab, k.y >> 16);
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const double *xv = x + (size_t)(b0 + v < ninst ? b0 + v : b0) * D * W;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) {
+                            acc[v][w][0] = fma(h0, __ldg(xv + (size_t)c.x * W + w), acc[v][w][0]);
+                            acc[v][w][1] = fma(h1, __ldg(xv + (size_t)c.y * W + w), acc[v][w][1]);
+                            acc[v][w][0] = fma(h2, __ldg(xv + (size_t)c.z * W + w), acc[v][w][0]);
+                            acc[v][w][1] = fma(h3, __ldg(xv + (size_t)c.w * W + w), acc[v][w][1]);
+                        }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            if (b0 + v >= ninst) continue;
+            double *yv = y + (size_t)(b0 + v) * D * W;
+            const double *xv = x + (size_t)(b0 + v) * D * W;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                double s = acc[v][w][0] + acc[v][w][1];
+#pragma unroll
+                for (int o = RPW; o < 32; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (r < D && sub == 0) {
+                    yv[r * W + w] = s;
+                    if (NV == 1) e = fma(s, xv[r * W + w], e);
+                }
+            }
+        }
+    }
+    if (NV == 1 && epart) {
+        e = block_sum(e, red);
+        if (threadIdx.x == 0) epart[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = e;
     }
 }
 
@@ -1452,6 +1697,7 @@ struct aegpu_engine {
     int64_t launches = 0;
     cudaStream_t stream = nullptr;
     int sm_count = 152;
+    int smem_per_sm = 228 * 1024;
 
     Basis B;
     bool cplx = false;
@@ -1520,6 +1766,9 @@ struct aegpu_engine {
     int64_t *d_rowptr = nullptr;
     int32_t *d_col = nullptr;
     double *d_val = nullptr;
+    // coded stored rows (k_vell_build; used when the value table fits, N <= 12)
+    bool ell_coded = false;
+    VellArgs vell{};
     IntArgs ints{};
     double *d_h1 = nullptr, *d_g2 = nullptr;
     int ell_width = 0;
@@ -1711,6 +1960,8 @@ struct aegpu_engine {
         d_rowptr = nullptr;
         d_col = nullptr;
         d_val = nullptr;
+        ell_coded = false;
+        vell = VellArgs{};
         d_h1 = d_g2 = nullptr;
         drop_graph();
         h_valid = false;
@@ -1809,6 +2060,22 @@ int set_smem_limits(int dev)
     int bad = 0;
     bad += set_smem(k_block_tangent<1>, need(1, 1), optin);
     bad += set_smem(k_block_tangent<2>, need(1, 2), optin);
+    // the coded-row product stages its value table (<= 196 KB at 12 orbitals): allow the most
+    {
+        const void *kerns[] = {(const void *)k_spmv_vell<1, 1, 1>, (const void *)k_spmv_vell<1, 2, 1>,
+                               (const void *)k_spmv_vell<1, 4, 1>, (const void *)k_spmv_vell<1, 8, 1>,
+                               (const void *)k_spmv_vell<2, 1, 1>, (const void *)k_spmv_vell<2, 2, 1>,
+                               (const void *)k_spmv_vell<2, 4, 1>, (const void *)k_spmv_vell<2, 8, 1>,
+                               (const void *)k_spmv_vell<1, 1, kVellNV1>, (const void *)k_spmv_vell<1, 2, kVellNV1>,
+                               (const void *)k_spmv_vell<1, 4, kVellNV1>, (const void *)k_spmv_vell<1, 8, kVellNV1>,
+                               (const void *)k_spmv_vell<2, 1, kVellNV2>, (const void *)k_spmv_vell<2, 2, kVellNV2>,
+                               (const void *)k_spmv_vell<2, 4, kVellNV2>, (const void *)k_spmv_vell<2, 8, kVellNV2>};
+        for (const void *kern : kerns) {
+            cudaFuncAttributes fa{};
+            if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess)
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+        }
+    }
     // the on-the-fly kernel's need depends on N (<= 150 KB at 14 orbitals): allow the most
     for (int W = 1; W <= 2; ++W) {
         cudaFuncAttributes fa{};
@@ -1903,6 +2170,39 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         else
             k_spmv<2, false><<<g, kSpmvThreads, 0, e->stream>>>(e->d_rowptr, 0, e->d_col, e->d_val, x, y, D, epart,
                                                                 act);
+    } else if (e->ham_kind == 2 && e->ell_coded) {
+        const int T = e->spmv_tpr();
+        const int64_t rows_per_cta = kVellThreads / T;
+        const int64_t nblk = (D + rows_per_cta - 1) / rows_per_cta;
+        const size_t smem = (size_t)e->vell.vtab_len * sizeof(double);
+        // one 1024-thread CTA per SM (its 64 registers per thread fill the register file)
+        const int gx = (int)std::min<int64_t>(nblk, (int64_t)e->sm_count);
+        // several right-hand sides per thread when the instances share the matrix and
+        // need neither energies nor the instance mask (the Hessian's tangents, Lanczos)
+        const bool multi = ninst > 1 && !epart && !act && e->vell.inst_e == 0;
+        const int nv = multi ? (e->W == 1 ? kVellNV1 : kVellNV2) : 1;
+        const dim3 g(gx, (ninst + nv - 1) / nv);
+#define AE_VELL(WW, TT, NN) \
+    k_spmv_vell<WW, TT, NN><<<g, kVellThreads, smem, e->stream>>>(e->vell, x, y, D, ninst, epart, act)
+        if (e->W == 1) {
+            if (multi) {
+                if (T == 1) AE_VELL(1, 1, kVellNV1); else if (T == 2) AE_VELL(1, 2, kVellNV1);
+                else if (T == 4) AE_VELL(1, 4, kVellNV1); else AE_VELL(1, 8, kVellNV1);
+            } else {
+                if (T == 1) AE_VELL(1, 1, 1); else if (T == 2) AE_VELL(1, 2, 1); else if (T == 4) AE_VELL(1, 4, 1);
+                else AE_VELL(1, 8, 1);
+            }
+        } else {
+            if (multi) {
+                if (T == 1) AE_VELL(2, 1, kVellNV2); else if (T == 2) AE_VELL(2, 2, kVellNV2);
+                else if (T == 4) AE_VELL(2, 4, kVellNV2); else AE_VELL(2, 8, kVellNV2);
+            } else {
+                if (T == 1) AE_VELL(2, 1, 1); else if (T == 2) AE_VELL(2, 2, 1); else if (T == 4) AE_VELL(2, 4, 1);
+                else AE_VELL(2, 8, 1);
+            }
+        }
+#undef AE_VELL
+        if (nparts) *nparts = gx;
     } else if (e->ham_kind == 2) {
         const int T = e->spmv_tpr();
         const int64_t rows_per_cta = kSpmvThreads / T;
@@ -2184,6 +2484,7 @@ int aegpu_create(aegpu_engine **out)
     }
     auto *e = new aegpu_engine();
     cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&e->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (const char *v = std::getenv("AEGPU_REUSE_HPSI")) e->reuse_hpsi = std::strcmp(v, "0") != 0;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
@@ -2429,6 +2730,34 @@ namespace {
 
 // Hamiltonian from integrals for ntab table sets: ntab = 1 shares one Hamiltonian
 // between all instances, ntab = nb gives instance b the integrals h1s[b], g2s[b].
+// Value tables and coded rows of every instance (the engine's integrals already on the
+// device; e->vell and e->ints set).
+static void build_coded_rows(aegpu_engine *e, int ntab)
+{
+    const IntArgs a = e->ints;
+    const int N = a.N;
+    const size_t NN = (size_t)N * N, N4 = NN * NN;
+    const int64_t D = (int64_t)e->B.D, Dpad = (D + 31) & ~(int64_t)31;
+    const size_t per_e = (size_t)Dpad * a.stride_e, per_d = (size_t)Dpad * a.stride_d;
+    const VellArgs &v = e->vell;
+    const int64_t chunk = 1 << 16;
+    for (int t = 0; t < ntab; ++t) {
+        IntArgs ai = a;
+        ai.h1 = e->d_h1 + NN * t;
+        ai.g2 = e->d_g2 + N4 * t;
+        k_vtab_build<<<(int)((v.vtab_len + 255) / 256), 256, 0, e->stream>>>(ai, (double *)v.vtab + (size_t)v.vtab_len * t);
+        e->launches += 1;
+        for (int64_t r0 = 0; r0 < Dpad; r0 += chunk) {
+            k_vell_build<<<e->sm_count * 8, 256, 0, e->stream>>>(ai, (int32_t *)v.colE + per_e * t,
+                                                                (double *)v.valE + per_e * t,
+                                                                (int32_t *)v.colD + per_d * t,
+                                                                (uint16_t *)v.codeD + per_d * t, r0,
+                                                                std::min(Dpad, r0 + chunk));
+            e->launches += 1;
+        }
+    }
+}
+
 // New integral values for an integral Hamiltonian of the same shape (same instances
 // and representation): the values are written into the existing buffers -- stored rows
 // rebuilt, on-the-fly integral tables and diagonal rebuilt; the string tables do not
@@ -2445,7 +2774,9 @@ static int refresh_integrals(aegpu_engine *e, const double *h1s, const double *g
     cudaMemcpy(e->d_g2, g2s, sizeof(double) * N4 * ntab, cudaMemcpyHostToDevice);
     const int64_t D = (int64_t)e->B.D;
     IntArgs a = e->ints;
-    if (e->ham_kind == 2) {
+    if (e->ham_kind == 2 && e->ell_coded) {
+        build_coded_rows(e, ntab);
+    } else if (e->ham_kind == 2) {
         const int64_t Dpad = (D + 31) & ~(int64_t)31;
         const size_t per = (size_t)Dpad * a.stride;
         const int64_t chunk = 1 << 16;
@@ -2519,6 +2850,15 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
     a.width = 1 + (int64_t)a.nOa * a.nVa + (int64_t)a.nOb * a.nVb + c2(a.nOa) * c2(a.nVa) + c2(a.nOb) * c2(a.nVb) +
               (int64_t)a.nOa * a.nVa * a.nOb * a.nVb;
     a.stride = (a.width + 3) & ~(int64_t)3;
+    a.NP = N * (N - 1) / 2;
+    a.width_e = 1 + (int64_t)a.nOa * a.nVa + (int64_t)a.nOb * a.nVb;
+    a.stride_e = (a.width_e + 3) & ~(int64_t)3;
+    a.width_d = a.width - a.width_e;
+    a.stride_d = (a.width_d + 3) & ~(int64_t)3;
+    // coded rows when the value table has at most 2^15 entries (N <= 12), unless the
+    // environment says AEGPU_CODED_ROWS=0
+    const char *cenv = std::getenv("AEGPU_CODED_ROWS");
+    const bool coded = vtab_len(N) <= kVtabMax && !(cenv && std::strcmp(cenv, "0") == 0);
     e->drop_ham();
     auto ham_alloc = [&](auto *&ptr, size_t count) {
         using T = std::remove_reference_t<decltype(*ptr)>;
@@ -2544,13 +2884,43 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
     e->ell_width = (int)a.stride;
     const int64_t D = (int64_t)e->B.D;
     const int64_t Dpad = (D + 31) & ~(int64_t)31;
-    const double ell_bytes = (double)Dpad * a.stride * 12.0 * ntab;
+    const double ell_bytes = coded ? ((double)Dpad * (a.stride_e * 12.0 + a.stride_d * 6.0) + vtab_len(N) * 8.0) * ntab
+                                   : (double)Dpad * a.stride * 12.0 * ntab;
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const int mode_asked = mode;
     if (mode == AEGPU_HAM_AUTO) mode = ell_bytes < 0.6 * (double)free_b ? AEGPU_HAM_STORED : AEGPU_HAM_ON_THE_FLY;
     e->ham_per_instance = ntab > 1;
-    if (mode == AEGPU_HAM_STORED) {
+    if (mode == AEGPU_HAM_STORED && coded) {
+        const size_t per_e = (size_t)Dpad * a.stride_e, per_d = (size_t)Dpad * a.stride_d;
+        const int64_t L = vtab_len(N);
+        VellArgs v{};
+        int32_t *colE = nullptr, *colD = nullptr;
+        double *valE = nullptr, *vtab = nullptr;
+        uint16_t *codeD = nullptr;
+        if (!ham_alloc(colE, per_e * ntab) || !ham_alloc(valE, per_e * ntab) || !ham_alloc(colD, per_d * ntab) ||
+            !ham_alloc(codeD, per_d * ntab) || !ham_alloc(vtab, (size_t)L * ntab))
+            return e->fail(AEGPU_ERR_NOMEM, "coded row allocation failed");
+        v.colE = colE;
+        v.valE = valE;
+        v.colD = colD;
+        v.codeD = codeD;
+        v.vtab = vtab;
+        v.qe = a.stride_e >> 2;
+        v.qd = a.stride_d >> 2;
+        v.inst_e = ntab > 1 ? (int64_t)per_e : 0;
+        v.inst_d = ntab > 1 ? (int64_t)per_d : 0;
+        v.vtab_len = L;
+        v.vtab_inst = ntab > 1 ? L : 0;
+        e->vell = v;
+        e->ell_coded = true;
+        e->ints = a;
+        build_coded_rows(e, ntab);
+        e->ham_kind = 2;
+        e->ham_entries = D * (a.stride_e + a.stride_d);
+        e->ell_width = (int)(a.stride_e + a.stride_d);
+        e->ell_stride_inst = 0;
+    } else if (mode == AEGPU_HAM_STORED) {
         const size_t per = (size_t)Dpad * a.stride;
         if (!ham_alloc(e->d_col, per * ntab) || !ham_alloc(e->d_val, per * ntab))
             return e->fail(AEGPU_ERR_NOMEM, "ELL allocation failed");

@@ -59,9 +59,26 @@ def workload_desc(D, P, nops, ham):
 
 
 LUCJ = False
-# DRAM traffic / algorithmic bytes of k_spmv_sell measured by ncu on the 10-orbital
-# launch (669.27 MB read + 3.68 MB written for 668.57 MB algorithmic)
+# DRAM traffic / algorithmic bytes of k_spmv_sell (uncoded rows) measured by ncu on the
+# 10-orbital launch (669.27 MB read + 3.68 MB written for 668.57 MB algorithmic)
 SELL_TRAFFIC_RATIO = (669.273856 + 3.678720) / 668.570112
+# DRAM traffic / streamed bytes of k_spmv_vell (coded rows) measured by ncu on the
+# 10-orbital launch (355.99 MB read + 4.28 MB written for 356.13 MB of coded rows,
+# x and y); profiles/k_spmv_vell_tups10_stored.md
+VELL_TRAFFIC_RATIO = (355.988992 + 4.284160) / 356.130432
+
+
+def coded_row_bytes(D, W, width):
+    """Bytes one coded-row product streams: explicit entries (diagonal + singles) at
+    12 B, coded doubles at 6 B (4-byte column + 2-byte code), each part padded to a
+    multiple of 4 entries, plus x and y; None where the engine keeps uncoded rows
+    (value table over 2^15 entries, N > 12, or AEGPU_CODED_ROWS=0)."""
+    NP = N_ORB * (N_ORB - 1) // 2
+    if 1 + NP * NP + N_ORB ** 4 > (1 << 15) or os.environ.get("AEGPU_CODED_ROWS") == "0":
+        return None
+    we = 1 + N_A * (N_ORB - N_A) + N_B * (N_ORB - N_B)
+    se, sd = (we + 3) // 4 * 4, (width - we + 3) // 4 * 4
+    return D * (se * 12 + sd * 6) + 16 * D * W
 
 
 # the LUCJ circuit's seeds (K, J and the integrals), those of the reference-pinned
@@ -818,12 +835,14 @@ def main():
     hpsi_bytes = nnz * 12 + 16 * D * W if mode == ae.HAM_STORED else 16 * D * W
     t_hpsi = phase_ms[1] / max(nph, 1) / 1e3
     achieved = hpsi_bytes / t_hpsi / 1e9
+    stream = coded_row_bytes(D, W, nnz // D) if mode == ae.HAM_STORED else None
     # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
     passes = info["blocks"]
     step_bytes = passes * 16 * D * W + hpsi_bytes + passes * 32 * D * W
     # FP64-pipe roofline of the same step: FP64 instructions per evaluation against the
     # DFMA throughput measured on this device right now
     fw = eng.fp64_work()
+    fw_h = fw[0]
     peak_t = ae.fp64_peak() / 2.0  # T DFMA/s
     ph = [phase_ms[k] / max(nph, 1) / 1e3 for k in range(3)]
     fp64 = {"unit": "T FP64 instr/s", "peak": peak_t, "peak_source": "measured (aegpu_fp64_peak)",
@@ -837,17 +856,30 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random integrals)",
         "config": workload_desc(D, pb["P"], len(pb["ops0"]),
-                                "stored as %d-wide rows in HBM (%.1f GB)" % (info["ell_width"], nnz * 12 / 1e9)
+                                ("stored in HBM as coded rows (%.1f GB: diagonal and singles explicit, doubles as "
+                                 "2-byte codes into a value table)" % ((stream - 16 * D * W) / 1e9) if stream else
+                                 "stored as %d-wide rows in HBM (%.1f GB)" % (info["ell_width"], nnz * 12 / 1e9))
                                 if mode == ae.HAM_STORED else "regenerated on the fly"),
-        "roofline": {"bound": "hbm", "kernel": "k_spmv_sell (H*psi)" if mode == ae.HAM_STORED else "k_otf_strings (H*psi)",
+        "roofline": {"bound": "hbm",
+                     "kernel": ("k_spmv_vell (H*psi, coded rows)" if stream else "k_spmv_sell (H*psi)")
+                     if mode == ae.HAM_STORED else "k_otf_strings (H*psi)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
-                     # DRAM bytes per launch: the ncu count of the 10-orbital launch of this kernel
-                     # (traffic / algorithmic = 1.0066) scaled by nonzeros to this launch
-                     "traffic": hpsi_bytes * SELL_TRAFFIC_RATIO if mode == ae.HAM_STORED else None,
-                     "traffic_source": "profiles/k_spmv_sell_tups10_stored.md (scaled by nonzeros)"
-                     if mode == ae.HAM_STORED else None,
+                     # algorithmic bytes: 12 B per nonzero (FP64 value + int32 column) + x, y
                      "algorithmic_bytes": hpsi_bytes,
+                     # DRAM bytes per launch: the ncu count of the 10-orbital launch of this kernel
+                     # (traffic / streamed bytes) scaled to this launch
+                     "traffic": (stream * VELL_TRAFFIC_RATIO if stream else hpsi_bytes * SELL_TRAFFIC_RATIO)
+                     if mode == ae.HAM_STORED else None,
+                     "traffic_source": ("profiles/k_spmv_vell_tups10_stored.md (scaled by streamed bytes)" if stream
+                                        else "profiles/k_spmv_sell_tups10_stored.md (scaled by nonzeros)")
+                     if mode == ae.HAM_STORED else None,
+                     "stream_bytes": stream, "stream_frac": stream / t_hpsi / 1e9 / peak if stream else None,
+                     "fp64_frac": fw_h / t_hpsi / 1e12 / peak_t if fw_h else None,
+                     "note": "coded rows stream 6 B per double excitation (column + 2-byte code into a value table "
+                             "in shared memory) instead of 12 B, so the kernel moves about half the algorithmic "
+                             "bytes and is bound by the FP64 pipe (fp64_frac); achieved counts the algorithmic "
+                             "bytes" if stream else None,
                      "launch_ms": t_hpsi * 1e3},
         "step_roofline": {"algorithmic_bytes": step_bytes, "achieved_gbs": step_bytes / (ms_step / 1e3) / 1e9,
                           "frac": step_bytes / (ms_step / 1e3) / 1e9 / peak,
