@@ -170,6 +170,11 @@ def lib(build_if_missing=True):
         "getProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, _DP, _P]),
         "getLowestEigenvalue": (ctypes.c_int, [_DP, _DP, _P]),
         "writeProperties": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, ctypes.c_int, ctypes.c_char_p, _P]),
+        "setNumberOfOverlapsToCompute": (ctypes.c_int, [ctypes.c_int, _P]),
+        "aegpu_host_tridiag_lowest_k": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _DP, _DP]),
+        "aegpu_lowest_eigenpairs": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, _DP,
+                                                   _DP, _IP]),
+        "aegpu_ground_overlaps": (ctypes.c_int, [_P, _DP, ctypes.c_int, _DP]),
         "getSubspaceEigenvalues": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _DP, _DP, _IP, _P]),
         # run-file readers (include/aegpu_runfiles.h)
         "aegpu_run_files_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(_P)]),
@@ -388,6 +393,22 @@ class Engine:
         self._check(self.L.aegpu_lowest_eigenpair(self.h, float(tol), int(basis), int(max_products), dptr(lam),
                                                   dptr(res), ctypes.byref(nprod)))
         return lam[0], res[0], nprod.value
+
+    def lowest_eigenpairs(self, nstates, tol=1e-8, basis=100, max_products=20000):
+        """(eigenvalues [nstates], residuals [nstates], H products) of the nstates lowest
+        eigenpairs of H in the sector (every spin symmetry); the eigenvectors stay on the
+        device (ground_overlaps)."""
+        lam, res = np.zeros(nstates), np.zeros(nstates)
+        nprod = ctypes.c_int()
+        self._check(self.L.aegpu_lowest_eigenpairs(self.h, int(nstates), float(tol), int(basis), int(max_products),
+                                                   dptr(lam), dptr(res), ctypes.byref(nprod)))
+        return lam, res, nprod.value
+
+    def ground_overlaps(self, angles_ops, nstates):
+        """<psi(angles)|v_i> for the first nstates eigenvectors held (complex array)."""
+        ov = np.zeros(2 * nstates)
+        self._check(self.L.aegpu_ground_overlaps(self.h, dptr(self._angles(angles_ops)), int(nstates), dptr(ov)))
+        return ov[0::2] + 1j * ov[1::2]
 
     def ground_state(self):
         v = np.zeros(self.D * self.W)
@@ -865,6 +886,14 @@ class stateAnsatzManager:
                                     None if runPath is None else str(runPath).encode(), self.ctx)
         if rc:
             raise AegpuError("writeProperties returned %d" % rc)
+
+    def setNumberOfOverlapsToCompute(self, n):
+        """The reference's numberOfOverlapsToCompute option of writeProperties: overlaps
+        with the n lowest eigenstates when H has fewer than 5,000 rows, else the lowest."""
+        rc = self.L.setNumberOfOverlapsToCompute(int(n), self.ctx)
+        if rc:
+            raise AegpuError("setNumberOfOverlapsToCompute returned %d" % rc)
+        return True
 
     def getLowestEigenvalue(self):
         """(lowest eigenvalue of H in the sector, without the nuclear energy; residual)."""

@@ -1480,6 +1480,7 @@ __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const
                 const size_t base = ell_pos(r, 0, m.qd);
                 const int4 *c4 = reinterpret_cast<const int4 *>(colD + base);
                 const uint2 *k2 = reinterpret_cast<const uint2 *>(codeD + base);
+#pragma unroll 2
                 for (int64_t g = sub; g < m.qd; g += T) {
                     const int4 c = __ldg(c4 + 32 * g);
                     const uint2 k = __ldg(k2 + 32 * g);
@@ -1843,6 +1844,8 @@ struct aegpu_engine {
 
     // lowest eigenpair of H (aegpu_lowest_eigenpair), valid until H is replaced
     double *d_ground = nullptr;
+    int n_ground = 0;       // columns allocated in d_ground
+    int ground_states = 0;  // eigenpairs held there
     // scalar results and dot-product partial sums of the properties pass
     double *d_small = nullptr;
     size_t small_len() const { return 8 + 16 * (size_t)sm_count; }
@@ -3704,18 +3707,32 @@ static double *small_scratch(aegpu_engine *e)
 
 extern "C" {
 
-int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
-                           double *residual, int *products)
+}  // extern "C"
+
+// Lanczos with full reorthogonalisation for the nst lowest eigenpairs of H in the sector,
+// restarted after `basis` products.  nst = 1 starts from the initial state and restarts
+// from the Ritz vector; nst > 1 starts from a seeded pseudo-random real vector (so that
+// eigenstates of every spin symmetry of the sector are present, as in a dense
+// eigensolver) and restarts from the sum of the nst Ritz vectors.  The vectors stay in
+// e->d_ground (nst columns).  Signs: <start|v> > 0, or, where that overlap vanishes, the
+// largest-magnitude entry positive.
+static int lanczos_lowest(aegpu_engine *e, int nst, double tol, int basis, int max_products, double *eigenvalues,
+                          double *residuals, int *products)
 {
-    NvtxRange r("aegpu lowest eigenpair");
-    if (!e || !eigenvalue || !(tol > 0) || basis < 2 || max_products < 2) return AEGPU_ERR_ARG;
+    NvtxRange r("aegpu lowest eigenpairs");
     if (!e->ham_kind) return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
     if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "the ground state needs a batch size of 1");
     const size_t n = e->vec_elems();
-    const int m = (int)std::min<size_t>((size_t)basis, n);
+    if ((size_t)nst > n) return e->fail(AEGPU_ERR_ARG, "more eigenstates than determinants");
+    const int m = (int)std::min<size_t>((size_t)std::max(basis, nst + 1), n);
     if (m + 1 > 4096) return e->fail(AEGPU_ERR_UNSUPPORTED, "Lanczos basis larger than 4095 vectors");
     e->ground_valid = false;
-    if (!e->d_ground && !(e->d_ground = e->alloc<double>(n))) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
+    if (e->n_ground < nst) {
+        if (e->d_ground) e->release(e->d_ground, (size_t)e->n_ground * n * sizeof(double));
+        e->d_ground = e->alloc<double>(n * (size_t)nst);
+        e->n_ground = e->d_ground ? nst : 0;
+        if (!e->d_ground) return e->fail(AEGPU_ERR_NOMEM, "ground state allocation failed");
+    }
     double *sm = small_scratch(e);
     if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
     // basis vectors; reorthogonalisation coefficients, alpha / beta of the recurrence, a
@@ -3741,15 +3758,33 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
         cudaMemcpyAsync(out, d_res, k * sizeof(double), cudaMemcpyDeviceToHost, s);
         return stream_sync(e, "Lanczos");
     };
-    // Lanczos with full reorthogonalisation from the initial state, restarted from the
-    // Ritz vector when the basis is full.  The recurrence runs on the device (alpha and
-    // beta stay in device memory); the host reads them and checks the Ritz pair every
-    // kCheck products.
+    // Lanczos with full reorthogonalisation, restarted when the basis is full.  The
+    // recurrence runs on the device (alpha and beta stay in device memory); the host reads
+    // them and checks the Ritz pairs every kCheck products.
     constexpr int kCheck = 8;
-    cudaMemcpyAsync(e->d_ground, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (nst == 1) {
+        cudaMemcpyAsync(e->d_ground, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    } else {
+        std::vector<double> r0(n);
+        uint64_t st = 0x9e3779b97f4a7c15ull;
+        for (size_t i = 0; i < n; ++i) {
+            st += 0x9e3779b97f4a7c15ull;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+            z ^= z >> 31;
+            // complex mode: imaginary parts zero (H is real, so the eigenvectors stay real)
+            r0[i] = (e->W == 2 && (i & 1)) ? 0.0 : (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        }
+        cudaMemcpyAsync(e->d_ground, r0.data(), n * sizeof(double), cudaMemcpyHostToDevice, s);
+        if (int rc = stream_sync(e, "Lanczos start")) {
+            release();
+            return rc;
+        }
+    }
     int prod = 0, rc = 0;
     bool done = false;
-    std::vector<double> al, be, sv;
+    std::vector<double> al, be, sv, th;
     while (!done) {
         double nx = 0.0;
         e->launches += ae::dot(e->d_ground, e->d_ground, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
@@ -3792,7 +3827,7 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             e->launches += ae::axpby(w, w, ni, 1.0, 0.0, d_beta + j, s);
             const int jn = j + 1;
             if (jn - checked < kCheck && jn < m && prod < max_products && jn < ni) continue;
-            // read alpha / beta so far; the first k at which the Ritz pair converged, or the
+            // read alpha / beta so far; the first k at which the Ritz pairs converged, or the
             // basis is exhausted (beta ~ 0), ends the run
             al.resize(jn);
             be.resize(jn);
@@ -3804,51 +3839,152 @@ int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_produ
             }
             for (int kk = checked + 1; kk <= jn; ++kk) {
                 std::vector<double> a(al.begin(), al.begin() + kk), b(be.begin(), be.begin() + kk);
-                ae::tridiag_lowest(a, b, kk, sv);
                 k = kk;
-                if (std::abs(be[kk - 1] * sv[kk - 1]) <= 0.5 * tol || !(be[kk - 1] > 1e-300)) {
-                    done = true;
-                    break;
+                if (nst == 1) {
+                    ae::tridiag_lowest(a, b, kk, sv);
+                    if (std::abs(be[kk - 1] * sv[kk - 1]) <= 0.5 * tol || !(be[kk - 1] > 1e-300)) {
+                        done = true;
+                        break;
+                    }
+                } else {
+                    ae::tridiag_lowest_k(a, b, kk, nst, th, sv);
+                    bool conv = kk >= nst;
+                    for (int i = 0; conv && i < nst; ++i)
+                        conv = std::abs(be[kk - 1] * sv[(size_t)i * kk + kk - 1]) <= 0.5 * tol;
+                    if (conv || (kk >= nst && !(be[kk - 1] > 1e-300))) {
+                        done = true;
+                        break;
+                    }
                 }
             }
             checked = jn;
             if (prod >= max_products || jn == ni) done = true;
         }
-        // Ritz vector: x = V s over the first k basis vectors (restart vector, or the result)
-        cudaMemcpyAsync(d_c, sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
-        e->launches += gemv_n(Vb, ni, ni, k, d_c, 1.0, 0.0, e->d_ground, s);
+        // Ritz vectors x_i = V s_i over the first k basis vectors (the result, or the
+        // restart vector: x_0, or the sum of the x_i)
+        if (nst == 1) {
+            cudaMemcpyAsync(d_c, sv.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, s);
+            e->launches += gemv_n(Vb, ni, ni, k, d_c, 1.0, 0.0, e->d_ground, s);
+        } else {
+            const int kk = k;
+            std::vector<double> a(al.begin(), al.begin() + kk), b(be.begin(), be.begin() + kk);
+            ae::tridiag_lowest_k(a, b, kk, nst, th, sv);
+            const int got = std::min(nst, kk);
+            for (int i = 0; i < got; ++i) {
+                cudaMemcpyAsync(d_c, sv.data() + (size_t)i * kk, (size_t)kk * sizeof(double), cudaMemcpyHostToDevice, s);
+                e->launches += gemv_n(Vb, ni, ni, kk, d_c, 1.0, 0.0, e->d_ground + (size_t)i * n, s);
+                if ((rc = stream_sync(e, "Lanczos"))) {  // d_c is reused by the next vector
+                    release();
+                    return rc;
+                }
+            }
+            if (got < nst) {
+                release();
+                return e->fail(AEGPU_ERR_STATE, "the Krylov space holds fewer eigenvectors than requested");
+            }
+            if (!done)
+                for (int i = 1; i < nst; ++i)
+                    e->launches += ae::axpby(e->d_ground, e->d_ground + (size_t)i * n, ni, 1.0, 1.0, nullptr, s);
+        }
+        if ((rc = stream_sync(e, "Lanczos"))) {
+            release();
+            return rc;
+        }
     }
-    // unit norm, <start|x> >= 0, and the Rayleigh quotient and true residual
-    double sc[2] = {0.0, 0.0};
-    e->launches += ae::dot(e->d_ground, e->d_ground, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
-    e->launches += ae::dot(e->d_start, e->d_ground, ni, 1, d_res + 1, 0, d_dpart, e->sm_count, s);
-    if ((rc = host_scalars(2, sc))) {
-        release();
-        return rc;
+    // unit norm, the sign convention, and the Rayleigh quotient and true residual
+    for (int i = 0; i < nst; ++i) {
+        double *x = e->d_ground + (size_t)i * n;
+        double sc[2] = {0.0, 0.0};
+        e->launches += ae::dot(x, x, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
+        e->launches += ae::dot(e->d_start, x, ni, 1, d_res + 1, 0, d_dpart, e->sm_count, s);
+        if ((rc = host_scalars(2, sc))) {
+            release();
+            return rc;
+        }
+        double sign = sc[1] < 0 ? -1.0 : 1.0;
+        if (nst > 1 && std::abs(sc[1]) < 1e-12 * sc[0]) {
+            std::vector<double> hx(n);
+            cudaMemcpyAsync(hx.data(), x, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+            if ((rc = stream_sync(e, "Lanczos"))) {
+                release();
+                return rc;
+            }
+            size_t best = 0;
+            for (size_t q = 1; q < n; ++q)
+                if (std::abs(hx[q]) > std::abs(hx[best]) * (1.0 + 1e-12)) best = q;
+            sign = hx[best] < 0 ? -1.0 : 1.0;
+        }
+        e->launches += ae::axpby(x, x, ni, sign / sc[0], 0.0, nullptr, s);
+        double *w = Vb;
+        if ((rc = run_apply(e, x, w, nullptr, 1, nullptr, false))) {
+            release();
+            return rc;
+        }
+        ++prod;
+        double lam = 0.0, res = 0.0;
+        e->launches += ae::dot(x, w, ni, 1, d_res, 0, d_dpart, e->sm_count, s);
+        if ((rc = host_scalars(1, &lam))) {
+            release();
+            return rc;
+        }
+        e->launches += ae::axpby(w, x, ni, 1.0, -lam, nullptr, s);
+        e->launches += ae::dot(w, w, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
+        if ((rc = host_scalars(1, &res))) {
+            release();
+            return rc;
+        }
+        eigenvalues[i] = lam;
+        if (residuals) residuals[i] = res;
+        if (i == 0) e->ground_value = lam;
     }
-    e->launches += ae::axpby(e->d_ground, e->d_ground, ni, (sc[1] < 0 ? -1.0 : 1.0) / sc[0], 0.0, nullptr, s);
-    double *w = Vb;
-    if ((rc = run_apply(e, e->d_ground, w, nullptr, 1, nullptr, false))) {
-        release();
-        return rc;
-    }
-    ++prod;
-    double lam = 0.0, res = 0.0;
-    e->launches += ae::dot(e->d_ground, w, ni, 1, d_res, 0, d_dpart, e->sm_count, s);
-    if ((rc = host_scalars(1, &lam))) {
-        release();
-        return rc;
-    }
-    e->launches += ae::axpby(w, e->d_ground, ni, 1.0, -lam, nullptr, s);
-    e->launches += ae::dot(w, w, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
-    rc = host_scalars(1, &res);
     release();
-    if (rc) return rc;
-    e->ground_value = lam;
+    e->ground_states = nst;
     e->ground_valid = true;
-    *eigenvalue = lam;
-    if (residual) *residual = res;
     if (products) *products = prod;
+    return AEGPU_OK;
+}
+
+extern "C" {
+
+int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
+                           double *residual, int *products)
+{
+    if (!e || !eigenvalue || !(tol > 0) || basis < 2 || max_products < 2) return AEGPU_ERR_ARG;
+    return lanczos_lowest(e, 1, tol, basis, max_products, eigenvalue, residual, products);
+}
+
+int aegpu_lowest_eigenpairs(aegpu_engine *e, int nstates, double tol, int basis, int max_products, double *eigenvalues,
+                            double *residuals, int *products)
+{
+    if (!e || nstates < 1 || !eigenvalues || !(tol > 0) || basis < 2 || max_products < 2) return AEGPU_ERR_ARG;
+    return lanczos_lowest(e, nstates, tol, basis, max_products, eigenvalues, residuals, products);
+}
+
+int aegpu_ground_overlaps(aegpu_engine *e, const double *angles, int nstates, double *overlaps)
+{
+    NvtxRange r("aegpu ground overlaps");
+    if (!e || !angles || !overlaps || nstates < 1) return AEGPU_ERR_ARG;
+    if (e->nb != 1) return e->fail(AEGPU_ERR_UNSUPPORTED, "overlaps need a batch size of 1");
+    if (!e->ground_valid) return e->fail(AEGPU_ERR_STATE, "no ground state: call aegpu_lowest_eigenpairs first");
+    if (nstates > e->ground_states) return e->fail(AEGPU_ERR_ARG, "fewer eigenstates computed than requested");
+    int rc = ensure_state(e, angles);
+    if (rc) return rc;
+    double *sm = small_scratch(e);
+    if (!sm) return e->fail(AEGPU_ERR_NOMEM, "scratch allocation failed");
+    const int64_t D = (int64_t)e->B.D;
+    const size_t n = e->vec_elems();
+    for (int i = 0; i < nstates; ++i) {
+        const double *v = e->d_ground + (size_t)i * n;
+        if (e->W == 1) {
+            e->launches += ae::dot(e->d_psi, v, D, 1, sm, 0, sm + 4, e->sm_count, e->stream);
+            cudaMemsetAsync(sm + 1, 0, sizeof(double), e->stream);
+        } else {
+            // <psi|v> = sum conj(psi) v
+            e->launches += ae::dotc(e->d_psi, v, D, sm, sm + 4, e->sm_count, e->stream);
+        }
+        cudaMemcpyAsync(overlaps + 2 * i, sm, 2 * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+        if ((rc = stream_sync(e, "ground overlaps"))) return rc;
+    }
     return AEGPU_OK;
 }
 

@@ -388,6 +388,16 @@ int writeProperties(int npaths, int nangles, const double *angles, int flags, co
                : 3;
 }
 
+int setNumberOfOverlapsToCompute(int n, void *ctx)
+{
+    if (ctx == nullptr) return 1;
+    auto *m = static_cast<stateAnsatzManager *>(ctx);
+    std::lock_guard<std::mutex> lock(m->m_interfaceLock);
+    if (n <= 0) return 2;
+    m->setNumberOfOverlapsToCompute(n);
+    return 0;
+}
+
 int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx)
 {
     if (ctx == nullptr) return 1;

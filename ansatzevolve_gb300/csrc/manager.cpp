@@ -636,6 +636,7 @@ bool stateAnsatzManager::getLowestEigenvalue(double &eigenvalue, double &residua
     if (!validateToRun()) return false;
     // the Hamiltonian is fixed once constructed: one Lanczos run per tolerance
     if (!m_haveGround || tol < m_groundTol) {
+        m_haveStates = 0;  // the single-state run replaces a k-state one on the device
         int products = 0;
         int rc = aegpu_lowest_eigenpair(m_engine, tol, 100, 100000, &m_groundE, &m_groundRes, &products);
         if (rc) { log_line(std::string("lowest eigenpair failed: ") + aegpu_last_error(m_engine)); return false; }
@@ -646,6 +647,46 @@ bool stateAnsatzManager::getLowestEigenvalue(double &eigenvalue, double &residua
     eigenvalue = m_groundE;
     residual = m_groundRes;
     return true;
+}
+
+bool stateAnsatzManager::setNumberOfOverlapsToCompute(int n)
+{
+    if (n <= 0) {
+        log_line("numberOfOverlapsToCompute must be positive, set to 1");  // main.cpp:182-185
+        n = 1;
+    }
+    m_numberOfOverlaps = n;
+    return true;
+}
+
+bool stateAnsatzManager::getEigenstateOverlaps(const std::vector<std::vector<double>> &paths, int k,
+                                               std::vector<double> &eigenvalues, std::vector<double> &overlaps)
+{
+    if (!validateToRun()) return false;
+    if (m_haveStates < k) {
+        // the k-state run replaces the single ground state on the device
+        std::vector<double> E(k), res(k);
+        int products = 0;
+        int rc = aegpu_lowest_eigenpairs(m_engine, k, 1e-10, std::max(100, 20 * k), 100000, E.data(), res.data(),
+                                         &products);
+        if (rc) { log_line(std::string("lowest eigenpairs failed: ") + aegpu_last_error(m_engine)); return false; }
+        for (int i = 0; i < k; ++i)
+            if (res[i] > 1e-10) log_line("eigenpair " + std::to_string(i) + ": residual " + std::to_string(res[i]) +
+                                         " above the tolerance");
+        m_stateE = E;
+        m_haveStates = k;
+        m_haveGround = false;
+    }
+    eigenvalues.assign(m_stateE.begin(), m_stateE.begin() + k);
+    overlaps.assign(paths.size() * 2 * (size_t)k, 0.0);
+    for (size_t p = 0; p < paths.size(); ++p) {
+        std::vector<double> a;
+        if (!decompress(paths[p], a)) return false;
+        int rc = aegpu_ground_overlaps(m_engine, a.data(), k, &overlaps[p * 2 * k]);
+        if (rc) { log_line(std::string("overlaps failed: ") + aegpu_last_error(m_engine)); return false; }
+    }
+    m_haveEvolved = false;
+    return evolveIfNeeded();
 }
 
 bool stateAnsatzManager::getProperties(const std::vector<std::vector<double>> &paths, int flags, std::vector<double> &table,
@@ -729,9 +770,25 @@ bool stateAnsatzManager::writeProperties(const std::vector<std::vector<double>> 
     if (!validateToRun()) return false;
     std::vector<double> table;
     std::vector<std::vector<double>> H, M;
-    const int flags = (noHess ? 0 : AEGPU_PROP_HESSIAN) | (lowestEigenvalue ? AEGPU_PROP_OVERLAP : 0);
+    // overlaps with more than the lowest eigenstate below 5,000 rows (the reference's dense
+    // eigensolver regime, tupsquantities.cpp:229-276); computed after the table, which
+    // then leaves its own overlap rows out
+    const int64_t D = aegpu_dim(m_engine);
+    const int nov = lowestEigenvalue ? (D < 5000 ? (int)std::min<int64_t>(m_numberOfOverlaps, D) : 1) : 0;
+    const int flags = (noHess ? 0 : AEGPU_PROP_HESSIAN) | (nov == 1 ? AEGPU_PROP_OVERLAP : 0);
     if (!getProperties(paths, flags, table, noHess ? nullptr : &H, noHess ? nullptr : &M)) return false;
     const size_t np = paths.size(), P = (size_t)m_numberOfUniqueParameters;
+    std::vector<double> ovl;  // [path][state][re, im]
+    if (nov == 1) {
+        ovl.assign(np * 2, 0.0);
+        for (size_t k = 0; k < np; ++k) {
+            ovl[2 * k] = table[k * AEGPU_PROPERTY_ROWS + AEGPU_PROP_OVERLAP_RE];
+            ovl[2 * k + 1] = table[k * AEGPU_PROPERTY_ROWS + AEGPU_PROP_OVERLAP_IM];
+        }
+    } else if (nov > 1) {
+        std::vector<double> eigs;
+        if (!getEigenstateOverlaps(paths, nov, eigs, ovl)) return false;
+    }
     if (!noHess && !runPath.empty())
         for (size_t k = 0; k < np; ++k) {
             write_matrix(runPath + "_Path_" + std::to_string(k) + "_Hessian", H[k], P, false);
@@ -755,21 +812,21 @@ bool stateAnsatzManager::writeProperties(const std::vector<std::vector<double>> 
         for (size_t k = 0; k < np; ++k) fprintf(out, "%-*.16g", col, table[k * AEGPU_PROPERTY_ROWS + r]);
         fprintf(out, "\n");
     }
-    if (lowestEigenvalue) {
+    for (int st = 0; st < nov; ++st) {
         std::vector<double> mag(np);
-        fprintf(out, "%-40s", "OverlapWithState_0");
+        fprintf(out, "%-40s", ("OverlapWithState_" + std::to_string(st)).c_str());
         for (size_t k = 0; k < np; ++k) {
-            const double *row = &table[k * AEGPU_PROPERTY_ROWS];
+            const double re = ovl[(k * nov + st) * 2], im = ovl[(k * nov + st) * 2 + 1];
             if (m_complex)
-                fprintf(out, "%-20.16g, %-20.16g", row[AEGPU_PROP_OVERLAP_RE], row[AEGPU_PROP_OVERLAP_IM]);
+                fprintf(out, "%-20.16g, %-20.16g", re, im);
             else
-                fprintf(out, "%-*.16g", col, row[AEGPU_PROP_OVERLAP_RE]);
-            mag[k] = row[AEGPU_PROP_OVERLAP_MAG];
+                fprintf(out, "%-*.16g", col, re);
+            mag[k] = std::hypot(re, im);
         }
-        fprintf(out, "\n%-40s", "MagOfOverlapWithState_0");
+        fprintf(out, "\n%-40s", ("MagOfOverlapWithState_" + std::to_string(st)).c_str());
         for (double v : mag) fprintf(out, "%-*.16g", col, v);
         fprintf(out, "\n");
-        if (!runPath.empty()) write_vector(runPath + "_MagOfOverlapWithGroundState_0", mag);
+        if (!runPath.empty()) write_vector(runPath + "_MagOfOverlapWithGroundState_" + std::to_string(st), mag);
     }
     fflush(out);
     return true;

@@ -86,6 +86,16 @@ public:
                          bool haveHF, const std::string &runPath, FILE *out = nullptr);
     // Lowest eigenvalue of H in the sector (electronic, without the nuclear energy).
     bool getLowestEigenvalue(double &eigenvalue, double &residual, double tol = 1e-10);
+    // The reference's TUPSQuantitiesOptions::numberOfOverlapsToCompute (tupsquantities.h:22,
+    // the CLI's option, main.cpp:181-185): writeProperties reports the overlaps with the
+    // n lowest eigenstates when H has fewer than 5,000 rows (at most its row count), else
+    // with the lowest one only (tupsquantities.cpp:229-276).
+    bool setNumberOfOverlapsToCompute(int n);
+    int numberOfOverlapsToCompute() const { return m_numberOfOverlaps; }
+    // The k lowest eigenvalues of H in the sector (every spin symmetry of the sector) and
+    // the overlaps <psi(path)|v_i> (re, im per state) for each path.
+    bool getEigenstateOverlaps(const std::vector<std::vector<double>> &paths, int k, std::vector<double> &eigenvalues,
+                               std::vector<double> &overlaps);
     // TUPSQuantities::doSubspaceDiagonalisation (tupsquantities.cpp:1600-1700).
     bool getSubspaceEigenvalues(const std::vector<std::vector<double>> &paths, std::vector<double> &eigenvalues,
                                 int &nullRank);
@@ -135,6 +145,9 @@ private:
     bool m_haveEvolved = false;
     bool m_haveGround = false;             // lowest eigenpair computed (kept on the device)
     double m_groundE = 0, m_groundRes = 0, m_groundTol = 0;
+    int m_numberOfOverlaps = 1;
+    int m_haveStates = 0;                  // eigenpairs of the k-state run kept on the device
+    std::vector<double> m_stateE;
 };
 
 void log_line(const std::string &s);

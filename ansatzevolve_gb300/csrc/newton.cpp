@@ -72,6 +72,71 @@ void sym_eig(int n, const std::vector<double> &A_in, std::vector<double> &w, std
 // off-diagonal b[0..k-2]: the eigenvalue by Sturm-sequence bisection, the unit
 // eigenvector by inverse iteration with the LDL^T factors of the shifted matrix, which
 // the shift just below the eigenvalue keeps positive definite.
+void tridiag_lowest_k(const std::vector<double> &a, const std::vector<double> &b, int k, int nev,
+                      std::vector<double> &theta, std::vector<double> &V)
+{
+    // eigenvalue j by bisection on the Sturm count (below(x) = eigenvalues below x),
+    // its vector by shifted inverse iteration, orthogonalised against the earlier ones
+    // (close eigenvalues give nearly parallel iterates otherwise)
+    nev = std::min(nev, k);
+    double lo0 = a[0], hi0 = a[0], scale = 0.0;
+    for (int i = 0; i < k; ++i) {
+        const double r = (i > 0 ? std::abs(b[i - 1]) : 0.0) + (i + 1 < k ? std::abs(b[i]) : 0.0);
+        lo0 = std::min(lo0, a[i] - r);
+        hi0 = std::max(hi0, a[i] + r);
+        scale = std::max(scale, std::abs(a[i]) + r);
+    }
+    const double tiny = std::max(scale, 1e-300) * 1e-300;
+    auto below = [&](double x) {
+        int c = 0;
+        double q = a[0] - x;
+        for (int i = 0;; ++i) {
+            if (q < 0) ++c;
+            if (i + 1 == k) break;
+            if (std::abs(q) < tiny) q = -tiny;
+            q = a[i + 1] - x - b[i] * b[i] / q;
+        }
+        return c;
+    };
+    theta.assign(nev, 0.0);
+    V.assign((size_t)nev * k, 0.0);
+    for (int j = 0; j < nev; ++j) {
+        double lo = lo0, hi = hi0;
+        for (int it = 0; it < 2100 && hi - lo > 4e-16 * std::max(std::abs(lo), std::abs(hi)); ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (mid <= lo || mid >= hi) break;
+            if (below(mid) >= j + 1) hi = mid; else lo = mid;
+        }
+        theta[j] = 0.5 * (lo + hi);
+        const double sigma = theta[j] - std::max(scale, 1e-300) * 1e-13;
+        std::vector<double> d(k), l(k, 0.0);
+        d[0] = a[0] - sigma;
+        for (int i = 1; i < k; ++i) {
+            l[i] = b[i - 1] / (std::abs(d[i - 1]) < tiny ? tiny : d[i - 1]);
+            d[i] = a[i] - sigma - l[i] * b[i - 1];
+        }
+        for (int i = 0; i < k; ++i)
+            if (std::abs(d[i]) < tiny) d[i] = tiny;
+        double *v = &V[(size_t)j * k];
+        for (int i = 0; i < k; ++i) v[i] = 1.0 / std::sqrt((double)k) * ((i + j) % 2 ? -1.0 : 1.0);
+        for (int it = 0; it < 4; ++it) {
+            for (int i = 1; i < k; ++i) v[i] -= l[i] * v[i - 1];
+            for (int i = 0; i < k; ++i) v[i] /= d[i];
+            for (int i = k - 2; i >= 0; --i) v[i] -= l[i + 1] * v[i + 1];
+            for (int q = 0; q < j; ++q) {
+                const double *u = &V[(size_t)q * k];
+                double c = 0.0;
+                for (int i = 0; i < k; ++i) c += u[i] * v[i];
+                for (int i = 0; i < k; ++i) v[i] -= c * u[i];
+            }
+            double nv = 0.0;
+            for (int i = 0; i < k; ++i) nv += v[i] * v[i];
+            nv = std::sqrt(nv);
+            for (int i = 0; i < k; ++i) v[i] /= nv;
+        }
+    }
+}
+
 double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int k, std::vector<double> &v)
 {
     double lo = a[0], hi = a[0], scale = 0.0;

@@ -25,6 +25,10 @@ void sym_eig(int n, const std::vector<double> &A, std::vector<double> &w, std::v
 // Lowest eigenvalue (returned) and unit eigenvector v of the symmetric tridiagonal
 // matrix with diagonal a[0..k-1] and off-diagonal b[0..k-2].
 double tridiag_lowest(const std::vector<double> &a, const std::vector<double> &b, int k, std::vector<double> &v);
+// The nev lowest eigenvalues (ascending) and unit eigenvectors V[j * k + i] of the same
+// matrix.
+void tridiag_lowest_k(const std::vector<double> &a, const std::vector<double> &b, int k, int nev,
+                      std::vector<double> &theta, std::vector<double> &V);
 bool optimise_newton(NewtonProblem &p, std::vector<double> &theta, NewtonStats &st, bool verbose);
 
 // The projected iteration (TUPSQuantities::iterativeTups, tupsquantities.cpp:2044-2145,

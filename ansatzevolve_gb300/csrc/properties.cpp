@@ -132,6 +132,16 @@ int aegpu_host_tridiag_lowest(int k, const double *a, const double *b, double *v
     return AEGPU_OK;
 }
 
+int aegpu_host_tridiag_lowest_k(int k, int nev, const double *a, const double *b, double *theta, double *V)
+{
+    if (k < 1 || nev < 1 || nev > k || !a || (k > 1 && !b) || !theta || !V) return AEGPU_ERR_ARG;
+    std::vector<double> av(a, a + k), bv(b ? b : a, b ? b + (k - 1) : a), th, vv;
+    ae::tridiag_lowest_k(av, bv, k, nev, th, vv);
+    std::copy(th.begin(), th.end(), theta);
+    std::copy(vv.begin(), vv.end(), V);
+    return AEGPU_OK;
+}
+
 int aegpu_subspace_eigenvalues(aegpu_engine *e, int nsets, const double *angles, double *eigenvalues, int *null_rank)
 {
     if (!e || nsets < 1 || !angles || !eigenvalues) return AEGPU_ERR_ARG;

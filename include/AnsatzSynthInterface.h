@@ -96,6 +96,12 @@ int getLowestEigenvalue(double *eigenvalue, double *residual, void *ctx);
  * the metric as .CMatbin / .CMatcsv) and <runPath>_MagOfOverlapWithGroundState_0
  * (.Vecbin / .Veccsv / .ColVeccsv); flags as getProperties plus AEGPU_PROP_HF_PATH. */
 int writeProperties(int npaths, int nangles, const double *angles, int flags, const char *runPath, void *ctx);
+/* setNumberOfOverlapsToCompute: the reference's numberOfOverlapsToCompute option
+ * (TUPSQuantitiesOptions, tupsquantities.h:22; CLI main.cpp:181-185): writeProperties then
+ * reports OverlapWithState_i / MagOfOverlapWithState_i for the n lowest eigenstates of H
+ * when H has fewer than 5,000 rows (at most its row count), else for the lowest only.
+ * 1 null context, 2 n < 1. */
+int setNumberOfOverlapsToCompute(int n, void *ctx);
 int getSubspaceEigenvalues(int npaths, int nangles, const double *angles, double *eigenvalues, int *nullRank,
                            void *ctx);
 

@@ -148,6 +148,21 @@ int aegpu_hessian_metric(aegpu_engine *e, const double *angles, const int *param
  * compare the residual with tol. */
 int aegpu_lowest_eigenpair(aegpu_engine *e, double tol, int basis, int max_products, double *eigenvalue,
                            double *residual, int *products);
+/* The nstates lowest eigenpairs (eigenvalues ascending; residuals nullable), for the
+ * overlaps with several eigenstates that writeProperties reports
+ * (TUPSQuantitiesOptions::numberOfOverlapsToCompute, tupsquantities.cpp:229-276, where the
+ * reference takes every eigenvector of a dense H below 5,000 rows).  The same Lanczos
+ * iteration as aegpu_lowest_eigenpair, but started from a seeded pseudo-random real vector so
+ * that eigenstates of every spin symmetry of the sector appear in their order, restarted
+ * from the sum of the Ritz vectors, converged when every one of the nstates residual
+ * estimates is below tol / 2.  The eigenvectors replace the one of aegpu_lowest_eigenpair
+ * on the device (state 0 is then the lowest of all symmetries).  Signs: <start|v> > 0, or
+ * the largest-magnitude entry positive where that overlap vanishes. */
+int aegpu_lowest_eigenpairs(aegpu_engine *e, int nstates, double tol, int basis, int max_products, double *eigenvalues,
+                            double *residuals, int *products);
+/* <psi(angles)|v_i> for the first nstates eigenvectors held: overlaps[2 i] real part,
+ * overlaps[2 i + 1] imaginary part. */
+int aegpu_ground_overlaps(aegpu_engine *e, const double *angles, int nstates, double *overlaps);
 /* The eigenvector, D*(1+complex) doubles in sector order. */
 int aegpu_ground_state(aegpu_engine *e, double *state);
 /* <psi(angles)|v>: overlap[0] real part, overlap[1] imaginary part. */
@@ -301,6 +316,9 @@ int aegpu_state_dev(aegpu_engine *e, const double **psi, const double **hpsi);
 /* Host-only (no GPU): the lowest eigenpair of a symmetric tridiagonal matrix
  * (diagonal a[k], off-diagonal b[k-1]) as aegpu_lowest_eigenpair's Lanczos step solves it. */
 int aegpu_host_tridiag_lowest(int k, const double *a, const double *b, double *v, double *theta);
+/* Host-only: the nev lowest eigenpairs of the same matrix as aegpu_lowest_eigenpairs solves
+ * it: theta[nev] ascending, V[j * k + i] the unit eigenvectors. */
+int aegpu_host_tridiag_lowest_k(int k, int nev, const double *a, const double *b, double *theta, double *V);
 /* Host-only: the eigen-analysis of aegpu_subspace_eigenvalues on given matrices
  * (row-major nsets x nsets real / imaginary parts; the imaginary parts may be NULL). */
 int aegpu_host_subspace_eigenvalues(int nsets, const double *h_re, const double *h_im, const double *s_re,

@@ -27,6 +27,7 @@
 //   properties <prefix>                  (TUPSQuantities::writeProperties over the zero
 //                                         path + the angle sets; its table goes to
 //                                         <prefix>_table.txt, its matrices to <prefix>_Path_*)
+//   overlaps k                           (with properties: numberOfOverlapsToCompute)
 //   subspace n                           (with properties: doSubspaceDiagonalisation of
 //                                         the first n angle sets; printed on stderr)
 //   end
@@ -75,7 +76,7 @@ int main(int argc, char **argv)
     int wantE = 1, wantG = 1, wantH = 0, wantS = 0, wantPairs = 0, wantOpt = 0, timeK = 0, timeWarm = 1;
     double timeBudget = 0.0;
     std::string propsPrefix, pairsPath;
-    int subspaceN = 0;
+    int subspaceN = 0, overlapsK = 1;
 
     std::string tok;
     while (in >> tok) {
@@ -116,6 +117,7 @@ int main(int argc, char **argv)
         else if (tok == "timebudget") in >> timeBudget;
         else if (tok == "properties") in >> propsPrefix;
         else if (tok == "subspace") in >> subspaceN;
+        else if (tok == "overlaps") in >> overlapsK;
         else if (tok == "end") break;
         else { fprintf(stderr, "bad token %s\n", tok.c_str()); return 2; }
     }
@@ -270,6 +272,7 @@ int main(int argc, char **argv)
                 paths.back()[i].second = a0.size() == excs.size() ? a0[i] : a0[order[i].first] * order[i].second;
         }
         TUPSQuantitiesOptions opts;
+        opts.numberOfOverlapsToCompute = overlapsK;
         q.writeProperties(nullptr, FE, paths, opts);
         fclose(table);
         if (subspaceN > 0) q.doSubspaceDiagonalisation(nullptr, FE, (size_t)subspaceN, paths);

@@ -21,6 +21,9 @@ Sources of the inputs:
   lucj14   -- the complex LUCJ circuit exp(-K) exp(iJ) exp(K) at 14 orbitals (K, J of
               ansatzevolve_gb300.lucj.random_lucj(14, 3), integrals of seed 7), every
               operator its own parameter: E, gradient, sampled final-state amplitudes
+  overlaps_syn6, overlaps_h4c
+           -- writeProperties with numberOfOverlapsToCompute = 4 / 3 over the zero path and
+              the syn6 / h4c angle sets: overlaps with the lowest eigenstates
   pairs12  -- the excitation rule of every operator of the 12-orbital, 3-layer TUPS circuit
               over every determinant of the 6a+6b sector: SHA-256 digests of the partner
               bitstrings and signs, active counts and a seeded sample of raw entries
@@ -30,8 +33,8 @@ Sources of the inputs:
               with the lowest eigenvector), its Hessian and metric matrices per path, and
               doSubspaceDiagonalisation's eigenvalues, over the zero path and the angle
               sets of the h4 / h4c / syn6 inputs plus a repeat of the first set
-Only the ref10 / ref12 / ref14 / lucj14 / pairs12 / props_* cases can be regenerated alone:
-    python tests/golden/make_golden.py ref10 ref12 ref14 lucj14 pairs12 props_h4 props_h4c props_syn6
+Only the ref10 / ref12 / ref14 / lucj14 / pairs12 / overlaps_* / props_* cases can be regenerated alone:
+    python tests/golden/make_golden.py ref10 ref12 ref14 lucj14 pairs12 overlaps_syn6 overlaps_h4c props_h4 props_h4c props_syn6
 The reference checkout is AE_REFERENCE (default: a `reference` directory beside this
 repository).
 """
@@ -237,6 +240,67 @@ PROPERTY_ROWS = ("Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
                  "NormOfGradVector", "OverlapWithState_0", "MagOfOverlapWithState_0")
 
 
+def table_floats(text):
+    """The numbers of one printed table row.  The complex rows print "%-20.16g, %-20.16g"
+    per path, which runs two numbers together when the first fills its width
+    ("4.1e-161.2e-15"): such a token is split after the first number's exponent (%g
+    writes at least two exponent digits)."""
+    out = []
+    for t in text.replace(",", " ").split():
+        try:
+            out.append(float(t))
+            continue
+        except ValueError:
+            pass
+        m = re.match(r"^([-+]?[0-9.]+e[-+][0-9]{2})([-+]?[0-9.].*)$", t)
+        if not m:
+            raise ValueError("cannot read %r" % t)
+        out += [float(m.group(1)), float(m.group(2))]
+    return out
+
+
+def overlaps_case(tag, base, k, cplx=False):
+    """The reference's writeProperties with numberOfOverlapsToCompute = k over the zero
+    path and the angle sets of fixture `base` (below 5,000 rows: overlaps with the k
+    lowest eigenvectors of the dense H): OverlapWithState_i and MagOfOverlapWithState_i
+    for i < k per path (eigenvector signs are the reference eigensolver's own)."""
+    fx = dict(np.load(os.path.join(OUT, base + ".npz")))
+    if base.startswith("syn"):
+        N = int(fx["N"])
+        h1, g2 = synthetic_integrals(N, int(fx["seed"]))
+        nq, init, nuclear = 2 * N, [(int(fx["hf"]), 1.0, 0.0)], 0.0
+    else:
+        h1, g2 = fx["h1"], fx["g2"]
+        nq, nuclear = int(fx["nq"]), float(fx["nuclear"])
+        init = [(int(i), float(r), float(m)) for i, r, m in
+                zip(fx["init_idx"], fx["init_re"], fx.get("init_im", np.zeros(len(fx["init_idx"]))))]
+    sets = [np.asarray(a) for a in fx["angles"]]
+    with tempfile.TemporaryDirectory() as td:
+        prefix = os.path.join(td, "p")
+        write_integrals(prefix, h1, g2)
+        sp = spec(nq, init, np.asarray(fx["ops_1b"]) - 1, np.asarray(fx["order_1b"]) - 1, fx["scale"],
+                  [f"ham ints {prefix}"], sets, want=(1, 0, 0, 0), nuclear=nuclear)
+        sp += [f"properties {prefix}", f"overlaps {k}"]
+        sf, of = os.path.join(td, "spec"), os.path.join(td, "out")
+        open(sf, "w").write("\n".join(sp) + "\nend\n")
+        subprocess.run([DRV + ("_cplx" if cplx else ""), sf, of], check=True, capture_output=True, text=True,
+                       env=dict(os.environ, OMP_NUM_THREADS="4"))
+        npath = len(sets) + 1
+        ov = np.zeros((k, npath), dtype=complex)
+        mag = np.zeros((k, npath))
+        for ln in open(prefix + "_table.txt").read().splitlines():
+            name = ln[:40].strip()
+            for i in range(k):
+                vals = None
+                if name == f"OverlapWithState_{i}":
+                    vals = table_floats(ln[40:])
+                    ov[i] = np.array(vals[0::2]) + 1j * np.array(vals[1::2]) if cplx else np.array(vals)
+                elif name == f"MagOfOverlapWithState_{i}":
+                    mag[i] = table_floats(ln[40:])
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), base=base, k=k, sets=np.array(sets), overlap=ov, mag=mag)
+    print(tag, np.round(mag, 6))
+
+
 def properties_case(tag, base, cplx=False):
     """writeProperties + doSubspaceDiagonalisation of the reference over the zero path,
     the angle sets of fixture `base` and a repeat of its first set (a rank-deficient
@@ -405,6 +469,8 @@ if __name__ == "__main__":
         "ref14": lambda: large_case("ref14", 14, 7, 7, 4, 0, hess=False),
         "lucj14": lambda: lucj_case("lucj14", 14, 7, 3, 7),
         "pairs12": lambda: pairs_case("pairs12", 12, 6, 6, 3),
+        "overlaps_syn6": lambda: overlaps_case("overlaps_syn6", "syn6", 4),
+        "overlaps_h4c": lambda: overlaps_case("overlaps_h4c", "h4c", 3, cplx=True),
     }
     if len(sys.argv) > 1:
         for t in sys.argv[1:]:
@@ -420,6 +486,8 @@ if __name__ == "__main__":
     synthetic_case("syn6", 6, 3, 3, 2, 3, pairs=True)
     synthetic_case("syn8", 8, 4, 4, 2, 0)
     for t in ("ref10", "ref12", "ref14", "lucj14", "pairs12"):
+        single[t]()
+    for t in ("overlaps_syn6", "overlaps_h4c"):
         single[t]()
     properties_case("props_h4", "h4")
     properties_case("props_h4c", "h4c", cplx=True)

@@ -67,8 +67,11 @@ def test_extension_status_codes():
     assert L.iterativeOptimise(4, dptr(a), dptr(a), None) == 1
     assert L.generatePathsForSubspace(2, dptr(a), ctypes.byref(nr), dptr(a), None) == 1
     assert L.writeProperties(1, 4, dptr(a), 3, None, None) == 1
+    assert L.setNumberOfOverlapsToCompute(2, None) == 1
     ctx = ctypes.c_void_p(L.init())
     try:
+        assert L.setNumberOfOverlapsToCompute(0, ctx) == 2
+        assert L.setNumberOfOverlapsToCompute(3, ctx) == 0
         assert L.getGradient(0, dptr(a), dptr(a), ctx) == 2
         assert L.getHessian(4, None, dptr(a), ctx) == 2
         assert L.getExpectationValues(0, 4, dptr(a), dptr(a), ctx) == 2

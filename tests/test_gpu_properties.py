@@ -257,3 +257,55 @@ def test_writeproperties_files(golden, tmp_path, capfd, name):
     mag = np.fromfile(prefix + "_MagOfOverlapWithGroundState_0.Vecbin")
     np.testing.assert_allclose(mag, px["rows"][14], atol=1e-9, rtol=0)
     assert open(prefix + "_MagOfOverlapWithGroundState_0.ColVeccsv").read().count("\n") == len(mag)
+
+
+@pytest.mark.parametrize("tag", ["overlaps_syn6", "overlaps_h4c"])
+def test_overlaps_with_several_eigenstates_match_reference(golden, tag):
+    """The overlaps of every path with the k lowest eigenstates of H (the reference's
+    numberOfOverlapsToCompute, from its dense eigensolver): magnitudes at 1e-9, values up
+    to one sign per eigenstate (the eigensolvers choose signs independently).  States of
+    another spin symmetry than the paths (zero overlap) must appear in their place in the
+    spectrum, so the Lanczos has to find them too."""
+    e, paths, p0, scale, nuclear, px = engine_for(golden, tag)
+    k = int(px["k"])
+    lam, res, nprod = e.lowest_eigenpairs(k, tol=1e-11, basis=200)
+    assert np.all(res < 1e-10), res
+    assert np.all(np.diff(lam) > 1e-8)
+    got = np.array([e.ground_overlaps(scale * x[p0], k) for x in paths]).T  # [state][path]
+    np.testing.assert_allclose(np.abs(got), px["mag"], atol=1e-9, rtol=0)
+    for i in range(k):
+        ref = px["overlap"][i]
+        j = int(np.argmax(np.abs(ref)))
+        if abs(ref[j]) < 1e-8:
+            continue
+        sgn = np.sign((ref[j] / got[i][j]).real)
+        np.testing.assert_allclose(sgn * got[i], ref, atol=1e-9, rtol=0)
+    # the single-state entry point afterwards still gives the lowest eigenpair
+    lam1, res1, _ = e.lowest_eigenpair(tol=1e-11)
+    assert abs(lam1 - lam[0]) < 1e-9 or abs(px["mag"][0]).max() < 1e-8
+    e.close()
+
+
+def test_writeproperties_number_of_overlaps(golden, tmp_path, capfd):
+    """The manager's writeProperties with setNumberOfOverlapsToCompute(4): one
+    OverlapWithState_i / MagOfOverlapWithState_i row pair and one
+    _MagOfOverlapWithGroundState_i file per state, equal to the reference's."""
+    px = golden("overlaps_syn6")
+    fx = golden("syn6")
+    pb = synthetic_problem(int(fx["N"]), int(fx["na"]), int(fx["nb"]), int(fx["layers"]), int(fx["seed"]))
+    m = ae.stateAnsatzManager()
+    assert m.storeInitial(pb["nq"], [pb["hf"]], [1.0])
+    assert m.storeOperators(np.asarray(fx["ops_1b"]).tolist())
+    assert m.storeParameterDependencies(list(zip(np.asarray(fx["order_1b"]) - 1, fx["scale"])))
+    assert m.storeIntegrals(pb["h1"], pb["g2"], ae.HAM_STORED)
+    assert m.setNumberOfOverlapsToCompute(4)
+    P = int(np.asarray(fx["order_1b"]).max())
+    paths = np.vstack([np.zeros(P)] + list(px["sets"]))
+    prefix = str(tmp_path / "syn6")
+    m.writeProperties(paths, runPath=prefix, hessian=False)
+    out = capfd.readouterr().out
+    for i in range(4):
+        assert "OverlapWithState_%d " % i in out and "MagOfOverlapWithState_%d " % i in out
+        mag = np.fromfile("%s_MagOfOverlapWithGroundState_%d.Vecbin" % (prefix, i))
+        np.testing.assert_allclose(mag, px["mag"][i], atol=1e-9, rtol=0)
+    m.close()

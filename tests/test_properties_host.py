@@ -119,3 +119,25 @@ def test_pulay_with_rank_deficient_errors():
     c = np.zeros(4)
     assert lib().aegpu_host_diis_coefficients(4, dptr(np.ascontiguousarray(B)), 0, dptr(c)) == 0
     np.testing.assert_allclose(c, pulay(B), atol=1e-9, rtol=0)
+
+
+def test_tridiagonal_lowest_eigenpairs_match_numpy():
+    """The k lowest eigenpairs of symmetric tridiagonal matrices (the Ritz step of the
+    multi-state Lanczos): eigenvalues and eigenvectors (up to sign) against numpy, with a
+    close pair of eigenvalues among them."""
+    from ansatzevolve_gb300 import dptr, lib
+    rng = np.random.default_rng(3)
+    for k, nev in [(1, 1), (5, 3), (40, 6), (200, 4)]:
+        a = rng.normal(size=k)
+        b = rng.normal(size=max(k - 1, 1))[: k - 1] if k > 1 else np.zeros(1)
+        if k >= 40:
+            a[:2] = [-5.0, -5.0 + 1e-7]
+            b[0] = 1e-9
+        T = np.diag(a) + (np.diag(b, 1) + np.diag(b, -1) if k > 1 else 0)
+        w, V = np.linalg.eigh(T)
+        th, Vk = np.zeros(nev), np.zeros(nev * k)
+        assert lib().aegpu_host_tridiag_lowest_k(k, nev, dptr(a), dptr(b), dptr(th), dptr(Vk)) == 0
+        np.testing.assert_allclose(th, w[:nev], atol=1e-12 * max(1.0, np.abs(w).max()), rtol=0)
+        Vk = Vk.reshape(nev, k)
+        for j in range(nev):
+            np.testing.assert_allclose(np.abs(Vk[j] @ V[:, j]), 1.0, atol=1e-8)
