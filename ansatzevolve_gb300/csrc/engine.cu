@@ -8,9 +8,10 @@
 //   orbit tables       per pass: uint32 ranks and bitstrings of every touched
 //                      determinant, grouped into orbits (hypercubes of the active
 //                      excitations), plus group/tile/warp-task descriptors (setup.cpp)
-//   Hamiltonian        CSR (general), sliced-ELL rows built from integrals, or the
-//                      string tables of the on-the-fly product (one set per instance
-//                      for a Hamiltonian family)
+//   Hamiltonian        CSR (general), coded sliced rows built from integrals (the
+//                      doubles as 2-byte codes into a value table; uncoded sliced rows
+//                      above 12 orbitals), or the string tables of the on-the-fly
+//                      product (one set per instance for a Hamiltonian family)
 //   Hessian scratch    per-operator tangents FP64[nops][D*W], compressed tangents
 //                      and H*tangents column-major [P+1][D*W]
 //
@@ -31,15 +32,18 @@
 //   k_pass_prep      per evaluation: sin/cos and the scaled-Givens constants of every
 //                    pass and direction, and the scale products of every active mask
 //   k_spmv           warp-per-row CSR y = H x fused with the <x|y> partial sums
-//   k_spmv_sell      sliced-ELL y = H x (1-8 threads per row) fused with <x|y>; the
-//                    Hessian applies it to its P+1 compressed tangents as a batch
-//   k_ell_build      fixed-width rows of H generated from h_pq/(pq|rs): diagonal,
+//   k_spmv_vell      y = H x over coded rows (value table in shared memory, 1-8
+//                    threads per row, equal row shares per CTA) fused with <x|y>; with
+//                    several right-hand sides per thread for the Hessian's tangents
+//   k_spmv_sell      the same over uncoded sliced rows
+//   k_vtab_build, k_vell_build, k_ell_build
+//                    value table and rows of H generated from h_pq/(pq|rs): diagonal,
 //                    alpha/beta singles, alpha-alpha/beta-beta/alpha-beta doubles
 //   k_otf_strings    y = H x with no stored matrix: CTA per alpha string, thread per
 //                    determinant, one FP64 FMA per matrix element (otf_tables.cpp)
-//   k_lanczos_update, k_scale_inverse, k_dot_partial, k_dot_finish
-//                    the device side of the Lanczos recurrence for the lowest eigenpair
-//                    (alpha and beta stay in device memory between the H products)
+//   k_lanczos_update the three-term step of the Lanczos recurrence (alpha and beta stay
+//                    in device memory; the dot products, norms and the basis products
+//                    of the reorthogonalisation are the kernels of dense.cu)
 // All reductions are two-stage and in a fixed order, so results are bit-identical
 // from run to run.
 #include "../../include/aegpu.h"
