@@ -411,6 +411,7 @@ def batched_bench(stream, steps=10, warmup=3):
     setup_s = time.perf_counter() - t0
     grp = ae.Group(engines)
     sp = stream.cuda_stream
+    peak_t = ae.fp64_peak() / 2.0  # T DFMA/s
     for _ in range(warmup):
         grp.launch(sp)
     torch.cuda.synchronize()
@@ -432,8 +433,16 @@ def batched_bench(stream, steps=10, warmup=3):
         torch.cuda.synchronize()
         pc["ms_per_batch"] = a.elapsed_time(b) / 3
         pc["evals_per_s"] = pc["instances"] / (pc["ms_per_batch"] / 1e3)
+        # the class against the FP64 pipe: FP64 instructions of its evaluations (one DFMA
+        # per matrix element, per amplitude-layer forward, two adjoint) over the measured
+        # DFMA rate
+        fw = sum(e.fp64_work())
+        pc["fp64_instr_per_batch"] = int(fw * pc["instances"])
+        pc["fp64_frac"] = fw * pc["instances"] / (pc["ms_per_batch"] / 1e3) / 1e12 / peak_t
     E, g = engines[0].io_get_results()
+    fp64_all = sum(pc["fp64_instr_per_batch"] for pc in per_class)
     out = {"value": 512 / (ms / 1e3), "unit": "instance energy+gradient evals/s", "instances": 512,
+           "fp64_frac": fp64_all / (ms / 1e3) / 1e12 / peak_t, "fp64_peak_T_per_s": peak_t,
            "ms_per_step": ms, "steps": steps, "warmup": warmup, "graph_launches_per_step": 1,
            "gpu_launches_per_step": grp.launch_count(), "classes": per_class, "setup_s": setup_s,
            "finite": bool(np.all(np.isfinite(E)) and np.all(np.isfinite(g)))}

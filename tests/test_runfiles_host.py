@@ -20,7 +20,9 @@ from ansatzevolve_gb300.runfiles import (load_run_files, write_extracted_min, wr
                                          write_run_files)
 from ansatzevolve_gb300.checkpoint import write_parameters
 
-REF = os.environ.get("AE_REFERENCE", "/root/reference")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+# the reference checkout (only its Hams/ fixtures are read; tests skip without it)
+REF = os.environ.get("AE_REFERENCE") or os.path.join(os.path.dirname(ROOT), "reference")
 
 
 def _case(tmp_path, **kw):
