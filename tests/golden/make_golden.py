@@ -24,6 +24,8 @@ Sources of the inputs:
   overlaps_syn6, overlaps_h4c
            -- writeProperties with numberOfOverlapsToCompute = 4 / 3 over the zero path and
               the syn6 / h4c angle sets: overlaps with the lowest eigenstates
+  batched4 -- instance 0 of each size class of the benchmark's batched launch (8, 10, 12
+              orbitals, its own integrals and angles): energy and gradient
   pairs12  -- the excitation rule of every operator of the 12-orbital, 3-layer TUPS circuit
               over every determinant of the 6a+6b sector: SHA-256 digests of the partner
               bitstrings and signs, active counts and a seeded sample of raw entries
@@ -33,8 +35,8 @@ Sources of the inputs:
               with the lowest eigenvector), its Hessian and metric matrices per path, and
               doSubspaceDiagonalisation's eigenvalues, over the zero path and the angle
               sets of the h4 / h4c / syn6 inputs plus a repeat of the first set
-Only the ref10 / ref12 / ref14 / lucj14 / pairs12 / overlaps_* / props_* cases can be regenerated alone:
-    python tests/golden/make_golden.py ref10 ref12 ref14 lucj14 pairs12 overlaps_syn6 overlaps_h4c props_h4 props_h4c props_syn6
+Only the ref10 / ref12 / ref14 / lucj14 / pairs12 / overlaps_* / batched4 / props_* cases can be regenerated alone:
+    python tests/golden/make_golden.py ref10 ref12 ref14 lucj14 pairs12 overlaps_syn6 overlaps_h4c batched4 props_h4 props_h4c props_syn6
 The reference checkout is AE_REFERENCE (default: a `reference` directory beside this
 repository).
 """
@@ -238,6 +240,34 @@ PROPERTY_ROWS = ("Elec. Energy", "Real Elec. Energy", "Elec. + Nuc. Energy",
                  "NumberOfNearZeroHessianDiagValues", "NumberOfPositiveHessianDiagValues",
                  "NumberOfPositiveMetricEValues", "NumberOfZeroMetricEValues", "NumberOfZeroMetricDiagonalValues",
                  "NormOfGradVector", "OverlapWithState_0", "MagOfOverlapWithState_0")
+
+
+def batched_case(tag):
+    """Configuration 4's batched instances against the reference: instance 0 of each size
+    class of the benchmark's 512-instance launch -- 8 orbitals (4a+4b, 2 layers, integral
+    seed 0), 10 (5a+5b, 3 layers, seed 256), 12 (6a+6b, 3 layers, seed 448) -- with the
+    bench's own per-operator angles (default_rng(0).uniform(-0.3, 0.3) drawn class by
+    class, [instances, operators]): energy and compressed gradient."""
+    classes = [(8, 4, 2, 256, 0), (10, 5, 3, 192, 256), (12, 6, 3, 64, 448)]
+    rng = np.random.default_rng(0)
+    fx = {}
+    for N, na, L, nb, s0 in classes:
+        ops, param, scale = tups_operators(N, L)
+        ang = rng.uniform(-0.3, 0.3, (nb, len(ops)))[0]
+        h, g = synthetic_integrals(N, s0)
+        P = int(param.max())
+        with tempfile.TemporaryDirectory() as td:
+            prefix = os.path.join(td, "syn")
+            write_integrals(prefix, h, g)
+            hf = hartree_fock_index(N, na, na)
+            d = run(spec(2 * N, [(hf, 1.0, 0.0)], ops - 1, param - 1, scale, [f"ham ints {prefix}"], [ang],
+                         want=(1, 1, 0, 0)), threads=8)
+        fx[f"E{N}"] = d[0]
+        fx[f"G{N}"] = d[1:1 + P]
+        fx[f"x{N}"] = ang
+        fx[f"seed{N}"] = s0
+        print(tag, N, d[0])
+    np.savez_compressed(os.path.join(OUT, tag + ".npz"), **fx)
 
 
 def table_floats(text):
@@ -469,6 +499,7 @@ if __name__ == "__main__":
         "ref14": lambda: large_case("ref14", 14, 7, 7, 4, 0, hess=False),
         "lucj14": lambda: lucj_case("lucj14", 14, 7, 3, 7),
         "pairs12": lambda: pairs_case("pairs12", 12, 6, 6, 3),
+        "batched4": lambda: batched_case("batched4"),
         "overlaps_syn6": lambda: overlaps_case("overlaps_syn6", "syn6", 4),
         "overlaps_h4c": lambda: overlaps_case("overlaps_h4c", "h4c", 3, cplx=True),
     }
@@ -487,7 +518,7 @@ if __name__ == "__main__":
     synthetic_case("syn8", 8, 4, 4, 2, 0)
     for t in ("ref10", "ref12", "ref14", "lucj14", "pairs12"):
         single[t]()
-    for t in ("overlaps_syn6", "overlaps_h4c"):
+    for t in ("overlaps_syn6", "overlaps_h4c", "batched4"):
         single[t]()
     properties_case("props_h4", "h4")
     properties_case("props_h4c", "h4c", cplx=True)

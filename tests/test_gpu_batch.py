@@ -383,3 +383,28 @@ def test_new_integral_values_refresh_in_place(mode):
         assert np.array_equal(g1, g2)
         ref.close()
         e.close()
+
+
+@pytest.mark.parametrize("N,na,L,s0,mode", [(8, 4, 2, 0, ae.HAM_STORED), (10, 5, 3, 256, ae.HAM_ON_THE_FLY),
+                                            (12, 6, 3, 448, ae.HAM_ON_THE_FLY)])
+def test_batched_classes_match_reference(golden, N, na, L, s0, mode):
+    """Instance 0 of each size class of the benchmark's batched launch (its integrals and
+    angles) inside a batch with per-instance integrals, against the reference's own
+    energy and gradient (tests/golden/batched4.npz)."""
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
+    fx = golden("batched4")
+    ops, param, scale = tups_operators(N, L)
+    e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1)
+    init = np.zeros(e.D)
+    init[np.searchsorted(e.states(), hartree_fock_index(N, na, na))] = 1.0
+    e.set_initial(init)
+    e.set_batch(2)
+    ints = [synthetic_integrals(N, s0), synthetic_integrals(N, s0 + 1)]
+    e.set_ham_integrals_batch(np.stack([a for a, _ in ints]), np.stack([b for _, b in ints]), mode)
+    x = np.asarray(fx["x%d" % N])
+    E, g = e.gradient(np.vstack([x, np.random.default_rng(1).uniform(-0.3, 0.3, len(x))]))
+    gc = np.zeros(int(param.max()))
+    np.add.at(gc, param - 1, scale * g[0])
+    assert abs(E[0] - float(fx["E%d" % N])) < 1e-10
+    np.testing.assert_allclose(gc, fx["G%d" % N], atol=1e-9, rtol=0)
+    e.close()
