@@ -390,3 +390,36 @@ def test_python_binding_current_angles_and_per_operator_derivatives(golden, name
         Eopt, xopt = m.optimise()
         assert abs(Eopt - float(fx["nuclear"]) - (-2.838345804245581)) < 1e-8
         assert np.array_equal(m.getAngles(), xopt)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_coded_and_uncoded_stored_rows_agree(cplx, monkeypatch):
+    """The two stored row formats (coded doubles with a value table, and uncoded rows,
+    AEGPU_CODED_ROWS=0) give the same H x, energy, gradient and Hessian up to summation
+    order, real and complex."""
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals, tups_operators
+    N, na = 8, 4
+    ops, param, scale = tups_operators(N, 2)
+    h1, g2 = synthetic_integrals(N, 5)
+    ang = np.random.default_rng(6).uniform(-0.3, 0.3, len(ops))
+    out = []
+    for coded in ("1", "0"):
+        monkeypatch.setenv("AEGPU_CODED_ROWS", coded)
+        e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1, complex_mode=cplx)
+        W = 2 if cplx else 1
+        init = np.zeros(e.D * W)
+        init[W * np.searchsorted(e.states(), hartree_fock_index(N, na, na))] = 1.0
+        e.set_initial(init)
+        e.set_ham_integrals(h1, g2, ae.HAM_STORED)
+        x = np.random.default_rng(7).normal(size=e.D * W)
+        Hx = e.apply_h(x)
+        E, g = e.gradient(ang)
+        _, _, H = e.hessian(ang, param - 1, scale) if not cplx else (None, None, None)
+        out.append((Hx, E, g, H))
+        e.close()
+    (Hx1, E1, g1, H1), (Hx0, E0, g0, H0) = out
+    np.testing.assert_allclose(Hx1, Hx0, atol=1e-11, rtol=0)
+    assert abs(E1 - E0) < 1e-12
+    np.testing.assert_allclose(g1, g0, atol=1e-12, rtol=0)
+    if H1 is not None:
+        np.testing.assert_allclose(H1, H0, atol=1e-11, rtol=0)
