@@ -1662,6 +1662,7 @@ __global__ void __launch_bounds__(1024) k_otf_strings(OtfArgs a, const double *_
             const int32_t tc = sbc[t];
             const int kb = (tc & 31) * N + ((tc >> 5) & 31);
             const size_t ct = (size_t)sbr[t];
+#pragma unroll 4
             for (int s = 0; s < nsa; ++s) {
                 const double v = flipc(vsl[s * NN + kb], sa_code[s] ^ tc);
                 const size_t c = (size_t)sa_rank[s] * nB + ct;
