@@ -161,17 +161,21 @@ __global__ void k_mse(const float *__restrict__ Y, const float *__restrict__ T, 
                       int cols, const float *__restrict__ mean, const float *__restrict__ inv_scale,
                       float *__restrict__ dY, float *__restrict__ rowloss)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per row: lanes take columns lane, lane + 32, ... (coalesced), the row's
+    // squared error meets in a fixed butterfly
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (r >= rows) return;
     const int src = idx ? idx[r] : r;
     const float w = 2.0f / ((float)rows * (float)cols);
     float s = 0;
-    for (int c = 0; c < cols; ++c) {
+    for (int c = lane; c < cols; c += 32) {
         const float d = Y[(int64_t)r * cols + c] - (T[(int64_t)src * cols + c] - mean[c]) * inv_scale[c];
         s += d * d;
         dY[(int64_t)r * cols + c] = w * d;
     }
-    rowloss[r] = s;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) rowloss[r] = s;
 }
 
 // Y = Yn * scale + mean (outputs back to angle units)
@@ -515,7 +519,7 @@ int aegpu_mlp_loss_grad(aegpu_mlp *m, const float *X, const float *T, int n, flo
     cudaMemcpyAsync(dt, T, (size_t)n * m->n_out * sizeof(float), cudaMemcpyHostToDevice, s);
     k_standardise<<<256, 256, 0, s>>>(dx, nullptr, n, m->n_in, m->in_mean(), m->in_inv(), m->X0);
     forward(m, n);
-    k_mse<<<(n + 127) / 128, 128, 0, s>>>(m->Y, dt, nullptr, n, m->n_out, m->out_mean(), m->out_inv(), m->dY,
+    k_mse<<<(n + 7) / 8, 256, 0, s>>>(m->Y, dt, nullptr, n, m->n_out, m->out_mean(), m->out_inv(), m->dY,
                                           m->rowloss);
     backward(m, n);
     std::vector<float> rl(n);
@@ -571,7 +575,7 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
             const int *idx = didx + (size_t)ep * n + r0;
             k_standardise<<<256, 256, 0, s>>>(dx, idx, rows, m->n_in, m->in_mean(), m->in_inv(), m->X0);
             forward(m, rows);
-            k_mse<<<(rows + 127) / 128, 128, 0, s>>>(m->Y, dt, idx, rows, m->n_out, m->out_mean(), m->out_inv(), m->dY,
+            k_mse<<<(rows + 7) / 8, 256, 0, s>>>(m->Y, dt, idx, rows, m->n_out, m->out_mean(), m->out_inv(), m->dY,
                                                      dloss + lpos);
             lpos += batch;
             backward(m, rows);
