@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libansatzevolve_gb300.so")
 _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
-TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL, TUNE_REUSE_HPSI = 1, 2, 3, 4, 5, 6
+TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL, TUNE_REUSE_HPSI, TUNE_FLIP = 1, 2, 3, 4, 5, 6, 7
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 PROP_HESSIAN, PROP_OVERLAP, PROP_HF_PATH = 1, 2, 4
 # rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)
@@ -71,6 +71,7 @@ def lib(build_if_missing=True):
         "aegpu_batch_size": (ctypes.c_int, [_P]),
         "aegpu_set_active": (ctypes.c_int, [_P, _IP]),
         "aegpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
+        "aegpu_flip_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
         "aegpu_get_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_io_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
         "aegpu_io_put_angles": (ctypes.c_int, [_P, _DP, _P]),
@@ -541,6 +542,21 @@ class Engine:
         return {k: int(self.L.aegpu_get_tuning(self.h, k))
                 for k in (TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL)}
 
+    def set_tuning(self, knob, value):
+        """One knob (TUNE_*) where the engine accepts it at this point of its set-up
+        (TUNE_PDL, TUNE_REUSE_HPSI and TUNE_FLIP at any time)."""
+        self._check(self.L.aegpu_set_tuning(self.h, knob, int(value)))
+
+    def get_tuning(self, knob):
+        return int(self.L.aegpu_get_tuning(self.h, knob))
+
+    def flip_status(self):
+        """Per instance: True where the last energy evaluation's H psi took the spin-flip
+        half product."""
+        u = np.zeros(self.nb, dtype=np.int32)
+        self._check(self.L.aegpu_flip_status(self.h, iptr(u)))
+        return u.astype(bool)
+
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))
 
@@ -559,11 +575,16 @@ class Engine:
         keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active", "nnz")
         return dict(zip(keys, map(int, out)))
 
-    def fp64_work(self):
-        """FP64 instructions per evaluation and instance: (H psi, forward, adjoint)."""
-        w = np.zeros(3, dtype=np.int64)
+    def fp64_work(self, half=None):
+        """FP64 instructions per evaluation and instance: (H psi, forward, adjoint).  H psi
+        counts the spin-flip half product where half is true, the full product where it
+        is false, and by default what the last energy evaluation took (averaged over
+        the instances)."""
+        w = np.zeros(4, dtype=np.int64)
         self._check(self.L.aegpu_fp64_work(self.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
-        return tuple(int(x) for x in w)
+        frac = float(np.mean(self.flip_status())) if half is None else float(bool(half))
+        hpsi = int(round(w[0] * (1.0 - frac) + w[3] * frac))
+        return hpsi, int(w[1]), int(w[2])
 
     def device_bytes(self):
         return int(self.L.aegpu_device_bytes(self.h))

@@ -1369,9 +1369,11 @@ __device__ void row_code(const IntArgs &a, uint32_t J, int64_t d, uint32_t &I, u
 }
 
 // Coded rows of rows [r0, r1): both parts in the sliced layout of ell_pos (slabs of 32
-// rows, inside a slab the 4-entry groups of the 32 rows contiguous).
+// rows, inside a slab the 4-entry groups of the 32 rows contiguous).  values_only: new
+// integrals for rows already built -- columns and codes depend on the determinants
+// alone, so only the explicit values are rewritten (the table is rebuilt apart).
 __global__ void k_vell_build(IntArgs a, int32_t *__restrict__ colE, double *__restrict__ valE, int32_t *__restrict__ colD,
-                             uint16_t *__restrict__ codeD, int64_t r0, int64_t r1)
+                             uint16_t *__restrict__ codeD, int64_t r0, int64_t r1, bool values_only)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -1387,12 +1389,13 @@ __global__ void k_vell_build(IntArgs a, int32_t *__restrict__ colE, double *__re
             int32_t c = self;
             if (r < D && e < a.width_e) {
                 row_entry(a, J, e, I, v);
-                c = (int32_t)a.basis.rank_of(I);
+                if (!values_only) c = (int32_t)a.basis.rank_of(I);
             }
             const size_t p = ell_pos(r, e, qe);
-            colE[p] = c;
+            if (!values_only) colE[p] = c;
             valE[p] = v;
         }
+        if (values_only) continue;
         for (int64_t e = lane; e < a.stride_d; e += 32) {
             uint32_t I = J;
             uint16_t code = 0;
@@ -1423,6 +1426,90 @@ __device__ __forceinline__ double signed_value(const double *tab, uint32_t code)
     return __longlong_as_double(__double_as_longlong(t) ^ ((long long)(code >> 15) << 63));
 }
 
+// ------------------------------------------------ spin-flip half product --
+// With as many alpha as beta electrons, the Sz basis pairs determinant (a, b) (alpha
+// string a, beta string b; row a * nB + b) with its spin-flipped partner (b, a).  A
+// Hamiltonian built from spin-free integrals takes the same value on both members of
+// every pair of pairs (H[(b,a),(b',a')] = H[(a,b),(a',b')], the sign of the flip being
+// the same for every determinant), so when x(b, a) = x(a, b) for every pair -- true, up
+// to rounding, of every state a spin-adapted ansatz with one angle per spatial
+// excitation makes from a closed-shell start (tUPS through its compressed parameters,
+// LUCJ) -- (H x)(b, a) = (H x)(a, b) as well: the product computes the rows with
+// a <= b and writes each result to its mirror row too, half the matrix elements (the
+// symmetry the direct-CI literature uses for Ms = 0: Knowles & Handy, Chem. Phys. Lett.
+// 111, 315 (1984); Olsen et al., J. Chem. Phys. 89, 2185 (1988)).  Every product that
+// may take this path first measures the invariance of its input on the device
+// (k_flip_check); the product kernels read the partial sums in a fixed order and take
+// the half product only when ||x - flip x|| <= kFlipTol ||x||, the full one otherwise.
+constexpr double kFlipTol = 1e-12;
+
+struct FlipArgs {
+    const double *part;     // per instance, G pairs (sum |x|^2, sum over a < b of |x(a,b) - x(b,a)|^2); null: full product
+    const int32_t *slabs;   // stored rows: the 32-row slabs that hold a row with a <= b, ascending
+    int64_t nslabs;
+    int *used;              // per instance: 1 where the product took the half path (nullable)
+    int G;
+    uint32_t nB, div_m, div_l;  // z / nB as in DevBasis
+    __device__ __forceinline__ uint32_t alpha_of(uint32_t z) const
+    {
+        if (div_l == 0) return z;
+        const uint32_t hi = __umulhi(div_m, z);
+        return (hi + ((z - hi) >> 1)) >> (div_l - 1);
+    }
+};
+
+// Partial sums of the invariance test for instance blockIdx.y: sum |x|^2 and the sum
+// over a < b of |x(a,b) - x(b,a)|^2, one pair per CTA, in a fixed order.
+template <int W>
+__global__ void k_flip_check(FlipArgs f, const double *__restrict__ x, int64_t D, double *__restrict__ part,
+                             const int *__restrict__ active)
+{
+    __shared__ double red[32];
+    if (skip_instance(active, blockIdx.y)) return;
+    x += (size_t)blockIdx.y * D * W;
+    double s0 = 0.0, s1 = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < D; r += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = f.alpha_of((uint32_t)r), b = (uint32_t)r - a * f.nB;
+        const int64_t rf = (int64_t)b * f.nB + a;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const double v = x[r * W + w];
+            s0 = fma(v, v, s0);
+            if (a < b) {
+                const double d = v - x[rf * W + w];
+                s1 = fma(d, d, s1);
+            }
+        }
+    }
+    s0 = block_sum(s0, red);
+    s1 = block_sum(s1, red);
+    if (threadIdx.x == 0) {
+        double *p = part + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 2;
+        p[0] = s0;
+        p[1] = s1;
+    }
+}
+
+// The half-product decision for instance b, by warp 0 of the calling CTA (every lane
+// returns it): the G partial pairs summed lane-strided, then a fixed butterfly.
+__device__ __forceinline__ bool flip_half(const FlipArgs &f, int b)
+{
+    if (!f.part) return false;
+    const double *p = f.part + (size_t)b * f.G * 2;
+    const int lane = threadIdx.x & 31;
+    double s0 = 0.0, s1 = 0.0;
+    for (int i = lane; i < f.G; i += 32) {
+        s0 += p[2 * i];
+        s1 += p[2 * i + 1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    return s0 > 0.0 && s1 <= kFlipTol * kFlipTol * s0;
+}
+
 // y = H x with coded rows.  T threads per row as in k_spmv_sell.  Each CTA owns an
 // equal contiguous share of the rows (a multiple of 32), walked 1024 / T rows at a
 // time, so that every SM ends with the same work (the FP64 pipe is the limit, and a
@@ -1430,30 +1517,57 @@ __device__ __forceinline__ double signed_value(const double *tab, uint32_t code)
 // staged once per CTA, in shared memory.  NV > 1: one thread carries NV right-hand sides (instances
 // blockIdx.y * NV + v, shared matrix, no energy and no mask), so each matrix entry read
 // serves NV products.  Energy partial per CTA: sum over its rows of y_r x_r.
+// Half product (NV = 1, flip.part set and the instance's input flip-invariant): the
+// CTAs share the slabs of flip.slabs instead of all rows, rows with a > b are left to
+// their mirror, and each row's result also goes to its mirror row (energy: both rows).
 template <int W, int T, int NV>
 __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const double *__restrict__ x,
                                                                double *__restrict__ y, int64_t D, int ninst,
-                                                               double *__restrict__ epart, const int *__restrict__ active)
+                                                               double *__restrict__ epart, const int *__restrict__ active,
+                                                               FlipArgs flip)
 {
     extern __shared__ double tab[];
     __shared__ double red[kVellThreads / 32];
+    __shared__ int s_half;
     const int b0 = blockIdx.y * NV;
     if (NV == 1 && skip_instance(active, b0)) return;
+    if (threadIdx.x < 32) {
+        const bool h = NV == 1 && flip_half(flip, b0);
+        if (threadIdx.x == 0) {
+            s_half = h;
+            if (NV == 1 && flip.used && blockIdx.x == 0) flip.used[b0] = h;
+        }
+    }
     const double *vt = m.vtab + (size_t)b0 * m.vtab_inst;
     for (int64_t i = threadIdx.x; i < m.vtab_len; i += blockDim.x) tab[i] = vt[i];
     __syncthreads();
+    const bool half = NV == 1 && s_half;
     const int32_t *colE = m.colE + (size_t)b0 * m.inst_e, *colD = m.colD + (size_t)b0 * m.inst_d;
     const double *valE = m.valE + (size_t)b0 * m.inst_e;
     const uint16_t *codeD = m.codeD + (size_t)b0 * m.inst_d;
     constexpr int RPW = 32 / T;
     const int lane = threadIdx.x & 31, sub = lane / RPW;
     const int64_t rows_per_iter = kVellThreads / T;
-    const int64_t share = ((D + gridDim.x - 1) / gridDim.x + 31) & ~(int64_t)31;
-    const int64_t r_lo = (int64_t)blockIdx.x * share, r_hi = r_lo + share < D ? r_lo + share : D;
+    // units: rows (full product) or the rows of the listed slabs (half product)
+    const int64_t nunits = half ? flip.nslabs * 32 : D;
+    const int64_t share = ((nunits + gridDim.x - 1) / gridDim.x + 31) & ~(int64_t)31;
+    const int64_t u_lo = (int64_t)blockIdx.x * share, u_hi = u_lo + share < nunits ? u_lo + share : nunits;
     double e = 0.0;
-    for (int64_t rb = r_lo; rb < r_hi; rb += rows_per_iter) {
-        const int64_t rr = rb + (threadIdx.x - lane) / T + lane % RPW;
-        const int64_t r = rr < r_hi ? rr : D;  // rows past the share: none
+    for (int64_t ub = u_lo; ub < u_hi; ub += rows_per_iter) {
+        const int64_t uu = ub + (threadIdx.x - lane) / T + lane % RPW;
+        int64_t r = D, rf = -1;  // r = D: no row; rf >= 0: the mirror row also gets the result
+        if (uu < u_hi) {
+            if (!half) {
+                r = uu;
+            } else {
+                const int64_t rr = (int64_t)flip.slabs[uu >> 5] * 32 + (uu & 31);
+                if (rr < D) {
+                    const uint32_t a = flip.alpha_of((uint32_t)rr), b = (uint32_t)rr - a * flip.nB;
+                    if (a <= b) r = rr;
+                    if (a < b) rf = (int64_t)b * flip.nB + a;
+                }
+            }
+        }
         double acc[NV][W][2];
 #pragma unroll
         for (int v = 0; v < NV; ++v)
@@ -1517,6 +1631,10 @@ __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const
                 if (r < D && sub == 0) {
                     yv[r * W + w] = s;
                     if (NV == 1) e = fma(s, xv[r * W + w], e);
+                    if (NV == 1 && rf >= 0) {
+                        yv[rf * W + w] = s;
+                        e = fma(s, xv[rf * W + w], e);
+                    }
                 }
             }
         }
@@ -1564,15 +1682,33 @@ __device__ __forceinline__ double flipc(double v, int32_t code)
     return __longlong_as_double(__double_as_longlong(v) ^ ((unsigned long long)((uint32_t)code >> 31) << 63));
 }
 
+// Half product (flip.part set and the instance's input flip-invariant): only the
+// determinants with beta string rb >= ra, each result also written to its mirror
+// (rb, ra); a CTA whose beta strings all lie below ra writes a zero energy partial.
 template <int W>
 __global__ void __launch_bounds__(1024) k_otf_strings(OtfArgs a, const double *__restrict__ x, double *__restrict__ y,
-                                                      double *__restrict__ epart)
+                                                      double *__restrict__ epart, FlipArgs flip)
 {
     extern __shared__ double sm[];
     __shared__ double red[32];
+    __shared__ int s_half;
     const int N = a.N, NN = a.N * a.N, nsa = a.nsa, nda = a.nda;
     const int ra = blockIdx.x;
     if (skip_instance(a.active, blockIdx.z)) return;
+    if (threadIdx.x < 32) {
+        const bool h = flip_half(flip, blockIdx.z);
+        if (threadIdx.x == 0) {
+            s_half = h;
+            if (flip.used && blockIdx.x == 0 && blockIdx.y == 0) flip.used[blockIdx.z] = h;
+        }
+    }
+    __syncthreads();
+    const bool half = s_half;
+    if (half && (int64_t)(blockIdx.y + 1) * blockDim.x <= ra) {
+        if (threadIdx.x == 0 && epart)
+            epart[(size_t)blockIdx.z * gridDim.x * gridDim.y + (size_t)blockIdx.y * gridDim.x + blockIdx.x] = 0.0;
+        return;
+    }
     {
         // instance blockIdx.z: its vectors and (unless shared) its integral tables
         const size_t b = blockIdx.z, D = (size_t)a.nA * a.nB, bt = a.shared ? 0 : b;
@@ -1615,7 +1751,7 @@ __global__ void __launch_bounds__(1024) k_otf_strings(OtfArgs a, const double *_
     const int nB = a.nB;
     const int rb = blockIdx.y * blockDim.x + threadIdx.x;
     double en = 0;
-    if (rb < nB) {
+    if (rb < nB && (!half || rb >= ra)) {
         const size_t row = (size_t)ra * nB + rb;
         const double dg = a.diag[row];
         double acc[W];
@@ -1670,10 +1806,15 @@ __global__ void __launch_bounds__(1024) k_otf_strings(OtfArgs a, const double *_
                 for (int w = 0; w < W; ++w) acc[w] = fma(v, x[c * W + w], acc[w]);
             }
         }
+        const size_t mir = (size_t)rb * nB + ra;
 #pragma unroll
         for (int w = 0; w < W; ++w) {
             y[row * W + w] = acc[w];
             en = fma(acc[w], x[row * W + w], en);
+            if (half && rb > ra) {
+                y[mir * W + w] = acc[w];
+                en = fma(acc[w], x[mir * W + w], en);
+            }
         }
     }
     en = block_sum(en, red);
@@ -1758,6 +1899,9 @@ struct aegpu_engine {
     PassConst *d_pc = nullptr;
     double *d_psi = nullptr, *d_h = nullptr, *d_tmp = nullptr;
     double *d_partials = nullptr, *d_epart = nullptr, *d_scalar = nullptr, *d_grad = nullptr;
+    double *d_flip_part = nullptr;  // per instance, sm_count pairs of the invariance test
+    int *d_flip_used = nullptr;     // per instance, the last energy product's choice
+    bool flip_tried = false;        // the last energy product ran the invariance test
     double *d_ckpt = nullptr;  // per pass: amplitudes after the pass (adjoint sweep input)
     int *d_active = nullptr;   // per instance: 0 = skip it in batched launches
     std::vector<std::pair<void *, size_t>> inst_allocs;
@@ -1796,6 +1940,14 @@ struct aegpu_engine {
     // keep H psi between an energy and a gradient at the same angles (AEGPU_REUSE_HPSI=0
     // in the environment, or the knob, makes the gradient recompute it)
     bool reuse_hpsi = true;
+    // spin-flip half product of the energy's H psi (knob AEGPU_TUNE_FLIP, environment
+    // AEGPU_FLIP=0 to switch it off); possible for integral Hamiltonians in the Sz
+    // basis with as many alpha as beta electrons (flip_ok), taken per evaluation when
+    // the state passes the device test
+    bool tune_flip = true;
+    bool flip_ok = false;
+    int32_t *d_flip_slabs = nullptr;  // coded rows: slabs holding a row with a <= b
+    int64_t n_flip_slabs = 0;
     bool pdl_on() const { return tune_pdl >= 0 ? tune_pdl != 0 : (int64_t)B.D * W * nb <= (int64_t)1 << 19; }
     int spmv_tpr() const
     {
@@ -1971,6 +2123,9 @@ struct aegpu_engine {
         ell_coded = false;
         vell = VellArgs{};
         d_h1 = d_g2 = nullptr;
+        flip_ok = false;
+        d_flip_slabs = nullptr;
+        n_flip_slabs = 0;
         drop_graph();
         h_valid = false;
         ground_valid = false;
@@ -2011,6 +2166,9 @@ struct aegpu_engine {
         get(d_tmp, B_ * n);
         get(d_partials, B_ * std::max<int64_t>(n_partials, 1));
         get(d_epart, B_ * std::max<int64_t>(n_epart, 1));
+        get(d_flip_part, B_ * 2 * (size_t)sm_count);
+        get(d_flip_used, B_);
+        flip_tried = false;
         get(d_scalar, std::max<size_t>(B_, 4));
         get(d_grad, B_ * nops);
         get(d_ckpt, B_ * std::max<int64_t>(n_ckpt, 1));
@@ -2165,11 +2323,33 @@ int upload_angles(aegpu_engine *e, const double *angles, bool host, int ninst, b
 // y = H x for the first ninst instances (vectors at stride D*W), with <x|y> partial
 // sums into epart (nullable; *nparts partial sums per instance).
 int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ninst, int *nparts = nullptr,
-              bool masked = true)
+              bool masked = true, bool flip = false)
 {
     const int *act = masked ? e->d_active : nullptr;
     if (nparts) *nparts = e->spmv_grid;
     const int64_t D = (int64_t)e->B.D;
+    // spin-flip half product: test every instance's input first (one launch); the
+    // product kernels read the test's partials and pick the half or the full product
+    FlipArgs fa{};
+    const bool coded = e->ham_kind == 2 && e->ell_coded;
+    if (flip) e->flip_tried = false;
+    if (flip && e->tune_flip && e->flip_ok && (coded || e->ham_kind == 3)) {
+        e->flip_tried = true;
+        fa.part = e->d_flip_part;
+        fa.used = e->d_flip_used;
+        fa.slabs = e->d_flip_slabs;
+        fa.nslabs = e->n_flip_slabs;
+        fa.G = e->sm_count;
+        fa.nB = e->db.nB;
+        fa.div_m = e->db.div_m;
+        fa.div_l = e->db.div_l;
+        const dim3 g(e->sm_count, ninst);
+        if (e->W == 1)
+            k_flip_check<1><<<g, 256, 0, e->stream>>>(fa, x, D, e->d_flip_part, act);
+        else
+            k_flip_check<2><<<g, 256, 0, e->stream>>>(fa, x, D, e->d_flip_part, act);
+        e->launches += 1;
+    }
     if (e->ham_kind == 1) {
         const dim3 g(e->spmv_grid, ninst);
         if (e->W == 1)
@@ -2191,7 +2371,8 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         const int nv = multi ? (e->W == 1 ? kVellNV1 : kVellNV2) : 1;
         const dim3 g(gx, (ninst + nv - 1) / nv);
 #define AE_VELL(WW, TT, NN) \
-    k_spmv_vell<WW, TT, NN><<<g, kVellThreads, smem, e->stream>>>(e->vell, x, y, D, ninst, epart, act)
+    k_spmv_vell<WW, TT, NN><<<g, kVellThreads, smem, e->stream>>>(e->vell, x, y, D, ninst, epart, act, \
+                                                                   multi ? FlipArgs{} : fa)
         if (e->W == 1) {
             if (multi) {
                 if (T == 1) AE_VELL(1, 1, kVellNV1); else if (T == 2) AE_VELL(1, 2, kVellNV1);
@@ -2232,9 +2413,9 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         OtfArgs o = e->otf;
         o.active = act;
         if (e->W == 1)
-            k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart);
+            k_otf_strings<1><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart, fa);
         else
-            k_otf_strings<2><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart);
+            k_otf_strings<2><<<g, e->otf_threads, smem, e->stream>>>(o, x, y, epart, fa);
         if (nparts) *nparts = e->otf.nA * e->otf_chunks;
     } else {
         return e->fail(AEGPU_ERR_STATE, "no Hamiltonian set");
@@ -2248,7 +2429,7 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 {
     NvtxRange r("aegpu H*psi + energy");
     int np = 0;
-    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np);
+    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np, true, true);
     if (rc) return rc;
     k_reduce_sum<<<ninst, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0, e->d_active);
     e->launches += 1;
@@ -2494,6 +2675,7 @@ int aegpu_create(aegpu_engine **out)
     cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&e->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (const char *v = std::getenv("AEGPU_REUSE_HPSI")) e->reuse_hpsi = std::strcmp(v, "0") != 0;
+    if (const char *v = std::getenv("AEGPU_FLIP")) e->tune_flip = std::strcmp(v, "0") != 0;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete e;
@@ -2740,7 +2922,7 @@ namespace {
 // between all instances, ntab = nb gives instance b the integrals h1s[b], g2s[b].
 // Value tables and coded rows of every instance (the engine's integrals already on the
 // device; e->vell and e->ints set).
-static void build_coded_rows(aegpu_engine *e, int ntab)
+static void build_coded_rows(aegpu_engine *e, int ntab, bool values_only)
 {
     const IntArgs a = e->ints;
     const int N = a.N;
@@ -2760,7 +2942,7 @@ static void build_coded_rows(aegpu_engine *e, int ntab)
                                                                 (double *)v.valE + per_e * t,
                                                                 (int32_t *)v.colD + per_d * t,
                                                                 (uint16_t *)v.codeD + per_d * t, r0,
-                                                                std::min(Dpad, r0 + chunk));
+                                                                std::min(Dpad, r0 + chunk), values_only);
             e->launches += 1;
         }
     }
@@ -2783,7 +2965,7 @@ static int refresh_integrals(aegpu_engine *e, const double *h1s, const double *g
     const int64_t D = (int64_t)e->B.D;
     IntArgs a = e->ints;
     if (e->ham_kind == 2 && e->ell_coded) {
-        build_coded_rows(e, ntab);
+        build_coded_rows(e, ntab, true);
     } else if (e->ham_kind == 2) {
         const int64_t Dpad = (D + 31) & ~(int64_t)31;
         const size_t per = (size_t)Dpad * a.stride;
@@ -2923,11 +3105,27 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
         e->vell = v;
         e->ell_coded = true;
         e->ints = a;
-        build_coded_rows(e, ntab);
+        build_coded_rows(e, ntab, false);
         e->ham_kind = 2;
         e->ham_entries = D * (a.stride_e + a.stride_d);
         e->ell_width = (int)(a.stride_e + a.stride_d);
         e->ell_stride_inst = 0;
+        if (e->B.na == e->B.nb) {
+            // the 32-row slabs that hold a row (a, b) with a <= b, for the half product
+            std::vector<int32_t> slabs;
+            const uint32_t nB = e->B.nB;
+            for (int64_t sl = 0; sl * 32 < D; ++sl) {
+                const int64_t r0 = sl * 32, r1 = std::min<int64_t>(D, r0 + 32);
+                // rows r0..r1-1 cover alpha strings r0 / nB .. (r1 - 1) / nB; a row with
+                // a <= b exists unless every row of the slab lies below the diagonal
+                bool any = false;
+                for (int64_t r = r0; r < r1 && !any; ++r) any = (uint64_t)r / nB <= (uint64_t)r % nB;
+                if (any) slabs.push_back((int32_t)sl);
+            }
+            if (!ham_upload(e->d_flip_slabs, slabs)) return e->fail(AEGPU_ERR_NOMEM, "slab list allocation failed");
+            e->n_flip_slabs = (int64_t)slabs.size();
+            e->flip_ok = true;
+        }
     } else if (mode == AEGPU_HAM_STORED) {
         const size_t per = (size_t)Dpad * a.stride;
         if (!ham_alloc(e->d_col, per * ntab) || !ham_alloc(e->d_val, per * ntab))
@@ -3024,6 +3222,7 @@ int set_integrals(aegpu_engine *e, const double *h1s, const double *g2s, int nta
         e->ham_kind = 3;
         e->ham_entries = 0;
         e->ell_stride_inst = 0;
+        e->flip_ok = e->B.na == e->B.nb;
     }
     e->ints_ntab = ntab;
     e->ints_mode_asked = mode_asked;
@@ -3103,6 +3302,12 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         if (value != 0 && value != 1) return e->fail(AEGPU_ERR_ARG, "H psi reuse must be 0 or 1");
         e->reuse_hpsi = value != 0;
         return AEGPU_OK;
+    case AEGPU_TUNE_FLIP:
+        if (value != 0 && value != 1) return e->fail(AEGPU_ERR_ARG, "the spin-flip half product must be 0 or 1");
+        e->tune_flip = value != 0;
+        e->drop_graph();
+        e->h_valid = false;
+        return AEGPU_OK;
     case AEGPU_TUNE_SPMV_TPR:
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return e->fail(AEGPU_ERR_ARG, "threads per row must be 0 (by size), 1, 2, 4 or 8");
@@ -3112,6 +3317,19 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
     default:
         return e->fail(AEGPU_ERR_ARG, "unknown tuning knob");
     }
+}
+
+int aegpu_flip_status(aegpu_engine *e, int *used)
+{
+    if (!e || !used) return AEGPU_ERR_ARG;
+    if (!e->d_flip_used) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    if (!e->flip_tried) {
+        std::fill(used, used + e->nb, 0);
+        return AEGPU_OK;
+    }
+    if (stream_sync(e, "flip status")) return AEGPU_ERR_CUDA;
+    cudaMemcpy(used, e->d_flip_used, sizeof(int) * e->nb, cudaMemcpyDeviceToHost);
+    return e->cuda_check("flip status");
 }
 
 int aegpu_get_tuning(const aegpu_engine *e, int knob)
@@ -3124,6 +3342,7 @@ int aegpu_get_tuning(const aegpu_engine *e, int knob)
     case AEGPU_TUNE_SPMV_TPR: return e->spmv_tpr();
     case AEGPU_TUNE_PDL: return e->pdl_on() ? 1 : 0;
     case AEGPU_TUNE_REUSE_HPSI: return e->reuse_hpsi ? 1 : 0;
+    case AEGPU_TUNE_FLIP: return e->tune_flip ? 1 : 0;
     default: return -1;
     }
 }
@@ -4194,6 +4413,14 @@ int aegpu_fp64_work(const aegpu_engine *e, int64_t *work)
     work[0] = (elems + D) * W;
     work[1] = (al + act) * W;
     work[2] = (2 * al + act) * W + al / 2;
+    // [3] H psi by the spin-flip half product: the rows with a <= b, the energy FMAs of
+    // every row, and the invariance test (one FMA per amplitude, one per pair a < b)
+    work[3] = 0;
+    const bool coded = e->ham_kind == 2 && e->ell_coded;
+    if (e->flip_ok && (coded || e->ham_kind == 3)) {
+        const int64_t nA = e->B.nA, Dh = nA * (nA + 1) / 2;
+        work[3] = (Dh * e->ints.width + D + D + (D - nA) / 2) * W;
+    }
     return AEGPU_OK;
 }
 

@@ -191,11 +191,13 @@ __global__ void k_unstandardise(float *__restrict__ Y, int rows, int cols, const
 
 // Adam (Kingma & Ba 2015, Algorithm 1) on the FP32 master weights, refreshing the
 // BF16 copies used by the products.  Weight tensors only have BF16 copies (wq != null
-// for them); biases stay FP32.
+// for them); biases stay FP32.  c12 = the step's bias corrections (1 - b1^t, 1 - b2^t),
+// read from device memory so that a captured step serves every t.
 __global__ void k_adam(float *__restrict__ w, __nv_bfloat16 *__restrict__ wq, const float *__restrict__ g,
                        float *__restrict__ m, float *__restrict__ v, int64_t n, float lr, float b1, float b2, float eps,
-                       float c1, float c2)
+                       const float *__restrict__ c12)
 {
+    const float c1 = c12[0], c2 = c12[1];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float gi = g[i];
         const float mi = b1 * m[i] + (1.0f - b1) * gi;
@@ -557,7 +559,10 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
     cudaStream_t s = m->stream;
     cudaMemcpyAsync(dx, X, (size_t)n * m->n_in * sizeof(float), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(dt, T, (size_t)n * m->n_out * sizeof(float), cudaMemcpyHostToDevice, s);
-    // every epoch's permutation up front (Fisher-Yates on a seeded generator)
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    const int nbat = (n + batch - 1) / batch;
+    // every epoch's permutation (Fisher-Yates on a seeded generator) and every step's
+    // Adam bias corrections up front
     std::vector<int> perm((size_t)epochs * n);
     uint64_t rs = seed;
     for (int ep = 0; ep < epochs; ++ep) {
@@ -565,31 +570,70 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
         for (int i = 0; i < n; ++i) p[i] = i;
         for (int i = n - 1; i > 0; --i) std::swap(p[i], p[(int)(splitmix64(rs) % (uint64_t)(i + 1))]);
     }
-    if (epochs) cudaMemcpyAsync(didx, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s);
-    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-    const int nbat = (n + batch - 1) / batch;
-    int64_t lpos = 0;
-    for (int ep = 0; ep < epochs; ++ep) {
+    std::vector<float> coef((size_t)2 * nbat * epochs);
+    for (size_t k = 0; k < (size_t)nbat * epochs; ++k) {
+        const int64_t t = m->adam_t + 1 + (int64_t)k;
+        coef[2 * k] = 1.0f - std::pow(b1, (float)t);
+        coef[2 * k + 1] = 1.0f - std::pow(b2, (float)t);
+    }
+    // one epoch's steps are captured once as a CUDA graph over fixed buffers (the
+    // epoch's permutation, bias corrections and minibatch losses) and replayed per epoch
+    int *ep_idx = m->alloc<int>(n);
+    float *dcoef = m->alloc<float>(coef.size() + 2), *ep_coef = m->alloc<float>((size_t)2 * nbat);
+    float *ep_loss = m->alloc<float>((size_t)nbat * batch);
+    auto release = [&]() {
+        for (void *p : {(void *)dx, (void *)dt, (void *)didx, (void *)dloss, (void *)ep_idx, (void *)dcoef,
+                        (void *)ep_coef, (void *)ep_loss})
+            m->free_ptr(p);
+    };
+    if (!ep_idx || !dcoef || !ep_coef || !ep_loss) {
+        release();
+        return m->fail(AEGPU_ERR_NOMEM, "training buffers");
+    }
+    if (epochs) {
+        cudaMemcpyAsync(didx, perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(dcoef, coef.data(), coef.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    }
+    const int64_t cnt = m->nparams();
+    auto epoch = [&]() {
         for (int bi = 0; bi < nbat; ++bi) {
             const int r0 = bi * batch, rows = std::min(batch, n - r0);
-            const int *idx = didx + (size_t)ep * n + r0;
+            const int *idx = ep_idx + r0;
             k_standardise<<<256, 256, 0, s>>>(dx, idx, rows, m->n_in, m->in_mean(), m->in_inv(), m->X0);
             forward(m, rows);
             k_mse<<<(rows + 7) / 8, 256, 0, s>>>(m->Y, dt, idx, rows, m->n_out, m->out_mean(), m->out_inv(), m->dY,
-                                                     dloss + lpos);
-            lpos += batch;
+                                                     ep_loss + (size_t)bi * batch);
             backward(m, rows);
-            m->adam_t += 1;
-            const float c1 = 1.0f - std::pow(b1, (float)m->adam_t), c2 = 1.0f - std::pow(b2, (float)m->adam_t);
             // every weight and bias in one launch (the parameters are contiguous); the BF16
             // copies of the biases are written too but never read (biases stay FP32)
-            const int64_t cnt = m->nparams();
             k_adam<<<std::min<int64_t>((cnt + 255) / 256, 1024), 256, 0, s>>>(m->w, m->wq, m->g, m->m, m->v, cnt, lr, b1,
-                                                                              b2, eps, c1, c2);
+                                                                              b2, eps, ep_coef + 2 * bi);
+        }
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int rc = AEGPU_OK;
+    if (epochs) {
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            rc = m->check("mlp_train capture");
+        } else {
+            epoch();
+            const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            if (ce != cudaSuccess || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+                rc = m->check("mlp_train capture");
         }
     }
-    int rc = AEGPU_OK;
-    if (epoch_loss && epochs) {
+    for (int ep = 0; ep < epochs && rc == AEGPU_OK; ++ep) {
+        cudaMemcpyAsync(ep_idx, didx + (size_t)ep * n, (size_t)n * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(ep_coef, dcoef + (size_t)2 * nbat * ep, (size_t)2 * nbat * sizeof(float),
+                        cudaMemcpyDeviceToDevice, s);
+        if (cudaGraphLaunch(exec, s) != cudaSuccess) rc = m->check("mlp_train graph launch");
+        cudaMemcpyAsync(dloss + (size_t)ep * nbat * batch, ep_loss, (size_t)nbat * batch * sizeof(float),
+                        cudaMemcpyDeviceToDevice, s);
+    }
+    m->adam_t += (int64_t)nbat * epochs;
+    const int64_t lpos = (int64_t)nbat * batch * epochs;
+    if (rc == AEGPU_OK && epoch_loss && epochs) {
         std::vector<float> l(lpos);
         cudaMemcpyAsync(l.data(), dloss, lpos * sizeof(float), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
@@ -606,11 +650,10 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
         }
     }
     cudaStreamSynchronize(s);
-    rc = m->check("mlp_train");
-    m->free_ptr(dx);
-    m->free_ptr(dt);
-    m->free_ptr(didx);
-    m->free_ptr(dloss);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc == AEGPU_OK) rc = m->check("mlp_train");
+    release();
     return rc;
 }
 

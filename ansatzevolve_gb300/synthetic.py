@@ -59,6 +59,50 @@ def family_integrals_from(tensors, s):
     return np.ascontiguousarray(h), np.ascontiguousarray(g)
 
 
+def family_integrals_batch(tensors, svals):
+    """family_integrals_from at every s in svals at once: (h [S, N, N], g [S, N, N, N, N]).
+    Each element goes through the same operations in the same order as the one-at-a-time
+    form, so the two agree bit for bit."""
+    damp, a0, a1, ls = tensors
+    s = np.asarray(svals, dtype=np.float64).reshape(-1, 1, 1)
+    a = a0 + s * a1
+    h = 0.5 * (a + a.transpose(0, 2, 1)) * damp
+    N = a0.shape[0]
+    g = np.zeros((s.shape[0],) + (N,) * 4)
+    lk = []
+    for l0, l1 in ls:
+        l = l0 + s * l1
+        lk.append(0.5 * (l + l.transpose(0, 2, 1)))
+    # a few instances at a time, so that the outer-product temporary stays in cache
+    chunk = 8
+    tmp = np.empty((chunk,) + (N,) * 4)
+    for c in range(0, s.shape[0], chunk):
+        gc = g[c:c + chunk]
+        t = tmp[:gc.shape[0]]
+        for l in lk:
+            lc = l[c:c + chunk]
+            np.multiply(lc[:, :, :, None, None], lc[:, None, None, :, :], out=t)
+            gc += t
+    return np.ascontiguousarray(h), g
+
+
+def family_h_and_coulomb_batch(tensors, svals):
+    """h(s) [S, N, N] and the Coulomb diagonal g_ppqq(s) [S, N, N] of family_integrals_from
+    at every s in svals, without forming g (bit-identical to slicing it)."""
+    damp, a0, a1, ls = tensors
+    s = np.asarray(svals, dtype=np.float64).reshape(-1, 1, 1)
+    a = a0 + s * a1
+    h = 0.5 * (a + a.transpose(0, 2, 1)) * damp
+    N = a0.shape[0]
+    d = np.zeros((s.shape[0], N, N))
+    for l0, l1 in ls:
+        l = l0 + s * l1
+        l = 0.5 * (l + l.transpose(0, 2, 1))
+        dg = np.diagonal(l, axis1=1, axis2=2)
+        d += dg[:, :, None] * dg[:, None, :]
+    return np.ascontiguousarray(h), d
+
+
 def family_integrals(n_orb, s, seed=0, n_factors=None, pert=1.0):
     """h(s) = h0 + s*h1 and L^k(s) = L^k0 + s*L^k1 for a Hamiltonian family scan; the
     perturbation tensors h1, L^k1 are drawn at `pert` times the base tensors' scale."""

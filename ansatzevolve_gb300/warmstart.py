@@ -183,14 +183,26 @@ class FamilySpec:
         self.scale = np.asarray(scale, dtype=np.float64)
         self.P = int(self.param0.max()) + 1
 
-    def integrals(self, s):
-        from .synthetic import family_integrals_from, family_tensors
+    def tensors(self):
+        from .synthetic import family_tensors
         if getattr(self, "_tensors", None) is None:
             self._tensors = family_tensors(self.n_orb, seed=self.seed, pert=self.pert)
-        return family_integrals_from(self._tensors, float(s))
+        return self._tensors
+
+    def integrals(self, s):
+        from .synthetic import family_integrals_from
+        return family_integrals_from(self.tensors(), float(s))
+
+    def integrals_batch(self, svals):
+        """(h [S, N, N], g [S, N, N, N, N]) at every s, bit-identical to integrals(s)."""
+        from .synthetic import family_integrals_batch
+        return family_integrals_batch(self.tensors(), svals)
 
     def features(self, svals):
-        return np.stack([features(*self.integrals(s)) for s in svals])
+        """features(*integrals(s)) for every s (bit-identical), without forming g."""
+        from .synthetic import family_h_and_coulomb_batch
+        h, d = family_h_and_coulomb_batch(self.tensors(), svals)
+        return np.concatenate([h.reshape(len(h), -1), d.reshape(len(d), -1)], axis=1)
 
     def engine(self, nb=1, integrals=None, mode=None):
         e, _, _ = family_engine(self.n_orb, self.n_alpha, self.layers, nb, integrals, mode)
@@ -301,9 +313,7 @@ def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None):
     for t in range(1, L):
         idx = np.minimum(heads + t, ends - 1)
         live = heads + t < ends
-        ints = [spec.integrals(svals[i]) for i in idx]
-        eb.set_ham_integrals_batch(np.stack([a for a, _ in ints]), np.stack([b for _, b in ints]),
-                                   HAM_ON_THE_FLY if mode is None else mode)
+        eb.set_ham_integrals_batch(*spec.integrals_batch(svals[idx]), HAM_ON_THE_FLY if mode is None else mode)
         X, E, gn, it, _ = eb.optimise_batch(X, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=H)
         E, gn = np.atleast_1d(E), np.atleast_1d(gn)
         xs[idx[live]], Es[idx[live]], gs[idx[live]], its[idx[live]] = X[live], E[live], gn[live], it[live]
@@ -334,9 +344,11 @@ def scan_batched_warm(spec, svals, model, x_fallback, gtol=1e-6, n_anchor=4, mod
     from . import HAM_ON_THE_FLY, HAM_STORED
     svals = np.asarray(svals, dtype=np.float64)
     M = len(svals)
-    ints = [spec.integrals(s) for s in svals]
-    feats = np.stack([features(*i) for i in ints])
-    e = spec.engine(M, ints, HAM_ON_THE_FLY if mode is None else mode)
+    h1s, g2s = spec.integrals_batch(svals)
+    ints = list(zip(h1s, g2s))
+    feats = spec.features(svals)
+    e = spec.engine(M)
+    e.set_ham_integrals_batch(h1s, g2s, HAM_ON_THE_FLY if mode is None else mode)
     anchors = np.argsort(svals)[(np.arange(n_anchor) * M + M // 2) // n_anchor] if n_anchor else []
     ea = spec.engine(1)
     t0 = time.perf_counter()

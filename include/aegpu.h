@@ -99,11 +99,21 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * same angles (1, the default, or 0: the gradient recomputes H psi as the reference's
  * evolveDerivative does, fusedevolve.cpp:2292; the environment variable
  * AEGPU_REUSE_HPSI=0 sets 0 for engines created afterwards, e.g. the one behind the
- * reference-compatible C ABI).  No counterpart in the reference. */
+ * reference-compatible C ABI), and the spin-flip half product of the energy's H psi
+ * (1, the default, or 0; AEGPU_FLIP=0 in the environment sets 0 for engines created
+ * afterwards): with as many alpha as beta electrons and an integral Hamiltonian (coded
+ * stored rows or on the fly), a state with psi(a,b) = psi(b,a) for every pair of alpha
+ * and beta strings, which the device tests before every such product (relative norm
+ * of the difference <= 1e-12), has H psi of the same symmetry, so only the rows with
+ * a <= b are computed and mirrored.  No counterpart in the reference. */
 enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
-       AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6 };
+       AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6, AEGPU_TUNE_FLIP = 7 };
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
+/* used[b] = 1 where the last energy evaluation's H psi of instance b took the spin-flip
+ * half product, 0 where it took the full one (or did not test; masked instances keep
+ * their earlier value).  Synchronises the engine's stream. */
+int aegpu_flip_status(aegpu_engine *e, int *used);
 int aegpu_batch_size(const aegpu_engine *e);
 /* Instance mask of batched evaluations: active[b] = 0 skips instance b (its results are
  * left as they were); NULL makes every instance active.  The Hessian and the H*x
@@ -388,7 +398,9 @@ int64_t aegpu_device_bytes(const aegpu_engine *e);
 void aegpu_debug_fail_alloc_after(int64_t n);
 /* FP64 instructions of one energy + gradient evaluation per instance: work[0] H psi
  * (one DFMA per matrix element + the energy FMA), work[1] forward passes, work[2]
- * adjoint passes (complex mode counts each real part). */
+ * adjoint passes (complex mode counts each real part), work[3] H psi by the spin-flip
+ * half product (its rows, the energy FMAs and the invariance test; 0 where the engine
+ * cannot take it).  work holds 4 entries. */
 int aegpu_fp64_work(const aegpu_engine *e, int64_t *work);
 /* Measured DFMA throughput of the current device, TFLOP/s (FMA = 2 flops). */
 int aegpu_fp64_peak(double *tflops);
