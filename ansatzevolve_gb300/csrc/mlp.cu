@@ -21,7 +21,7 @@
 
 namespace {
 
-constexpr int kTM = 64, kTN = 64, kTK = 16, kGemmThreads = 256;
+constexpr int kTM = 64, kTN = 64, kTK = 32, kGemmThreads = 256;
 
 enum Epilogue { kPlain = 0, kBiasGelu = 1, kBias = 2, kGeluGrad = 3 };
 
@@ -66,32 +66,54 @@ __device__ __forceinline__ float epilogue(float v, int64_t o, int n, const float
 // Split K (gridDim.z > 1, for products with few output tiles): CTA z sums k in
 // [z * kz, (z + 1) * kz) and writes its raw partial to C + z * M * N (a workspace);
 // k_gemm_reduce adds the partials in z order and applies the epilogue.  The tile loads
-// walk the operand's unit-stride dimension fastest, so they coalesce.
+// walk the operand's unit-stride dimension fastest, so they coalesce; the next K tile's
+// loads are issued into registers before the current tile's products, so their latency
+// overlaps the arithmetic.
 template <typename TB>
 __global__ void __launch_bounds__(kGemmThreads) k_gemm(const float *__restrict__ A, int64_t a_rs, int64_t a_cs,
                                                        const TB *__restrict__ B, int64_t b_rs, int64_t b_cs,
                                                        float *__restrict__ C, int M, int N, int K, int kz,
                                                        const float *__restrict__ bias, float *__restrict__ Z, int epi)
 {
+    constexpr int LA = kTK * kTM / kGemmThreads, LB = kTK * kTN / kGemmThreads;
     __shared__ float As[kTK][kTM + 1];
     __shared__ float Bs[kTK][kTN + 1];
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
     const int kb = blockIdx.z * kz, ke = kb + kz < K ? kb + kz : K;
     const bool a_k_fast = a_cs == 1, b_k_fast = b_rs == 1;
-    float acc[4][4] = {};
-    for (int k0 = kb; k0 < ke; k0 += kTK) {
-        for (int i = threadIdx.x; i < kTK * kTM; i += kGemmThreads) {
+    float ra[LA], rb[LB];
+    auto load = [&](int k0) {
+#pragma unroll
+        for (int t = 0; t < LA; ++t) {
+            const int i = threadIdx.x + t * kGemmThreads;
             const int kk = a_k_fast ? i % kTK : i / kTM, mm = a_k_fast ? i / kTK : i % kTM;
             const int m = m0 + mm, k = k0 + kk;
-            As[kk][mm] = (m < M && k < ke) ? A[(int64_t)m * a_rs + (int64_t)k * a_cs] : 0.0f;
+            ra[t] = (m < M && k < ke) ? A[(int64_t)m * a_rs + (int64_t)k * a_cs] : 0.0f;
         }
-        for (int i = threadIdx.x; i < kTK * kTN; i += kGemmThreads) {
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int i = threadIdx.x + t * kGemmThreads;
             const int kk = b_k_fast ? i % kTK : i / kTN, nn = b_k_fast ? i / kTK : i % kTN;
             const int n = n0 + nn, k = k0 + kk;
-            Bs[kk][nn] = (n < N && k < ke) ? ldf(B + (int64_t)k * b_rs + (int64_t)n * b_cs) : 0.0f;
+            rb[t] = (n < N && k < ke) ? ldf(B + (int64_t)k * b_rs + (int64_t)n * b_cs) : 0.0f;
+        }
+    };
+    float acc[4][4] = {};
+    if (kb < ke) load(kb);
+    for (int k0 = kb; k0 < ke; k0 += kTK) {
+#pragma unroll
+        for (int t = 0; t < LA; ++t) {
+            const int i = threadIdx.x + t * kGemmThreads;
+            As[a_k_fast ? i % kTK : i / kTM][a_k_fast ? i / kTK : i % kTM] = ra[t];
+        }
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int i = threadIdx.x + t * kGemmThreads;
+            Bs[b_k_fast ? i % kTK : i / kTN][b_k_fast ? i / kTK : i % kTN] = rb[t];
         }
         __syncthreads();
+        if (k0 + kTK < ke) load(k0 + kTK);
 #pragma unroll
         for (int kk = 0; kk < kTK; ++kk) {
             float a[4], b[4];
@@ -131,15 +153,25 @@ __global__ void k_gemm_reduce(const float *__restrict__ ws, int ksplit, int M, i
     }
 }
 
-// column sums: out[n] = sum_m X[m][n] (bias gradients); one thread per column,
-// fixed summation order
+// column sums: out[n] = sum_m X[m][n] (bias gradients).  A CTA of 8 warps per 32
+// columns: warp w sums rows w, w + 8, ... of column lane (coalesced), then the eight
+// warp sums are added in warp order (fixed summation order).
+constexpr int kColsumWarps = 8;
 __global__ void k_colsum(const float *__restrict__ X, int M, int N, float *__restrict__ out)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
+    __shared__ float part[kColsumWarps][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = blockIdx.x * 32 + lane;
     float s = 0;
-    for (int m = 0; m < M; ++m) s += X[(int64_t)m * N + n];
-    out[n] = s;
+    if (n < N)
+        for (int m = w; m < M; m += kColsumWarps) s += X[(int64_t)m * N + n];
+    part[w][lane] = s;
+    __syncthreads();
+    if (w == 0 && n < N) {
+        float t = 0;
+        for (int k = 0; k < kColsumWarps; ++k) t += part[k][lane];
+        out[n] = t;
+    }
 }
 
 // rows of X (indexed through idx, nullable) standardised into Xn
@@ -311,7 +343,7 @@ struct aegpu_mlp {
 
 namespace {
 
-// Products with fewer than 64 output tiles split K over up to kMaxSplit CTAs per tile
+// Products with fewer than 128 output tiles split K over up to kMaxSplit CTAs per tile
 // (at least 64 k per CTA), so that more SMs share the latency-bound K loop.
 constexpr int kMaxSplit = 8;
 constexpr int64_t kSplitWorkspace = (int64_t)kMaxSplit * 64 * kTM * kTN;
@@ -323,7 +355,7 @@ void gemm(cudaStream_t s, float *ws, const float *A, int64_t a_rs, int64_t a_cs,
     dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM);
     const int tiles = grid.x * grid.y;
     int split = 1;
-    if (tiles < 64 && ws)
+    if (tiles < 128 && ws)
         while (split < kMaxSplit && K / (split * 2) >= 64 && (int64_t)split * 2 * M * N <= kSplitWorkspace) split *= 2;
     const int kz = (K + split - 1) / split;
     grid.z = split;
@@ -356,15 +388,15 @@ void backward(aegpu_mlp *m, int rows)
     cudaStream_t s = m->stream;
     // layer 3: dW3[o][k] = sum_b dY[b][o] A2[b][k]; db3; dA2 = dY W3 (gelu' of Z2 fused)
     gemm(s, m->ws, m->dY, 1, no, m->A2, H, 1, g + m->off[4], no, H, rows, nullptr, nullptr, kPlain);
-    k_colsum<<<(no + 127) / 128, 128, 0, s>>>(m->dY, rows, no, g + m->off[5]);
+    k_colsum<<<(no + 31) / 32, 32 * kColsumWarps, 0, s>>>(m->dY, rows, no, g + m->off[5]);
     gemm(s, m->ws, m->dY, no, 1, W3, H, 1, m->dZ, rows, H, no, nullptr, m->Z2, kGeluGrad);
     // layer 2
     gemm(s, m->ws, m->dZ, 1, H, m->A1, H, 1, g + m->off[2], H, H, rows, nullptr, nullptr, kPlain);
-    k_colsum<<<(H + 127) / 128, 128, 0, s>>>(m->dZ, rows, H, g + m->off[3]);
+    k_colsum<<<(H + 31) / 32, 32 * kColsumWarps, 0, s>>>(m->dZ, rows, H, g + m->off[3]);
     gemm(s, m->ws, m->dZ, H, 1, W2, H, 1, m->dA, rows, H, H, nullptr, m->Z1, kGeluGrad);
     // layer 1 (no input gradient needed)
     gemm(s, m->ws, m->dA, 1, H, m->X0, ni, 1, g + m->off[0], H, ni, rows, nullptr, nullptr, kPlain);
-    k_colsum<<<(H + 127) / 128, 128, 0, s>>>(m->dA, rows, H, g + m->off[1]);
+    k_colsum<<<(H + 31) / 32, 32 * kColsumWarps, 0, s>>>(m->dA, rows, H, g + m->off[1]);
 }
 
 }  // namespace

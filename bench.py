@@ -66,6 +66,9 @@ SELL_TRAFFIC_RATIO = (669.273856 + 3.678720) / 668.570112
 # 10-orbital launch (355.99 MB read + 4.28 MB written for 356.13 MB of coded rows,
 # x and y); profiles/k_spmv_vell_tups10_stored.md
 VELL_TRAFFIC_RATIO = (355.988992 + 4.284160) / 356.130432
+# the same for the spin-flip half product (profiles/k_spmv_vell_tups10_half.md): DRAM
+# bytes of one launch over the coded rows with a <= b (31,878 of 63,504) plus x and y
+VELL_HALF_TRAFFIC_RATIO = (189.438720 + 3.268096) / (31878 * 5592 / 1e6 + 16 * 63504 / 1e6)
 
 
 def coded_row_bytes(D, W, width):
@@ -379,7 +382,8 @@ def tuned(key):
 
 
 def batched_bench(stream, steps=10, warmup=3):
-    """512 instances with their own seeded integrals and U(-0.3, 0.3) angles, evaluated
+    """512 instances with their own seeded integrals and U(-0.3, 0.3) TUPS angles (one per
+    parameter, drawn [instances, parameters] class by class), evaluated
     by ONE graph launch: 256 x 8 orbitals (4a+4b, 2 layers), 192 x 10 orbitals (5a+5b,
     3 layers), 64 x 12 orbitals (6a+6b, 3 layers); instance i uses integral seed i."""
     import torch
@@ -394,7 +398,7 @@ def batched_bench(stream, steps=10, warmup=3):
     for N, na, L, nb, s0, mode in classes:
         key = autotune.problem_key(N, na, na, L, nb, mode, True)
         tuning = tuned(key)
-        ops, _, _ = tups_operators(N, L)
+        ops, param, scale = tups_operators(N, L)
         e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops - 1, tuning=tuning or None)
         init = np.zeros(e.D)
         init[np.searchsorted(e.states(), hartree_fock_index(N, na, na))] = 1.0
@@ -402,7 +406,9 @@ def batched_bench(stream, steps=10, warmup=3):
         e.set_batch(nb)
         ints = [synthetic_integrals(N, s) for s in range(s0, s0 + nb)]
         e.set_ham_integrals_batch(np.stack([i[0] for i in ints]), np.stack([i[1] for i in ints]), mode)
-        e.io_put_angles(rng.uniform(-0.3, 0.3, (nb, e.nops)))
+        # TUPS angles: one per parameter (an alpha-beta pair of singles shares it)
+        X = rng.uniform(-0.3, 0.3, (nb, int(param.max())))
+        e.io_put_angles(np.asarray(scale, dtype=float)[None, :] * X[:, param - 1])
         e.io_get_results()
         engines.append(e)
         per_class.append({"orbitals": N, "instances": nb, "D": e.D, "ham": "stored" if mode == ae.HAM_STORED else
@@ -628,7 +634,7 @@ def batched_columns_bench(stream, h=1e-4, n_line=8):
             "api": "aegpu_launch_io: one captured graph of the batched energy + gradient evaluation per class"}
 
 
-def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=250):
+def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=125, batch=256):
     """Time to converge over a 10-orbital Hamiltonian family scan (5a+5b, 3 layers,
     81 parameters): h(s) = h0 + s h1, L^k(s) = L^k0 + s L^k1.  Both paths start the scan
     from the s = 0 member's lowest minimum found by a 64-start batched search (shared,
@@ -655,7 +661,7 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=250):
     xtr, Etr, gtr, its = ws.scan_segmented_chain(spec, s_tr, x0, n_seg=n_seg, gtol=1e-8)
     t_chain = time.perf_counter() - t0
     t0 = time.perf_counter()
-    model, hist = ws.train_warmstart(spec.features(s_tr), xtr, epochs=epochs, batch=128, lr=1e-3)
+    model, hist = ws.train_warmstart(spec.features(s_tr), xtr, epochs=epochs, batch=batch, lr=1e-3)
     t_train = time.perf_counter() - t0
     r = ws.scan_batched_warm(spec, s_ho, model, x0, gtol=1e-6, n_anchor=8)
     mode, mode_info = plain_mode(spec, s_ho[0], x0)
@@ -680,23 +686,11 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=250):
             "training": {"instances": n_train, "chain_s": t_chain, "chain_iters_median": float(np.median(its)),
                          "chain": "%d heads in sequence, then the %d segments walked in lockstep batches" % (n_seg, n_seg),
                          "chain_max_gnorm": float(np.max(gtr)),
-                         "mlp_train_s": t_train, "epochs": epochs, "loss_first": float(hist[0]),
+                         "mlp_train_s": t_train, "epochs": epochs, "minibatch": batch, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1]), "origin_s": t_origin, "origin_energy": float(E0)},
             "workload": "10 orbitals 5a+5b, 3 layers (81 parameters), family h(s)=h0+s h1, L(s)=L0+s L1, seed 0, "
                         "h1 and L1 at %.2f of the base scale; %d training / %d held-out s ~ U(0,1)"
                         % (spec.pert, n_train, n_heldout)}
-
-
-def flip_slab_fraction(nA):
-    """Fraction of the 32-row slabs of an nA x nA Sz basis (row a * nA + b) that hold a
-    row with a <= b: the slabs the spin-flip half product streams."""
-    D = nA * nA
-    r = np.arange(D, dtype=np.int64)
-    upper = (r // nA) <= (r % nA)
-    ns = (D + 31) // 32
-    pad = np.zeros(ns * 32, dtype=bool)
-    pad[:D] = upper
-    return float(pad.reshape(ns, 32).any(axis=1).mean())
 
 
 def gram_kernel_bench(args, n=853776, V=100):
@@ -909,8 +903,9 @@ def main():
     achieved = hpsi_bytes / t_hpsi / 1e9
     coded_bytes = coded_row_bytes(D, W, nnz // D) if mode == ae.HAM_STORED else None
     if coded_bytes and half:
-        # the half product streams the listed 32-row slabs of the coded rows
-        coded_bytes = int((coded_bytes - 16 * D * W) * flip_slab_fraction(nA)) + 16 * D * W
+        # the half product streams the coded rows with a <= b (the other rows of the
+        # listed 32-row slabs are skipped without loads)
+        coded_bytes = int((coded_bytes - 16 * D * W) * row_frac) + 16 * D * W
     # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
     passes = info["blocks"]
     step_bytes = passes * 16 * D * W + hpsi_bytes + passes * 32 * D * W
@@ -948,10 +943,11 @@ def main():
                      "full_product_algorithmic_bytes": full_hpsi_bytes,
                      # DRAM bytes per launch: the ncu count of the 10-orbital launch of this kernel
                      # (traffic / streamed bytes) scaled to this launch
-                     "traffic": (coded_bytes * VELL_TRAFFIC_RATIO if coded_bytes else hpsi_bytes * SELL_TRAFFIC_RATIO)
-                     if mode == ae.HAM_STORED else None,
-                     "traffic_source": ("profiles/k_spmv_vell_tups10_stored.md (scaled by streamed bytes)" if coded_bytes
-                                        else "profiles/k_spmv_sell_tups10_stored.md (scaled by nonzeros)")
+                     "traffic": (coded_bytes * (VELL_HALF_TRAFFIC_RATIO if half else VELL_TRAFFIC_RATIO) if coded_bytes
+                                 else hpsi_bytes * SELL_TRAFFIC_RATIO) if mode == ae.HAM_STORED else None,
+                     "traffic_source": (("profiles/k_spmv_vell_tups10_half.md" if half else
+                                         "profiles/k_spmv_vell_tups10_stored.md") + " (scaled by streamed bytes)"
+                                        if coded_bytes else "profiles/k_spmv_sell_tups10_stored.md (scaled by nonzeros)")
                      if mode == ae.HAM_STORED else None,
                      "stream_bytes": coded_bytes, "stream_frac": coded_bytes / t_hpsi / 1e9 / peak if coded_bytes else None,
                      "fp64_frac": fw_h / t_hpsi / 1e12 / peak_t if fw_h else None,

@@ -246,16 +246,18 @@ def batched_case(tag):
     """Configuration 4's batched instances against the reference: instance 0 of each size
     class of the benchmark's 512-instance launch -- 8 orbitals (4a+4b, 2 layers, integral
     seed 0), 10 (5a+5b, 3 layers, seed 256), 12 (6a+6b, 3 layers, seed 448) -- with the
-    bench's own per-operator angles (default_rng(0).uniform(-0.3, 0.3) drawn class by
-    class, [instances, operators]): energy and compressed gradient."""
+    bench's own TUPS angles (default_rng(0).uniform(-0.3, 0.3) drawn class by class,
+    [instances, parameters], each operator taking scale * x[param]): energy and
+    compressed gradient.  x{N} holds the operators' angles, xc{N} the parameters."""
     classes = [(8, 4, 2, 256, 0), (10, 5, 3, 192, 256), (12, 6, 3, 64, 448)]
     rng = np.random.default_rng(0)
     fx = {}
     for N, na, L, nb, s0 in classes:
         ops, param, scale = tups_operators(N, L)
-        ang = rng.uniform(-0.3, 0.3, (nb, len(ops)))[0]
-        h, g = synthetic_integrals(N, s0)
         P = int(param.max())
+        xc = rng.uniform(-0.3, 0.3, (nb, P))[0]
+        ang = np.asarray(scale, dtype=float) * xc[param - 1]
+        h, g = synthetic_integrals(N, s0)
         with tempfile.TemporaryDirectory() as td:
             prefix = os.path.join(td, "syn")
             write_integrals(prefix, h, g)
@@ -265,6 +267,7 @@ def batched_case(tag):
         fx[f"E{N}"] = d[0]
         fx[f"G{N}"] = d[1:1 + P]
         fx[f"x{N}"] = ang
+        fx[f"xc{N}"] = xc
         fx[f"seed{N}"] = s0
         print(tag, N, d[0])
     np.savez_compressed(os.path.join(OUT, tag + ".npz"), **fx)
