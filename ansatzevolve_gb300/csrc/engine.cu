@@ -1507,7 +1507,7 @@ __device__ __forceinline__ bool flip_half(const FlipArgs &f, int b)
         s0 += __shfl_xor_sync(0xffffffffu, s0, o);
         s1 += __shfl_xor_sync(0xffffffffu, s1, o);
     }
-    return s0 > 0.0 && s1 <= kFlipTol * kFlipTol * s0;
+    return s1 <= kFlipTol * kFlipTol * s0;  // a zero vector passes (s1 = s0 = 0)
 }
 
 // y = H x with coded rows.  T threads per row as in k_spmv_sell.  Each CTA owns an
@@ -1517,9 +1517,9 @@ __device__ __forceinline__ bool flip_half(const FlipArgs &f, int b)
 // staged once per CTA, in shared memory.  NV > 1: one thread carries NV right-hand sides (instances
 // blockIdx.y * NV + v, shared matrix, no energy and no mask), so each matrix entry read
 // serves NV products.  Energy partial per CTA: sum over its rows of y_r x_r.
-// Half product (NV = 1, flip.part set and the instance's input flip-invariant): the
-// CTAs share the slabs of flip.slabs instead of all rows, rows with a > b are left to
-// their mirror, and each row's result also goes to its mirror row (energy: both rows).
+// Half product (flip.part set and every right-hand side of the CTA flip-invariant):
+// the CTAs share the slabs of flip.slabs instead of all rows, rows with a > b are left
+// to their mirror, and each row's result also goes to its mirror row (energy: both rows).
 template <int W, int T, int NV>
 __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const double *__restrict__ x,
                                                                double *__restrict__ y, int64_t D, int ninst,
@@ -1532,7 +1532,10 @@ __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const
     const int b0 = blockIdx.y * NV;
     if (NV == 1 && skip_instance(active, b0)) return;
     if (threadIdx.x < 32) {
-        const bool h = NV == 1 && flip_half(flip, b0);
+        // half product only when every right-hand side of the CTA passed the test
+        bool h = flip.part != nullptr;
+        for (int v = 0; v < NV && h; ++v)
+            if (b0 + v < ninst) h = flip_half(flip, b0 + v);
         if (threadIdx.x == 0) {
             s_half = h;
             if (NV == 1 && flip.used && blockIdx.x == 0) flip.used[b0] = h;
@@ -1541,7 +1544,7 @@ __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const
     const double *vt = m.vtab + (size_t)b0 * m.vtab_inst;
     for (int64_t i = threadIdx.x; i < m.vtab_len; i += blockDim.x) tab[i] = vt[i];
     __syncthreads();
-    const bool half = NV == 1 && s_half;
+    const bool half = s_half;
     const int32_t *colE = m.colE + (size_t)b0 * m.inst_e, *colD = m.colD + (size_t)b0 * m.inst_d;
     const double *valE = m.valE + (size_t)b0 * m.inst_e;
     const uint16_t *codeD = m.codeD + (size_t)b0 * m.inst_d;
@@ -1631,9 +1634,9 @@ __global__ void __launch_bounds__(kVellThreads, 1) k_spmv_vell(VellArgs m, const
                 if (r < D && sub == 0) {
                     yv[r * W + w] = s;
                     if (NV == 1) e = fma(s, xv[r * W + w], e);
-                    if (NV == 1 && rf >= 0) {
+                    if (rf >= 0) {
                         yv[rf * W + w] = s;
-                        e = fma(s, xv[rf * W + w], e);
+                        if (NV == 1) e = fma(s, xv[rf * W + w], e);
                     }
                 }
             }
@@ -1996,6 +1999,7 @@ struct aegpu_engine {
         double *gram = nullptr; // partial sums of the Gram / projection contractions
         int *pptr = nullptr, *ppos = nullptr;
         double *pscale = nullptr;
+        double *flip = nullptr;  // invariance-test partials of the V columns
         std::vector<std::pair<void *, size_t>> allocs;
     } hess;
 
@@ -2322,8 +2326,11 @@ int upload_angles(aegpu_engine *e, const double *angles, bool host, int ninst, b
 
 // y = H x for the first ninst instances (vectors at stride D*W), with <x|y> partial
 // sums into epart (nullable; *nparts partial sums per instance).
+// flip: try the spin-flip half product, with the invariance test's partials in
+// flip_part (2 * sm_count doubles per instance) and the per-instance choice recorded in
+// flip_used (nullable; the energy evaluation's record for aegpu_flip_status).
 int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ninst, int *nparts = nullptr,
-              bool masked = true, bool flip = false)
+              bool masked = true, bool flip = false, double *flip_part = nullptr, int *flip_used = nullptr)
 {
     const int *act = masked ? e->d_active : nullptr;
     if (nparts) *nparts = e->spmv_grid;
@@ -2332,11 +2339,11 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
     // product kernels read the test's partials and pick the half or the full product
     FlipArgs fa{};
     const bool coded = e->ham_kind == 2 && e->ell_coded;
-    if (flip) e->flip_tried = false;
-    if (flip && e->tune_flip && e->flip_ok && (coded || e->ham_kind == 3)) {
-        e->flip_tried = true;
-        fa.part = e->d_flip_part;
-        fa.used = e->d_flip_used;
+    if (flip_used) e->flip_tried = false;
+    if (flip && flip_part && e->tune_flip && e->flip_ok && (coded || e->ham_kind == 3)) {
+        if (flip_used) e->flip_tried = true;
+        fa.part = flip_part;
+        fa.used = flip_used;
         fa.slabs = e->d_flip_slabs;
         fa.nslabs = e->n_flip_slabs;
         fa.G = e->sm_count;
@@ -2345,9 +2352,9 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         fa.div_l = e->db.div_l;
         const dim3 g(e->sm_count, ninst);
         if (e->W == 1)
-            k_flip_check<1><<<g, 256, 0, e->stream>>>(fa, x, D, e->d_flip_part, act);
+            k_flip_check<1><<<g, 256, 0, e->stream>>>(fa, x, D, flip_part, act);
         else
-            k_flip_check<2><<<g, 256, 0, e->stream>>>(fa, x, D, e->d_flip_part, act);
+            k_flip_check<2><<<g, 256, 0, e->stream>>>(fa, x, D, flip_part, act);
         e->launches += 1;
     }
     if (e->ham_kind == 1) {
@@ -2371,8 +2378,7 @@ int run_apply(aegpu_engine *e, const double *x, double *y, double *epart, int ni
         const int nv = multi ? (e->W == 1 ? kVellNV1 : kVellNV2) : 1;
         const dim3 g(gx, (ninst + nv - 1) / nv);
 #define AE_VELL(WW, TT, NN) \
-    k_spmv_vell<WW, TT, NN><<<g, kVellThreads, smem, e->stream>>>(e->vell, x, y, D, ninst, epart, act, \
-                                                                   multi ? FlipArgs{} : fa)
+    k_spmv_vell<WW, TT, NN><<<g, kVellThreads, smem, e->stream>>>(e->vell, x, y, D, ninst, epart, act, fa)
         if (e->W == 1) {
             if (multi) {
                 if (T == 1) AE_VELL(1, 1, kVellNV1); else if (T == 2) AE_VELL(1, 2, kVellNV1);
@@ -2429,7 +2435,7 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 {
     NvtxRange r("aegpu H*psi + energy");
     int np = 0;
-    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np, true, true);
+    int rc = run_apply(e, e->d_psi, e->d_h, e->d_epart, ninst, &np, true, true, e->d_flip_part, e->d_flip_used);
     if (rc) return rc;
     k_reduce_sum<<<ninst, 256, 0, e->stream>>>(e->d_epart, np, E_dev, 1.0, e->d_active);
     e->launches += 1;
@@ -3737,7 +3743,8 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         bool ok = get(hs.T, n * nops) && get(hs.TC, n * V) && get(hs.HTC, n * V) && get(hs.THT, (size_t)V * V) &&
                   get(hs.MET, (size_t)V * V) && get(hs.gram, (size_t)ngram) &&
                   get(hs.Hops, (size_t)nops * nops) && get(hs.hpart, maxpart) && get(hs.pptr, (size_t)nparams + 1) &&
-                  get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops);
+                  get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops) &&
+                  get(hs.flip, (size_t)V * 2 * e->sm_count);
         if (!ok) {
             for (auto &pa : hs.allocs) e->release(pa.first, pa.second);
             hs = aegpu_engine::HessScratch{};
@@ -3804,7 +3811,9 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         e->launches += gemv_t(TC, (int64_t)n, (int64_t)n, V, e->d_h, 1.0, THT, hs.gram, e->sm_count, s);
     } else {
         // the V columns as V instances of the H product (the matrix or tables are shared)
-        rc = run_apply(e, TC, HTC, nullptr, V, nullptr, false);
+        // (every compressed tangent of a spin-adapted ansatz is flip-invariant when psi is:
+        // the half product where all columns of a CTA pass the test)
+        rc = run_apply(e, TC, HTC, nullptr, V, nullptr, false, true, hs.flip, nullptr);
         if (rc) return rc;
         // 2 Re(T_C^dagger H T_C) (fusedevolve.cpp:2633-2650) is symmetric (H is): only its
         // upper triangle is computed; column P holds the gradient and twice the energy
@@ -4338,7 +4347,8 @@ int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double 
     cudaStream_t saved = e->stream;
     if (stream) e->stream = (cudaStream_t)stream;
     int np = 0;
-    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, e->nb, &np, false);
+    int rc = run_apply(e, x_dev, y_dev, energy_dev ? e->d_epart : nullptr, e->nb, &np, false, true, e->d_flip_part,
+                       nullptr);
     if (!rc && energy_dev) {
         k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, np, energy_dev, 1.0, nullptr);
         e->launches += 1;

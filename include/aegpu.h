@@ -310,7 +310,9 @@ int aegpu_mlp_train(aegpu_mlp *m, const float *X, const float *T, int n, int epo
 int aegpu_mlp_loss_grad(aegpu_mlp *m, const float *X, const float *T, int n, float *loss, float *grads);
 int aegpu_mlp_predict(aegpu_mlp *m, const float *X, int n, float *Y);
 int aegpu_mlp_predict_dev(aegpu_mlp *m, const float *X_dev, int n, float *Y_dev, void *stream);
-/* y_dev = H x_dev on device vectors; energy_dev (nullable) receives <x|H x>. */
+/* y_dev = H x_dev on device vectors (one per instance of the batch, one launch);
+ * energy_dev (nullable) receives <x|H x>.  Flip-invariant inputs take the spin-flip half
+ * product (AEGPU_TUNE_FLIP). */
 int aegpu_apply_dev(aegpu_engine *e, const double *x_dev, double *y_dev, double *energy_dev, void *stream);
 /* CUDA-event timing of the phases of aegpu_gradient_dev (evolve, H*psi + energy,
  * adjoint sweep): enable, then read the accumulated milliseconds (and the number of

@@ -160,3 +160,35 @@ def test_flip_knob_checks():
     assert e.get_tuning(ae.TUNE_FLIP) == 0
     assert not e.flip_status()[0]  # nothing evaluated yet
     e.close()
+
+
+@pytest.mark.parametrize("mode", [ae.HAM_STORED, ae.HAM_ON_THE_FLY])
+def test_half_product_several_vectors(mode):
+    """aegpu_apply_dev over a batch of vectors in one launch (several right-hand sides per
+    thread with stored rows, the Hessian's form): invariant vectors, a zero one among
+    them, share the half product, a group holding a broken vector takes the full one,
+    and every result agrees with the full product."""
+    torch = pytest.importorskip("torch")
+    N, na, nb = 8, 4, 6
+    pb = synthetic_problem(N, na, na, 2, 1)
+    e = make_engine(pb, nb)
+    e.set_ham_integrals(pb["h1"], pb["g2"], mode)
+    D, nA = e.D, int(round(e.D ** 0.5))
+    r = np.random.default_rng(9).normal(size=(nb, nA, nA))
+    X = r + r.transpose(0, 2, 1)
+    X[1] = 0.0
+    X[4] = r[4]
+    x = torch.tensor(X.reshape(nb, D), dtype=torch.float64, device="cuda")
+    ys = []
+    s = torch.cuda.Stream()
+    for flip in (1, 0):
+        e.set_tuning(ae.TUNE_FLIP, flip)
+        y = torch.zeros_like(x)
+        with torch.cuda.stream(s):
+            e.apply_dev(x.data_ptr(), y.data_ptr(), None, s.cuda_stream)
+        s.synchronize()
+        ys.append(y.cpu().numpy())
+    y1, y0 = ys
+    assert np.max(np.abs(y1 - y0)) <= 1e-12 * np.max(np.abs(y0))
+    assert not np.any(y1[1]) and np.array_equal(y1[4], y0[4])
+    e.close()
