@@ -275,13 +275,18 @@ def scan_bfgs_chain(spec, svals, x_start, gtol=1e-8, mode=None):
     return np.array(xs), np.array(Es), np.array(gs), np.array(its)
 
 
-def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None):
+def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None, predict=True):
     """Training targets as a two-level continuation over the given (sorted) s values:
     a sequential BFGS chain over n_seg segment heads (every L-th value, L = ceil(M /
     n_seg)), then every segment walked at once -- step t optimises the t-th member of
     all segments in one lockstep batch, each instance from its predecessor's converged
     angles and final inverse Hessian (on-the-fly H per instance).  The same
     continuation as scan_bfgs_chain, with n_seg + L sequential solves instead of M.
+    predict: start each solve from the secant predictor through the two previous
+    converged points of its chain, x1 + (x1 - x2) (s - s1) / (s1 - s2) (the
+    predictor-corrector continuation of Allgower & Georg, Introduction to Numerical
+    Continuation Methods, ch. 2), instead of the previous point; the minima reached are
+    the same (to the tolerance), the solves shorter.
     Returns (x [M, P], E [M], |g| [M], iterations [M])."""
     from . import HAM_ON_THE_FLY, HAM_STORED
     svals = np.asarray(svals, dtype=np.float64)
@@ -301,6 +306,9 @@ def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None):
         e1.set_ham_integrals(*spec.integrals(svals[h]), HAM_STORED if mode is None else mode)
         if hinv is None:
             hinv = np.ascontiguousarray(inverse_hessian(e1, x[0], spec)[None])
+        if predict and k >= 2:
+            h1, h2 = heads[k - 1], heads[k - 2]
+            x = (xs[h1] + (xs[h1] - xs[h2]) * (svals[h] - svals[h1]) / (svals[h1] - svals[h2])).reshape(1, -1)
         x, E, gn, it, _ = e1.optimise_batch(x, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=hinv)
         xs[h], Es[h], gs[h], its[h] = x[0], np.atleast_1d(E)[0], np.atleast_1d(gn)[0], it[0]
         hinv_heads[k] = hinv[0]
@@ -310,11 +318,20 @@ def scan_segmented_chain(spec, svals, x_start, n_seg=32, gtol=1e-8, mode=None):
     eb = spec.engine(S)
     X = xs[heads].copy()
     H = np.ascontiguousarray(hinv_heads)
+    s_cur = svals[heads].copy()
+    X_prev = s_prev = None
     for t in range(1, L):
         idx = np.minimum(heads + t, ends - 1)
         live = heads + t < ends
         eb.set_ham_integrals_batch(*spec.integrals_batch(svals[idx]), HAM_ON_THE_FLY if mode is None else mode)
-        X, E, gn, it, _ = eb.optimise_batch(X, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=H)
+        start = X
+        if predict and X_prev is not None:
+            ds = s_cur - s_prev
+            ratio = np.where(live & (ds != 0), (svals[idx] - s_cur) / np.where(ds != 0, ds, 1.0), 0.0)
+            start = X + (X - X_prev) * ratio[:, None]
+        Xn, E, gn, it, _ = eb.optimise_batch(start, spec.param0, spec.scale, gtol=gtol, max_rounds=5000, hinv=H)
+        X_prev, s_prev = X, s_cur
+        X, s_cur = Xn, np.where(live, svals[idx], s_cur)
         E, gn = np.atleast_1d(E), np.atleast_1d(gn)
         xs[idx[live]], Es[idx[live]], gs[idx[live]], its[idx[live]] = X[live], E[live], gn[live], it[live]
     eb.close()

@@ -684,7 +684,8 @@ def ttc_bench(n_train=2000, n_heldout=200, n_plain=200, epochs=400, n_seg=125, b
             "energy_match_1e-8": int(np.sum(np.abs(dE) < 1e-8)), "energy_compared": n_plain,
             "max_abs_dE": float(np.abs(dE).max()),
             "training": {"instances": n_train, "chain_s": t_chain, "chain_iters_median": float(np.median(its)),
-                         "chain": "%d heads in sequence, then the %d segments walked in lockstep batches" % (n_seg, n_seg),
+                         "chain": "%d heads in sequence, then the %d segments walked in lockstep batches; each solve "
+                                  "starts from the secant predictor of its chain" % (n_seg, n_seg),
                          "chain_max_gnorm": float(np.max(gtr)),
                          "mlp_train_s": t_train, "epochs": epochs, "minibatch": batch, "loss_first": float(hist[0]),
                          "loss_last": float(hist[-1]), "origin_s": t_origin, "origin_energy": float(E0)},
