@@ -127,9 +127,35 @@ std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std:
 std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass)
 {
     std::vector<Block> out;
+    // Consecutive diagonal blocks form one run (any two diagonal operators commute):
+    // the divisor rule of the grouping cuts a run of prime length into single-operator
+    // blocks, each of which would be a full sweep over the statevector.  The run is
+    // cut into the fewest near-equal passes of <= kMaxDiagSlots operators instead, in
+    // the same operator order.
+    std::vector<int> run;
+    auto flush = [&]() {
+        const int n = (int)run.size();
+        if (!n) return;
+        const int parts = (n + kMaxDiagSlots - 1) / kMaxDiagSlots;
+        int start = 0;
+        for (int p = 0; p < parts; ++p) {
+            const int len = n / parts + (p < n % parts ? 1 : 0);
+            Block c;
+            c.diagonal = true;
+            c.ops.assign(run.begin() + start, run.begin() + start + len);
+            start += len;
+            out.push_back(std::move(c));
+        }
+        run.clear();
+    };
     for (const auto &b : blocks) {
         const int n = (int)b.ops.size();
-        if (b.diagonal || n <= max_pass) {
+        if (b.diagonal) {
+            run.insert(run.end(), b.ops.begin(), b.ops.end());
+            continue;
+        }
+        flush();
+        if (n <= max_pass) {
             out.push_back(b);
             continue;
         }
@@ -144,6 +170,7 @@ std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass)
             out.push_back(std::move(c));
         }
     }
+    flush();
     return out;
 }
 

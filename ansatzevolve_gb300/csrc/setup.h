@@ -53,8 +53,14 @@ struct Block {
     std::vector<int> ops;   // operator indices (original order) in application order
 };
 
-// Cut every block into passes of at most max_pass excitations (commuting, so any
-// cut gives the same product); orbits of a pass then have at most 2^max_pass members.
+// Operators per diagonal pass: the phase table of a pass has 2^kMaxDiagSlots entries.
+constexpr int kMaxDiagSlots = 12;
+
+// Cut every paired block into passes of at most max_pass excitations (commuting, so
+// any cut gives the same product); orbits of a pass then have at most 2^max_pass
+// members.  Runs of consecutive diagonal blocks are merged and cut into the fewest
+// near-equal passes of at most kMaxDiagSlots operators.  The operator order (the
+// grouping's permutation) is unchanged.
 std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass);
 
 // Greedy commuting-block grouping with forward moves, restating
