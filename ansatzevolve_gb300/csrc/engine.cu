@@ -30,7 +30,8 @@
 //   k_diag_*         the same four for diagonal (number / density-density) blocks,
 //                    complex mode (fusedevolve.cpp:625-717)
 //   k_pass_prep      per evaluation: sin/cos and the scaled-Givens constants of every
-//                    pass and direction, and the scale products of every active mask
+//                    pass and direction, the scale products of every active mask, and
+//                    the phase table of every diagonal pass
 //   k_spmv           warp-per-row CSR y = H x fused with the <x|y> partial sums
 //   k_spmv_vell      y = H x over coded rows (value table in shared memory, 1-8
 //                    threads per row, equal row shares per CTA) fused with <x|y>; with
@@ -89,6 +90,7 @@ struct NvtxRange {
 namespace {
 
 constexpr int kMaxSlots = 12;          // excitations per fused block (the reference's maxFuse)
+static_assert(kMaxDiagSlots <= kMaxSlots, "a diagonal pass's phase table and partial sums hold kMaxSlots slots");
 constexpr int kRotThreads = 256;
 constexpr int kSpmvThreads = 256;
 constexpr int kDiagGrid = 152 * 4;
@@ -399,18 +401,37 @@ struct PrepArgs {
     const int *pass_off;    // first operator of each pass
     const int *pass_n;      // operators per pass
     const int *pass_diag;   // 1 for diagonal passes (no scaled-Givens constants)
+    const int64_t *pass_tab; // diagonal passes: offset of the pass's phase table
+    int64_t tab_stride;     // phase-table doubles per instance
     const ExcCode *codes;
     int nops, npass;
     const int *active;      // instance mask (nullable)
 };
 
+// A diagonal pass's phase table: tab[2m], tab[2m + 1] = cos, sin of the sum of the
+// angles of the slots in m (the adjoint direction negates the sine where it reads it).
+__device__ void diag_phase_table(const int *ops, int ns, const double *__restrict__ ang, double *__restrict__ tab)
+{
+    for (int m = threadIdx.x; m < (1 << ns); m += blockDim.x) {
+        double th = 0;
+        for (int i = 0; i < ns; ++i)
+            if (m & (1 << i)) th += ang[ops[i]];
+        double s, c;
+        sincos(th, &s, &c);
+        tab[2 * m] = c;
+        tab[2 * m + 1] = s;
+    }
+}
+
 __global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *__restrict__ sc,
-                            PassConst *__restrict__ pc, double *__restrict__ sig)
+                            PassConst *__restrict__ pc, double *__restrict__ sig, double *__restrict__ tab)
 {
     const int pass = blockIdx.x, b = blockIdx.y;
     if (skip_instance(a.active, b)) return;
     const int ns = a.pass_n[pass];
     const int *ops = a.pass_ops + a.pass_off[pass];
+    if (a.pass_diag[pass])
+        diag_phase_table(ops, ns, ang + (size_t)b * a.nops, tab + (size_t)b * a.tab_stride + a.pass_tab[pass]);
     __shared__ double f[2][kMaxWarpLayers];
     const bool paired = !a.pass_diag[pass] && ns <= kMaxWarpLayers;
     if (threadIdx.x < (unsigned)ns) {
@@ -732,29 +753,18 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const W
 // ------------------------------------------------------- diagonal blocks --
 // Complex mode only: number / density-density operators multiply every active
 // amplitude by exp(+i * sum of the active angles) (RunFuseNDiagonal,
-// fusedevolve.cpp:625-717).  table[m] = (cos, sin) of dir * sum_{i in m} theta_i.
-__global__ void k_diag_table(const double *__restrict__ ang, const int *__restrict__ ops, int nslots, double dir,
-                             double *__restrict__ table, int nops, const int *__restrict__ active)
-{
-    if (skip_instance(active, blockIdx.y)) return;
-    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= (1u << nslots)) return;
-    ang += (size_t)blockIdx.y * nops;                          // instance blockIdx.y
-    table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
-    double th = 0;
-    for (int i = 0; i < nslots; ++i)
-        if (m & (1u << i)) th += ang[ops[i]];
-    double s, c;
-    sincos(dir * th, &s, &c);
-    table[2 * m] = c;
-    table[2 * m + 1] = s;
-}
-
+// fusedevolve.cpp:625-717), exp(-i * ...) in the adjoint direction.  The pass's table
+// (k_pass_prep) holds (cos, sin) of the angle sum of every slot subset m.
 struct DiagArgs {
     const int *ops;
     int nslots;
     const ExcCode *codes;
-    const double *table;  // instance 0; instance b at + b * 2 * 2^kMaxSlots
+    const double *table;  // this pass's phase table, instance 0; instance b at + b * tab_stride
+    int64_t tab_stride;
+    uint64_t sin_flip;    // 0 forward; sign bit (adjoint direction: the conjugate phase)
+    // Sz basis: slot mask of determinant (a, b) = smA[a] & smB[b] (the slots whose
+    // alpha / beta annihilation bits the string holds); null: from the bitstring
+    const uint16_t *smA, *smB;
     DevBasis basis;
     const int *active;    // instance mask (nullable)
 };
@@ -767,6 +777,13 @@ __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
         if ((bits & ann) == ann) m |= 1u << i;
     }
     return m;
+}
+
+// (cos, sin) of the phase of slot subset m in this pass's direction
+__device__ __forceinline__ double2 diag_phase(const DiagArgs &a, uint32_t m)
+{
+    const double2 t = __ldg(reinterpret_cast<const double2 *>(a.table) + m);
+    return make_double2(t.x, __longlong_as_double(__double_as_longlong(t.y) ^ a.sin_flip));
 }
 
 // The streaming diagonal kernels take kDiagUnroll amplitudes z, z + S, ... (S = grid
@@ -791,6 +808,17 @@ __device__ __forceinline__ uint32_t diag_mask_s(const uint32_t *ann, int nslots,
     return m;
 }
 
+// slot mask of amplitude z (< D): two string-table loads in the Sz basis, else the
+// slots' annihilation masks (ann, shared memory) against the bitstring
+__device__ __forceinline__ uint32_t diag_mask_z(const DiagArgs &a, const uint32_t *ann, uint32_t z)
+{
+    if (a.smA) {
+        const uint32_t r = a.basis.div_nB(z);
+        return (uint32_t)__ldg(a.smA + r) & (uint32_t)__ldg(a.smB + (z - r * a.basis.nB));
+    }
+    return diag_mask_s(ann, a.nslots, a.basis.bits(z));
+}
+
 // ckpt (nullable, single vector): the amplitudes after the pass, for the adjoint sweep.
 __global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, size_t vstride, int nvec,
                                                      double *__restrict__ ckpt, int64_t inst_stride, int64_t ckpt_stride)
@@ -799,7 +827,7 @@ __global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, s
     const uint64_t D = a.basis.D;
     if (skip_instance(a.active, blockIdx.y)) return;
     diag_load_masks(a, ann);
-    a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
+    a.table += (size_t)blockIdx.y * a.tab_stride;
     vecs += (size_t)blockIdx.y * inst_stride;
     if (ckpt) ckpt += (size_t)blockIdx.y * ckpt_stride;
     const uint64_t S = (uint64_t)gridDim.x * blockDim.x;
@@ -808,7 +836,7 @@ __global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, s
 #pragma unroll
         for (int u = 0; u < kDiagUnroll; ++u) {
             const uint64_t z = z0 + u * S;
-            m[u] = z < D ? diag_mask_s(ann, a.nslots, a.basis.bits((uint32_t)z)) : 0u;
+            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z) : 0u;
         }
         for (int vec = 0; vec < nvec; ++vec) {
             double *p = vecs + vec * vstride;
@@ -820,8 +848,8 @@ __global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, s
             for (int u = 0; u < kDiagUnroll; ++u) {
                 if (!m[u]) continue;
                 const uint64_t z = z0 + u * S;
-                const double c = a.table[2 * m[u]], s = a.table[2 * m[u] + 1];
-                const double2 r = make_double2(c * v[u].x - s * v[u].y, s * v[u].x + c * v[u].y);
+                const double2 t = diag_phase(a, m[u]);
+                const double2 r = make_double2(t.x * v[u].x - t.y * v[u].y, t.y * v[u].x + t.x * v[u].y);
                 *reinterpret_cast<double2 *>(p + 2 * z) = r;
                 if (ckpt) *reinterpret_cast<double2 *>(ckpt + 2 * z) = r;
             }
@@ -845,7 +873,7 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
     __shared__ uint32_t ann[kMaxSlots];
     if (skip_instance(a.active, blockIdx.y)) return;
     diag_load_masks(a, ann);
-    a.table += (size_t)blockIdx.y * 2 * (1u << kMaxSlots);
+    a.table += (size_t)blockIdx.y * a.tab_stride;
     ckpt += (size_t)blockIdx.y * ckpt_stride;
     h += (size_t)blockIdx.y * inst_stride;
     partials += (size_t)blockIdx.y * part_stride;
@@ -860,7 +888,7 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint64_t z = z0 + u * S;
-            m[u] = z < D ? diag_mask_s(ann, a.nslots, a.basis.bits((uint32_t)z)) : 0u;
+            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z) : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
@@ -880,9 +908,9 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
                 if (i == a.nslots) break;
                 if (ONE || (m[u] & (1u << i))) acc[i] += q;
             }
-            const double c = a.table[2 * m[u]], s = a.table[2 * m[u] + 1];
+            const double2 t = diag_phase(a, m[u]);
             *reinterpret_cast<double2 *>(h + 2 * (z0 + u * S)) =
-                make_double2(c * y[u].x - s * y[u].y, s * y[u].x + c * y[u].y);
+                make_double2(t.x * y[u].x - t.y * y[u].y, t.y * y[u].x + t.x * y[u].y);
         }
     }
 #pragma unroll
@@ -893,13 +921,111 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
     }
 }
 
+// Adjoint of a diagonal pass in the Sz basis, psi viewed as the nA x nB matrix of
+// (alpha string, beta string) amplitudes.  A CTA owns sp.cols columns (beta strings;
+// the smallest power of two >= nB between 32 and 256) and a run of rows; thread t keeps
+// column b and walks its rows a, so a warp always works on one row and the row's alpha
+// slot mask smA[a] is the same on all its lanes.
+// With q = Im(h psi*) at (a, b) (psi from the checkpoint), the gradient of slot i is the
+// sum of q over the amplitudes where i is active, which the kernel splits three ways:
+//   beta-only slots (no alpha bits in the annihilation mask): active on every row of a
+//     column in which they are active at all: one running column sum per thread,
+//     added to those slots once at the end;
+//   alpha-only and mixed slots: the bits of smA[a] & (alpha-only | mixed), the same on
+//     the whole warp, so that only the slots active on this row issue an FP64 add
+//     (mixed ones add q where the column's beta bits also hold, else 0), into
+//     per-thread sums in shared memory.
+// So an amplitude costs the phase product (2 FP64), one add for the column, one per
+// slot active on its row and the back-rotation (4), in place of one predicated add per
+// slot of the pass.  The sums are fixed-order (per thread, then block_sum per slot).
+constexpr int kDiagAdjThreads = 256;
+// Passes with fewer slots keep k_diag_adj: the predicated adds it saves are few, and
+// on GB300 (14-orbital LUCJ, ncu) a 2-slot pass took 149 us there against 211 us here,
+// a 6-slot pass 292 us against 262 us.
+constexpr int kDiagAdjSzMinSlots = 5;
+
+struct DiagSplit {
+    int cols;         // columns per CTA (power of two, <= kDiagAdjThreads)
+    int col_blocks;   // CTAs across the columns
+    int row_chunks;   // CTAs down the rows
+    uint32_t b_only;  // slots with no alpha bits
+    uint32_t a_rows;  // alpha-only and mixed slots
+    uint32_t mixed;   // slots with both alpha and beta bits
+};
+
+__global__ void __launch_bounds__(kDiagAdjThreads, 4) k_diag_adj_sz(DiagArgs a, DiagSplit sp,
+                                                                    const double *__restrict__ ckpt,
+                                                                    int64_t ckpt_stride, double *h,
+                                                                    int64_t inst_stride, double *partials,
+                                                                    int64_t part_stride)
+{
+    constexpr int U = 4;  // rows in flight per thread
+    __shared__ double sacc[kMaxSlots][kDiagAdjThreads];
+    __shared__ double red[kDiagAdjThreads / 32];
+    if (skip_instance(a.active, blockIdx.y)) return;
+    a.table += (size_t)blockIdx.y * a.tab_stride;
+    ckpt += (size_t)blockIdx.y * ckpt_stride;
+    h += (size_t)blockIdx.y * inst_stride;
+    partials += (size_t)blockIdx.y * part_stride;
+    const int tid = threadIdx.x;
+    for (int i = 0; i < a.nslots; ++i) sacc[i][tid] = 0.0;
+    const uint32_t nA = a.basis.nA, nB = a.basis.nB;
+    const int cb = blockIdx.x % sp.col_blocks, rc = blockIdx.x / sp.col_blocks;
+    const uint32_t b = (uint32_t)(cb * sp.cols + (tid & (sp.cols - 1)));
+    const bool col_ok = b < nB;
+    const uint32_t mb = col_ok ? (uint32_t)__ldg(a.smB + b) : 0u;
+    const int lanes = kDiagAdjThreads / sp.cols;  // row lanes per CTA
+    const uint32_t r0 = (uint32_t)((uint64_t)nA * rc / sp.row_chunks);
+    const uint32_t r1 = (uint32_t)((uint64_t)nA * (rc + 1) / sp.row_chunks);
+    double col = 0.0;
+    for (uint32_t a0 = r0 + (uint32_t)(tid / sp.cols); a0 < r1; a0 += U * lanes) {
+        uint32_t ma[U], m[U];
+        double2 x[U], y[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t ar = a0 + u * lanes;
+            ma[u] = ar < r1 ? (uint32_t)__ldg(a.smA + ar) : 0u;
+            m[u] = col_ok ? ma[u] & mb : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (m[u]) {
+                const size_t z = (size_t)(a0 + u * lanes) * nB + b;
+                x[u] = __ldg(reinterpret_cast<const double2 *>(ckpt + 2 * z));
+                y[u] = *reinterpret_cast<const double2 *>(h + 2 * z);
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const double q = m[u] ? y[u].y * x[u].x - y[u].x * x[u].y : 0.0;
+            if (sp.b_only) col += q;
+            for (uint32_t r = ma[u] & sp.a_rows; r; r &= r - 1u) {  // uniform over the warp
+                const int i = __ffs(r) - 1;
+                const bool on = !((sp.mixed >> i) & 1u) || ((mb >> i) & 1u);
+                sacc[i][tid] += on ? q : 0.0;
+            }
+            if (m[u]) {
+                const size_t z = (size_t)(a0 + u * lanes) * nB + b;
+                const double2 t = diag_phase(a, m[u]);
+                *reinterpret_cast<double2 *>(h + 2 * z) =
+                    make_double2(t.x * y[u].x - t.y * y[u].y, t.y * y[u].x + t.x * y[u].y);
+            }
+        }
+    }
+    for (int i = 0; i < a.nslots; ++i) {  // uniform bound: block_sum synchronises
+        const double v = sacc[i][tid] + ((((sp.b_only & mb) >> i) & 1u) ? col : 0.0);
+        const double g = block_sum(v, red);
+        if (tid == 0) partials[(size_t)blockIdx.x * kMaxSlots + i] = g;
+    }
+}
+
 __global__ void k_diag_tangent(DiagArgs a, double *psi, double *T, size_t tstride, const int *tpos)
 {
     const uint64_t D = a.basis.D;
     for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        const uint32_t m = a.smA ? diag_mask_z(a, nullptr, (uint32_t)z) : diag_mask(a, a.basis.bits((uint32_t)z));
         if (!m) continue;
-        const double c = a.table[2 * m], s = a.table[2 * m + 1];
+        const double2 ph = diag_phase(a, m);
+        const double c = ph.x, s = ph.y;
         double *p = psi + 2 * z;
         const double re = c * p[0] - s * p[1], im = s * p[0] + c * p[1];
         p[0] = re;
@@ -924,7 +1050,7 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
     const uint64_t D = a.basis.D;
     double *t = T + (size_t)vec * tstride;
     for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < D; z += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t m = diag_mask(a, a.basis.bits((uint32_t)z));
+        const uint32_t m = a.smA ? diag_mask_z(a, nullptr, (uint32_t)z) : diag_mask(a, a.basis.bits((uint32_t)z));
         if (!m) continue;
         double *x = t + 2 * z;
         const double xr = x[0], xi = x[1], hr = h[2 * z], hi = h[2 * z + 1];
@@ -934,9 +1060,9 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
             if (i == a.nslots) break;  // uniform bound, as in k_diag_adj
             if ((m & (1u << i)) && block_pos0 + i >= vec) acc[i] += q;
         }
-        const double c = a.table[2 * m], s = a.table[2 * m + 1];
-        x[0] = c * xr - s * xi;
-        x[1] = s * xr + c * xi;
+        const double2 ph = diag_phase(a, m);
+        x[0] = ph.x * xr - ph.y * xi;
+        x[1] = ph.y * xr + ph.x * xi;
     }
 #pragma unroll
     for (int i = 0; i < kMaxSlots; ++i) {  // compile-time indices keep acc in registers
@@ -1875,6 +2001,13 @@ struct aegpu_engine {
         int *ops = nullptr;
         uint64_t active = 0;
         uint64_t amp_layers = 0;  // touched amplitudes x their active layers
+        // diagonal passes: phase-table offset (doubles, per instance), Sz-basis slot
+        // masks of the alpha / beta strings (null in other bases), and the slot
+        // activations summed over the determinants (FP64 work accounting)
+        int64_t tab_off = 0;
+        uint16_t *smA = nullptr, *smB = nullptr;
+        uint64_t slot_acts = 0;
+        DiagSplit split{};        // Sz basis: launch shape and slot classes of k_diag_adj_sz
     };
     std::vector<DevBlock> dblocks;
     std::vector<void *> allocs;
@@ -1891,6 +2024,7 @@ struct aegpu_engine {
     double *d_start = nullptr;      // start vector, shared by every instance
     int64_t n_partials = 0;         // gradient partial sums per instance
     int64_t n_ckpt = 0;             // checkpoint doubles per instance
+    int64_t n_diag_tab = 0;         // phase-table doubles of the diagonal passes per instance
     int64_t n_epart = 0;            // H psi partial sums per instance
     int spmv_grid = 0;
 
@@ -2164,7 +2298,7 @@ struct aegpu_engine {
         get(d_sc, B_ * 2 * nops);
         get(d_pc, B_ * npass * 2 * kMaxWarpLayers);
         get(d_sig, B_ * npass * 2 * (1 << kMaxWarpLayers));
-        get(d_diag_table, B_ * 2 * (1 << kMaxSlots));
+        get(d_diag_table, B_ * std::max<int64_t>(n_diag_tab, 1));
         get(d_psi, B_ * n);
         get(d_h, B_ * n);
         get(d_tmp, B_ * n);
@@ -2188,14 +2322,19 @@ struct aegpu_engine {
         if (!ok) return fail(AEGPU_ERR_NOMEM, "device allocation of the instance buffers failed");
         return AEGPU_OK;
     }
-    DiagArgs diag_args(const DevBlock &b, bool masked = true) const
+    // Arguments of diagonal pass b in direction dir (+1 forward, -1 adjoint).
+    DiagArgs diag_args(const DevBlock &b, double dir, bool masked = true) const
     {
         DiagArgs a;
         a.active = masked ? d_active : nullptr;
         a.ops = b.ops;
         a.nslots = b.nslots;
         a.codes = d_codes;
-        a.table = d_diag_table;
+        a.table = d_diag_table + b.tab_off;
+        a.tab_stride = n_diag_tab;
+        a.sin_flip = dir > 0 ? 0ull : 1ull << 63;
+        a.smA = b.smA;
+        a.smB = b.smB;
         a.basis = db;
         return a;
     }
@@ -2288,10 +2427,9 @@ int run_evolve(aegpu_engine *e, int ninst)
         auto &b = e->dblocks[bi];
         double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
-            k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
-                e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table, (int)e->excs.size(), e->d_active);
-            k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), e->d_psi, 0, 1, ck, n, e->n_ckpt);
-            e->launches += 2;
+            k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, 1.0), e->d_psi, 0, 1, ck, n,
+                                                                       e->n_ckpt);
+            e->launches += 1;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, 1.0);
             const dim3 g(b.wgrid, ninst);
@@ -2311,7 +2449,7 @@ int run_prep(aegpu_engine *e, int ninst, bool masked = true)
     PrepArgs pa = e->prep;
     pa.active = masked ? e->d_active : nullptr;
     k_pass_prep<<<dim3((unsigned)e->dblocks.size(), ninst), 64, 0, e->stream>>>(pa, e->d_ang, e->d_sc, e->d_pc,
-                                                                             e->d_sig);
+                                                                             e->d_sig, e->d_diag_table);
     e->launches += 1;
     return e->cuda_check("pass constants");
 }
@@ -2455,15 +2593,16 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         double *part = e->d_partials + b.part_off;
         const double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
-            k_diag_table<<<dim3(((1 << b.nslots) + 255) / 256, ninst), 256, 0, e->stream>>>(
-                e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table, nops, e->d_active);
-            if (b.nslots == 1)
-                k_diag_adj<true><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h,
-                                                                               n, part, e->n_partials);
+            if (b.smA && b.nslots >= kDiagAdjSzMinSlots)
+                k_diag_adj_sz<<<dim3(b.wgrid, ninst), kDiagAdjThreads, 0, e->stream>>>(
+                    e->diag_args(b, -1.0), b.split, ck, e->n_ckpt, e->d_h, n, part, e->n_partials);
+            else if (b.nslots == 1)
+                k_diag_adj<true><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, -1.0), ck, e->n_ckpt,
+                                                                               e->d_h, n, part, e->n_partials);
             else
-                k_diag_adj<false><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b), ck, e->n_ckpt, e->d_h,
-                                                                                n, part, e->n_partials);
-            e->launches += 2;
+                k_diag_adj<false><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, -1.0), ck, e->n_ckpt,
+                                                                                e->d_h, n, part, e->n_partials);
+            e->launches += 1;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, -1.0);
             const dim3 g(b.wgrid, ninst);
@@ -2700,6 +2839,86 @@ void aegpu_destroy(aegpu_engine *e) { delete e; }
 
 const char *aegpu_last_error(const aegpu_engine *e) { return e ? e->err.c_str() : "null engine"; }
 
+// Slot masks of a diagonal pass by string (Sz basis): slot i is active on determinant
+// (a, b) when the alpha string a holds the alpha bits of its annihilation mask and the
+// beta string b the beta bits, so the mask is smA[a] & smB[b] (two table loads in place
+// of a loop over the slots).  Also the slot activations summed over all determinants.
+static void diag_string_masks(aegpu_engine *e, const Block &b, aegpu_engine::DevBlock &d)
+{
+    const Basis &B = e->B;
+    const int ns = (int)b.ops.size();
+    if (B.kind != BASIS_SZ) {
+        // counted for the work accounting only; above 2^22 determinants the counts are
+        // left as estimates (half the determinants per slot)
+        d.slot_acts = (uint64_t)ns * B.D / 2;
+        d.active = B.D;
+        if (B.D > (1u << 22)) return;
+        d.slot_acts = d.active = 0;
+        for (uint64_t z = 0; z < B.D; ++z) {
+            const uint32_t bits = B.bits(z);
+            bool any = false;
+            for (int op : b.ops)
+                if ((bits & e->codes[op].annihilate) == e->codes[op].annihilate) {
+                    d.slot_acts++;
+                    any = true;
+                }
+            d.active += any;
+        }
+        return;
+    }
+    const uint32_t lo = (1u << B.N) - 1u;
+    std::vector<uint16_t> mA(B.nA), mB(B.nB);
+    std::vector<uint64_t> cA(ns, 0), cB(ns, 0);
+    for (uint32_t r = 0; r < B.nA; ++r) {
+        uint32_t m = 0;
+        for (int i = 0; i < ns; ++i) {
+            const uint32_t ann = e->codes[b.ops[i]].annihilate >> B.N;
+            if ((B.strA[r] & ann) == ann) { m |= 1u << i; cA[i]++; }
+        }
+        mA[r] = (uint16_t)m;
+    }
+    for (uint32_t r = 0; r < B.nB; ++r) {
+        uint32_t m = 0;
+        for (int i = 0; i < ns; ++i) {
+            const uint32_t ann = e->codes[b.ops[i]].annihilate & lo;
+            if ((B.strB[r] & ann) == ann) { m |= 1u << i; cB[i]++; }
+        }
+        mB[r] = (uint16_t)m;
+    }
+    d.slot_acts = 0;
+    for (int i = 0; i < ns; ++i) d.slot_acts += cA[i] * cB[i];
+    // launch shape and slot classes of the adjoint kernel k_diag_adj_sz
+    DiagSplit &sp = d.split;
+    sp.cols = 32;
+    while (sp.cols < kDiagAdjThreads && (uint32_t)sp.cols < B.nB) sp.cols *= 2;
+    sp.col_blocks = (int)((B.nB + sp.cols - 1) / sp.cols);
+    sp.row_chunks = (int)std::max<int64_t>(1, std::min<int64_t>(B.nA, kDiagGrid / sp.col_blocks));
+    sp.b_only = sp.a_rows = sp.mixed = 0;
+    for (int i = 0; i < ns; ++i) {
+        const uint32_t ann = e->codes[b.ops[i]].annihilate;
+        const bool ha = (ann >> B.N) != 0, hb = (ann & lo) != 0;
+        if (!ha) sp.b_only |= 1u << i;
+        else sp.a_rows |= 1u << i;
+        if (ha && hb) sp.mixed |= 1u << i;
+    }
+    if (ns >= kDiagAdjSzMinSlots) d.wgrid = sp.col_blocks * sp.row_chunks;
+    // determinants with at least one active slot, from the histograms of the two masks
+    std::vector<uint64_t> hA((size_t)1 << ns, 0), hB((size_t)1 << ns, 0);
+    for (uint16_t m : mA) hA[m]++;
+    for (uint16_t m : mB) hB[m]++;
+    std::vector<uint32_t> uA, uB;
+    for (uint32_t m = 1; m < hA.size(); ++m)
+        if (hA[m]) uA.push_back(m);
+    for (uint32_t m = 1; m < hB.size(); ++m)
+        if (hB[m]) uB.push_back(m);
+    d.active = 0;
+    for (uint32_t u : uA)
+        for (uint32_t v : uB)
+            if (u & v) d.active += hA[u] * hB[v];
+    d.smA = e->upload(mA);
+    d.smB = e->upload(mB);
+}
+
 int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int complex_mode,
                       int nops, const int *ops)
 {
@@ -2769,6 +2988,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     // orbit tables per block
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     e->dblocks.clear();
+    e->n_diag_tab = 0;
     e->block_pos0.clear();
     e->op_block.assign(nops, 0);
     e->op_slot.assign(nops, 0);
@@ -2804,6 +3024,9 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
         } else {
             d.ntiles = kDiagGrid;
             d.wgrid = kDiagGrid;
+            d.tab_off = e->n_diag_tab;
+            e->n_diag_tab += (int64_t)2 << d.nslots;
+            diag_string_masks(e, b, d);
         }
         d.part_off = part_off;
         part_off += (int64_t)d.wgrid * kMaxSlots;
@@ -2828,10 +3051,13 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
 
     // pass lists for the per-evaluation constant preparation
     std::vector<int> pops, poff, pn, pdiag;
-    for (const Block &b : e->blocks) {
+    std::vector<int64_t> ptab;
+    for (size_t bi = 0; bi < e->blocks.size(); ++bi) {
+        const Block &b = e->blocks[bi];
         poff.push_back((int)pops.size());
         pn.push_back((int)b.ops.size());
         pdiag.push_back(b.diagonal ? 1 : 0);
+        ptab.push_back(b.diagonal ? e->dblocks[bi].tab_off : 0);
         pops.insert(pops.end(), b.ops.begin(), b.ops.end());
     }
     PrepArgs pa{};
@@ -2839,6 +3065,8 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     pa.pass_off = e->upload(poff);
     pa.pass_n = e->upload(pn);
     pa.pass_diag = e->upload(pdiag);
+    pa.pass_tab = e->upload(ptab);
+    pa.tab_stride = e->n_diag_tab;
     pa.codes = e->d_codes;
     pa.nops = nops;
     pa.npass = (int)e->blocks.size();
@@ -3769,11 +3997,9 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         auto &b = e->dblocks[bi];
         const int p0 = e->block_pos0[bi];
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, 1.0, e->d_diag_table,
-                                                                       nops, nullptr);
-            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), T, n, p0, nullptr, 0, 0);
-            k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), e->d_psi, T, n, e->d_tpos);
-            e->launches += 3;
+            if (p0 > 0) k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, 1.0, false), T, n, p0, nullptr, 0, 0);
+            k_diag_tangent<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, 1.0, false), e->d_psi, T, n, e->d_tpos);
+            e->launches += p0 > 0 ? 2 : 1;
         } else if (b.ntiles) {
             BlockArgs a = e->block_args((int)bi, 1.0);
             // earlier tangents carried through the pass by the warp-register pass kernel:
@@ -3828,14 +4054,12 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
         const int p0 = e->block_pos0[bi];
         const int nvec = p0 + b.nslots;
         if (b.diagonal) {
-            k_diag_table<<<((1 << b.nslots) + 255) / 256, 256, 0, s>>>(e->d_ang, b.ops, b.nslots, -1.0, e->d_diag_table,
-                                                                       nops, nullptr);
             dim3 g(kDiagGrid, nvec);
-            k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b, false), e->d_h, T, n, nvec, p0, hpart);
+            k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b, -1.0, false), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
                                                                             b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
-            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, false), e->d_h, 0, 1, nullptr, 0, 0);
-            e->launches += 4;
+            k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, -1.0, false), e->d_h, 0, 1, nullptr, 0, 0);
+            e->launches += 3;
         } else if (b.nwtasks) {
             // warp-register pass kernels, adjoint direction, one vector per grid.y row
             BlockArgs a = e->block_args(bi, -1.0);
@@ -4410,19 +4634,26 @@ int aegpu_fp64_work(const aegpu_engine *e, int64_t *work)
     // [0] H psi (one DFMA per stored / regenerated matrix element + the energy FMA),
     // [1] forward passes (one DFMA per amplitude-layer + one DMUL per amplitude),
     // [2] adjoint passes (two DFMA per amplitude-layer + one DMUL per amplitude + one
-    //     DADD per lane-layer for the gradient sums)
+    //     DADD per lane-layer for the gradient sums);
     if (!e || !work) return AEGPU_ERR_ARG;
-    int64_t al = 0, act = 0;
+    // diagonal passes (complex): a complex multiply (4) per amplitude with an active slot
+    // forward; adjoint the phase product (2), the back-rotation (4) and one DADD per
+    // active slot
+    int64_t al = 0, act = 0, dact = 0, dslots = 0;
     for (auto &b : e->dblocks) {
-        if (b.diagonal) continue;
+        if (b.diagonal) {
+            dact += (int64_t)b.active;
+            dslots += (int64_t)b.slot_acts;
+            continue;
+        }
         al += (int64_t)b.amp_layers;
         act += (int64_t)b.active;
     }
     const int64_t D = (int64_t)e->B.D, W = e->W;
     const int64_t elems = e->ham_kind == 1 ? e->ham_entries : (e->ham_kind ? D * e->ints.width : 0);
     work[0] = (elems + D) * W;
-    work[1] = (al + act) * W;
-    work[2] = (2 * al + act) * W + al / 2;
+    work[1] = (al + act) * W + 4 * dact;
+    work[2] = (2 * al + act) * W + al / 2 + 6 * dact + dslots;
     // [3] H psi by the spin-flip half product: the rows with a <= b, the energy FMAs of
     // every row, and the invariance test (one FMA per amplitude, one per pair a < b)
     work[3] = 0;
