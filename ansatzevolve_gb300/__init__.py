@@ -20,6 +20,7 @@ _LIB = None
 
 HAM_AUTO, HAM_STORED, HAM_ON_THE_FLY = 0, 1, 2
 TUNE_PASS_OPS, TUNE_CTAS_PER_SM, TUNE_OTF_THREADS, TUNE_SPMV_TPR, TUNE_PDL, TUNE_REUSE_HPSI, TUNE_FLIP = 1, 2, 3, 4, 5, 6, 7
+TUNE_HALF = 8
 BASIS_FULL, BASIS_NUMBER, BASIS_SZ = 0, 1, 2
 PROP_HESSIAN, PROP_OVERLAP, PROP_HF_PATH = 1, 2, 4
 # rows of the properties table, in the reference's print order (tupsquantities.cpp:538-566)
@@ -72,6 +73,8 @@ def lib(build_if_missing=True):
         "aegpu_set_active": (ctypes.c_int, [_P, _IP]),
         "aegpu_set_tuning": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
         "aegpu_flip_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+        "aegpu_half_status": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+        "aegpu_half_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
         "aegpu_get_tuning": (ctypes.c_int, [_P, ctypes.c_int]),
         "aegpu_io_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
         "aegpu_io_put_angles": (ctypes.c_int, [_P, _DP, _P]),
@@ -544,7 +547,7 @@ class Engine:
 
     def set_tuning(self, knob, value):
         """One knob (TUNE_*) where the engine accepts it at this point of its set-up
-        (TUNE_PDL, TUNE_REUSE_HPSI and TUNE_FLIP at any time)."""
+        (TUNE_PDL, TUNE_REUSE_HPSI, TUNE_FLIP and TUNE_HALF at any time)."""
         self._check(self.L.aegpu_set_tuning(self.h, knob, int(value)))
 
     def get_tuning(self, knob):
@@ -556,6 +559,19 @@ class Engine:
         u = np.zeros(self.nb, dtype=np.int32)
         self._check(self.L.aegpu_flip_status(self.h, iptr(u)))
         return u.astype(bool)
+
+    def half_status(self):
+        """Per instance: True where the last evaluation ran the spin-flip half passes."""
+        u = np.zeros(self.nb, dtype=np.int32)
+        self._check(self.L.aegpu_half_status(self.h, iptr(u)))
+        return u.astype(bool)
+
+    def half_info(self):
+        """Whether the problem allows the spin-flip half passes, the amplitudes they touch
+        per sweep and the FP64 instructions of their forward and adjoint passes."""
+        out = np.zeros(4, dtype=np.int64)
+        self._check(self.L.aegpu_half_info(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+        return {"available": bool(out[0]), "active": int(out[1]), "fwd_fp64": int(out[2]), "adj_fp64": int(out[3])}
 
     def use_graphs(self, enable=True):
         self._check(self.L.aegpu_use_graphs(self.h, int(enable)))
@@ -575,16 +591,22 @@ class Engine:
         keys = ("D", "nops", "blocks", "ham_kind", "ham_entries", "ell_width", "active", "nnz")
         return dict(zip(keys, map(int, out)))
 
-    def fp64_work(self, half=None):
+    def fp64_work(self, half=None, half_passes=None):
         """FP64 instructions per evaluation and instance: (H psi, forward, adjoint).  H psi
         counts the spin-flip half product where half is true, the full product where it
         is false, and by default what the last energy evaluation took (averaged over
-        the instances)."""
+        the instances); the passes likewise the spin-flip half passes (half_passes)."""
         w = np.zeros(4, dtype=np.int64)
         self._check(self.L.aegpu_fp64_work(self.h, w.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
         frac = float(np.mean(self.flip_status())) if half is None else float(bool(half))
         hpsi = int(round(w[0] * (1.0 - frac) + w[3] * frac))
-        return hpsi, int(w[1]), int(w[2])
+        hi = self.half_info()
+        pf = 0.0
+        if hi["available"]:
+            pf = float(np.mean(self.half_status())) if half_passes is None else float(bool(half_passes))
+        fwd = int(round(w[1] * (1.0 - pf) + hi["fwd_fp64"] * pf))
+        adj = int(round(w[2] * (1.0 - pf) + hi["adj_fp64"] * pf))
+        return hpsi, fwd, adj
 
     def device_bytes(self):
         return int(self.L.aegpu_device_bytes(self.h))

@@ -152,7 +152,26 @@ struct BlockArgs {
     const double *sigma;     // this pass's scale products per active mask (instance 0)
     int64_t pc_stride, sig_stride;  // per-instance strides of pc / sigma
     const int *active;       // instance mask of the warp kernels (nullable)
+    // spin-flip half passes (warp kernels): where half[b] is set, instance b runs the
+    // pass's half tables (canonical ranks, no-write bits, self-mirror tasks) instead
+    const int *half;         // per instance (nullable: full tables)
+    const uint32_t *idx_h, *obits_h;
+    const WarpTask *tasks_h;
+    int ntasks_h;
 };
+
+// The tables instance b runs: the half tables where its half flag is set.
+struct PassTables {
+    const uint32_t *idx, *obits;
+    const WarpTask *tasks;
+    int ntasks;
+    bool half;
+};
+__device__ __forceinline__ PassTables pass_tables(const BlockArgs &a, const WarpTask *tasks, int ntasks, int b)
+{
+    if (a.half && a.half[b]) return PassTables{a.idx_h, a.obits_h, a.tasks_h, a.ntasks_h, true};
+    return PassTables{a.idx, a.obits, tasks, ntasks, false};
+}
 
 __device__ __forceinline__ uint32_t insert_zero_bit(uint32_t p, int i)
 {
@@ -406,6 +425,11 @@ struct PrepArgs {
     const ExcCode *codes;
     int nops, npass;
     const int *active;      // instance mask (nullable)
+    // spin-flip half passes (nullable: none): operator -> mirror operator, the gate
+    // (one int: tables built, symmetric start state, knob on) and the per-instance flag
+    const int *mirror;
+    const int *half_gate;
+    int *half;
 };
 
 // A diagonal pass's phase table: tab[2m], tab[2m + 1] = cos, sin of the sum of the
@@ -428,6 +452,19 @@ __global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *
 {
     const int pass = blockIdx.x, b = blockIdx.y;
     if (skip_instance(a.active, b)) return;
+    if (pass == 0 && a.half) {
+        // instance b takes the half passes when the gate is open and every operator's
+        // angle equals its mirror's (the evolution then commutes with the exchange of
+        // the alpha and beta strings)
+        __shared__ int ok;
+        if (threadIdx.x == 0) ok = *a.half_gate;
+        __syncthreads();
+        const double *ab = ang + (size_t)b * a.nops;
+        for (int o = threadIdx.x; o < a.nops; o += blockDim.x)
+            if (ab[o] != ab[a.mirror[o]]) ok = 0;  // every writer stores 0
+        __syncthreads();
+        if (threadIdx.x == 0) a.half[b] = ok;
+    }
     const int ns = a.pass_n[pass];
     const int *ops = a.pass_ops + a.pass_off[pass];
     if (a.pass_diag[pass])
@@ -504,14 +541,17 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
     double *psi = vecs + (size_t)b * inst_stride;
     if (ckpt) ckpt += (size_t)b * ckpt_stride;
+    const PassTables pt = pass_tables(a, tasks, ntasks, b);
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
-        const WarpTask task = tasks[t];
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < pt.ntasks; t += nw) {
+        const WarpTask task = pt.tasks[t];
         const uint32_t mask = task.mask;
-        const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
+        const uint32_t *idx = pt.idx + task.elem_off, *obits = pt.obits + task.elem_off;
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
         const uint32_t b0 = ok0 ? obits[lane] : 0u, b1 = ok1 ? obits[lane + 32] : 0u;
+        // half tables: the mirror member of a self-mirror orbit writes this amplitude
+        const bool w0 = ok0 && !(b0 & kNoWriteBit), w1 = ok1 && !(b1 & kNoWriteBit);
         double v0[W], v1[W];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
@@ -542,8 +582,8 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
 #pragma unroll
         for (int w = 0; w < W; ++w) {
             const double t0 = sigma * v0[w], t1 = sigma * v1[w];
-            if (ok0) psi[(size_t)z0 * W + w] = t0;
-            if (ok1) psi[(size_t)z1 * W + w] = t1;
+            if (w0) psi[(size_t)z0 * W + w] = t0;
+            if (w1) psi[(size_t)z1 * W + w] = t1;
             if (ckpt) {
                 if (ok0) ckpt[((size_t)task.elem_off + lane) * W + w] = t0;
                 if (ok1) ckpt[((size_t)task.elem_off + lane + 32) * W + w] = t1;
@@ -572,17 +612,22 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
     double *h = hv + (size_t)b * inst_stride;
     ckpt += (size_t)b * ckpt_stride;
+    const PassTables pt = pass_tables(a, tasks, ntasks, b);
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double accS[kMaxWarpLayers];
 #pragma unroll
     for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
-    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntasks; t += nw) {
-        const WarpTask task = tasks[t];
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < pt.ntasks; t += nw) {
+        const WarpTask task = pt.tasks[t];
         const uint32_t mask = task.mask;
-        const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
+        const uint32_t *idx = pt.idx + task.elem_off, *obits = pt.obits + task.elem_off;
         const bool ok0 = lane < (int)task.n, ok1 = lane + 32 < (int)task.n;
         const uint32_t z0 = ok0 ? idx[lane] : 0u, z1 = ok1 ? idx[lane + 32] : 0u;
         const uint32_t b0 = ok0 ? obits[lane] : 0u, b1 = ok1 ? obits[lane + 32] : 0u;
+        const bool w0 = ok0 && !(b0 & kNoWriteBit), w1 = ok1 && !(b1 & kNoWriteBit);
+        // a self-mirror orbit of the half tables is its own mirror: half weight, so that
+        // the operator's sum plus its mirror's counts it once
+        const double wt = (task.group & kSelfMirrorTask) ? 0.5 : 1.0;
         const double *cp = ckpt + (size_t)task.elem_off * W;
         double v0[W], v1[W], h0[W], h1[W];
 #pragma unroll
@@ -612,7 +657,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
                 g = fma(h0[w], flip(p0, s0), g);
                 g = fma(h1[w], flip(p1, s1), g);
             }
-            accS[j] += g;
+            accS[j] = fma(wt, g, accS[j]);
         }
 #pragma unroll
         for (int j = 0; j < kMaxWarpLayers; ++j) {
@@ -637,8 +682,8 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
         const double sigma = sig[mask];
 #pragma unroll
         for (int w = 0; w < W; ++w) {
-            if (ok0) h[(size_t)z0 * W + w] = sigma * h0[w];
-            if (ok1) h[(size_t)z1 * W + w] = sigma * h1[w];
+            if (w0) h[(size_t)z0 * W + w] = sigma * h0[w];
+            if (w1) h[(size_t)z1 * W + w] = sigma * h1[w];
         }
     }
     // fixed-order CTA sum: the warp's six sums by recursive halving, then the warps in order
@@ -1072,23 +1117,51 @@ __global__ void __launch_bounds__(256) k_diag_hess(DiagArgs a, const double *h, 
     }
 }
 
+// After a sweep of spin-flip half passes only the amplitudes (a, b) with a <= b are
+// current: each is copied to its mirror (b, a), for the instances that took them.
+template <int W>
+__global__ void k_flip_fill(DevBasis B, double *psi, int64_t inst_stride, const int *__restrict__ half,
+                            const int *__restrict__ active)
+{
+    const int inst = blockIdx.y;
+    if (!half[inst] || skip_instance(active, inst)) return;
+    psi += (size_t)inst * inst_stride;
+    for (uint64_t z = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z < B.D; z += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = B.div_nB((uint32_t)z), c = (uint32_t)z - a * B.nB;
+        if (a <= c) continue;
+        const size_t src = (size_t)c * B.nB + a;
+#pragma unroll
+        for (int w = 0; w < W; ++w) psi[z * W + w] = psi[src * W + w];
+    }
+}
+
+__global__ void k_set_int(int *p, int v) { *p = v; }
+
 // ------------------------------------------------------------ reductions --
 // grad[op] = scale * sum over the tiles of op's block of partials[tile][slot].
 // warp per (instance, operator); instance b's partial sums start at b * part_stride.
+// Spin-flip half passes (half[b] set; mirror: operator -> mirror operator): the
+// sweep visited one orbit of every mirror pair, so the gradient of an operator is its
+// own sum plus its mirror's (the two results are the same sum, bit for bit).
 __global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t *__restrict__ op_part_off,
                               const int *__restrict__ op_ntiles, const int *__restrict__ op_slot, int nops, double scale,
-                              double *__restrict__ grad, int nb, int64_t part_stride, const int *__restrict__ active)
+                              double *__restrict__ grad, int nb, int64_t part_stride, const int *__restrict__ active,
+                              const int *__restrict__ mirror, const int *__restrict__ half)
 {
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (gw >= nops * nb) return;
     const int b = gw / nops, warp = gw - b * nops;
     if (skip_instance(active, b)) return;
     grad += (size_t)b * nops;
-    const double *p = partials + (size_t)b * part_stride + op_part_off[warp];
-    const int nt = op_ntiles[warp], sl = op_slot[warp];
-    double s = 0;
-    for (int t = lane; t < nt; t += 32) s += p[(size_t)t * kMaxSlots + sl];
-    s = warp_sum(s);
+    auto op_sum = [&](int op) {
+        const double *p = partials + (size_t)b * part_stride + op_part_off[op];
+        const int nt = op_ntiles[op], sl = op_slot[op];
+        double s = 0;
+        for (int t = lane; t < nt; t += 32) s += p[(size_t)t * kMaxSlots + sl];
+        return warp_sum(s);
+    };
+    double s = op_sum(warp);
+    if (mirror && half && half[b]) s += op_sum(mirror[warp]);
     if (lane == 0) grad[warp] = scale * s;
 }
 
@@ -2008,6 +2081,11 @@ struct aegpu_engine {
         uint16_t *smA = nullptr, *smB = nullptr;
         uint64_t slot_acts = 0;
         DiagSplit split{};        // Sz basis: launch shape and slot classes of k_diag_adj_sz
+        // spin-flip half tables (paired passes; build_half_orbits)
+        uint32_t *idx_h = nullptr, *bits_h = nullptr;
+        WarpTask *wtasks_h = nullptr;
+        int nwtasks_h = 0;
+        uint64_t active_h = 0, amp_layers_h = 0;
     };
     std::vector<DevBlock> dblocks;
     std::vector<void *> allocs;
@@ -2025,6 +2103,15 @@ struct aegpu_engine {
     int64_t n_partials = 0;         // gradient partial sums per instance
     int64_t n_ckpt = 0;             // checkpoint doubles per instance
     int64_t n_diag_tab = 0;         // phase-table doubles of the diagonal passes per instance
+    // spin-flip half passes: possible for this problem (Sz basis, as many alpha as beta
+    // strings, no diagonal passes, every pass closed under the mirror with matching
+    // signs), the start state symmetric, the knob (AEGPU_TUNE_HALF; AEGPU_HALF=0 in the
+    // environment switches it off); the device gate is their conjunction, the
+    // per-instance flag adds the angle test of each evaluation
+    bool half_static = false, start_sym = true, tune_half = true;
+    std::vector<int> mirror;        // operator -> mirror operator (half passes only)
+    int *d_mirror = nullptr, *d_half_gate = nullptr;
+    int *d_half = nullptr;          // per instance (alloc_instances)
     int64_t n_epart = 0;            // H psi partial sums per instance
     int spmv_grid = 0;
 
@@ -2208,8 +2295,9 @@ struct aegpu_engine {
         return p;
     }
 
-    // Arguments of pass bi in direction dir (+1 forward, -1 adjoint).
-    BlockArgs block_args(int bi, double dir) const
+    // Arguments of pass bi in direction dir (+1 forward, -1 adjoint); half: the
+    // instances may take the spin-flip half tables (evolution and energy gradient).
+    BlockArgs block_args(int bi, double dir, bool half = false) const
     {
         const DevBlock &b = dblocks[bi];
         const int d = dir > 0 ? 0 : 1;
@@ -2230,8 +2318,16 @@ struct aegpu_engine {
         a.pc_stride = (int64_t)npass * 2 * kMaxWarpLayers;
         a.sig_stride = (int64_t)npass * 2 * (1 << kMaxWarpLayers);
         a.active = d_active;
+        a.half = half && half_static ? d_half : nullptr;
+        a.idx_h = b.idx_h;
+        a.obits_h = b.bits_h;
+        a.tasks_h = b.wtasks_h;
+        a.ntasks_h = b.nwtasks_h;
         return a;
     }
+    // Device gate of the half passes: the tables are built, the start state is
+    // symmetric and the knob is on.
+    void write_half_gate();  // in order on the engine's stream (k_set_int)
     size_t vec_elems() const { return (size_t)B.D * W; }
 
     template <typename T>
@@ -2306,6 +2402,8 @@ struct aegpu_engine {
         get(d_epart, B_ * std::max<int64_t>(n_epart, 1));
         get(d_flip_part, B_ * 2 * (size_t)sm_count);
         get(d_flip_used, B_);
+        get(d_half, B_);
+        if (d_half) cudaMemset(d_half, 0, B_ * sizeof(int));
         flip_tried = false;
         get(d_scalar, std::max<size_t>(B_, 4));
         get(d_grad, B_ * nops);
@@ -2316,6 +2414,7 @@ struct aegpu_engine {
             cudaMemcpy(d_active, ones.data(), B_ * sizeof(int), cudaMemcpyHostToDevice);
         }
         prep.active = d_active;
+        prep.half = half_static ? d_half : nullptr;
         drop_graph();
         cached_angles.clear();
         psi_valid = h_valid = false;
@@ -2431,7 +2530,7 @@ int run_evolve(aegpu_engine *e, int ninst)
                                                                        e->n_ckpt);
             e->launches += 1;
         } else if (b.nwtasks) {
-            BlockArgs a = e->block_args(bi, 1.0);
+            BlockArgs a = e->block_args(bi, 1.0, true);
             const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
                 launch_pass(e, k_warp_rot<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
@@ -2439,6 +2538,15 @@ int run_evolve(aegpu_engine *e, int ninst)
                 launch_pass(e, k_warp_rot<2>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             e->launches += 1;
         }
+    }
+    if (e->half_static) {
+        // instances that took the half passes: complete psi from its a <= b amplitudes
+        const dim3 g((unsigned)std::min<int64_t>(((int64_t)e->B.D + 255) / 256, e->sm_count * 4), ninst);
+        if (e->W == 1)
+            k_flip_fill<1><<<g, 256, 0, e->stream>>>(e->db, e->d_psi, n, e->d_half, e->d_active);
+        else
+            k_flip_fill<2><<<g, 256, 0, e->stream>>>(e->db, e->d_psi, n, e->d_half, e->d_active);
+        e->launches += 1;
     }
     return e->cuda_check("evolve");
 }
@@ -2583,7 +2691,9 @@ int run_energy(aegpu_engine *e, double *E_dev, int ninst)
 // Adjoint sweep over all passes for the first ninst instances (h updated in place,
 // psi taken from the checkpoints), per-op gradients scale * <h|G_op psi> in
 // grad_dev[b * nops + op] (scale 2 for the energy gradient, 1 for a projection).
-int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.0)
+// half: the instances that took the spin-flip half passes in the forward sweep take
+// them here too (h = H psi has the symmetry); false only after a full forward sweep.
+int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.0, bool half = true)
 {
     NvtxRange r("aegpu adjoint sweep");
     const int64_t n = (int64_t)e->vec_elems();
@@ -2604,7 +2714,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
                                                                                 e->d_h, n, part, e->n_partials);
             e->launches += 1;
         } else if (b.nwtasks) {
-            BlockArgs a = e->block_args(bi, -1.0);
+            BlockArgs a = e->block_args(bi, -1.0, half);
             const dim3 g(b.wgrid, ninst);
             if (e->W == 1)
                 launch_pass(e, k_warp_adj<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n,
@@ -2619,9 +2729,12 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         }
     }
     const int warps = nops * ninst;
+    const bool hm = half && e->half_static;
     k_grad_reduce<<<(warps * 32 + 255) / 256, 256, 0, e->stream>>>(e->d_partials, e->d_op_part_off, e->d_op_ntiles,
                                                                    e->d_op_slot, nops, scale, grad_dev, ninst,
-                                                                   e->n_partials, e->d_active);
+                                                                   e->n_partials, e->d_active,
+                                                                   hm ? e->d_mirror : nullptr,
+                                                                   hm ? e->d_half : nullptr);
     e->launches += 1;
     return e->cuda_check("backward");
 }
@@ -2821,6 +2934,7 @@ int aegpu_create(aegpu_engine **out)
     cudaDeviceGetAttribute(&e->smem_per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (const char *v = std::getenv("AEGPU_REUSE_HPSI")) e->reuse_hpsi = std::strcmp(v, "0") != 0;
     if (const char *v = std::getenv("AEGPU_FLIP")) e->tune_flip = std::strcmp(v, "0") != 0;
+    if (const char *v = std::getenv("AEGPU_HALF")) e->tune_half = std::strcmp(v, "0") != 0;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete e;
@@ -2951,7 +3065,21 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     }
     // the reference's commuting blocks, cut into passes of <= 6 excitations so that
     // every orbit fits one warp's registers
-    e->blocks = split_passes(group_blocks(e->excs, kMaxSlots, e->perm), e->tune_pass_ops);
+    {
+        // spin-flip half passes need the Sz basis with as many alpha as beta strings, no
+        // diagonal operator and every operator's mirror in its block (then in its pass)
+        std::vector<Block> grouped = group_blocks(e->excs, kMaxSlots, e->perm);
+        std::vector<int> mir;
+        bool half = e->B.kind == BASIS_SZ && e->B.nA == e->B.nB;
+        for (const Block &b : grouped) half = half && !b.diagonal;
+        if (half) {
+            mir = mirror_ops(e->codes, grouped, e->B.N);
+            for (int m : mir) half = half && m >= 0;
+        }
+        e->blocks = split_passes(grouped, e->tune_pass_ops, half ? &mir : nullptr);
+        e->half_static = half;
+        e->mirror = half ? mir : std::vector<int>();
+    }
     e->pos_of_op.assign(nops, 0);
     for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;
 
@@ -3021,6 +3149,23 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             d.wgrid = std::max(1, std::min(e->sm_count * e->tune_ctas_per_sm, (d.nwtasks + 7) / 8));
             d.active = T.active;
             d.amp_layers = T.amp_layers;
+            if (e->half_static) {
+                std::vector<int> mslot(b.ops.size(), -1);
+                for (size_t i = 0; i < b.ops.size(); ++i)
+                    for (size_t j = 0; j < b.ops.size(); ++j)
+                        if (b.ops[j] == e->mirror[b.ops[i]]) mslot[i] = (int)j;
+                HalfTables H = build_half_orbits(e->B, T, bc, mslot);
+                if (!H.ok) {
+                    e->half_static = false;
+                } else {
+                    d.idx_h = e->upload(H.idx);
+                    d.bits_h = e->upload(H.bits);
+                    d.wtasks_h = e->upload(H.wtasks);
+                    d.nwtasks_h = (int)H.wtasks.size();
+                    d.active_h = H.active;
+                    d.amp_layers_h = H.amp_layers;
+                }
+            }
         } else {
             d.ntiles = kDiagGrid;
             d.wgrid = kDiagGrid;
@@ -3070,6 +3215,12 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     pa.codes = e->d_codes;
     pa.nops = nops;
     pa.npass = (int)e->blocks.size();
+    if (e->half_static) {
+        e->d_mirror = e->upload(e->mirror);
+        e->d_half_gate = e->alloc<int>(1);
+        pa.mirror = e->d_mirror;
+        pa.half_gate = e->d_half_gate;
+    }
     e->prep = pa;
 
     if (e->alloc_failed) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed while building the passes");
@@ -3084,6 +3235,8 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     if (rc) return rc;
     if (e->alloc_failed) return e->fail(AEGPU_ERR_NOMEM, "device allocation failed");
     cudaMemset(e->d_start, 0, n * sizeof(double));
+    e->start_sym = true;
+    e->write_half_gate();
     // setup copies ran on the legacy stream: finish them before any engine-stream work
     if (cudaDeviceSynchronize() != cudaSuccess) return e->cuda_check("set_problem");
     return e->cuda_check("set_problem");
@@ -3117,6 +3270,17 @@ int aegpu_set_initial(aegpu_engine *e, const double *amps)
     if (!e->d_start) return e->fail(AEGPU_ERR_STATE, "set the problem first");
     cudaMemcpy(e->d_start, amps, (size_t)e->B.D * e->W * sizeof(double), cudaMemcpyHostToDevice);
     e->psi_valid = e->h_valid = false;
+    if (e->half_static) {
+        // the half passes need a start state with psi(a,b) = psi(b,a)
+        bool sym = true;
+        const uint64_t nB = e->B.nB;
+        for (uint64_t x = 0; x < nB && sym; ++x)
+            for (uint64_t y = x + 1; y < nB && sym; ++y)
+                for (int w = 0; w < e->W; ++w)
+                    if (amps[(x * nB + y) * e->W + w] != amps[(y * nB + x) * e->W + w]) sym = false;
+        e->start_sym = sym;
+        e->write_half_gate();
+    }
     cudaDeviceSynchronize();
     return e->cuda_check("set_initial");
 }
@@ -3542,6 +3706,12 @@ int aegpu_set_tuning(aegpu_engine *e, int knob, int value)
         e->drop_graph();
         e->h_valid = false;
         return AEGPU_OK;
+    case AEGPU_TUNE_HALF:
+        if (value != 0 && value != 1) return e->fail(AEGPU_ERR_ARG, "the spin-flip half passes must be 0 or 1");
+        e->tune_half = value != 0;
+        e->write_half_gate();
+        e->psi_valid = e->h_valid = false;
+        return AEGPU_OK;
     case AEGPU_TUNE_SPMV_TPR:
         if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
             return e->fail(AEGPU_ERR_ARG, "threads per row must be 0 (by size), 1, 2, 4 or 8");
@@ -3566,6 +3736,41 @@ int aegpu_flip_status(aegpu_engine *e, int *used)
     return e->cuda_check("flip status");
 }
 
+void aegpu_engine::write_half_gate()
+{
+    if (!d_half_gate) return;
+    k_set_int<<<1, 1, 0, stream>>>(d_half_gate, half_static && start_sym && tune_half ? 1 : 0);
+}
+
+int aegpu_half_status(aegpu_engine *e, int *used)
+{
+    if (!e || !used) return AEGPU_ERR_ARG;
+    if (!e->d_half) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    if (!e->half_static) {
+        std::fill(used, used + e->nb, 0);
+        return AEGPU_OK;
+    }
+    if (stream_sync(e, "half status")) return AEGPU_ERR_CUDA;
+    cudaMemcpy(used, e->d_half, sizeof(int) * e->nb, cudaMemcpyDeviceToHost);
+    return e->cuda_check("half status");
+}
+
+int aegpu_half_info(const aegpu_engine *e, int64_t *info)
+{
+    if (!e || !info) return AEGPU_ERR_ARG;
+    int64_t act = 0, al = 0;
+    for (auto &b : e->dblocks) {
+        act += (int64_t)b.active_h;
+        al += (int64_t)b.amp_layers_h;
+    }
+    const int64_t W = e->W;
+    info[0] = e->half_static ? 1 : 0;
+    info[1] = e->half_static ? act : 0;
+    info[2] = e->half_static ? (al + act) * W : 0;
+    info[3] = e->half_static ? (2 * al + act) * W + al / 2 : 0;
+    return AEGPU_OK;
+}
+
 int aegpu_get_tuning(const aegpu_engine *e, int knob)
 {
     if (!e) return -1;
@@ -3577,6 +3782,7 @@ int aegpu_get_tuning(const aegpu_engine *e, int knob)
     case AEGPU_TUNE_PDL: return e->pdl_on() ? 1 : 0;
     case AEGPU_TUNE_REUSE_HPSI: return e->reuse_hpsi ? 1 : 0;
     case AEGPU_TUNE_FLIP: return e->tune_flip ? 1 : 0;
+    case AEGPU_TUNE_HALF: return e->tune_half ? 1 : 0;
     default: return -1;
     }
 }
@@ -3671,7 +3877,19 @@ int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *pro
 {
     if (!e || !angles || !proj || !grad_ops) return AEGPU_ERR_ARG;
     if (!e->d_psi) return e->fail(AEGPU_ERR_STATE, "set the problem first");
+    // the fixed bra has no mirror symmetry: a full forward sweep (its checkpoints) for
+    // the full adjoint sweep
+    const bool gate = e->half_static && e->start_sym && e->tune_half;
+    if (gate) {
+        e->tune_half = false;
+        e->write_half_gate();
+        e->psi_valid = false;
+    }
     int rc = ensure_state(e, angles);
+    if (gate) {
+        e->tune_half = true;
+        e->write_half_gate();
+    }
     if (rc) return rc;
     const int64_t n = (int64_t)e->vec_elems();
     cudaMemcpyAsync(e->d_h, proj, (size_t)n * e->nb * sizeof(double), cudaMemcpyHostToDevice, e->stream);
@@ -3680,7 +3898,7 @@ int aegpu_gradient_proj(aegpu_engine *e, const double *angles, const double *pro
     k_dot<<<dim3(grid, e->nb), 256, 0, e->stream>>>(e->d_h, e->d_psi, n, e->d_epart, e->d_active);
     k_reduce_sum<<<e->nb, 256, 0, e->stream>>>(e->d_epart, grid, e->d_scalar, 1.0, e->d_active);
     e->launches += 2;
-    rc = run_backward(e, e->d_grad, e->nb, 1.0);
+    rc = run_backward(e, e->d_grad, e->nb, 1.0, false);
     if (rc) return rc;
     if (overlap) cudaMemcpyAsync(overlap, e->d_scalar, e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);
     cudaMemcpyAsync(grad_ops, e->d_grad, e->excs.size() * e->nb * sizeof(double), cudaMemcpyDeviceToHost, e->stream);

@@ -124,7 +124,68 @@ std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std:
     return out;
 }
 
-std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass)
+std::vector<int> mirror_ops(const std::vector<ExcCode> &codes, const std::vector<Block> &blocks, int N)
+{
+    std::vector<int> mir(codes.size(), -1);
+    for (const auto &b : blocks)
+        for (int o : b.ops) {
+            if (mir[o] >= 0) continue;
+            const uint32_t fc = flip_bits(codes[o].create, N), fa = flip_bits(codes[o].annihilate, N);
+            for (int p : b.ops)
+                if (mir[p] < 0 && codes[p].create == fc && codes[p].annihilate == fa && (p != o || fc == codes[o].create)) {
+                    mir[o] = p;
+                    mir[p] = o;
+                    break;
+                }
+        }
+    return mir;
+}
+
+// A paired block cut between mirror units: the units in order of first appearance,
+// packed greedily into the fewest passes of <= max_pass operators with near-equal
+// operator counts.  Empty result: the block is not closed under the mirror.
+static std::vector<Block> split_by_mirror(const Block &b, int max_pass, const std::vector<int> &mir)
+{
+    std::vector<std::vector<int>> units;
+    std::vector<char> seen(mir.size(), 0);
+    for (int o : b.ops) {
+        if (seen[o]) continue;
+        const int m = mir[o];
+        if (m < 0 || std::find(b.ops.begin(), b.ops.end(), m) == b.ops.end()) return {};
+        seen[o] = 1;
+        if (m == o) {
+            units.push_back({o});
+        } else {
+            seen[m] = 1;
+            units.push_back({o, m});
+        }
+    }
+    const int n = (int)b.ops.size();
+    for (auto &u : units)
+        if ((int)u.size() > max_pass) return {};
+    int parts = (n + max_pass - 1) / max_pass;
+    for (;; ++parts) {  // the fewest passes the units fit in, near-equal by count
+        std::vector<Block> out;
+        Block cur;
+        int done = 0, k = 0;
+        bool fits = true;
+        for (auto &u : units) {
+            const int bound = (int)((int64_t)n * (k + 1) / parts);
+            if (!cur.ops.empty() && (done + (int)u.size() > bound || (int)(cur.ops.size() + u.size()) > max_pass)) {
+                out.push_back(cur);
+                cur = Block{};
+                ++k;
+            }
+            cur.ops.insert(cur.ops.end(), u.begin(), u.end());
+            done += (int)u.size();
+            if ((int)cur.ops.size() > max_pass) fits = false;
+        }
+        if (!cur.ops.empty()) out.push_back(cur);
+        if (fits && (int)out.size() <= parts) return out;
+    }
+}
+
+std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass, const std::vector<int> *mirror)
 {
     std::vector<Block> out;
     // Consecutive diagonal blocks form one run (any two diagonal operators commute):
@@ -158,6 +219,13 @@ std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass)
         if (n <= max_pass) {
             out.push_back(b);
             continue;
+        }
+        if (mirror) {
+            std::vector<Block> cut = split_by_mirror(b, max_pass, *mirror);
+            if (!cut.empty()) {
+                out.insert(out.end(), cut.begin(), cut.end());
+                continue;
+            }
         }
         const int parts = (n + max_pass - 1) / max_pass;
         int start = 0;
@@ -264,6 +332,74 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
         T.amp_layers += nroots * osz * g.k;
     }
     return T;
+}
+
+HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::vector<ExcCode> &codes,
+                             const std::vector<int> &mslot)
+{
+    HalfTables H;
+    const int N = B.N;
+    const uint32_t lo = (1u << N) - 1u;
+    if (B.kind != BASIS_SZ || B.nA != B.nB) {
+        H.ok = false;
+        return H;
+    }
+    for (size_t gi = 0; gi < T.groups.size(); ++gi) {
+        const OrbitGroup &g = T.groups[gi];
+        if (g.k > (uint32_t)kMaxWarpLayers) {
+            H.ok = false;
+            return H;
+        }
+        const uint32_t osz = 1u << g.k;
+        std::vector<uint32_t> keep[2];  // orbits kept: [0] one of a mirror pair, [1] self-mirror
+        for (uint32_t o = 0; o < g.n_orbits; ++o) {
+            const size_t off = g.idx_off + (size_t)o * osz;
+            uint32_t key = UINT32_MAX, mkey = UINT32_MAX;
+            for (uint32_t q = 0; q < osz; ++q) {
+                const uint32_t s = T.bits[off + q], fs = flip_bits(s, N);
+                const int64_t r = B.rank_of(fs);
+                if (r < 0) {
+                    H.ok = false;
+                    return H;
+                }
+                key = std::min(key, T.idx[off + q]);
+                mkey = std::min(mkey, (uint32_t)r);
+                for (uint32_t l = 0; l < g.k; ++l) {
+                    const int sl = g.slot[l];
+                    if (mslot[sl] < 0 || exc_sign(codes[sl], s) != exc_sign(codes[mslot[sl]], fs)) {
+                        H.ok = false;
+                        return H;
+                    }
+                }
+            }
+            if (key < mkey) keep[0].push_back(o);
+            else if (key == mkey) keep[1].push_back(o);
+        }
+        for (int self = 0; self < 2; ++self) {
+            const uint32_t first = (uint32_t)H.idx.size();
+            for (uint32_t o : keep[self]) {
+                const size_t off = g.idx_off + (size_t)o * osz;
+                for (uint32_t q = 0; q < osz; ++q) {
+                    const uint32_t s = T.bits[off + q];
+                    const uint32_t x = (uint32_t)B.rankA[s >> N], y = (uint32_t)B.rankB[s & lo];
+                    H.idx.push_back(std::min(x, y) * B.nB + std::max(x, y));
+                    H.bits.push_back(s | ((self && x > y) ? kNoWriteBit : 0u));
+                }
+            }
+            const uint32_t per_task = (uint32_t)kWarpElems / osz, nk = (uint32_t)keep[self].size();
+            for (uint32_t o = 0; o < nk; o += per_task) {
+                WarpTask w{};
+                w.group = (uint32_t)gi | (self ? kSelfMirrorTask : 0u);
+                w.elem_off = first + o * osz;
+                w.n = std::min(per_task, nk - o) * osz;
+                w.mask = g.mask;
+                H.wtasks.push_back(w);
+            }
+            H.active += (uint64_t)nk * osz;
+            H.amp_layers += (uint64_t)nk * osz * g.k;
+        }
+    }
+    return H;
 }
 
 }  // namespace ae

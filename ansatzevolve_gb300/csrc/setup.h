@@ -61,7 +61,25 @@ constexpr int kMaxDiagSlots = 12;
 // members.  Runs of consecutive diagonal blocks are merged and cut into the fewest
 // near-equal passes of at most kMaxDiagSlots operators.  The operator order (the
 // grouping's permutation) is unchanged.
-std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass);
+// mirror (nullable): operator -> its spin-flip mirror (mirror_ops); a paired block in
+// which every operator's mirror lies is cut between mirror units (a pair, or one
+// operator that is its own mirror), so that every pass holds the mirrors of its
+// operators.
+std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass,
+                                const std::vector<int> *mirror = nullptr);
+
+// Spin-flip mirror of every operator (Sz basis, N spatial orbitals): the operator of
+// the same block whose created and annihilated orbitals are this one's with alpha and
+// beta exchanged (itself for a paired double of one alpha-beta pair), -1 if the block
+// has none.  Operators with equal masks are paired in order.
+std::vector<int> mirror_ops(const std::vector<ExcCode> &codes, const std::vector<Block> &blocks, int N);
+
+// Bitstring with the alpha (high N bits) and beta (low N bits) strings exchanged.
+inline uint32_t flip_bits(uint32_t s, int N)
+{
+    const uint32_t lo = (1u << N) - 1u;
+    return ((s & lo) << N) | ((s >> N) & lo);
+}
 
 // Greedy commuting-block grouping with forward moves, restating
 // FusedEvolve::regenCache (fusedevolve.cpp:1797-1967): a block grows while the next
@@ -126,5 +144,28 @@ struct OrbitTables {
 };
 
 OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int nthreads);
+
+// Spin-flip half tables of a pass (Sz basis with as many alpha as beta strings).  When
+// the pass holds the mirror of each of its operators and each operator's sign on a
+// determinant equals its mirror's sign on the mirrored determinant, the pass commutes
+// with the exchange of the alpha and beta strings, so a state with psi(a,b) =
+// psi(b,a) keeps that symmetry and only the amplitudes with a <= b need to be stored.
+// Orbits then come in mirror pairs (kept: the one whose smallest rank is below its
+// mirror's) or are their own mirror (kept, weight 1/2 in the gradient sums).  Entries
+// hold the rank of the stored (canonical) amplitude (min(a,b), max(a,b)); bit 31 of
+// an entry's bitstring marks the member of a self-mirror orbit that must not write
+// (its mirror, also in the orbit, writes the same canonical amplitude).  Warp tasks
+// of self-mirror orbits carry bit 31 in their group field.  mslot: slot -> slot of
+// its mirror operator.
+struct HalfTables {
+    std::vector<uint32_t> idx, bits;
+    std::vector<WarpTask> wtasks;
+    uint64_t active = 0, amp_layers = 0;
+    bool ok = true;   // false: a sign or rank check failed (no half passes)
+};
+constexpr uint32_t kNoWriteBit = 1u << 31;
+constexpr uint32_t kSelfMirrorTask = 1u << 31;
+HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::vector<ExcCode> &codes,
+                             const std::vector<int> &mslot);
 
 }  // namespace ae

@@ -535,10 +535,14 @@ def aux_case_bench(n_orb, lucj, stream, steps=5, warmup=2):
         peak, peak_kind = measured_peak()
         passes = info["blocks"]
         touched = info["active"]  # amplitudes touched per sweep (a diagonal pass touches all D)
+        half_passes = bool(eng.half_status()[0])
+        if half_passes:  # the spin-flip half passes touch one orbit of every mirror pair
+            touched = eng.half_info()["active"]
         fwd_bytes, adj_bytes = 16 * touched * W, 32 * touched * W
         out = {"value": 1e3 / ms, "unit": "evals/s", "ms_per_step": ms, "steps": steps, "warmup": warmup,
                "config": workload_desc(D, pb["P"], len(pb["ops0"]), "regenerated on the fly"),
-               "setup_s": setup_s, "passes": passes, "phase_ms": {"evolve": ph[0], "hpsi_energy": ph[1], "adjoint": ph[2]},
+               "setup_s": setup_s, "passes": passes, "half_passes": half_passes,
+               "phase_ms": {"evolve": ph[0], "hpsi_energy": ph[1], "adjoint": ph[2]},
                "hpsi_fp64": {"instructions": int(fw[0]), "achieved_T_per_s": fw[0] / (ph[1] / 1e3) / 1e12,
                              "peak_T_per_s": peak_t, "frac": fw[0] / (ph[1] / 1e3) / 1e12 / peak_t,
                              "peak_source": "measured (aegpu_fp64_peak)"},
@@ -838,11 +842,14 @@ def main():
     phase_ms, nph = eng.phase_times()
     eng.phase_timing(False)
     half = bool(eng.flip_status()[0])
-    # the same timed loop with the spin-flip half product switched off (every row of
-    # H psi computed, as the reference does), reported beside the headline
-    full_product = None
-    if half:
-        eng.set_tuning(ae.TUNE_FLIP, 0)
+    half_passes = bool(eng.half_status()[0])
+
+    def timed_without(knobs, note):
+        """The same timed loop with the given symmetry knobs switched off (then back on):
+        evals/s, per-phase ms and the energy's distance from the headline run's."""
+        E_sym = float(E_d.item())
+        for k in knobs:
+            eng.set_tuning(k, 0)
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
                 eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
@@ -854,7 +861,7 @@ def main():
         f1.record(stream)
         torch.cuda.synchronize()
         fms = f0.elapsed_time(f1) / args.steps
-        E_full = float(E_d.item())
+        E_off = float(E_d.item())
         eng.phase_timing(True)
         eng.phase_times()
         with torch.cuda.stream(stream):
@@ -863,13 +870,27 @@ def main():
         torch.cuda.synchronize()
         fph, fn = eng.phase_times()
         eng.phase_timing(False)
-        eng.set_tuning(ae.TUNE_FLIP, 1)
+        for k in knobs:
+            eng.set_tuning(k, 1)
         with torch.cuda.stream(stream):
             eng.gradient_dev(ang.data_ptr(), E_d.data_ptr(), g_d.data_ptr(), sp)
         torch.cuda.synchronize()
-        full_product = {"value": 1e3 / fms, "unit": "evals/s", "ms_per_step": fms,
-                        "hpsi_energy_ms": fph[1] / max(fn, 1), "dE_vs_half": abs(E_full - float(E_d.item())),
-                        "note": "the same loop with AEGPU_TUNE_FLIP = 0: every row of H psi computed"}
+        return {"value": 1e3 / fms, "unit": "evals/s", "ms_per_step": fms,
+                "phase_ms": {"evolve": fph[0] / max(fn, 1), "hpsi_energy": fph[1] / max(fn, 1),
+                             "adjoint": fph[2] / max(fn, 1)},
+                "dE_vs_headline": abs(E_off - E_sym), "note": note}
+
+    # the same timed loop with the spin-flip symmetry switched off, reported beside the
+    # headline: the half product alone (every row of H psi computed), and everything
+    # (every row and every orbit of every pass, as the reference computes them)
+    full_product = full_evaluation = None
+    if half:
+        full_product = timed_without([ae.TUNE_FLIP], "the same loop with AEGPU_TUNE_FLIP = 0: every row of H psi "
+                                                     "computed")
+    if half or half_passes:
+        full_evaluation = timed_without([ae.TUNE_FLIP, ae.TUNE_HALF],
+                                        "the same loop with AEGPU_TUNE_FLIP = 0 and AEGPU_TUNE_HALF = 0: every row "
+                                        "of H psi and every orbit of every pass computed, as the reference does")
     # one full analytic Hessian (evolveHessian), median of three, host buffers
     hess_ms = None
     if not args.no_hessian:
@@ -915,9 +936,11 @@ def main():
         # the half product streams the coded rows with a <= b (the other rows of the
         # listed 32-row slabs are skipped without loads)
         coded_bytes = int((coded_bytes - 16 * D * W) * row_frac) + 16 * D * W
-    # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass)
+    # whole-step algorithmic bytes (forward 16 B/amp/pass, H*psi, backward 32 B/amp/pass);
+    # the spin-flip half passes keep the nA (nA + 1) / 2 amplitudes with a <= b
     passes = info["blocks"]
-    step_bytes = passes * 16 * D * W + hpsi_bytes + passes * 32 * D * W
+    amp_frac = (nA * (nA + 1) // 2) / D if half_passes else 1.0
+    step_bytes = int(passes * 48 * D * W * amp_frac) + hpsi_bytes
     # FP64-pipe roofline of the same step: FP64 instructions per evaluation against the
     # DFMA throughput measured on this device right now
     fw = eng.fp64_work()
@@ -975,8 +998,14 @@ def main():
         "clocks": clk.summary(),
         "setup_s": setup_s,
     }
+    line["passes"] = {"count": passes,
+                      "kind": ("spin-flip half passes: one orbit of every mirror pair, the amplitudes with alpha "
+                               "string <= beta string kept current (every excitation's angle equals its "
+                               "mirror's and the start state is symmetric)" if half_passes else "full passes")}
     if full_product:
         line["full_product"] = full_product
+    if full_evaluation:
+        line["full_evaluation"] = full_evaluation
     if e2e:
         line["e2e"] = e2e
         line["e2e_uncached"] = e2e_uncached

@@ -105,15 +105,32 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * stored rows or on the fly), a state with psi(a,b) = psi(b,a) for every pair of alpha
  * and beta strings, which the device tests before every such product (relative norm
  * of the difference <= 1e-12), has H psi of the same symmetry, so only the rows with
- * a <= b are computed and mirrored.  No counterpart in the reference. */
+ * a <= b are computed and mirrored; and the spin-flip half passes (1, the default, or
+ * 0; AEGPU_HALF=0 in the environment sets 0 for engines created afterwards): where
+ * every pass holds the mirror of each of its excitations (alpha and beta orbitals
+ * exchanged) with the same sign rule, the start state has psi(a,b) = psi(b,a) and, at
+ * each evaluation, every excitation's angle equals its mirror's (a device test per
+ * instance), the evolution keeps that symmetry, so the forward and adjoint passes
+ * visit one orbit of every mirror pair, only the amplitudes with a <= b are kept
+ * current during the sweeps (the evolved state is completed by copying them to their
+ * mirrors), and each gradient is the sum over the visited orbits for the excitation
+ * and its mirror.  Projected gradients and Hessians always run the full passes.
+ * No counterpart in the reference. */
 enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
-       AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6, AEGPU_TUNE_FLIP = 7 };
+       AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6, AEGPU_TUNE_FLIP = 7, AEGPU_TUNE_HALF = 8 };
 int aegpu_set_tuning(aegpu_engine *e, int knob, int value);
 int aegpu_get_tuning(const aegpu_engine *e, int knob);
 /* used[b] = 1 where the last energy evaluation's H psi of instance b took the spin-flip
  * half product, 0 where it took the full one (or did not test; masked instances keep
  * their earlier value).  Synchronises the engine's stream. */
 int aegpu_flip_status(aegpu_engine *e, int *used);
+/* used[b] = 1 where the last evaluation of instance b ran the spin-flip half passes
+ * (AEGPU_TUNE_HALF).  info[4]: whether the problem allows them, amplitudes touched per
+ * sweep over all passes with them, FP64 instructions of their forward and adjoint
+ * passes per evaluation (as aegpu_fp64_work counts the full ones).  No counterpart in
+ * the reference. */
+int aegpu_half_status(aegpu_engine *e, int *used);
+int aegpu_half_info(const aegpu_engine *e, int64_t *info);
 int aegpu_batch_size(const aegpu_engine *e);
 /* Instance mask of batched evaluations: active[b] = 0 skips instance b (its results are
  * left as they were); NULL makes every instance active.  The Hessian and the H*x
