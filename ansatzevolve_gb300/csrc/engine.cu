@@ -812,6 +812,10 @@ struct DiagArgs {
     const uint16_t *smA, *smB;
     DevBasis basis;
     const int *active;    // instance mask (nullable)
+    // spin-flip half passes (nullable): where half[b] is set, instance b keeps only the
+    // amplitudes (a, b) with a <= b current (the others are skipped), and the adjoint
+    // counts a = b at half weight (the gradient adds the mirror operator's sum)
+    const int *half;
 };
 
 __device__ __forceinline__ uint32_t diag_mask(const DiagArgs &a, uint32_t bits)
@@ -854,13 +858,18 @@ __device__ __forceinline__ uint32_t diag_mask_s(const uint32_t *ann, int nslots,
 }
 
 // slot mask of amplitude z (< D): two string-table loads in the Sz basis, else the
-// slots' annihilation masks (ann, shared memory) against the bitstring
-__device__ __forceinline__ uint32_t diag_mask_z(const DiagArgs &a, const uint32_t *ann, uint32_t z)
+// slots' annihilation masks (ann, shared memory) against the bitstring.  hm (half
+// passes, Sz basis only): 0 for the amplitudes (a, b) with a > b; *same: a == b.
+__device__ __forceinline__ uint32_t diag_mask_z(const DiagArgs &a, const uint32_t *ann, uint32_t z, bool hm = false,
+                                                bool *same = nullptr)
 {
     if (a.smA) {
-        const uint32_t r = a.basis.div_nB(z);
-        return (uint32_t)__ldg(a.smA + r) & (uint32_t)__ldg(a.smB + (z - r * a.basis.nB));
+        const uint32_t r = a.basis.div_nB(z), c = z - r * a.basis.nB;
+        if (same) *same = r == c;
+        if (hm && r > c) return 0u;
+        return (uint32_t)__ldg(a.smA + r) & (uint32_t)__ldg(a.smB + c);
     }
+    if (same) *same = false;
     return diag_mask_s(ann, a.nslots, a.basis.bits(z));
 }
 
@@ -875,13 +884,14 @@ __global__ void __launch_bounds__(256, 4) k_diag_rot(DiagArgs a, double *vecs, s
     a.table += (size_t)blockIdx.y * a.tab_stride;
     vecs += (size_t)blockIdx.y * inst_stride;
     if (ckpt) ckpt += (size_t)blockIdx.y * ckpt_stride;
+    const bool hm = a.half && a.half[blockIdx.y];
     const uint64_t S = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t z0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z0 < D; z0 += kDiagUnroll * S) {
         uint32_t m[kDiagUnroll];
 #pragma unroll
         for (int u = 0; u < kDiagUnroll; ++u) {
             const uint64_t z = z0 + u * S;
-            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z) : 0u;
+            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z, hm) : 0u;
         }
         for (int vec = 0; vec < nvec; ++vec) {
             double *p = vecs + vec * vstride;
@@ -927,13 +937,16 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
     for (int i = 0; i < NS; ++i) acc[i] = 0;
     const uint64_t D = a.basis.D;
     const uint64_t S = (uint64_t)gridDim.x * blockDim.x;
+    const bool hm = a.half && a.half[blockIdx.y];
     for (uint64_t z0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; z0 < D; z0 += U * S) {
         uint32_t m[U];
+        bool same[U];
         double2 x[U], y[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint64_t z = z0 + u * S;
-            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z) : 0u;
+            same[u] = false;
+            m[u] = z < D ? diag_mask_z(a, ann, (uint32_t)z, hm, &same[u]) : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
@@ -946,12 +959,14 @@ __global__ void __launch_bounds__(256, 4) k_diag_adj(DiagArgs a, const double *_
         for (int u = 0; u < U; ++u) {
             if (!m[u]) continue;
             const double q = y[u].y * x[u].x - y[u].x * x[u].y;
+            // half passes: a = b at half weight (an FMA costs what the add did)
+            const double wt = (hm && same[u]) ? 0.5 : 1.0;
             // FP64 adds past the pass's own slots would still take FP64 issue slots when
             // predicated off: leave the unrolled loop at the (uniform) slot count
 #pragma unroll
             for (int i = 0; i < NS; ++i) {
                 if (i == a.nslots) break;
-                if (ONE || (m[u] & (1u << i))) acc[i] += q;
+                if (ONE || (m[u] & (1u << i))) acc[i] = fma(wt, q, acc[i]);
             }
             const double2 t = diag_phase(a, m[u]);
             *reinterpret_cast<double2 *>(h + 2 * (z0 + u * S)) =
@@ -1023,14 +1038,19 @@ __global__ void __launch_bounds__(kDiagAdjThreads, 4) k_diag_adj_sz(DiagArgs a, 
     const uint32_t r0 = (uint32_t)((uint64_t)nA * rc / sp.row_chunks);
     const uint32_t r1 = (uint32_t)((uint64_t)nA * (rc + 1) / sp.row_chunks);
     double col = 0.0;
-    for (uint32_t a0 = r0 + (uint32_t)(tid / sp.cols); a0 < r1; a0 += U * lanes) {
+    // half passes: only the rows a <= b of this column, a = b at half weight; the warp
+    // stops after the last row that any of its 32 columns needs
+    const bool hm = a.half && a.half[blockIdx.y];
+    const uint32_t warp_b_end = (uint32_t)(cb * sp.cols + ((tid & (sp.cols - 1)) & ~31)) + 32u;
+    const uint32_t r_end = hm ? min(r1, warp_b_end) : r1;
+    for (uint32_t a0 = r0 + (uint32_t)(tid / sp.cols); a0 < r_end; a0 += U * lanes) {
         uint32_t ma[U], m[U];
         double2 x[U], y[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint32_t ar = a0 + u * lanes;
-            ma[u] = ar < r1 ? (uint32_t)__ldg(a.smA + ar) : 0u;
-            m[u] = col_ok ? ma[u] & mb : 0u;
+            ma[u] = ar < r_end ? (uint32_t)__ldg(a.smA + ar) : 0u;
+            m[u] = col_ok && !(hm && ar > b) ? ma[u] & mb : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
@@ -1042,11 +1062,12 @@ __global__ void __launch_bounds__(kDiagAdjThreads, 4) k_diag_adj_sz(DiagArgs a, 
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const double q = m[u] ? y[u].y * x[u].x - y[u].x * x[u].y : 0.0;
-            if (sp.b_only) col += q;
+            const double wt = (hm && a0 + u * lanes == b) ? 0.5 : 1.0;
+            if (sp.b_only) col = fma(wt, q, col);
             for (uint32_t r = ma[u] & sp.a_rows; r; r &= r - 1u) {  // uniform over the warp
                 const int i = __ffs(r) - 1;
                 const bool on = !((sp.mixed >> i) & 1u) || ((mb >> i) & 1u);
-                sacc[i][tid] += on ? q : 0.0;
+                sacc[i][tid] = fma(wt, on ? q : 0.0, sacc[i][tid]);
             }
             if (m[u]) {
                 const size_t z = (size_t)(a0 + u * lanes) * nB + b;
@@ -2422,10 +2443,11 @@ struct aegpu_engine {
         return AEGPU_OK;
     }
     // Arguments of diagonal pass b in direction dir (+1 forward, -1 adjoint).
-    DiagArgs diag_args(const DevBlock &b, double dir, bool masked = true) const
+    DiagArgs diag_args(const DevBlock &b, double dir, bool masked = true, bool half = false) const
     {
         DiagArgs a;
         a.active = masked ? d_active : nullptr;
+        a.half = half && half_static ? d_half : nullptr;
         a.ops = b.ops;
         a.nslots = b.nslots;
         a.codes = d_codes;
@@ -2526,8 +2548,8 @@ int run_evolve(aegpu_engine *e, int ninst)
         auto &b = e->dblocks[bi];
         double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
-            k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, 1.0), e->d_psi, 0, 1, ck, n,
-                                                                       e->n_ckpt);
+            k_diag_rot<<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, 1.0, true, true), e->d_psi, 0,
+                                                                       1, ck, n, e->n_ckpt);
             e->launches += 1;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, 1.0, true);
@@ -2703,15 +2725,16 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         double *part = e->d_partials + b.part_off;
         const double *ck = e->d_ckpt + b.ckpt_off;
         if (b.diagonal) {
+            const DiagArgs da = e->diag_args(b, -1.0, true, half);
             if (b.smA && b.nslots >= kDiagAdjSzMinSlots)
-                k_diag_adj_sz<<<dim3(b.wgrid, ninst), kDiagAdjThreads, 0, e->stream>>>(
-                    e->diag_args(b, -1.0), b.split, ck, e->n_ckpt, e->d_h, n, part, e->n_partials);
+                k_diag_adj_sz<<<dim3(b.wgrid, ninst), kDiagAdjThreads, 0, e->stream>>>(da, b.split, ck, e->n_ckpt,
+                                                                                      e->d_h, n, part, e->n_partials);
             else if (b.nslots == 1)
-                k_diag_adj<true><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, -1.0), ck, e->n_ckpt,
-                                                                               e->d_h, n, part, e->n_partials);
+                k_diag_adj<true><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(da, ck, e->n_ckpt, e->d_h, n, part,
+                                                                               e->n_partials);
             else
-                k_diag_adj<false><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(e->diag_args(b, -1.0), ck, e->n_ckpt,
-                                                                                e->d_h, n, part, e->n_partials);
+                k_diag_adj<false><<<dim3(kDiagGrid, ninst), 256, 0, e->stream>>>(da, ck, e->n_ckpt, e->d_h, n, part,
+                                                                                e->n_partials);
             e->launches += 1;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, -1.0, half);
@@ -3066,19 +3089,23 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     // the reference's commuting blocks, cut into passes of <= 6 excitations so that
     // every orbit fits one warp's registers
     {
-        // spin-flip half passes need the Sz basis with as many alpha as beta strings, no
-        // diagonal operator and every operator's mirror in its block (then in its pass)
+        // spin-flip half passes need the Sz basis with as many alpha as beta strings and
+        // every operator's mirror in its block or diagonal run (then in its pass)
         std::vector<Block> grouped = group_blocks(e->excs, kMaxSlots, e->perm);
         std::vector<int> mir;
         bool half = e->B.kind == BASIS_SZ && e->B.nA == e->B.nB;
-        for (const Block &b : grouped) half = half && !b.diagonal;
         if (half) {
+            grouped = merge_commuting(grouped, e->excs);
             mir = mirror_ops(e->codes, grouped, e->B.N);
             for (int m : mir) half = half && m >= 0;
         }
         e->blocks = split_passes(grouped, e->tune_pass_ops, half ? &mir : nullptr);
         e->half_static = half;
         e->mirror = half ? mir : std::vector<int>();
+        // the application order is the passes' order (a cut between mirror units may
+        // reorder operators inside a commuting run): the Hessian's positions follow it
+        e->perm.clear();
+        for (const Block &b : e->blocks) e->perm.insert(e->perm.end(), b.ops.begin(), b.ops.end());
     }
     e->pos_of_op.assign(nops, 0);
     for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;

@@ -124,14 +124,44 @@ std::vector<Block> group_blocks(const std::vector<Exc> &excs, int max_fuse, std:
     return out;
 }
 
+std::vector<Block> merge_commuting(const std::vector<Block> &blocks, const std::vector<Exc> &excs)
+{
+    std::vector<Block> out;
+    for (const auto &b : blocks) {
+        if (!out.empty() && !b.diagonal && !out.back().diagonal) {
+            bool all = true;
+            for (int x : out.back().ops) {
+                for (int y : b.ops)
+                    if (!exc_commutes(excs[x], excs[y])) { all = false; break; }
+                if (!all) break;
+            }
+            if (all) {
+                out.back().ops.insert(out.back().ops.end(), b.ops.begin(), b.ops.end());
+                continue;
+            }
+        }
+        out.push_back(b);
+    }
+    return out;
+}
+
 std::vector<int> mirror_ops(const std::vector<ExcCode> &codes, const std::vector<Block> &blocks, int N)
 {
+    // search domains: every paired block, and every run of consecutive diagonal blocks
+    // (split_passes merges such a run before cutting it into passes)
+    std::vector<std::vector<int>> domains;
+    bool run = false;
+    for (const auto &b : blocks) {
+        if (!(b.diagonal && run)) domains.emplace_back();
+        domains.back().insert(domains.back().end(), b.ops.begin(), b.ops.end());
+        run = b.diagonal;
+    }
     std::vector<int> mir(codes.size(), -1);
-    for (const auto &b : blocks)
-        for (int o : b.ops) {
+    for (const auto &dom : domains)
+        for (int o : dom) {
             if (mir[o] >= 0) continue;
             const uint32_t fc = flip_bits(codes[o].create, N), fa = flip_bits(codes[o].annihilate, N);
-            for (int p : b.ops)
+            for (int p : dom)
                 if (mir[p] < 0 && codes[p].create == fc && codes[p].annihilate == fa && (p != o || fc == codes[o].create)) {
                     mir[o] = p;
                     mir[p] = o;
@@ -197,6 +227,18 @@ std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass, 
     auto flush = [&]() {
         const int n = (int)run.size();
         if (!n) return;
+        if (mirror && n > kMaxDiagSlots) {
+            Block r;
+            r.diagonal = true;
+            r.ops = run;
+            std::vector<Block> cut = split_by_mirror(r, kMaxDiagSlots, *mirror);
+            if (!cut.empty()) {
+                for (auto &c : cut) c.diagonal = true;
+                out.insert(out.end(), cut.begin(), cut.end());
+                run.clear();
+                return;
+            }
+        }
         const int parts = (n + kMaxDiagSlots - 1) / kMaxDiagSlots;
         int start = 0;
         for (int p = 0; p < parts; ++p) {

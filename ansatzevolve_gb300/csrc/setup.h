@@ -68,10 +68,18 @@ constexpr int kMaxDiagSlots = 12;
 std::vector<Block> split_passes(const std::vector<Block> &blocks, int max_pass,
                                 const std::vector<int> *mirror = nullptr);
 
+// Consecutive paired blocks whose operators all commute (the grouping's divisor rule
+// cuts a commuting run of, e.g., 14 operators into two blocks of 7) merged into one,
+// in the same operator order, so that split_passes can cut the run between mirror
+// units.
+std::vector<Block> merge_commuting(const std::vector<Block> &blocks, const std::vector<Exc> &excs);
+
 // Spin-flip mirror of every operator (Sz basis, N spatial orbitals): the operator of
-// the same block whose created and annihilated orbitals are this one's with alpha and
-// beta exchanged (itself for a paired double of one alpha-beta pair), -1 if the block
-// has none.  Operators with equal masks are paired in order.
+// the same block (for a diagonal operator: of the same run of consecutive diagonal
+// blocks) whose created and annihilated orbitals are this one's with alpha and beta
+// exchanged (itself for a paired double or a density-density operator of one
+// alpha-beta pair), -1 if there is none.  Operators with equal masks are paired in
+// order.
 std::vector<int> mirror_ops(const std::vector<ExcCode> &codes, const std::vector<Block> &blocks, int N);
 
 // Bitstring with the alpha (high N bits) and beta (low N bits) strings exchanged.

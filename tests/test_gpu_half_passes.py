@@ -165,3 +165,41 @@ def test_projected_gradient_and_hessian_after_half_evaluation():
     Ho = o.hessian_comp(x)
     np.testing.assert_allclose(H, Ho, atol=1e-9, rtol=0)
     e.close()
+
+
+@pytest.mark.parametrize("mode", [ae.HAM_STORED, ae.HAM_ON_THE_FLY])
+def test_half_passes_complex_lucj(mode):
+    """The complex LUCJ circuit: its Givens and phase operators come in alpha/beta
+    mirror pairs with equal angles, its density-density operators are their own mirrors
+    or pairs, so rotation and diagonal passes both run halved; the results match the
+    full passes and the oracle."""
+    from oracle.oracle import Oracle
+    from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals
+    N, na = 8, 4
+    K, J = random_lucj(N, 2)
+    ops, ang = lucj_operators(K, J)
+    e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, ops, complex_mode=True)
+    init = np.zeros(2 * e.D)
+    init[2 * np.searchsorted(e.states(), hartree_fock_index(N, na, na))] = 1.0
+    e.set_initial(init)
+    h1, g2 = synthetic_integrals(N, 7)
+    e.set_ham_integrals(h1, g2, mode)
+    assert e.half_info()["available"]
+    E1, g1 = e.gradient(ang)
+    assert e.half_status()[0]
+    s1 = e.evolve(ang)
+    e.set_tuning(ae.TUNE_HALF, 0)
+    E0, g0 = e.gradient(ang)
+    s0 = e.evolve(ang)
+    assert abs(E1 - E0) < 1e-12 * max(1.0, abs(E0))
+    np.testing.assert_allclose(g1, g0, atol=1e-11, rtol=0)
+    np.testing.assert_allclose(s1, s0, atol=1e-13, rtol=0)
+    o = Oracle(2 * N, 2, 2 * na, na, na, cplx=True)
+    o.set_initial([hartree_fock_index(N, na, na)], [1.0])
+    o.set_ops(ops, np.arange(len(ops)), np.ones(len(ops)))
+    o.set_ham_integrals(h1, g2, csr=True)
+    Eo, go = o.energy_gradient_ops(ang)
+    assert abs(E1 - Eo) < 1e-10
+    np.testing.assert_allclose(g1, go, atol=1e-9, rtol=0)
+    e.close()
