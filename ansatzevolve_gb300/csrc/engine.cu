@@ -2086,6 +2086,7 @@ struct aegpu_engine {
         int ntiles = 0;           // shared-memory tiles (multi-vector Hessian kernels)
         int nwtasks = 0;          // warp tasks (evolve / adjoint kernels)
         int wgrid = 0;            // CTAs of the warp kernels; also partial-sum rows
+        int rgrid = 0;            // CTAs of the forward warp kernel (as many as stay resident)
         WarpTask *wtasks = nullptr;
         int64_t part_off = 0;     // offset of this block's gradient partials
         int64_t ckpt_off = 0;     // offset (doubles) of this pass's checkpoint
@@ -2553,7 +2554,7 @@ int run_evolve(aegpu_engine *e, int ninst)
             e->launches += 1;
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, 1.0, true);
-            const dim3 g(b.wgrid, ninst);
+            const dim3 g(b.rgrid, ninst);
             if (e->W == 1)
                 launch_pass(e, k_warp_rot<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             else
@@ -3140,6 +3141,13 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->db = db;
     e->d_codes = e->upload(e->codes);
 
+    // resident CTAs per SM of the forward warp kernel (its register count)
+    int rot_occ = 0;
+    if (e->cplx)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rot_occ, k_warp_rot<2>, kWarpThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rot_occ, k_warp_rot<1>, kWarpThreads, 0);
+    cudaGetLastError();
     // orbit tables per block
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     e->dblocks.clear();
@@ -3174,6 +3182,9 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
             d.wtasks = e->upload(T.wtasks);
             d.nwtasks = (int)T.wtasks.size();
             d.wgrid = std::max(1, std::min(e->sm_count * e->tune_ctas_per_sm, (d.nwtasks + 7) / 8));
+            // the forward kernel needs fewer registers than the adjoint: as many CTAs as stay
+            // resident, so that a warp takes at most one task where the tasks allow
+            d.rgrid = std::max(1, std::min(e->sm_count * std::max(e->tune_ctas_per_sm, rot_occ), (d.nwtasks + 7) / 8));
             d.active = T.active;
             d.amp_layers = T.amp_layers;
             if (e->half_static) {
