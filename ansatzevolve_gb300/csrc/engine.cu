@@ -1004,6 +1004,7 @@ constexpr int kDiagAdjThreads = 256;
 // a 6-slot pass 292 us against 262 us.
 constexpr int kDiagAdjSzMinSlots = 5;
 
+constexpr int kDiagMaxColBlocks = 32;
 struct DiagSplit {
     int cols;         // columns per CTA (power of two, <= kDiagAdjThreads)
     int col_blocks;   // CTAs across the columns
@@ -1011,7 +1012,29 @@ struct DiagSplit {
     uint32_t b_only;  // slots with no alpha bits
     uint32_t a_rows;  // alpha-only and mixed slots
     uint32_t mixed;   // slots with both alpha and beta bits
+    // half passes: the same col_blocks * row_chunks CTAs over the triangle a <= b, so
+    // that every CTA has a near-equal share: column block c gets the CTAs
+    // [half_first[c], half_first[c + 1]) for its rows 0 .. min(nA, (c + 1) * cols)
+    // (half_first[0] = -1: more column blocks than kDiagMaxColBlocks, no such split)
+    int half_first[kDiagMaxColBlocks + 1];
 };
+
+// Rows of column block [lo, lo + L) in the half passes: row r < lo meets all L
+// columns, row lo + j the L - j columns b >= r.  The first row at which the work of the
+// rows before it reaches x (W(r) = r L for r <= lo, lo L + j L - j (j - 1) / 2 past it);
+// the root of the quadratic in float, then exact integer steps.
+__device__ __forceinline__ uint32_t tri_row(uint64_t x, uint32_t lo, uint32_t L)
+{
+    if (x <= (uint64_t)lo * L) return (uint32_t)((x + L - 1) / L);
+    const uint64_t xp = x - (uint64_t)lo * L;
+    auto C = [L](int64_t j) { return (uint64_t)(j * (int64_t)L - j * (j - 1) / 2); };
+    const float t = 2.0f * L + 1.0f;
+    int64_t j = (int64_t)((t - sqrtf(fmaxf(0.0f, t * t - 8.0f * (float)xp))) * 0.5f);
+    if (j < 0) j = 0;
+    while (j > 0 && C(j - 1) >= xp) --j;
+    while (C(j) < xp) ++j;
+    return lo + (uint32_t)j;
+}
 
 __global__ void __launch_bounds__(kDiagAdjThreads, 4) k_diag_adj_sz(DiagArgs a, DiagSplit sp,
                                                                     const double *__restrict__ ckpt,
@@ -1030,17 +1053,28 @@ __global__ void __launch_bounds__(kDiagAdjThreads, 4) k_diag_adj_sz(DiagArgs a, 
     const int tid = threadIdx.x;
     for (int i = 0; i < a.nslots; ++i) sacc[i][tid] = 0.0;
     const uint32_t nA = a.basis.nA, nB = a.basis.nB;
-    const int cb = blockIdx.x % sp.col_blocks, rc = blockIdx.x / sp.col_blocks;
+    // half passes: only the rows a <= b of this column, a = b at half weight; the warp
+    // stops after the last row that any of its 32 columns needs
+    const bool hm = a.half && a.half[blockIdx.y];
+    int cb = blockIdx.x % sp.col_blocks, rc = blockIdx.x / sp.col_blocks;
+    uint32_t r0 = (uint32_t)((uint64_t)nA * rc / sp.row_chunks);
+    uint32_t r1 = (uint32_t)((uint64_t)nA * (rc + 1) / sp.row_chunks);
+    if (hm && sp.half_first[0] >= 0) {
+        // this column block's share of the CTAs, cut into rows of equal work
+        cb = 0;
+        while (cb + 1 < sp.col_blocks && (int)blockIdx.x >= sp.half_first[cb + 1]) ++cb;
+        rc = (int)blockIdx.x - sp.half_first[cb];
+        const int nch = sp.half_first[cb + 1] - sp.half_first[cb];
+        const uint32_t lo = (uint32_t)(cb * sp.cols), L = min(nB, lo + (uint32_t)sp.cols) - lo;
+        const uint64_t Wb = (uint64_t)lo * L + (uint64_t)L * (L + 1) / 2;
+        r0 = tri_row(Wb * rc / nch, lo, L);
+        r1 = tri_row(Wb * (rc + 1) / nch, lo, L);
+    }
     const uint32_t b = (uint32_t)(cb * sp.cols + (tid & (sp.cols - 1)));
     const bool col_ok = b < nB;
     const uint32_t mb = col_ok ? (uint32_t)__ldg(a.smB + b) : 0u;
     const int lanes = kDiagAdjThreads / sp.cols;  // row lanes per CTA
-    const uint32_t r0 = (uint32_t)((uint64_t)nA * rc / sp.row_chunks);
-    const uint32_t r1 = (uint32_t)((uint64_t)nA * (rc + 1) / sp.row_chunks);
     double col = 0.0;
-    // half passes: only the rows a <= b of this column, a = b at half weight; the warp
-    // stops after the last row that any of its 32 columns needs
-    const bool hm = a.half && a.half[blockIdx.y];
     const uint32_t warp_b_end = (uint32_t)(cb * sp.cols + ((tid & (sp.cols - 1)) & ~31)) + 32u;
     const uint32_t r_end = hm ? min(r1, warp_b_end) : r1;
     for (uint32_t a0 = r0 + (uint32_t)(tid / sp.cols); a0 < r_end; a0 += U * lanes) {
@@ -3040,6 +3074,33 @@ static void diag_string_masks(aegpu_engine *e, const Block &b, aegpu_engine::Dev
         if (ha && hb) sp.mixed |= 1u << i;
     }
     if (ns >= kDiagAdjSzMinSlots) d.wgrid = sp.col_blocks * sp.row_chunks;
+    // the half passes' split of the same CTAs over the triangle, by each column block's
+    // share of its amplitudes, every block at least one CTA
+    sp.half_first[0] = -1;
+    const int G = sp.col_blocks * sp.row_chunks;
+    if (sp.col_blocks <= kDiagMaxColBlocks && G >= sp.col_blocks) {
+        std::vector<double> w(sp.col_blocks);
+        double W = 0;
+        for (int c = 0; c < sp.col_blocks; ++c) {
+            // amplitudes (a, b) with a <= b in the block's columns (tri_row's total)
+            const double lo = (double)c * sp.cols, L = std::min<double>(B.nB, (double)(c + 1) * sp.cols) - lo;
+            w[c] = lo * L + L * (L + 1) / 2.0;
+            W += w[c];
+        }
+        std::vector<int> n(sp.col_blocks, 1);
+        int used = sp.col_blocks;
+        for (int c = 0; c < sp.col_blocks; ++c) {
+            const int extra = (int)std::floor((G - sp.col_blocks) * w[c] / W);
+            n[c] += extra;
+            used += extra;
+        }
+        for (int c = sp.col_blocks - 1; used < G; c = (c + sp.col_blocks - 1) % sp.col_blocks) {
+            n[c]++;
+            used++;
+        }
+        sp.half_first[0] = 0;
+        for (int c = 0; c < sp.col_blocks; ++c) sp.half_first[c + 1] = sp.half_first[c] + n[c];
+    }
     // determinants with at least one active slot, from the histograms of the two masks
     std::vector<uint64_t> hA((size_t)1 << ns, 0), hB((size_t)1 << ns, 0);
     for (uint16_t m : mA) hA[m]++;
