@@ -3253,7 +3253,7 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
                 for (size_t i = 0; i < b.ops.size(); ++i)
                     for (size_t j = 0; j < b.ops.size(); ++j)
                         if (b.ops[j] == e->mirror[b.ops[i]]) mslot[i] = (int)j;
-                HalfTables H = build_half_orbits(e->B, T, bc, mslot);
+                HalfTables H = build_half_orbits(e->B, T, bc, mslot, (int)hw);
                 if (!H.ok) {
                     e->half_static = false;
                 } else {

@@ -377,7 +377,7 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
 }
 
 HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::vector<ExcCode> &codes,
-                             const std::vector<int> &mslot)
+                             const std::vector<int> &mslot, int nthreads)
 {
     HalfTables H;
     const int N = B.N;
@@ -386,6 +386,7 @@ HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::ve
         H.ok = false;
         return H;
     }
+    if (nthreads < 1) nthreads = 1;
     for (size_t gi = 0; gi < T.groups.size(); ++gi) {
         const OrbitGroup &g = T.groups[gi];
         if (g.k > (uint32_t)kMaxWarpLayers) {
@@ -393,29 +394,47 @@ HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::ve
             return H;
         }
         const uint32_t osz = 1u << g.k;
-        std::vector<uint32_t> keep[2];  // orbits kept: [0] one of a mirror pair, [1] self-mirror
-        for (uint32_t o = 0; o < g.n_orbits; ++o) {
-            const size_t off = g.idx_off + (size_t)o * osz;
-            uint32_t key = UINT32_MAX, mkey = UINT32_MAX;
-            for (uint32_t q = 0; q < osz; ++q) {
-                const uint32_t s = T.bits[off + q], fs = flip_bits(s, N);
-                const int64_t r = B.rank_of(fs);
-                if (r < 0) {
-                    H.ok = false;
-                    return H;
-                }
-                key = std::min(key, T.idx[off + q]);
-                mkey = std::min(mkey, (uint32_t)r);
-                for (uint32_t l = 0; l < g.k; ++l) {
-                    const int sl = g.slot[l];
-                    if (mslot[sl] < 0 || exc_sign(codes[sl], s) != exc_sign(codes[mslot[sl]], fs)) {
-                        H.ok = false;
-                        return H;
+        // per orbit: 0 its mirror is kept, 1 kept (one of a mirror pair), 2 kept (its own
+        // mirror), 3 a rank or sign check failed; classified in parallel over orbit ranges
+        std::vector<uint8_t> cls(g.n_orbits, 0);
+        auto work = [&](int t) {
+            const uint32_t o0 = (uint32_t)((uint64_t)g.n_orbits * t / nthreads);
+            const uint32_t o1 = (uint32_t)((uint64_t)g.n_orbits * (t + 1) / nthreads);
+            for (uint32_t o = o0; o < o1; ++o) {
+                const size_t off = g.idx_off + (size_t)o * osz;
+                uint32_t key = UINT32_MAX, mkey = UINT32_MAX;
+                bool bad = false;
+                for (uint32_t q = 0; q < osz && !bad; ++q) {
+                    const uint32_t s = T.bits[off + q], fs = flip_bits(s, N);
+                    const int64_t r = B.rank_of(fs);
+                    if (r < 0) {
+                        bad = true;
+                        break;
+                    }
+                    key = std::min(key, T.idx[off + q]);
+                    mkey = std::min(mkey, (uint32_t)r);
+                    for (uint32_t l = 0; l < g.k; ++l) {
+                        const int sl = g.slot[l];
+                        if (mslot[sl] < 0 || exc_sign(codes[sl], s) != exc_sign(codes[mslot[sl]], fs)) {
+                            bad = true;
+                            break;
+                        }
                     }
                 }
+                cls[o] = bad ? 3 : key < mkey ? 1 : key == mkey ? 2 : 0;
             }
-            if (key < mkey) keep[0].push_back(o);
-            else if (key == mkey) keep[1].push_back(o);
+        };
+        std::vector<std::thread> th;
+        for (int t = 1; t < nthreads; ++t) th.emplace_back(work, t);
+        work(0);
+        for (auto &x : th) x.join();
+        std::vector<uint32_t> keep[2];  // [0] one of a mirror pair, [1] self-mirror
+        for (uint32_t o = 0; o < g.n_orbits; ++o) {
+            if (cls[o] == 3) {
+                H.ok = false;
+                return H;
+            }
+            if (cls[o]) keep[cls[o] - 1].push_back(o);
         }
         for (int self = 0; self < 2; ++self) {
             const uint32_t first = (uint32_t)H.idx.size();

@@ -174,6 +174,6 @@ struct HalfTables {
 constexpr uint32_t kNoWriteBit = 1u << 31;
 constexpr uint32_t kSelfMirrorTask = 1u << 31;
 HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::vector<ExcCode> &codes,
-                             const std::vector<int> &mslot);
+                             const std::vector<int> &mslot, int nthreads);
 
 }  // namespace ae
