@@ -158,6 +158,8 @@ struct BlockArgs {
     const uint32_t *idx_h, *obits_h;
     const WarpTask *tasks_h;
     int ntasks_h;
+    // the Hessian's tangent kernels: grid row v works on vector vmap[v] (nullable: v)
+    const int *vmap;
 };
 
 // The tables instance b runs: the half tables where its half flag is set.
@@ -539,7 +541,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
     if (skip_instance(a.active, b)) return;
     const PassConst *pc = a.pc + (size_t)b * a.pc_stride;
     const double *sig = a.sigma + (size_t)b * a.sig_stride;
-    double *psi = vecs + (size_t)b * inst_stride;
+    double *psi = vecs + (size_t)(a.vmap ? a.vmap[b] : b) * inst_stride;
     if (ckpt) ckpt += (size_t)b * ckpt_stride;
     const PassTables pt = pass_tables(a, tasks, ntasks, b);
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -712,9 +714,10 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const W
 {
     __shared__ double red[kMaxWarpLayers][kWarpThreads / 32];
     const int lane = threadIdx.x & 31, vec = blockIdx.y;
+    const int vpos = a.vmap ? a.vmap[vec] : vec;  // the tangent's application position
     const PassConst *pc = a.pc;
     const double *sig = a.sigma;
-    double *t = T + (size_t)vec * tstride;
+    double *t = T + (size_t)vpos * tstride;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double accS[kMaxWarpLayers];
 #pragma unroll
@@ -736,7 +739,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const W
         }
 #pragma unroll
         for (int j = 0; j < kMaxWarpLayers; ++j) {
-            if (!(mask & (1u << j)) || block_pos0 + j < vec) continue;
+            if (!(mask & (1u << j)) || block_pos0 + j < vpos) continue;
             const int i = __popc(mask & ((1u << j) - 1u));
             const PassConst q = pc[j];
             const int s0 = exc_sign(q.code, b0), s1 = exc_sign(q.code, b1);
@@ -1221,21 +1224,38 @@ __global__ void k_grad_reduce(const double *__restrict__ partials, const int64_t
 }
 
 // Hessian second-derivative partials of one block -> Hops (nops x nops, row-major).
+// Half tangents (vmap, mirror, tpos set): grid row vec carried the tangent at position
+// vmap[vec]; the pair of operators it yields also stands for its mirror pair, whose
+// value is the same (the circuit commutes with the exchange of the alpha and beta
+// strings), where the mirror pair's earlier operator is one whose tangent was not
+// carried (so that no pair is counted twice).
 __global__ void k_hess_reduce(const double *__restrict__ partials, int ntiles, int nvec, int nslots,
                               const int *__restrict__ pos_op, const int *__restrict__ block_ops, int block_pos0,
-                              double *__restrict__ Hops, int nops, double factor)
+                              double *__restrict__ Hops, int nops, double factor, const int *__restrict__ vmap,
+                              const int *__restrict__ mirror, const int *__restrict__ tpos)
 {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= nvec * nslots) return;
     const int vec = warp / nslots, sl = warp % nslots;
-    if (block_pos0 + sl < vec) return;
+    const int vpos = vmap ? vmap[vec] : vec;
+    if (block_pos0 + sl < vpos) return;
     double s = 0;
     for (int t = lane; t < ntiles; t += 32) s += partials[((size_t)t * nvec + vec) * kMaxSlots + sl];
     s = warp_sum(s);
     if (lane == 0) {
-        const int i = pos_op[vec], j = block_ops[sl];
+        const int i = pos_op[vpos], j = block_ops[sl];
         Hops[(size_t)i * nops + j] += factor * s;
         if (i != j) Hops[(size_t)j * nops + i] += factor * s;
+        if (vmap) {
+            const int mi = mirror[i], mj = mirror[j];
+            const bool same = (mi == i && mj == j) || (mi == j && mj == i);
+            const int first = tpos[mi] <= tpos[mj] ? mi : mj;        // the mirror pair's earlier operator
+            const bool carried = tpos[first] <= tpos[mirror[first]];  // its tangent was carried
+            if (!same && !carried) {
+                Hops[(size_t)mi * nops + mj] += factor * s;
+                if (mi != mj) Hops[(size_t)mj * nops + mi] += factor * s;
+            }
+        }
     }
 }
 
@@ -1341,9 +1361,14 @@ __global__ void __launch_bounds__(kSpmvThreads) k_spmv_sell(int64_t q, const int
 
 // Compressed tangents T_C[j][w][mu] = sum_{op: param(op)=mu} scale_op T[pos(op)][j][w];
 // column P holds psi (fusedevolve.cpp:2609-2612, m_compressMatrixPsi).
+// mpos (nullable; the Hessian's half tangents): for entry k, -1, or the position of the
+// mirror tangent that was carried in its place; the tangent is then that one with the
+// alpha and beta strings exchanged, read at the mirrored amplitude (rows and columns of
+// the nA x nA string matrix swapped; B gives nB and the division).
 __global__ void k_tc_build(const double *__restrict__ T, size_t tstride, const double *__restrict__ psi,
                            const int *__restrict__ prm_ptr, const int *__restrict__ prm_pos,
-                           const double *__restrict__ prm_scale, int P, int W, int64_t D, double *__restrict__ TC)
+                           const double *__restrict__ prm_scale, int P, int W, int64_t D, double *__restrict__ TC,
+                           const int *__restrict__ mpos, DevBasis B)
 {
     const int V = P + 1;
     const int64_t total = D * W * V;
@@ -1355,7 +1380,16 @@ __global__ void k_tc_build(const double *__restrict__ T, size_t tstride, const d
             s = psi[jw];
         } else {
             s = 0;
-            for (int k = prm_ptr[mu]; k < prm_ptr[mu + 1]; ++k) s += prm_scale[k] * T[(size_t)prm_pos[k] * tstride + jw];
+            for (int k = prm_ptr[mu]; k < prm_ptr[mu + 1]; ++k) {
+                if (mpos && mpos[k] >= 0) {
+                    const uint32_t z = (uint32_t)(jw / W), w = (uint32_t)(jw - (int64_t)z * W);
+                    const uint32_t ra = B.div_nB(z), rb = z - ra * B.nB;
+                    const size_t jm = ((size_t)rb * B.nB + ra) * W + w;
+                    s += prm_scale[k] * T[(size_t)mpos[k] * tstride + jm];
+                } else {
+                    s += prm_scale[k] * T[(size_t)prm_pos[k] * tstride + jw];
+                }
+            }
         }
         TC[(size_t)mu * D * W + jw] = s;  // column-major: column mu is a contiguous vector
     }
@@ -2277,6 +2311,7 @@ struct aegpu_engine {
         int *pptr = nullptr, *ppos = nullptr;
         double *pscale = nullptr;
         double *flip = nullptr;  // invariance-test partials of the V columns
+        int *vmap = nullptr, *mpos = nullptr;  // half tangents: carried positions, mirror reads
         std::vector<std::pair<void *, size_t>> allocs;
     } hess;
 
@@ -2379,6 +2414,7 @@ struct aegpu_engine {
         a.obits_h = b.bits_h;
         a.tasks_h = b.wtasks_h;
         a.ntasks_h = b.nwtasks_h;
+        a.vmap = nullptr;
         return a;
     }
     // Device gate of the half passes: the tables are built, the start state is
@@ -4289,7 +4325,7 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
                   get(hs.MET, (size_t)V * V) && get(hs.gram, (size_t)ngram) &&
                   get(hs.Hops, (size_t)nops * nops) && get(hs.hpart, maxpart) && get(hs.pptr, (size_t)nparams + 1) &&
                   get(hs.ppos, (size_t)nops) && get(hs.pscale, (size_t)nops) &&
-                  get(hs.flip, (size_t)V * 2 * e->sm_count);
+                  get(hs.flip, (size_t)V * 2 * e->sm_count) && get(hs.vmap, (size_t)nops) && get(hs.mpos, (size_t)nops);
         if (!ok) {
             for (auto &pa : hs.allocs) e->release(pa.first, pa.second);
             hs = aegpu_engine::HessScratch{};
@@ -4306,6 +4342,45 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     cudaMemcpyAsync(d_pscale, pscale.data(), pscale.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     int rc = upload_angles(e, angles, true, 1, false);
     if (rc) return rc;
+    // Half tangents: where the angles pass the half passes' test (the circuit commutes
+    // with the exchange of the alpha and beta strings), the tangent of an operator's
+    // mirror is the mirror image of its own, so only one of each pair (the earlier by
+    // position) is carried through the passes and swept; the compressed tangents read
+    // the other as a mirror image, and every second-derivative pair also stands for its
+    // mirror pair.  Not for the projected Hessian (its bra has no such symmetry) nor for
+    // circuits with diagonal passes.
+    bool hm = false;
+    bool all_paired = true;
+    for (auto &b : e->dblocks) all_paired = all_paired && !b.diagonal;
+    if (e->half_static && !proj && all_paired) {
+        int h = 0;
+        cudaMemcpyAsync(&h, e->d_half, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if ((rc = stream_sync(e, "hessian"))) return rc;
+        hm = h != 0;
+    }
+    const int nbl = (int)e->dblocks.size();
+    std::vector<int> nrep_before(nbl, 0), nrep_upto(nbl, 0);
+    if (hm) {
+        std::vector<char> rep(nops);
+        std::vector<int> vmap, mpos(nops, -1);
+        for (int v = 0; v < nops; ++v) {
+            rep[v] = v <= e->pos_of_op[e->mirror[e->perm[v]]];
+            if (rep[v]) vmap.push_back(v);
+        }
+        for (int bi = 0; bi < nbl; ++bi) {
+            const int p0 = e->block_pos0[bi], p1 = p0 + e->dblocks[bi].nslots;
+            for (int v = 0; v < p1; ++v)
+                if (rep[v]) {
+                    nrep_upto[bi]++;
+                    if (v < p0) nrep_before[bi]++;
+                }
+        }
+        for (int k = 0; k < nops; ++k)
+            if (!rep[ppos[k]]) mpos[k] = e->pos_of_op[e->mirror[e->perm[ppos[k]]]];
+        cudaMemcpyAsync(hs.vmap, vmap.data(), vmap.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(hs.mpos, mpos.data(), mpos.size() * sizeof(int), cudaMemcpyHostToDevice, s);
+        if ((rc = stream_sync(e, "hessian"))) return rc;  // the host vectors go out of scope
+    }
     cudaMemsetAsync(T, 0, n * nops * sizeof(double), s);
     cudaMemsetAsync(Hops, 0, (size_t)nops * nops * sizeof(double), s);
     cudaMemcpyAsync(e->d_psi, e->d_start, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
@@ -4324,12 +4399,14 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             BlockArgs av = a;
             av.pc_stride = av.sig_stride = 0;
             av.active = nullptr;
-            const dim3 gv(b.wgrid, std::min(p0, 65535));
+            if (hm) av.vmap = hs.vmap;
+            const int ncarry = hm ? nrep_before[bi] : p0;
+            const dim3 gv(b.wgrid, std::min(ncarry, 65535));
             if (W == 1) {
-                if (p0 > 0 && b.nwtasks) k_warp_rot<1><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
+                if (ncarry > 0 && b.nwtasks) k_warp_rot<1><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
                 k_block_tangent<1><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             } else {
-                if (p0 > 0 && b.nwtasks) k_warp_rot<2><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
+                if (ncarry > 0 && b.nwtasks) k_warp_rot<2><<<gv, kWarpThreads, 0, s>>>(av, b.wtasks, b.nwtasks, T, n, nullptr, 0);
                 k_block_tangent<2><<<b.ntiles, kRotThreads, e->rot_smem(1), s>>>(a, e->d_psi, T, n, e->d_tpos);
             }
             e->launches += 2;
@@ -4337,7 +4414,8 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     }
     // 2. compressed tangents (column-major: column v is T_C v, column P is psi), H on all
     //    of them as one batched product, Gram matrix 2 T_C^T H T_C
-    k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC);
+    k_tc_build<<<e->sm_count * 8, 256, 0, s>>>(T, n, e->d_psi, d_pptr, d_ppos, d_pscale, nparams, W, D, TC,
+                                               hm ? hs.mpos : nullptr, e->db);
     e->launches += 1;
     // With re / im interleaved, the real dot product over the D*W doubles of two columns
     // is Re(a^dagger b), so every contraction below runs on real columns of n doubles.
@@ -4369,12 +4447,13 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
     for (int bi = (int)e->dblocks.size() - 1; bi >= 0; --bi) {
         auto &b = e->dblocks[bi];
         const int p0 = e->block_pos0[bi];
-        const int nvec = p0 + b.nslots;
+        const int nvec = hm ? nrep_upto[bi] : p0 + b.nslots;
         if (b.diagonal) {
             dim3 g(kDiagGrid, nvec);
             k_diag_hess<<<g, 256, 0, s>>>(e->diag_args(b, -1.0, false), e->d_h, T, n, nvec, p0, hpart);
             k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, kDiagGrid, nvec, b.nslots, e->d_pos_op,
-                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
+                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0,
+                                                                            nullptr, nullptr, nullptr);
             k_diag_rot<<<kDiagGrid, 256, 0, s>>>(e->diag_args(b, -1.0, false), e->d_h, 0, 1, nullptr, 0, 0);
             e->launches += 3;
         } else if (b.nwtasks) {
@@ -4382,13 +4461,18 @@ static int hessian_impl(aegpu_engine *e, const double *angles, const int *param,
             BlockArgs a = e->block_args(bi, -1.0);
             a.pc_stride = a.sig_stride = 0;
             a.active = nullptr;
+            BlockArgs at = a;  // the tangents: the carried ones only with the half tangents
+            if (hm) at.vmap = hs.vmap;
             const dim3 g(b.wgrid, std::min(nvec, 65535));
-            if (W == 1)
-                k_warp_hess<1><<<g, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
-            else
-                k_warp_hess<2><<<g, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
-            k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(hpart, b.wgrid, nvec, b.nslots, e->d_pos_op,
-                                                                            b.ops, p0, Hops, nops, proj ? 1.0 : 2.0);
+            if (nvec > 0) {
+                if (W == 1)
+                    k_warp_hess<1><<<g, kWarpThreads, 0, s>>>(at, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
+                else
+                    k_warp_hess<2><<<g, kWarpThreads, 0, s>>>(at, b.wtasks, b.nwtasks, e->d_h, T, n, nvec, p0, hpart);
+                k_hess_reduce<<<(nvec * b.nslots * 32 + 255) / 256, 256, 0, s>>>(
+                    hpart, b.wgrid, nvec, b.nslots, e->d_pos_op, b.ops, p0, Hops, nops, proj ? 1.0 : 2.0,
+                    hm ? hs.vmap : nullptr, hm ? e->d_mirror : nullptr, hm ? e->d_tpos : nullptr);
+            }
             // the bra back through the pass
             if (W == 1)
                 k_warp_rot<1><<<b.wgrid, kWarpThreads, 0, s>>>(a, b.wtasks, b.nwtasks, e->d_h, 0, nullptr, 0);

@@ -203,3 +203,30 @@ def test_half_passes_complex_lucj(mode):
     assert abs(E1 - Eo) < 1e-10
     np.testing.assert_allclose(g1, go, atol=1e-9, rtol=0)
     e.close()
+
+
+@pytest.mark.parametrize("N,L,mode", [(8, 2, ae.HAM_STORED), (10, 2, ae.HAM_ON_THE_FLY)])
+def test_hessian_half_tangents_match_full(N, L, mode):
+    """With the half passes' symmetry the Hessian carries one tangent of every mirror
+    pair and counts each second-derivative pair for its mirror pair too; it matches the
+    full computation (knob off) and the oracle."""
+    na = N // 2
+    pb = synthetic_problem(N, na, na, L, 13)
+    P = int(np.max(pb["order_1b"]))
+    rng = np.random.default_rng(N + 7)
+    x = rng.uniform(-0.5, 0.5, P)
+    ang = compressed_angles(pb, x)
+    p0, sc = np.asarray(pb["order_1b"]) - 1, pb["scale"]
+    e = make_engine(pb)
+    e.set_ham_integrals(pb["h1"], pb["g2"], mode)
+    E1, g1, H1 = e.hessian(ang, p0, sc)
+    e.gradient(ang)
+    assert e.half_status()[0]
+    e.set_tuning(ae.TUNE_HALF, 0)
+    E0, g0, H0 = e.hessian(ang, p0, sc)
+    assert abs(E1 - E0) < 1e-12 * max(1.0, abs(E0))
+    np.testing.assert_allclose(g1, g0, atol=1e-11, rtol=0)
+    np.testing.assert_allclose(H1, H0, atol=1e-10, rtol=0)
+    o = oracle_synthetic(pb, csr=False)
+    np.testing.assert_allclose(H1, o.hessian_comp(x), atol=1e-9, rtol=0)
+    e.close()
