@@ -132,6 +132,10 @@ def lib(build_if_missing=True):
         "aegpu_energy_dev": (ctypes.c_int, [_P, _P, _P, _P]),
         "aegpu_state_dev": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
         "aegpu_host_block_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, _IP, _IP, _IP]),
+        "aegpu_host_half_orbits": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP,
+                                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                                  ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_uint32),
+                                                  ctypes.POINTER(i64)]),
         "aegpu_host_orbits": (ctypes.c_int, [ctypes.c_int] * 6 + [_IP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64)]),
@@ -692,6 +696,27 @@ def host_orbits(nq, kind, ne, na, nb, ops0):
     if rc:
         raise AegpuError("aegpu_host_orbits returned %d" % rc)
     return idx, g, t
+
+
+def host_half_orbits(nq, n_alpha, ops0):
+    """Spin-flip half tables of one pass (host setup, no GPU): (ranks, bitstrings,
+    tasks[:, group elem_off n mask]); AegpuError where the pass has no mirror symmetry."""
+    L = lib()
+    ops = _i32(ops0).reshape(-1, 4)
+    u32 = ctypes.POINTER(ctypes.c_uint32)
+    ni, nt = ctypes.c_int64(0), ctypes.c_int64(0)
+    args = [nq, n_alpha, len(ops), iptr(ops.reshape(-1))]
+    rc = L.aegpu_host_half_orbits(*args, None, None, ctypes.byref(ni), None, ctypes.byref(nt))
+    if rc:
+        raise AegpuError("aegpu_host_half_orbits returned %d" % rc)
+    idx = np.zeros(ni.value, dtype=np.uint32)
+    bits = np.zeros(ni.value, dtype=np.uint32)
+    t = np.zeros((nt.value, 4), dtype=np.uint32)
+    rc = L.aegpu_host_half_orbits(*args, idx.ctypes.data_as(u32), bits.ctypes.data_as(u32), ctypes.byref(ni),
+                                  t.ctypes.data_as(u32), ctypes.byref(nt))
+    if rc:
+        raise AegpuError("aegpu_host_half_orbits returned %d" % rc)
+    return idx, bits, t
 
 
 class stateAnsatzManager:

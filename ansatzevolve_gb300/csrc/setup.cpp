@@ -519,3 +519,42 @@ extern "C" int aegpu_host_orbits(int nq, int kind, int ne, int na, int nb, int n
         }
     return AEGPU_OK;
 }
+
+extern "C" int aegpu_host_half_orbits(int nq, int nA_elec, int nops, const int *ops, uint32_t *idx, uint32_t *bits,
+                                      int64_t *n_idx, uint32_t *tasks, int64_t *n_tasks)
+{
+    if (nops < 1 || nops > 12 || !ops || !n_idx || !n_tasks || nq % 2) return AEGPU_ERR_ARG;
+    ae::Basis B;
+    std::string err;
+    if (!B.init(nq, ae::BASIS_SZ, 2 * nA_elec, nA_elec, nA_elec, err)) return AEGPU_ERR_ARG;
+    std::vector<ae::ExcCode> codes;
+    ae::Block blk;
+    for (int i = 0; i < nops; ++i) {
+        for (int j = 0; j < 4; ++j)
+            if (ops[4 * i + j] < -1 || ops[4 * i + j] >= nq) return AEGPU_ERR_ARG;
+        codes.push_back(ae::make_exc_code(ops[4 * i], ops[4 * i + 1], ops[4 * i + 2], ops[4 * i + 3]));
+        blk.ops.push_back(i);
+    }
+    const std::vector<int> mir = ae::mirror_ops(codes, {blk}, B.N);
+    for (int m : mir)
+        if (m < 0) return AEGPU_ERR_UNSUPPORTED;
+    ae::OrbitTables T = ae::build_orbits(B, codes, 2);
+    if (!T.ok) return AEGPU_ERR_UNSUPPORTED;
+    ae::HalfTables H = ae::build_half_orbits(B, T, codes, mir, 2);
+    if (!H.ok) return AEGPU_ERR_UNSUPPORTED;
+    const int64_t ci = *n_idx, ct = *n_tasks;
+    *n_idx = (int64_t)H.idx.size();
+    *n_tasks = (int64_t)H.wtasks.size();
+    if (idx && bits && ci >= *n_idx) {
+        std::copy(H.idx.begin(), H.idx.end(), idx);
+        std::copy(H.bits.begin(), H.bits.end(), bits);
+    }
+    if (tasks && ct >= *n_tasks)
+        for (size_t t = 0; t < H.wtasks.size(); ++t) {
+            tasks[4 * t] = H.wtasks[t].group;
+            tasks[4 * t + 1] = H.wtasks[t].elem_off;
+            tasks[4 * t + 2] = H.wtasks[t].n;
+            tasks[4 * t + 3] = H.wtasks[t].mask;
+        }
+    return AEGPU_OK;
+}

@@ -358,6 +358,15 @@ int aegpu_host_subspace_eigenvalues(int nsets, const double *h_re, const double 
  * aegpu_host_orbits: n_idx / n_groups / n_tiles are in/out capacities -> sizes;
  * groups are 4 uint32 (idx_off, n_orbits, k, mask) each, tiles 4 uint32 each. */
 int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *block_sizes, int *n_blocks);
+/* Spin-flip half tables of one pass of commuting excitations (Sz basis, nA_elec alpha
+ * and as many beta electrons; host setup, no GPU; no counterpart in the reference):
+ * idx / bits are the entries (canonical ranks; bit 31 of a bitstring marks a member of a
+ * self-mirror orbit that does not write), tasks 4 uint32 each (group with bit 31 for a
+ * self-mirror task, elem_off, n, mask); n_idx / n_tasks are capacities -> sizes.
+ * AEGPU_ERR_UNSUPPORTED where an excitation has no mirror in the pass or a sign differs
+ * from its mirror's. */
+int aegpu_host_half_orbits(int nq, int nA_elec, int nops, const int *ops, uint32_t *idx, uint32_t *bits,
+                           int64_t *n_idx, uint32_t *tasks, int64_t *n_tasks);
 int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int nops, const int *ops,
                       uint32_t *idx, int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles);
 

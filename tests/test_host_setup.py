@@ -4,6 +4,8 @@
   (fusedevolve.cpp:1797-1967) for the TUPS circuits of the benchmark configurations;
 * orbit tables, interpreted step by step in numpy, evolve a vector exactly like the
   oracle applying the same excitations one at a time;
+* the spin-flip half tables of a pass cover the canonical amplitudes (alpha string <=
+  beta string) of the full pass once each, and a pass without mirrors is refused;
 * the shared library exports every symbol declared in include/*.h.
 """
 import os
@@ -100,3 +102,50 @@ def test_library_exports_every_declared_symbol():
     assert len(declared) >= 40
     missing = sorted(declared - exported)
     assert not missing, missing
+
+
+@pytest.mark.parametrize("block", [0, 1])
+def test_half_tables_cover_the_canonical_amplitudes_once(block):
+    """Spin-flip half tables of a tUPS pass (8 orbitals: three alpha/beta single pairs,
+    then the paired doubles): the amplitudes that write are the canonical (a <= b)
+    images of every amplitude the full pass touches, each exactly once; an entry's rank
+    is the canonical rank of its bitstring; members that do not write sit only in
+    self-mirror tasks; the tables hold about half the full pass."""
+    from ansatzevolve_gb300 import host_half_orbits
+    N, na = 8, 4
+    ops, _, _ = tups_operators(N, 2)
+    ops0 = np.asarray(ops) - 1
+    perm, sizes = host_block_layout(2 * N, ops0)
+    first = int(np.sum(np.abs(sizes[:block])))
+    sel = ops0[perm[first:first + min(6, abs(int(sizes[block])))]]
+    full, _, _ = host_orbits(2 * N, 2, 2 * na, na, na, sel)
+    idx, bits, tasks = host_half_orbits(2 * N, na, sel)
+    strs = np.array([s for s in range(1 << N) if bin(s).count("1") == na])
+    nB = len(strs)
+    rank = {int(s): i for i, s in enumerate(strs)}
+
+    def canon(r):
+        a, b = divmod(int(r), nB)
+        return min(a, b) * nB + max(a, b)
+
+    write = (bits & (1 << 31)) == 0
+    got = [int(r) for r in idx[write]]
+    want = sorted({canon(r) for r in full})
+    assert sorted(got) == want  # every canonical amplitude once
+    lo = (1 << N) - 1
+    for r, s in zip(idx, bits & 0x7FFFFFFF):
+        a, b = rank[int(s) >> N], rank[int(s) & lo]
+        assert int(r) == min(a, b) * nB + max(a, b)
+    for g, off, n, m in tasks:
+        if not (g >> 31):
+            assert np.all(write[off:off + n])
+    assert len(idx) < 0.6 * len(full)
+
+
+def test_half_tables_refuse_a_pass_without_mirrors():
+    """Alpha singles alone have no beta mirrors: no half tables."""
+    from ansatzevolve_gb300 import AegpuError, host_half_orbits
+    N = 8
+    sel = np.array([[N + 1, N + 0, -1, -1], [N + 3, N + 2, -1, -1]])
+    with pytest.raises(AegpuError):
+        host_half_orbits(2 * N, 4, sel)
