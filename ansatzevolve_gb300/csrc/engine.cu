@@ -1017,8 +1017,9 @@ struct DiagSplit {
     uint32_t mixed;   // slots with both alpha and beta bits
     // half passes: the same col_blocks * row_chunks CTAs over the triangle a <= b, so
     // that every CTA has a near-equal share: column block c gets the CTAs
-    // [half_first[c], half_first[c + 1]) for its rows 0 .. min(nA, (c + 1) * cols)
-    // (half_first[0] = -1: more column blocks than kDiagMaxColBlocks, no such split)
+    // [half_first[c], half_first[c + 1]) for its rows 0 .. (c + 1) * cols - 1, cut at
+    // equal work (tri_row) (half_first[0] = -1: more column blocks than
+    // kDiagMaxColBlocks, no such split)
     int half_first[kDiagMaxColBlocks + 1];
 };
 
