@@ -397,9 +397,10 @@ HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::ve
         // per orbit: 0 its mirror is kept, 1 kept (one of a mirror pair), 2 kept (its own
         // mirror), 3 a rank or sign check failed; classified in parallel over orbit ranges
         std::vector<uint8_t> cls(g.n_orbits, 0);
+        int nt = 1;
         auto work = [&](int t) {
-            const uint32_t o0 = (uint32_t)((uint64_t)g.n_orbits * t / nthreads);
-            const uint32_t o1 = (uint32_t)((uint64_t)g.n_orbits * (t + 1) / nthreads);
+            const uint32_t o0 = (uint32_t)((uint64_t)g.n_orbits * t / nt);
+            const uint32_t o1 = (uint32_t)((uint64_t)g.n_orbits * (t + 1) / nt);
             for (uint32_t o = o0; o < o1; ++o) {
                 const size_t off = g.idx_off + (size_t)o * osz;
                 uint32_t key = UINT32_MAX, mkey = UINT32_MAX;
@@ -424,8 +425,10 @@ HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::ve
                 cls[o] = bad ? 3 : key < mkey ? 1 : key == mkey ? 2 : 0;
             }
         };
+        // threads only for large groups (spawning them costs more than small groups' work)
+        nt = (int)std::min<uint64_t>((uint64_t)nthreads, std::max<uint64_t>(1, (uint64_t)g.n_orbits * osz >> 16));
         std::vector<std::thread> th;
-        for (int t = 1; t < nthreads; ++t) th.emplace_back(work, t);
+        for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
         work(0);
         for (auto &x : th) x.join();
         std::vector<uint32_t> keep[2];  // [0] one of a mirror pair, [1] self-mirror
