@@ -136,6 +136,8 @@ def lib(build_if_missing=True):
                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                                   ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_uint32),
                                                   ctypes.POINTER(i64)]),
+        "aegpu_host_pass_layout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _IP, ctypes.c_int, ctypes.c_int, _IP, _IP,
+                                                  _IP]),
         "aegpu_host_orbits": (ctypes.c_int, [ctypes.c_int] * 6 + [_IP, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64),
                                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(i64)]),
@@ -696,6 +698,26 @@ def host_orbits(nq, kind, ne, na, nb, ops0):
     if rc:
         raise AegpuError("aegpu_host_orbits returned %d" % rc)
     return idx, g, t
+
+
+def host_pass_layout(nq, ops0, max_pass=6, mirror_split=False):
+    """The engine's passes (host setup, no GPU): (list of operator arrays, diagonal flags,
+    mirror cut applied)."""
+    L = lib()
+    ops = _i32(ops0).reshape(-1, 4)
+    n = ctypes.c_int(len(ops) + 1)
+    po = np.zeros(len(ops), dtype=np.int32)
+    ps = np.zeros(len(ops) + 1, dtype=np.int32)
+    rc = L.aegpu_host_pass_layout(nq, len(ops), iptr(ops.reshape(-1)), max_pass, int(mirror_split), iptr(po), iptr(ps),
+                                  ctypes.byref(n))
+    if rc not in (0, 5):  # 5: AEGPU_ERR_UNSUPPORTED (no mirror cut)
+        raise AegpuError("aegpu_host_pass_layout returned %d" % rc)
+    passes, diag, k = [], [], 0
+    for sz in ps[:n.value]:
+        passes.append(po[k:k + abs(int(sz))].copy())
+        diag.append(sz < 0)
+        k += abs(int(sz))
+    return passes, diag, rc == 0 and bool(mirror_split)
 
 
 def host_half_orbits(nq, n_alpha, ops0):

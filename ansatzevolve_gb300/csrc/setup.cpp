@@ -561,3 +561,38 @@ extern "C" int aegpu_host_half_orbits(int nq, int nA_elec, int nops, const int *
         }
     return AEGPU_OK;
 }
+
+extern "C" int aegpu_host_pass_layout(int nq, int nops, const int *ops, int max_pass, int mirror_split, int *pass_ops,
+                                      int *pass_sizes, int *n_passes)
+{
+    if (nops < 1 || !ops || !n_passes || max_pass < 1 || max_pass > ae::kMaxWarpLayers || nq % 2) return AEGPU_ERR_ARG;
+    std::vector<ae::Exc> excs(nops);
+    std::vector<ae::ExcCode> codes(nops);
+    for (int i = 0; i < nops; ++i) {
+        for (int j = 0; j < 4; ++j) {
+            if (ops[4 * i + j] < -1 || ops[4 * i + j] >= nq) return AEGPU_ERR_ARG;
+            excs[i].v[j] = (int8_t)ops[4 * i + j];
+        }
+        codes[i] = ae::make_exc_code(ops[4 * i], ops[4 * i + 1], ops[4 * i + 2], ops[4 * i + 3]);
+    }
+    std::vector<int> perm;
+    std::vector<ae::Block> grouped = ae::group_blocks(excs, 12, perm);
+    std::vector<int> mir;
+    bool half = mirror_split != 0;
+    if (half) {
+        grouped = ae::merge_commuting(grouped, excs);
+        mir = ae::mirror_ops(codes, grouped, nq / 2);
+        for (int m : mir) half = half && m >= 0;
+    }
+    const std::vector<ae::Block> passes = ae::split_passes(grouped, max_pass, half ? &mir : nullptr);
+    const int cap = *n_passes;
+    *n_passes = (int)passes.size();
+    if (pass_sizes && pass_ops && cap >= *n_passes) {
+        int k = 0;
+        for (size_t p = 0; p < passes.size(); ++p) {
+            pass_sizes[p] = (int)passes[p].ops.size() * (passes[p].diagonal ? -1 : 1);
+            for (int o : passes[p].ops) pass_ops[k++] = o;
+        }
+    }
+    return half || !mirror_split ? AEGPU_OK : AEGPU_ERR_UNSUPPORTED;
+}

@@ -367,6 +367,15 @@ int aegpu_host_block_layout(int nq, int nops, const int *ops, int *perm, int *bl
  * from its mirror's. */
 int aegpu_host_half_orbits(int nq, int nA_elec, int nops, const int *ops, uint32_t *idx, uint32_t *bits,
                            int64_t *n_idx, uint32_t *tasks, int64_t *n_tasks);
+/* The engine's passes for an operator list (host setup, no GPU; no counterpart in the
+ * reference): the grouping of aegpu_host_block_layout cut into passes of <= max_pass
+ * paired operators (1..6), runs of diagonal blocks merged into passes of <= 12; with
+ * mirror_split, commuting blocks merged and cut between spin-flip mirror pairs, as for
+ * the half passes (AEGPU_ERR_UNSUPPORTED, with the plain cut, where an operator has no
+ * mirror).  pass_sizes[p] = operators of pass p (negative for a diagonal pass),
+ * pass_ops the operators pass by pass; n_passes is the capacity in, the count out. */
+int aegpu_host_pass_layout(int nq, int nops, const int *ops, int max_pass, int mirror_split, int *pass_ops,
+                           int *pass_sizes, int *n_passes);
 int aegpu_host_orbits(int nq, int basis_kind, int n_elec, int n_alpha, int n_beta, int nops, const int *ops,
                       uint32_t *idx, int64_t *n_idx, uint32_t *groups, int64_t *n_groups, uint32_t *tiles, int64_t *n_tiles);
 

@@ -6,6 +6,8 @@
   oracle applying the same excitations one at a time;
 * the spin-flip half tables of a pass cover the canonical amplitudes (alpha string <=
   beta string) of the full pass once each, and a pass without mirrors is refused;
+* the engine's passes merge runs of diagonal blocks and, for the half passes, keep
+  every operator's mirror in its pass;
 * the shared library exports every symbol declared in include/*.h.
 """
 import os
@@ -149,3 +151,40 @@ def test_half_tables_refuse_a_pass_without_mirrors():
     sel = np.array([[N + 1, N + 0, -1, -1], [N + 3, N + 2, -1, -1]])
     with pytest.raises(AegpuError):
         host_half_orbits(2 * N, 4, sel)
+
+
+def test_pass_layout_merges_diagonal_runs_and_cuts_between_mirrors():
+    """The engine's passes: the 14-orbital LUCJ circuit's runs of diagonal blocks merged
+    into passes of at most 12 operators (the grouping alone leaves 254 diagonal blocks,
+    177 of them single); with the mirror cut every pass holds the mirror of each of its
+    operators, and the 14-orbital tUPS blocks that the divisor rule cut in two (14 -> 7
+    + 7) are whole again; every operator appears once in grouping order within a run."""
+    from ansatzevolve_gb300 import host_pass_layout
+    from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+    N = 14
+    K, J = random_lucj(N, 3)
+    ops, _ = lucj_operators(K, J)
+    passes, diag, mirrored = host_pass_layout(2 * N, ops, 6, False)
+    assert not mirrored
+    assert sum(diag) == 90 and len(passes) == 170
+    assert all(len(p) <= (12 if d else 6) for p, d in zip(passes, diag))
+    assert sorted(np.concatenate(passes)) == list(range(len(ops)))
+    passes, diag, mirrored = host_pass_layout(2 * N, ops, 6, True)
+    assert mirrored
+
+    def mirror(o):
+        f = lambda i: -1 if i < 0 else (i + N if i < N else i - N)
+        return tuple(f(int(i)) for i in o)
+
+    def masks(o):
+        a, b, c, d = (int(i) for i in o)
+        return (frozenset([a]), frozenset([b])) if c < 0 else (frozenset([a, b]), frozenset([c, d]))
+
+    for p in passes:
+        ms = [masks(ops[o]) for o in p]
+        for o in p:
+            assert masks(mirror(ops[o])) in ms
+    tops, _, _ = tups_operators(N, 4)
+    tp, td, tm = host_pass_layout(2 * N, tops - 1, 6, True)
+    assert tm and not any(td)
+    assert len(tp) == 52  # 13 passes per layer: 14 -> 4+4+6, 7 -> 3+4, 14 -> 4+4+6, 12 -> 6+6, 6, 12 -> 6+6
