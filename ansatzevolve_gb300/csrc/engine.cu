@@ -3187,25 +3187,11 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     }
     // the reference's commuting blocks, cut into passes of <= 6 excitations so that
     // every orbit fits one warp's registers
-    {
-        // spin-flip half passes need the Sz basis with as many alpha as beta strings and
-        // every operator's mirror in its block or diagonal run (then in its pass)
-        std::vector<Block> grouped = group_blocks(e->excs, kMaxSlots, e->perm);
-        std::vector<int> mir;
-        bool half = e->B.kind == BASIS_SZ && e->B.nA == e->B.nB;
-        if (half) {
-            grouped = merge_commuting(grouped, e->excs);
-            mir = mirror_ops(e->codes, grouped, e->B.N);
-            for (int m : mir) half = half && m >= 0;
-        }
-        e->blocks = split_passes(grouped, e->tune_pass_ops, half ? &mir : nullptr);
-        e->half_static = half;
-        e->mirror = half ? mir : std::vector<int>();
-        // the application order is the passes' order (a cut between mirror units may
-        // reorder operators inside a commuting run): the Hessian's positions follow it
-        e->perm.clear();
-        for (const Block &b : e->blocks) e->perm.insert(e->perm.end(), b.ops.begin(), b.ops.end());
-    }
+    // spin-flip half passes need the Sz basis with as many alpha as beta strings and every
+    // operator's mirror in its block or diagonal run (then in its pass); the application
+    // order (the Hessian's positions) is the passes' order
+    e->half_static = make_passes(e->excs, e->codes, e->B.N, e->tune_pass_ops,
+                                 e->B.kind == BASIS_SZ && e->B.nA == e->B.nB, e->blocks, e->perm, e->mirror);
     e->pos_of_op.assign(nops, 0);
     for (int p = 0; p < nops; ++p) e->pos_of_op[e->perm[p]] = p;
 

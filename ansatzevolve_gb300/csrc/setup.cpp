@@ -376,6 +376,26 @@ OrbitTables build_orbits(const Basis &B, const std::vector<ExcCode> &codes, int 
     return T;
 }
 
+bool make_passes(const std::vector<Exc> &excs, const std::vector<ExcCode> &codes, int N, int max_pass,
+                 bool mirror_split, std::vector<Block> &passes, std::vector<int> &perm, std::vector<int> &mirror)
+{
+    std::vector<Block> grouped = group_blocks(excs, kMaxDiagSlots, perm);
+    mirror.clear();
+    bool half = mirror_split;
+    if (half) {
+        grouped = merge_commuting(grouped, excs);
+        mirror = mirror_ops(codes, grouped, N);
+        for (int m : mirror) half = half && m >= 0;
+        if (!half) mirror.clear();
+    }
+    passes = split_passes(grouped, max_pass, half ? &mirror : nullptr);
+    // the application order is the passes' order (a cut between mirror units may
+    // reorder operators inside a commuting run)
+    perm.clear();
+    for (const Block &b : passes) perm.insert(perm.end(), b.ops.begin(), b.ops.end());
+    return half;
+}
+
 HalfTables build_half_orbits(const Basis &B, const OrbitTables &T, const std::vector<ExcCode> &codes,
                              const std::vector<int> &mslot, int nthreads)
 {
@@ -575,16 +595,9 @@ extern "C" int aegpu_host_pass_layout(int nq, int nops, const int *ops, int max_
         }
         codes[i] = ae::make_exc_code(ops[4 * i], ops[4 * i + 1], ops[4 * i + 2], ops[4 * i + 3]);
     }
-    std::vector<int> perm;
-    std::vector<ae::Block> grouped = ae::group_blocks(excs, 12, perm);
-    std::vector<int> mir;
-    bool half = mirror_split != 0;
-    if (half) {
-        grouped = ae::merge_commuting(grouped, excs);
-        mir = ae::mirror_ops(codes, grouped, nq / 2);
-        for (int m : mir) half = half && m >= 0;
-    }
-    const std::vector<ae::Block> passes = ae::split_passes(grouped, max_pass, half ? &mir : nullptr);
+    std::vector<int> perm, mir;
+    std::vector<ae::Block> passes;
+    const bool half = ae::make_passes(excs, codes, nq / 2, max_pass, mirror_split != 0, passes, perm, mir);
     const int cap = *n_passes;
     *n_passes = (int)passes.size();
     if (pass_sizes && pass_ops && cap >= *n_passes) {

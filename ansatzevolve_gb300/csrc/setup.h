@@ -82,6 +82,15 @@ std::vector<Block> merge_commuting(const std::vector<Block> &blocks, const std::
 // order.
 std::vector<int> mirror_ops(const std::vector<ExcCode> &codes, const std::vector<Block> &blocks, int N);
 
+// The engine's passes for an operator list: the grouping (group_blocks), then with
+// mirror_split (Sz basis, as many alpha as beta strings) commuting blocks merged
+// (merge_commuting), mirrors found (mirror_ops) and the blocks cut between mirror units;
+// split_passes in either case.  perm receives the application order (the passes'
+// operators in order), mirror the operator -> mirror map where every operator has one
+// (empty otherwise), and the result tells whether the mirror cut was applied.
+bool make_passes(const std::vector<Exc> &excs, const std::vector<ExcCode> &codes, int N, int max_pass,
+                 bool mirror_split, std::vector<Block> &passes, std::vector<int> &perm, std::vector<int> &mirror);
+
 // Bitstring with the alpha (high N bits) and beta (low N bits) strings exchanged.
 inline uint32_t flip_bits(uint32_t s, int N)
 {
