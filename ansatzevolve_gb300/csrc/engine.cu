@@ -2177,6 +2177,9 @@ struct aegpu_engine {
         WarpTask *wtasks_h = nullptr;
         int nwtasks_h = 0;
         uint64_t active_h = 0, amp_layers_h = 0;
+        // diagonal passes as half passes: the amplitudes (a, b) with a <= b that hold an
+        // active slot, and their slot activations (FP64 work accounting)
+        uint64_t slot_acts_h = 0;
     };
     std::vector<DevBlock> dblocks;
     std::vector<void *> allocs;
@@ -3151,6 +3154,19 @@ static void diag_string_masks(aegpu_engine *e, const Block &b, aegpu_engine::Dev
     for (uint32_t u : uA)
         for (uint32_t v : uB)
             if (u & v) d.active += hA[u] * hB[v];
+    // the same counts over a <= b: a pass that holds the mirror of every slot is active on
+    // (a, b) exactly where it is active on (b, a), slot for mirror slot, so each count over
+    // a <= b is half of the full count plus half of its count on the diagonal a = b
+    if (B.nA == B.nB) {
+        uint64_t same_act = 0, same_slots = 0;
+        for (uint32_t r = 0; r < B.nA; ++r) {
+            const uint32_t m = (uint32_t)mA[r] & (uint32_t)mB[r];
+            same_act += m != 0;
+            same_slots += (uint64_t)__builtin_popcount(m);
+        }
+        d.active_h = (d.active + same_act) / 2;
+        d.slot_acts_h = (d.slot_acts + same_slots) / 2;
+    }
     d.smA = e->upload(mA);
     d.smB = e->upload(mB);
 }
@@ -3880,16 +3896,25 @@ int aegpu_half_status(aegpu_engine *e, int *used)
 int aegpu_half_info(const aegpu_engine *e, int64_t *info)
 {
     if (!e || !info) return AEGPU_ERR_ARG;
-    int64_t act = 0, al = 0;
+    // paired passes: their orbits' amplitudes and amplitude-layers; diagonal passes (as in
+    // aegpu_fp64_work, over a <= b): the amplitudes with an active slot and the slot
+    // activations, and as touched amplitudes every (a, b) with a <= b
+    int64_t act = 0, al = 0, dact = 0, dslots = 0, ndiag = 0;
     for (auto &b : e->dblocks) {
+        if (b.diagonal) {
+            dact += (int64_t)b.active_h;
+            dslots += (int64_t)b.slot_acts_h;
+            ndiag++;
+            continue;
+        }
         act += (int64_t)b.active_h;
         al += (int64_t)b.amp_layers_h;
     }
-    const int64_t W = e->W;
+    const int64_t W = e->W, nA = e->B.nA, Dh = nA * (nA + 1) / 2;
     info[0] = e->half_static ? 1 : 0;
-    info[1] = e->half_static ? act : 0;
-    info[2] = e->half_static ? (al + act) * W : 0;
-    info[3] = e->half_static ? (2 * al + act) * W + al / 2 : 0;
+    info[1] = e->half_static ? act + ndiag * Dh : 0;
+    info[2] = e->half_static ? (al + act) * W + 4 * dact : 0;
+    info[3] = e->half_static ? (2 * al + act) * W + al / 2 + 6 * dact + dslots : 0;
     return AEGPU_OK;
 }
 

@@ -536,7 +536,7 @@ def aux_case_bench(n_orb, lucj, stream, steps=5, warmup=2):
         passes = info["blocks"]
         touched = info["active"]  # amplitudes touched per sweep (a diagonal pass touches all D)
         half_passes = bool(eng.half_status()[0])
-        if half_passes:  # the spin-flip half passes touch one orbit of every mirror pair
+        if half_passes:  # one orbit of every mirror pair; a diagonal half pass every a <= b
             touched = eng.half_info()["active"]
         fwd_bytes, adj_bytes = 16 * touched * W, 32 * touched * W
         out = {"value": 1e3 / ms, "unit": "evals/s", "ms_per_step": ms, "steps": steps, "warmup": warmup,
@@ -552,6 +552,12 @@ def aux_case_bench(n_orb, lucj, stream, steps=5, warmup=2):
                               "frac": {"evolve": fwd_bytes / (ph[0] / 1e3) / 1e9 / peak,
                                        "adjoint": adj_bytes / (ph[2] / 1e3) / 1e9 / peak},
                               "peak_gbs": peak, "peak_source": peak_kind},
+               # the sweeps' own bound: their FP64 instructions (complex multiplies of the
+               # phase passes, Givens updates and gradient sums) against the measured rate
+               "sweeps_fp64": {"instructions": {"evolve": int(fw[1]), "adjoint": int(fw[2])},
+                               "frac": {"evolve": fw[1] / (ph[0] / 1e3) / 1e12 / peak_t if ph[0] else None,
+                                        "adjoint": fw[2] / (ph[2] / 1e3) / 1e12 / peak_t if ph[2] else None},
+                               "peak_T_per_s": peak_t, "peak_source": "measured (aegpu_fp64_peak)"},
                "tuning": {"settings": {str(k): v for k, v in eng.tuning().items()}, "tuned": bool(tuning)}}
         ref = os.path.join(ROOT, "tests", "golden", ("lucj%d.npz" if lucj else "ref%d.npz") % N_ORB)
         if os.path.exists(ref):

@@ -230,3 +230,37 @@ def test_hessian_half_tangents_match_full(N, L, mode):
     o = oracle_synthetic(pb, csr=False)
     np.testing.assert_allclose(H1, o.hessian_comp(x), atol=1e-9, rtol=0)
     e.close()
+
+
+def test_diagonal_half_pass_counts():
+    """The work accounting of the diagonal passes (the bench's FP64 and HBM figures of
+    the LUCJ sweeps): the amplitudes with an active slot and the slot activations over
+    every determinant (full passes) and over a <= b (half passes), against a count over
+    the basis with the engine's own pass layout."""
+    from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+    N, na = 8, 4
+    K, J = random_lucj(N, 2)
+    ops, _ = lucj_operators(K, J)
+    dops = np.array([o for o in ops if o[0] == o[1] or o[2] >= 0], dtype=np.int32)
+    e = ae.Engine(2 * N, ae.BASIS_SZ, 2 * na, na, na, dops, complex_mode=True)
+    hi = e.half_info()
+    assert hi["available"]
+    passes, diag, mirrored = ae.host_pass_layout(2 * N, dops, e.get_tuning(ae.TUNE_PASS_OPS), True)
+    assert mirrored and all(diag) and len(passes) == e.info()["blocks"]
+    bits = e.states().astype(np.int64)
+    nA = int(round(len(bits) ** 0.5))
+    a, b = np.divmod(np.arange(len(bits)), nA)
+    tri = a <= b
+    ann = np.array([(1 << int(o[0])) | (1 << int(o[1])) for o in dops], dtype=np.int64)
+    act = act_h = slots = slots_h = 0
+    for p in passes:
+        n = ((bits[:, None] & ann[p][None, :]) == ann[p][None, :]).sum(axis=1)
+        act += int(np.count_nonzero(n))
+        slots += int(n.sum())
+        act_h += int(np.count_nonzero(n[tri]))
+        slots_h += int(n[tri].sum())
+    assert hi["active"] == len(passes) * nA * (nA + 1) // 2
+    assert hi["fwd_fp64"] == 4 * act_h and hi["adj_fp64"] == 6 * act_h + slots_h
+    _, fwd, adj = e.fp64_work(half=False, half_passes=False)
+    assert fwd == 4 * act and adj == 6 * act + slots
+    e.close()
