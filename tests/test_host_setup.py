@@ -171,6 +171,7 @@ def test_pass_layout_merges_diagonal_runs_and_cuts_between_mirrors():
     assert sorted(np.concatenate(passes)) == list(range(len(ops)))
     passes, diag, mirrored = host_pass_layout(2 * N, ops, 6, True)
     assert mirrored
+    assert sum(diag) == 92 and len(passes) == 170  # the engine's layout (78 rotation passes)
 
     def mirror(o):
         f = lambda i: -1 if i < 0 else (i + N if i < N else i - N)
