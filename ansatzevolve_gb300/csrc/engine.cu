@@ -160,7 +160,19 @@ struct BlockArgs {
     int ntasks_h;
     // the Hessian's tangent kernels: grid row v works on vector vmap[v] (nullable: v)
     const int *vmap;
+    int task_order;          // warp kernels' first task: 0 CTA-major, 1 warp-major (task_first)
 };
+
+// First task of this warp in the warp kernels' grid-stride loop (stride: the grid's
+// warps).  CTA-major hands a CTA consecutive tasks; warp-major hands warp w of CTA c
+// task w * gridDim.x + c, so that the tasks left over after whole rounds spread over
+// every CTA (and so every SM) instead of filling the first CTAs.  Both orders visit
+// each task once.
+__device__ __forceinline__ int task_first(const BlockArgs &a)
+{
+    return a.task_order ? (int)((threadIdx.x >> 5) * gridDim.x + blockIdx.x)
+                        : (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+}
 
 // The tables instance b runs: the half tables where its half flag is set.
 struct PassTables {
@@ -519,7 +531,7 @@ __global__ void k_pass_prep(PrepArgs a, const double *__restrict__ ang, double *
 // wait once this grid has completed.  Without the attribute both are no-ops.
 __device__ __forceinline__ void pdl_prologue(const BlockArgs &a, const WarpTask *__restrict__ tasks, int ntasks)
 {
-    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int t = task_first(a), lane = threadIdx.x & 31;
     if (t < ntasks) {
         const WarpTask task = tasks[t];
         if (2 * lane < (int)task.n) {  // inside this task's entries
@@ -545,7 +557,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_rot(BlockArgs a, const Wa
     if (ckpt) ckpt += (size_t)b * ckpt_stride;
     const PassTables pt = pass_tables(a, tasks, ntasks, b);
     const int nw = (gridDim.x * blockDim.x) >> 5;
-    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < pt.ntasks; t += nw) {
+    for (int t = task_first(a); t < pt.ntasks; t += nw) {
         const WarpTask task = pt.tasks[t];
         const uint32_t mask = task.mask;
         const uint32_t *idx = pt.idx + task.elem_off, *obits = pt.obits + task.elem_off;
@@ -619,7 +631,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_adj(BlockArgs a, const Wa
     double accS[kMaxWarpLayers];
 #pragma unroll
     for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
-    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < pt.ntasks; t += nw) {
+    for (int t = task_first(a); t < pt.ntasks; t += nw) {
         const WarpTask task = pt.tasks[t];
         const uint32_t mask = task.mask;
         const uint32_t *idx = pt.idx + task.elem_off, *obits = pt.obits + task.elem_off;
@@ -722,7 +734,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_warp_hess(BlockArgs a, const W
     double accS[kMaxWarpLayers];
 #pragma unroll
     for (int j = 0; j < kMaxWarpLayers; ++j) accS[j] = 0.0;
-    for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < ntasks; k += nw) {
+    for (int k = task_first(a); k < ntasks; k += nw) {
         const WarpTask task = tasks[k];
         const uint32_t mask = task.mask;
         const uint32_t *idx = a.idx + task.elem_off, *obits = a.obits + task.elem_off;
@@ -2203,6 +2215,7 @@ struct aegpu_engine {
     // environment switches it off); the device gate is their conjunction, the
     // per-instance flag adds the angle test of each evaluation
     bool half_static = false, start_sym = true, tune_half = true;
+    int task_order = 1;  // BlockArgs::task_order (AEGPU_TASK_ORDER=0: CTA-major)
     std::vector<int> mirror;        // operator -> mirror operator (half passes only)
     int *d_mirror = nullptr, *d_half_gate = nullptr;
     int *d_half = nullptr;          // per instance (alloc_instances)
@@ -2419,6 +2432,7 @@ struct aegpu_engine {
         a.tasks_h = b.wtasks_h;
         a.ntasks_h = b.nwtasks_h;
         a.vmap = nullptr;
+        a.task_order = task_order;
         return a;
     }
     // Device gate of the half passes: the tables are built, the start state is
@@ -3033,6 +3047,7 @@ int aegpu_create(aegpu_engine **out)
     if (const char *v = std::getenv("AEGPU_REUSE_HPSI")) e->reuse_hpsi = std::strcmp(v, "0") != 0;
     if (const char *v = std::getenv("AEGPU_FLIP")) e->tune_flip = std::strcmp(v, "0") != 0;
     if (const char *v = std::getenv("AEGPU_HALF")) e->tune_half = std::strcmp(v, "0") != 0;
+    if (const char *v = std::getenv("AEGPU_TASK_ORDER")) e->task_order = std::strcmp(v, "0") != 0;
     if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete e;
