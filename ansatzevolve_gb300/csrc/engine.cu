@@ -165,9 +165,9 @@ struct BlockArgs {
 
 // First task of this warp in the warp kernels' grid-stride loop (stride: the grid's
 // warps).  CTA-major hands a CTA consecutive tasks; warp-major hands warp w of CTA c
-// task w * gridDim.x + c, so that the tasks left over after whole rounds spread over
-// every CTA (and so every SM) instead of filling the first CTAs.  Both orders visit
-// each task once.
+// task w * gridDim.x + c, so that, in a launch whose CTAs are all resident at once, the
+// tasks left over after whole rounds spread over every CTA (and so every SM) instead of
+// filling the first CTAs.  Both orders visit each task once.
 __device__ __forceinline__ int task_first(const BlockArgs &a)
 {
     return a.task_order ? (int)((threadIdx.x >> 5) * gridDim.x + blockIdx.x)
@@ -2215,7 +2215,8 @@ struct aegpu_engine {
     // environment switches it off); the device gate is their conjunction, the
     // per-instance flag adds the angle test of each evaluation
     bool half_static = false, start_sym = true, tune_half = true;
-    int task_order = 1;  // BlockArgs::task_order (AEGPU_TASK_ORDER=0: CTA-major)
+    int task_order = 1;  // warp-major where a launch fits one wave (order_for; AEGPU_TASK_ORDER=0: never)
+    int rot_occ = 0, adj_occ = 0;  // resident CTAs per SM of k_warp_rot / k_warp_adj
     std::vector<int> mirror;        // operator -> mirror operator (half passes only)
     int *d_mirror = nullptr, *d_half_gate = nullptr;
     int *d_half = nullptr;          // per instance (alloc_instances)
@@ -2432,8 +2433,16 @@ struct aegpu_engine {
         a.tasks_h = b.wtasks_h;
         a.ntasks_h = b.nwtasks_h;
         a.vmap = nullptr;
-        a.task_order = task_order;
+        a.task_order = 0;
         return a;
+    }
+    // Task order of a warp-kernel launch of grid g with occ resident CTAs per SM:
+    // warp-major when every CTA is resident at once (one wave; the single-instance
+    // sweeps), else CTA-major -- with several waves the CTA scheduler balances the SMs
+    // itself, and consecutive tasks in one CTA share cached table and amplitude lines.
+    int order_for(dim3 g, int occ) const
+    {
+        return task_order && (int64_t)g.x * g.y * g.z <= (int64_t)sm_count * occ ? 1 : 0;
     }
     // Device gate of the half passes: the tables are built, the start state is
     // symmetric and the knob is on.
@@ -2643,6 +2652,7 @@ int run_evolve(aegpu_engine *e, int ninst)
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, 1.0, true);
             const dim3 g(b.rgrid, ninst);
+            a.task_order = e->order_for(g, e->rot_occ);
             if (e->W == 1)
                 launch_pass(e, k_warp_rot<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, e->d_psi, n, ck, e->n_ckpt);
             else
@@ -2828,6 +2838,7 @@ int run_backward(aegpu_engine *e, double *grad_dev, int ninst, double scale = 2.
         } else if (b.nwtasks) {
             BlockArgs a = e->block_args(bi, -1.0, half);
             const dim3 g(b.wgrid, ninst);
+            a.task_order = e->order_for(g, e->adj_occ);
             if (e->W == 1)
                 launch_pass(e, k_warp_adj<1>, g, a, (const WarpTask *)b.wtasks, b.nwtasks, ck, e->n_ckpt, e->d_h, n,
                             part, e->n_partials);
@@ -3256,13 +3267,18 @@ int aegpu_set_problem(aegpu_engine *e, int nq, int basis_kind, int n_elec, int n
     e->db = db;
     e->d_codes = e->upload(e->codes);
 
-    // resident CTAs per SM of the forward warp kernel (its register count)
-    int rot_occ = 0;
-    if (e->cplx)
+    // resident CTAs per SM of the forward and adjoint warp kernels (their register counts)
+    int rot_occ = 0, adj_occ = 0;
+    if (e->cplx) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rot_occ, k_warp_rot<2>, kWarpThreads, 0);
-    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&adj_occ, k_warp_adj<2>, kWarpThreads, 0);
+    } else {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rot_occ, k_warp_rot<1>, kWarpThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&adj_occ, k_warp_adj<1>, kWarpThreads, 0);
+    }
     cudaGetLastError();
+    e->rot_occ = rot_occ;
+    e->adj_occ = adj_occ;
     // orbit tables per block
     const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     e->dblocks.clear();
