@@ -264,3 +264,47 @@ def test_diagonal_half_pass_counts():
     _, fwd, adj = e.fp64_work(half=False, half_passes=False)
     assert fwd == 4 * act and adj == 6 * act + slots
     e.close()
+
+
+@pytest.mark.parametrize("half", [1, 0])
+def test_task_orders_agree(half, monkeypatch):
+    """The sweeps' two task orders (warp-major where a launch fits one wave, the default;
+    CTA-major everywhere with AEGPU_TASK_ORDER=0) visit every warp task once: the same
+    state, energy and gradient up to the order of the gradient sums, with and without
+    the half passes, real and complex."""
+    from ansatzevolve_gb300.lucj import lucj_operators, random_lucj
+    from ansatzevolve_gb300.synthetic import hartree_fock_index, synthetic_integrals
+    N, na = 10, 5
+    pb = synthetic_problem(N, na, na, 2, 21)
+    P = int(np.max(pb["order_1b"]))
+    ang = compressed_angles(pb, np.random.default_rng(22).uniform(-0.5, 0.5, P))
+    K, J = random_lucj(8, 4)
+    lops, lang = lucj_operators(K, J)
+    h1, g2 = synthetic_integrals(8, 9)
+    out = []
+    for order in ("1", "0"):
+        monkeypatch.setenv("AEGPU_TASK_ORDER", order)
+        e = make_engine(pb)
+        e.set_tuning(ae.TUNE_HALF, half)
+        e.set_ham_integrals(pb["h1"], pb["g2"], ae.HAM_ON_THE_FLY)
+        E, g = e.gradient(ang)
+        assert bool(e.half_status()[0]) == bool(half)
+        psi = e.evolve(ang)
+        e.close()
+        c = ae.Engine(16, ae.BASIS_SZ, 8, 4, 4, lops, complex_mode=True)
+        init = np.zeros(2 * c.D)
+        init[2 * np.searchsorted(c.states(), hartree_fock_index(8, 4, 4))] = 1.0
+        c.set_initial(init)
+        c.set_tuning(ae.TUNE_HALF, half)
+        c.set_ham_integrals(h1, g2, ae.HAM_STORED)
+        Ec, gc = c.gradient(lang)
+        psic = c.evolve(lang)
+        c.close()
+        out.append((E, g, psi, Ec, gc, psic))
+    (E1, g1, p1, Ec1, gc1, pc1), (E0, g0, p0, Ec0, gc0, pc0) = out
+    for a, b in ((E1, E0), (Ec1, Ec0)):
+        assert abs(a - b) < 1e-12 * max(1.0, abs(b))
+    for a, b in ((g1, g0), (gc1, gc0)):
+        np.testing.assert_allclose(a, b, atol=1e-12, rtol=0)
+    for a, b in ((p1, p0), (pc1, pc0)):
+        np.testing.assert_allclose(a, b, atol=1e-14, rtol=0)
