@@ -4686,6 +4686,11 @@ static int lanczos_lowest(aegpu_engine *e, int nst, double tol, int basis, int m
     int prod = 0, rc = 0;
     bool done = false;
     std::vector<double> al, be, sv, th;
+    // nst = 1: from a start with psi(a,b) = psi(b,a) every Krylov vector keeps that
+    // symmetry exactly (H preserves it, and the recurrence, the reorthogonalisation and
+    // the restarts update mirrored amplitudes by the same arithmetic), so the products
+    // may take the spin-flip half product; each tests its input first (run_apply)
+    const bool flip = nst == 1;
     while (!done) {
         double nx = 0.0;
         e->launches += ae::dot(e->d_ground, e->d_ground, ni, 1, d_res, 1, d_dpart, e->sm_count, s);
@@ -4701,7 +4706,7 @@ static int lanczos_lowest(aegpu_engine *e, int nst, double tol, int basis, int m
         int k = 0, checked = 0;
         for (int j = 0; j < m && !done; ++j) {
             double *v = Vb + (size_t)j * n, *w = Vb + (size_t)(j + 1) * n;
-            if ((rc = run_apply(e, v, w, nullptr, 1, nullptr, false))) {
+            if ((rc = run_apply(e, v, w, nullptr, 1, nullptr, false, flip, flip ? e->d_flip_part : nullptr))) {
                 release();
                 return rc;
             }
@@ -4817,7 +4822,7 @@ static int lanczos_lowest(aegpu_engine *e, int nst, double tol, int basis, int m
         }
         e->launches += ae::axpby(x, x, ni, sign / sc[0], 0.0, nullptr, s);
         double *w = Vb;
-        if ((rc = run_apply(e, x, w, nullptr, 1, nullptr, false))) {
+        if ((rc = run_apply(e, x, w, nullptr, 1, nullptr, false, flip, flip ? e->d_flip_part : nullptr))) {
             release();
             return rc;
         }
