@@ -166,8 +166,8 @@ struct BlockArgs {
 // First task of this warp in the warp kernels' grid-stride loop (stride: the grid's
 // warps).  CTA-major hands a CTA consecutive tasks; warp-major hands warp w of CTA c
 // task w * gridDim.x + c, so that, in a launch whose CTAs are all resident at once, the
-// tasks left over after whole rounds spread over every CTA (and so every SM) instead of
-// filling the first CTAs.  Both orders visit each task once.
+// tasks left over once every warp has one spread over every CTA (and so every SM)
+// instead of filling the first CTAs.  Both orders visit each task once.
 __device__ __forceinline__ int task_first(const BlockArgs &a)
 {
     return a.task_order ? (int)((threadIdx.x >> 5) * gridDim.x + blockIdx.x)

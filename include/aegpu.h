@@ -117,7 +117,7 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * and its mirror.  Projected gradients and Hessians always run the full passes.
  * A sweep launch whose CTAs are all resident at once hands its warp tasks out
  * warp-major (warp w of CTA c starts at task w * CTAs + c, so that the tasks left over
- * after whole rounds spread over every SM); AEGPU_TASK_ORDER=0 in the environment keeps
+ * once every warp has one spread over every SM); AEGPU_TASK_ORDER=0 in the environment keeps
  * the CTA-major order of larger launches everywhere, for engines created afterwards (a
  * diagnostic switch; both orders give results equal to rounding).
  * No counterpart in the reference. */
