@@ -114,12 +114,14 @@ int aegpu_set_batch(aegpu_engine *e, int nb);
  * visit one orbit of every mirror pair, only the amplitudes with a <= b are kept
  * current during the sweeps (the evolved state is completed by copying them to their
  * mirrors), and each gradient is the sum over the visited orbits for the excitation
- * and its mirror.  Projected gradients and Hessians always run the full passes.
+ * and its mirror.  Projected gradients always run the full passes; Hessians run the
+ * full passes on one tangent of every mirror pair where the same symmetry holds (and
+ * on every tangent otherwise).
  * A sweep launch whose CTAs are all resident at once hands its warp tasks out
  * warp-major (warp w of CTA c starts at task w * CTAs + c, so that the tasks left over
- * once every warp has one spread over every SM); AEGPU_TASK_ORDER=0 in the environment keeps
- * the CTA-major order of larger launches everywhere, for engines created afterwards (a
- * diagnostic switch; both orders give results equal to rounding).
+ * once every warp has one spread over every SM); AEGPU_TASK_ORDER=0 in the
+ * environment keeps the CTA-major order of larger launches everywhere, for engines
+ * created afterwards (a diagnostic switch; both orders give results equal to rounding).
  * No counterpart in the reference. */
 enum { AEGPU_TUNE_PASS_OPS = 1, AEGPU_TUNE_CTAS_PER_SM = 2, AEGPU_TUNE_OTF_THREADS = 3, AEGPU_TUNE_SPMV_TPR = 4,
        AEGPU_TUNE_PDL = 5, AEGPU_TUNE_REUSE_HPSI = 6, AEGPU_TUNE_FLIP = 7, AEGPU_TUNE_HALF = 8 };
